@@ -1,0 +1,309 @@
+"""hspike_gb300 -- GB300-native SPIKE banded solver.
+
+The product is the C-ABI library ``_build/libspike_gb300.so`` (C host layer +
+sm_103a kernels).  This module is a thin ctypes mirror of its API for Python
+callers, tests and the benchmark:
+
+* ``dspike_core_host`` / ``zspike_core_host`` / ``sspike_core_host`` /
+  ``cspike_core_host`` / ``dspike_core_host_blocking`` -- the reference's
+  entry points (OpenMP/spike_interfaces.h:28-72), same argument order and
+  meaning, numpy arrays in place of pointers, ``Error_t`` returned;
+* ``Context`` / ``Factor`` -- the extensions of ``include/spike_gb300.h``;
+* ``solve`` -- convenience wrapper returning x.
+
+There is no Python or CPU compute path: if the library is missing, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import gen_path, lib_path
+
+SPIKE_SUCCESS = 0
+SPIKE_ERROR = 1
+
+SPIKE_OPT_PRECISION = 0
+SPIKE_OPT_PARTITIONS = 1
+SPIKE_OPT_MAX_REFINE = 2
+SPIKE_OPT_TOLERANCE = 3
+SPIKE_OPT_REDUCED_REFINE = 4
+SPIKE_PRECISION_MIXED = 0
+SPIKE_PRECISION_FP64 = 1
+
+ERR_NAMES = {0: "none", 1: "argument", 2: "csr", 3: "bandwidth", 4: "cuda", 5: "memory", 6: "pivot",
+             7: "convergence", 8: "no_device", 9: "handle"}
+
+EXPORTS = [
+    "sspike_core_host", "dspike_core_host", "cspike_core_host", "zspike_core_host", "dspike_core_host_blocking",
+    "SPIKE_SUCCESS", "SPIKE_ERROR", "spike_last_error_code", "spike_last_error", "spike_context_create",
+    "spike_context_destroy", "spike_context_set_stream", "spike_set_option", "spike_get_option", "spike_get_info",
+    "spike_dsolve_device", "spike_zsolve_device", "spike_dfactor", "spike_zfactor", "spike_dfactor_device",
+    "spike_dsolve_factored", "spike_zsolve_factored", "spike_dsolve_factored_device", "spike_factor_release",
+]
+
+
+class SpikeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{ERR_NAMES.get(code, code)}] {msg}")
+        self.code = code
+        self.name = ERR_NAMES.get(code, str(code))
+
+
+class Info(C.Structure):
+    _fields_ = [("relres_max", C.c_double), ("refine_sweeps", C.c_int), ("partitions", C.c_int), ("ku", C.c_int),
+                ("kl", C.c_int), ("block", C.c_int), ("kernel_launches", C.c_longlong),
+                ("device_bytes", C.c_size_t)]
+
+
+_LIB = None
+_GEN = None
+
+
+def load(path: str | None = None):
+    """Load libspike_gb300.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = path or lib_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"native library missing: {path} (run hspike_gb300.build.build())")
+    L = C.CDLL(path)
+    ip, vp, i = C.POINTER(C.c_int), C.c_void_p, C.c_int
+    for name in ("sspike_core_host", "dspike_core_host", "cspike_core_host", "zspike_core_host",
+                 "dspike_core_host_blocking"):
+        f = getattr(L, name)
+        f.argtypes = [i, i, i, vp, vp, vp, vp, vp]
+        f.restype = i
+    L.spike_last_error_code.restype = i
+    L.spike_last_error.restype = C.c_char_p
+    L.spike_context_create.argtypes = [C.POINTER(vp)]
+    L.spike_context_destroy.argtypes = [vp]
+    L.spike_context_set_stream.argtypes = [vp, vp]
+    L.spike_set_option.argtypes = [vp, i, C.c_double]
+    L.spike_get_option.argtypes = [vp, i, C.POINTER(C.c_double)]
+    L.spike_get_info.argtypes = [vp, C.POINTER(Info)]
+    for name in ("spike_dsolve_device", "spike_zsolve_device"):
+        getattr(L, name).argtypes = [vp, i, i, i, vp, vp, vp, vp, vp]
+    for name in ("spike_dfactor", "spike_zfactor", "spike_dfactor_device"):
+        getattr(L, name).argtypes = [vp, i, i, vp, vp, vp, C.POINTER(vp)]
+    for name in ("spike_dsolve_factored", "spike_zsolve_factored", "spike_dsolve_factored_device"):
+        getattr(L, name).argtypes = [vp, i, vp, vp]
+    L.spike_factor_release.argtypes = [vp]
+    _LIB = L
+    return L
+
+
+def last_error() -> tuple[int, str]:
+    L = load()
+    return L.spike_last_error_code(), (L.spike_last_error() or b"").decode()
+
+
+def _check(rc: int):
+    if rc != SPIKE_SUCCESS:
+        code, msg = last_error()
+        raise SpikeError(code, msg)
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data)
+
+
+_DT = {"s": (np.float32, np.float32), "d": (np.float64, np.float64), "c": (np.complex64, np.complex64),
+       "z": (np.complex128, np.complex128)}
+
+
+def _core(prefix: str, n, nnz, nrhs, colind, rowptr, aij, x, b, blocking=False) -> int:
+    """Call ``?spike_core_host`` with numpy arrays exactly like the C API.
+
+    ``x`` is overwritten in place (column-major n x nrhs), as in the reference.
+    """
+    L = load()
+    dt = _DT[prefix][0]
+    for name, arr, want in (("colind", colind, np.int32), ("rowptr", rowptr, np.int32), ("aij", aij, dt),
+                            ("x", x, dt), ("b", b, dt)):
+        if arr.dtype != want:
+            raise TypeError(f"{name} must be {np.dtype(want).name}, got {arr.dtype}")
+        if not (arr.flags.f_contiguous or arr.flags.c_contiguous):
+            raise ValueError(f"{name} must be contiguous")
+    if x.ndim == 2 and not x.flags.f_contiguous:
+        raise ValueError("x must be column-major (Fortran order)")
+    fn = L.dspike_core_host_blocking if blocking else getattr(L, prefix + "spike_core_host")
+    return fn(int(n), int(nnz), int(nrhs), _ptr(colind), _ptr(rowptr), _ptr(aij), _ptr(x), _ptr(b))
+
+
+def sspike_core_host(n, nnz, nrhs, colind, rowptr, aij, x, b):
+    return _core("s", n, nnz, nrhs, colind, rowptr, aij, x, b)
+
+
+def dspike_core_host(n, nnz, nrhs, colind, rowptr, aij, x, b):
+    return _core("d", n, nnz, nrhs, colind, rowptr, aij, x, b)
+
+
+def cspike_core_host(n, nnz, nrhs, colind, rowptr, aij, x, b):
+    return _core("c", n, nnz, nrhs, colind, rowptr, aij, x, b)
+
+
+def zspike_core_host(n, nnz, nrhs, colind, rowptr, aij, x, b):
+    return _core("z", n, nnz, nrhs, colind, rowptr, aij, x, b)
+
+
+def dspike_core_host_blocking(n, nnz, nrhs, colind, rowptr, aij, x, b):
+    return _core("d", n, nnz, nrhs, colind, rowptr, aij, x, b, blocking=True)
+
+
+def set_option(option: int, value: float, ctx=None):
+    _check(load().spike_set_option(ctx, option, float(value)))
+
+
+def get_option(option: int, ctx=None) -> float:
+    v = C.c_double()
+    _check(load().spike_get_option(ctx, option, C.byref(v)))
+    return v.value
+
+
+def get_info(ctx=None) -> Info:
+    info = Info()
+    _check(load().spike_get_info(ctx, C.byref(info)))
+    return info
+
+
+def solve(rowptr, colind, aij, b, precision=SPIKE_PRECISION_MIXED, partitions=0, ctx=None):
+    """x = A^{-1} b on the GPU through the C API; b may be 1-D or n x nrhs."""
+    cplx = np.iscomplexobj(aij) or np.iscomplexobj(b)
+    dt = np.complex128 if cplx else np.float64
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    aij = np.ascontiguousarray(aij, dt)
+    b2 = np.asfortranarray(np.asarray(b, dt).reshape(len(rowptr) - 1, -1))
+    x = np.zeros_like(b2, order="F")
+    if ctx is not None:
+        ctx.set_option(SPIKE_OPT_PRECISION, precision)
+        ctx.set_option(SPIKE_OPT_PARTITIONS, partitions)
+    else:
+        set_option(SPIKE_OPT_PRECISION, precision)
+        set_option(SPIKE_OPT_PARTITIONS, partitions)
+    n, nrhs = b2.shape
+    rc = _core("z" if cplx else "d", n, len(colind), nrhs, colind, rowptr, aij, x, b2)
+    _check(rc)
+    return x if np.ndim(b) == 2 else x[:, 0]
+
+
+class Context:
+    """An explicit solver context (own CUDA stream unless one is set)."""
+
+    def __init__(self):
+        self._h = C.c_void_p()
+        _check(load().spike_context_create(C.byref(self._h)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle: int | None):
+        _check(load().spike_context_set_stream(self._h, C.c_void_p(stream_handle or 0)))
+
+    def set_option(self, option, value):
+        set_option(option, value, self._h)
+
+    def get_option(self, option):
+        return get_option(option, self._h)
+
+    def info(self) -> Info:
+        return get_info(self._h)
+
+    def solve_device(self, n, nnz, nrhs, d_colind: int, d_rowptr: int, d_aij: int, d_x: int, d_b: int,
+                     complex_=False):
+        fn = load().spike_zsolve_device if complex_ else load().spike_dsolve_device
+        _check(fn(self._h, n, nnz, nrhs, C.c_void_p(d_colind), C.c_void_p(d_rowptr), C.c_void_p(d_aij),
+                  C.c_void_p(d_x), C.c_void_p(d_b)))
+
+    def close(self):
+        if self._h:
+            load().spike_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Factor:
+    """Factor once, solve many right-hand sides with resident factors."""
+
+    def __init__(self, rowptr, colind, aij, ctx: Context | None = None):
+        self.cplx = np.iscomplexobj(aij)
+        dt = np.complex128 if self.cplx else np.float64
+        self.rowptr = np.ascontiguousarray(rowptr, np.int32)
+        self.colind = np.ascontiguousarray(colind, np.int32)
+        self.aij = np.ascontiguousarray(aij, dt)
+        self.n = len(self.rowptr) - 1
+        self._h = C.c_void_p()
+        fn = load().spike_zfactor if self.cplx else load().spike_dfactor
+        _check(fn(ctx.handle if ctx else None, self.n, len(self.colind), _ptr(self.colind), _ptr(self.rowptr),
+                  _ptr(self.aij), C.byref(self._h)))
+
+    def solve(self, b):
+        dt = np.complex128 if self.cplx else np.float64
+        b2 = np.asfortranarray(np.asarray(b, dt).reshape(self.n, -1))
+        x = np.zeros_like(b2, order="F")
+        fn = load().spike_zsolve_factored if self.cplx else load().spike_dsolve_factored
+        _check(fn(self._h, b2.shape[1], _ptr(x), _ptr(b2)))
+        return x if np.ndim(b) == 2 else x[:, 0]
+
+    def release(self):
+        if self._h:
+            _check(load().spike_factor_release(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- generator
+def _gen():
+    global _GEN
+    if _GEN is None:
+        path = gen_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"generator library missing: {path} (run hspike_gb300.build.build())")
+        G = C.CDLL(path)
+        G.spike_gen_rowptr.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p]
+        G.spike_gen_rowptr.restype = C.c_longlong
+        G.spike_gen_fill.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_ulonglong, C.c_int, C.c_int,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        G.spike_gen_fill.restype = C.c_int
+        _GEN = G
+    return _GEN
+
+
+def gen_banded(n, ku, kl, dom, seed, complex_=False, nrhs=1, alloc=None):
+    """Seeded banded system: returns (rowptr, colind, aij, x_true, b).
+
+    Off-diagonals U[-1,1) (re/im i.i.d. for complex); diagonal = dom * (sum of
+    the row's off-diagonal magnitudes) * (random sign, or e^{i theta});
+    x_true U[-1,1); b = A x_true in double.  ``alloc(shape, dtype)`` may supply
+    the arrays (e.g. pinned host memory); it defaults to numpy.empty.
+    """
+    G = _gen()
+    alloc = alloc or (lambda shape, dtype: np.empty(shape, dtype))
+    rowptr = alloc((n + 1,), np.int32)
+    nnz = int(G.spike_gen_rowptr(n, ku, kl, _ptr(rowptr)))
+    colind = alloc((nnz,), np.int32)
+    dt = np.complex128 if complex_ else np.float64
+    aij = alloc((nnz,), dt)
+    x_true = alloc((n * nrhs,), dt)
+    b = alloc((n * nrhs,), dt)
+    G.spike_gen_fill(n, ku, kl, float(dom), int(seed), 1 if complex_ else 0, nrhs, _ptr(rowptr), _ptr(colind),
+                     _ptr(aij), _ptr(x_true), _ptr(b))
+    x_true = x_true.reshape((n, nrhs), order="F")
+    b = b.reshape((n, nrhs), order="F")
+    return rowptr, colind, aij, x_true, b

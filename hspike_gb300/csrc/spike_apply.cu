@@ -1,0 +1,295 @@
+// spike_apply.cu -- right-hand-side phases of the SPIKE solve on sm_103a.
+//
+//   k_apply      y_i = A_i^{-1} r_i with the resident block factors: forward
+//                z_J = r_J - L_J z_{J-1}, backward y_J = G_J (z_J - E_J y_{J+1}).
+//                Replaces the reference's per-partition directSolver_SolveForRHS
+//                on f_i (OpenMP/spike_interfaces.c:143) -- SuperLU dgstrs +
+//                dgsrfs per column (OpenMP/spike_superlu.c:986,1002).
+//   k_ytips      bottom / top tips of y into the reduced right-hand side
+//                (block_AddTipTOReducedRHS, OpenMP/spike_matrix.c:1272-1297).
+//   k_retrieve   x_i (+)= y_i - V_i t_{i+1} - W_i b_{i-1} with the stored spikes.
+//                The reference re-factors A_i and re-solves
+//                A_i x_i = f_i - B_i x_t - C_i x_b (OpenMP/spike_interfaces.c
+//                :259-396); with the spikes resident this is one parallel pass.
+#include "spike_common.cuh"
+
+namespace {
+
+constexpr int RC = 32; // right-hand-side columns per CTA
+
+// out[r][h] = sign * sum_k M[r][k] v[k][h] (+ base[r][h]), r < KB, h < nr.
+// M: shared tile (LD = KB+1); v, base, out: shared [KB][RC].
+template <class T, int KB, bool HAS_BASE>
+__device__ void tile_mv(T *out, const T *M, const T *v, const T *base, int nr, bool negate)
+{
+    constexpr int NT = NTOf<KB>::value;
+    constexpr int LD = KB + 1;
+    const int O = KB * nr;
+    int spl = 1;
+    while (spl < 32 && spl * 2 * O <= NT && spl * 2 <= KB) spl *= 2;
+    const int tid = threadIdx.x;
+    const int part = tid & (spl - 1);
+    const int groups = NT / spl;
+    // every thread runs the same number of iterations so the shuffles converge
+    const int iters = (O + groups - 1) / groups;
+    for (int it = 0; it < iters; it++) {
+        const int o = it * groups + tid / spl;
+        T acc = sc_zero<T>();
+        int r = 0, h = 0;
+        if (o < O) {
+            r = o / nr;
+            h = o - r * nr;
+            for (int k = part; k < KB; k += spl) acc = madd(acc, M[r * LD + k], v[k * RC + h]);
+        }
+        for (int off = spl >> 1; off > 0; off >>= 1) {
+            if constexpr (sizeof(T) == 4) {
+                acc = acc + __shfl_xor_sync(0xffffffffu, acc, off);
+            } else {
+                // generic path: shuffle the raw words
+                T other;
+                const unsigned *src = (const unsigned *)&acc;
+                unsigned *dst = (unsigned *)&other;
+#pragma unroll
+                for (int w = 0; w < (int)(sizeof(T) / 4); w++) dst[w] = __shfl_xor_sync(0xffffffffu, src[w], off);
+                acc = acc + other;
+                continue;
+            }
+        }
+        if (o < O && part == 0) {
+            T val = negate ? -acc : acc;
+            if (HAS_BASE) val = base[r * RC + h] + val;
+            out[r * RC + h] = val;
+        }
+    }
+}
+
+template <class T, int KB> __device__ void load_tile_s(T *s, const T *g)
+{
+    constexpr int NT = NTOf<KB>::value;
+    for (int q = threadIdx.x; q < KB * KB; q += NT) {
+        const int r = q / KB, c = q - r * KB;
+        s[r * (KB + 1) + c] = g[q];
+    }
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_apply(const int *__restrict__ part_start, const int *__restrict__ blk_off, const T *__restrict__ gL,
+            const T *__restrict__ gG, const T *__restrict__ gE, const typename HighOf<T>::type *__restrict__ r,
+            int n, int nrhs, long long NP, T *gz, T *gy)
+{
+    using H = typename HighOf<T>::type;
+    constexpr int NT = NTOf<KB>::value;
+    constexpr size_t TS = (size_t)KB * KB;
+    constexpr int LDT = KB + 1;
+    const int part = blockIdx.x;
+    const int h0 = blockIdx.y * RC;
+    const int nr = min(RC, nrhs - h0);
+    const int s = part_start[part], m = part_start[part + 1] - s;
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const long long rb = (long long)blk_off[part] * KB; // padded-row base
+
+    extern __shared__ char smraw[];
+    T *sM = (T *)smem_align(smraw);
+    T *sM2 = sM + KB * LDT;
+    T *sv = sM2 + KB * LDT; // [KB][RC]
+    T *sp = sv + KB * RC;   // previous block's vector
+    T *sw = sp + KB * RC;   // work vector
+
+    // forward: z_J = r_J - L_J z_{J-1}
+    for (int J = 0; J < N; J++) {
+        for (int q = threadIdx.x; q < KB * nr; q += NT) {
+            const int lr = q / nr, h = q - lr * nr;
+            const int lrow = J * KB + lr;
+            sv[lr * RC + h] = lrow < m ? sc_cvt<T, H>(r[(size_t)(h0 + h) * n + s + lrow]) : sc_zero<T>();
+        }
+        if (J > 0) load_tile_s<T, KB>(sM, gL + tb + J * TS);
+        __syncthreads();
+        if (J > 0) {
+            tile_mv<T, KB, true>(sw, sM, sp, sv, nr, true);
+            __syncthreads();
+        } else {
+            for (int q = threadIdx.x; q < KB * RC; q += NT) sw[q] = sv[q];
+            __syncthreads();
+        }
+        for (int q = threadIdx.x; q < KB * nr; q += NT) {
+            const int lr = q / nr, h = q - lr * nr;
+            const T v = sw[lr * RC + h];
+            sp[lr * RC + h] = v;
+            gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
+        }
+        __syncthreads();
+    }
+    // backward: y_J = G_J (z_J - E_J y_{J+1})
+    for (int J = N - 1; J >= 0; J--) {
+        load_tile_s<T, KB>(sM, gG + tb + J * TS);
+        if (J < N - 1) load_tile_s<T, KB>(sM2, gE + tb + J * TS);
+        for (int q = threadIdx.x; q < KB * nr; q += NT) {
+            const int lr = q / nr, h = q - lr * nr;
+            sv[lr * RC + h] = gz[(size_t)(h0 + h) * NP + rb + J * KB + lr];
+        }
+        __syncthreads();
+        if (J < N - 1) {
+            tile_mv<T, KB, true>(sw, sM2, sp, sv, nr, true);
+            __syncthreads();
+            tile_mv<T, KB, false>(sv, sM, sw, nullptr, nr, false);
+        } else {
+            tile_mv<T, KB, false>(sw, sM, sv, nullptr, nr, false);
+            __syncthreads();
+            for (int q = threadIdx.x; q < KB * RC; q += NT) sv[q] = sw[q];
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < KB * nr; q += NT) {
+            const int lr = q / nr, h = q - lr * nr;
+            const T v = sv[lr * RC + h];
+            sp[lr * RC + h] = v;
+            gy[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// g_i = (y_i bottom, y_{i+1} top), FP64 / complex128.
+template <class T, int KB>
+__global__ void k_ytips(const int *__restrict__ part_start, const int *__restrict__ blk_off, const T *__restrict__ gy,
+                        long long NP, int nrhs, int n_iface, typename HighOf<T>::type *g)
+{
+    using H = typename HighOf<T>::type;
+    const int i = blockIdx.x;
+    const int mi = part_start[i + 1] - part_start[i];
+    const long long NR = (long long)n_iface * 2 * KB;
+    for (int q = threadIdx.x; q < 2 * KB * nrhs; q += blockDim.x) {
+        const int h = q / (2 * KB), rr = q - h * 2 * KB;
+        long long prow;
+        if (rr < KB)
+            prow = (long long)blk_off[i] * KB + (mi - KB + rr);
+        else
+            prow = (long long)blk_off[i + 1] * KB + (rr - KB);
+        g[h * NR + (long long)i * 2 * KB + rr] = sc_cvt<H, T>(gy[(size_t)h * NP + prow]);
+    }
+}
+
+// x (+)= y - V_i t_{i+1} - W_i b_{i-1}; one CTA per (partition, block).
+template <class T, int KB>
+__global__ void __launch_bounds__(256)
+    k_retrieve(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const int *__restrict__ blk_part,
+               const T *__restrict__ gV, const T *__restrict__ gW, const T *__restrict__ gy,
+               const typename HighOf<T>::type *__restrict__ u, long long NP, int n_iface, int n, int nrhs,
+               typename HighOf<T>::type *x, int accumulate)
+{
+    using H = typename HighOf<T>::type;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int gb = blockIdx.x; // global block index
+    const int part = blk_part[gb];
+    const int J = gb - blk_off[part];
+    const int s = part_start[part], m = part_start[part + 1] - s;
+    const long long NR = (long long)n_iface * 2 * KB;
+    const bool hasV = part < p - 1, hasW = part > 0;
+    __shared__ H st[2 * KB * 8];
+    const int hchunk = 8;
+    for (int hb = 0; hb < nrhs; hb += hchunk) {
+        const int nr = min(hchunk, nrhs - hb);
+        __syncthreads();
+        for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+            const int c = q / nr, h = q - c * nr;
+            st[c * hchunk + h] = hasV ? u[(hb + h) * NR + (long long)part * 2 * KB + KB + c] : sc_zero<H>();
+            st[(KB + c) * hchunk + h] = hasW ? u[(hb + h) * NR + (long long)(part - 1) * 2 * KB + c] : sc_zero<H>();
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+            const int h = q / KB, lr = q - h * KB;
+            const int lrow = J * KB + lr;
+            if (lrow >= m) continue;
+            T acc = gy[(size_t)(hb + h) * NP + (long long)gb * KB + lr];
+            if (hasV)
+                for (int c = 0; c < KB; c++)
+                    acc = msub(acc, gV[(size_t)gb * TS + (size_t)c * KB + lr], sc_cvt<T, H>(st[c * hchunk + h]));
+            if (hasW)
+                for (int c = 0; c < KB; c++)
+                    acc = msub(acc, gW[(size_t)gb * TS + (size_t)c * KB + lr],
+                               sc_cvt<T, H>(st[(KB + c) * hchunk + h]));
+            H *xp = x + (size_t)(hb + h) * n + s + lrow;
+            const H d = sc_cvt<H, T>(acc);
+            *xp = accumulate ? *xp + d : d;
+        }
+    }
+}
+
+template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
+{
+    constexpr int NT = NTOf<KB>::value;
+    const size_t smem = 16 + sizeof(T) * (2 * KB * (KB + 1) + 3 * KB * RC);
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
+    dim3 grid(P->p, (nrhs + RC - 1) / RC);
+    k_apply<T, KB><<<grid, NT, smem, st>>>(P->d_part_start, P->d_blk_off, (const T *)P->d_L, (const T *)P->d_G,
+                                           (const T *)P->d_E, (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP,
+                                           (T *)P->d_z, (T *)P->d_y);
+    SPK_CHECK_LAUNCH();
+    P->launches++;
+    if (P->n_iface > 0) {
+        k_ytips<T, KB><<<P->n_iface, 128, 0, st>>>(P->d_part_start, P->d_blk_off, (const T *)P->d_y, P->NP, nrhs,
+                                                   P->n_iface, (typename HighOf<T>::type *)P->d_g);
+        SPK_CHECK_LAUNCH();
+        P->launches++;
+    }
+    return SPK_OK;
+}
+
+template <class T, int KB> int run_retrieve(spk_plan *P, void *x, int nrhs, int accumulate, cudaStream_t st)
+{
+    k_retrieve<T, KB><<<P->total_blocks, 256, 0, st>>>(
+        P->d_part_start, P->d_blk_off, P->p, P->d_blk_part, (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y,
+        (const typename HighOf<T>::type *)P->d_u, P->NP, P->n_iface, P->n, nrhs, (typename HighOf<T>::type *)x,
+        accumulate);
+    SPK_CHECK_LAUNCH();
+    P->launches++;
+    return SPK_OK;
+}
+
+#define SPK_KB_SWITCH(FN, T, ...)                                                                               \
+    switch (P->KB) {                                                                                            \
+    case 2: return FN<T, 2>(__VA_ARGS__);                                                                       \
+    case 4: return FN<T, 4>(__VA_ARGS__);                                                                       \
+    case 8: return FN<T, 8>(__VA_ARGS__);                                                                       \
+    case 16: return FN<T, 16>(__VA_ARGS__);                                                                     \
+    case 32: return FN<T, 32>(__VA_ARGS__);                                                                     \
+    case 64:                                                                                                    \
+        if constexpr (sizeof(T) <= 8) return FN<T, 64>(__VA_ARGS__);                                            \
+        else return SPK_EBAND;                                                                                  \
+    default: return SPK_EBAND;                                                                                  \
+    }
+
+template <class T> int disp_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
+{
+    SPK_KB_SWITCH(run_apply, T, P, r, nrhs, st)
+}
+template <class T> int disp_retrieve(spk_plan *P, void *x, int nrhs, int acc, cudaStream_t st)
+{
+    SPK_KB_SWITCH(run_retrieve, T, P, x, nrhs, acc, st)
+}
+
+} // namespace
+
+extern "C" int spk_apply(spk_plan *P, const void *d_r, int nrhs, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (P->is_complex)
+        return P->mode == SPK_MIXED ? disp_apply<cfloat>(P, d_r, nrhs, st) : disp_apply<cdouble>(P, d_r, nrhs, st);
+    return P->mode == SPK_MIXED ? disp_apply<float>(P, d_r, nrhs, st) : disp_apply<double>(P, d_r, nrhs, st);
+}
+
+extern "C" int spk_retrieve(spk_plan *P, void *d_x, int nrhs, int accumulate, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (P->is_complex)
+        return P->mode == SPK_MIXED ? disp_retrieve<cfloat>(P, d_x, nrhs, accumulate, st)
+                                    : disp_retrieve<cdouble>(P, d_x, nrhs, accumulate, st);
+    return P->mode == SPK_MIXED ? disp_retrieve<float>(P, d_x, nrhs, accumulate, st)
+                                : disp_retrieve<double>(P, d_x, nrhs, accumulate, st);
+}

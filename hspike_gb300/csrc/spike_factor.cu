@@ -1,0 +1,402 @@
+// spike_factor.cu -- factorization phase of the SPIKE solve on sm_103a.
+//
+// Replaces the reference's factorization loop (OpenMP/spike_interfaces.c
+// :105-237): per partition it extracted A_i as CSR (matrix_ExtractMatrix,
+// OpenMP/spike_matrix.c:563), factored it with SuperLU (OpenMP/
+// spike_superlu.c:763), extracted dense B_i / C_i (matrix_ExtractBlock,
+// OpenMP/spike_matrix.c:421) and solved A_i V_i = B_i, A_i W_i = C_i column by
+// column, then scattered the tips into R (OpenMP/spike_matrix.c:1414).
+//
+// Here one CTA owns one partition and walks it as a block-tridiagonal matrix
+// with KB x KB blocks (KB >= max(ku, kl)), reading its CSR rows exactly once:
+//
+//   k_factor_fwd   (K1 + K2) scatter CSR rows of block J into D_J, E_J, F_{J-1}
+//                  L_J = F_{J-1} G_{J-1},  S_J = D_J - L_J E_{J-1},
+//                  G_J = S_J^{-1} (Gauss-Jordan), and the forward sweep of the
+//                  W spike z_J = -L_J z_{J-1} (z_0 = C^_i).  Stores L, G, E, z.
+//   k_factor_bwd   (K3) backward sweep X_J = G_J (Z_J - E_J X_{J+1}) for
+//                  [V | W] (V's right-hand side B^_i lives in the last rows
+//                  only), storing the full spikes for explicit retrieval.
+//   k_tips         bottom/top tips of V and W into the FP64 interface blocks
+//                  of the reduced system.
+//
+// Pivot-free: A is required to be diagonally dominant enough that block
+// elimination needs no pivoting (every shipped workload is).  A zero or
+// non-finite pivot sets SPK_DEV_ERR_PIVOT and the host returns SPIKE_ERROR.
+#include "spike_common.cuh"
+
+namespace {
+
+template <class T, int KB> struct FactorSmem {
+    using TL = Tile<T, KB, NTOf<KB>::value>;
+    static constexpr size_t tile = sizeof(T) * TL::ELEMS;
+    static constexpr size_t fwd = 6 * tile + sizeof(T) * 4 * KB + 64;
+    static constexpr size_t bwd = 6 * tile + 64;
+};
+
+// Scatter the CSR rows of block J of partition [s, e) into the shared tiles.
+// F: columns of block J-1, D: block J, En: block J+1, Z: C^ coupling (J == 0,
+// columns s-KB..s-1), Bhat (global, row-major): B^ coupling (columns e..e+KB-1)
+template <class T, class H, int KB>
+__device__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
+                              const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *Z,
+                              T *gBhat, unsigned *err)
+{
+    constexpr int NT = NTOf<KB>::value;
+    constexpr int LD = KB + 1;
+    const int m = e - s;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int NW = NT / 32;
+    for (int lr = warp; lr < KB; lr += NW) {
+        const int lrow = J * KB + lr; // partition-local row
+        if (lrow >= m) {
+            if (lane == 0) D[lr * LD + lr] = sc_one<T>();
+            continue;
+        }
+        const int g = s + lrow;
+        const int t0 = rowptr[g], t1 = rowptr[g + 1];
+        for (int t = t0 + lane; t < t1; t += 32) {
+            const int c = colind[t];
+            const T v = sc_cvt<T, H>(aij[t]);
+            const int lc = c - s;
+            if (lc < 0) {
+                const int cc = lc + KB;
+                if (cc >= 0 && lrow < KB) {
+                    if (Z) Z[lr * LD + cc] = v;
+                } else
+                    atomicOr(err, SPK_DEV_ERR_BAND);
+            } else if (lc >= m) {
+                const int br = lrow - (m - KB), bc = lc - m;
+                if (br >= 0 && bc < KB) {
+                    if (gBhat) gBhat[br * KB + bc] = v;
+                } else
+                    atomicOr(err, SPK_DEV_ERR_BAND);
+            } else {
+                const int bc = lc / KB, cc = lc - bc * KB;
+                const int d = bc - J;
+                if (d == 0)
+                    D[lr * LD + cc] = v;
+                else if (d == -1)
+                    F[lr * LD + cc] = v;
+                else if (d == 1)
+                    En[lr * LD + cc] = v;
+                else
+                    atomicOr(err, SPK_DEV_ERR_BAND);
+            }
+        }
+    }
+}
+
+template <class T, int KB> __device__ void zero_tile(T *s)
+{
+    constexpr int NT = NTOf<KB>::value;
+    for (int q = threadIdx.x; q < KB * (KB + 1); q += NT) s[q] = sc_zero<T>();
+}
+
+// shared tile -> dense global tile (row-major)
+template <class T, int KB> __device__ void store_tile(T *g, const T *s)
+{
+    constexpr int NT = NTOf<KB>::value;
+    for (int q = threadIdx.x; q < KB * KB; q += NT) {
+        const int r = q / KB, c = q - r * KB;
+        g[q] = s[r * (KB + 1) + c];
+    }
+}
+// dense global tile (row-major) -> shared tile
+template <class T, int KB> __device__ void load_tile(T *s, const T *g)
+{
+    constexpr int NT = NTOf<KB>::value;
+    for (int q = threadIdx.x; q < KB * KB; q += NT) {
+        const int r = q / KB, c = q - r * KB;
+        s[r * (KB + 1) + c] = g[q];
+    }
+}
+// shared tile -> global tile, column-major (for the retrieval's coalesced reads)
+template <class T, int KB> __device__ void store_tile_cm(T *g, const T *s)
+{
+    constexpr int NT = NTOf<KB>::value;
+    for (int q = threadIdx.x; q < KB * KB; q += NT) {
+        const int c = q / KB, r = q - c * KB;
+        g[q] = s[r * (KB + 1) + c];
+    }
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_factor_fwd(const int *__restrict__ rowptr, const int *__restrict__ colind,
+                 const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
+                 const int *__restrict__ blk_off, T *gL, T *gG, T *gE, T *gZ, T *gBhat, unsigned *err)
+{
+    using H = typename HighOf<T>::type;
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int part = blockIdx.x;
+    const int s = part_start[part], e = part_start[part + 1];
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const bool doW = part > 0;
+
+    extern __shared__ char smraw[];
+    T *base = (T *)smem_align(smraw);
+    T *sG = base, *sEp = sG + TL::ELEMS, *sEn = sEp + TL::ELEMS;
+    T *sF = sEn + TL::ELEMS, *sD = sF + TL::ELEMS, *sZ = sD + TL::ELEMS;
+    T *buf = sZ + TL::ELEMS;
+
+    TL t(threadIdx.x);
+    typename TL::Reg acc, accZ;
+    bool ok = true;
+
+    for (int J = 0; J < N; J++) {
+        zero_tile<T, KB>(sF);
+        zero_tile<T, KB>(sD);
+        zero_tile<T, KB>(sEn);
+        if (J == 0) zero_tile<T, KB>(sZ);
+        __syncthreads();
+        scatter_block<T, H, KB>(rowptr, colind, aij, s, e, J, sF, sD, sEn, (J == 0 && doW) ? sZ : nullptr,
+                                gBhat + (size_t)part * TS, err);
+        __syncthreads();
+        store_tile<T, KB>(gE + tb + J * TS, sEn);
+        if (J > 0) {
+            // L_J = F_{J-1} G_{J-1}
+            t.rzero(acc);
+            t.mma(acc, sF, sG);
+            __syncthreads();
+            t.rstore(sF, acc); // sF now holds L_J
+            t.gstore(gL + tb + J * TS, acc);
+            __syncthreads();
+            // S_J = D_J - L_J E_{J-1};  z_J = -L_J z_{J-1}
+            t.rload(acc, sD);
+            t.mms(acc, sF, sEp);
+            if (doW) {
+                t.rzero(accZ);
+                t.mms(accZ, sF, sZ);
+                __syncthreads();
+                t.rstore(sZ, accZ);
+                t.gstore(gZ + tb + J * TS, accZ);
+            }
+        } else {
+            t.rload(acc, sD);
+            if (doW) store_tile<T, KB>(gZ + tb, sZ);
+        }
+        // G_J = S_J^{-1}
+        ok = t.inverse(acc, buf) && ok;
+        t.rstore(sG, acc);
+        t.gstore(gG + tb + J * TS, acc);
+        T *tmp = sEp;
+        sEp = sEn;
+        sEn = tmp;
+        __syncthreads();
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+
+// Backward sweep for the spikes: X_J = G_J (Z_J - E_J X_{J+1}), X = [V | W].
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_factor_bwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                 const T *__restrict__ gL, const T *__restrict__ gG, const T *__restrict__ gE, T *gZ,
+                 const T *__restrict__ gBhat, T *gV, T *gW)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    constexpr int LD = KB + 1;
+    const int part = blockIdx.x;
+    const int s = part_start[part], e = part_start[part + 1], m = e - s;
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const bool doW = part > 0, doV = part < p - 1;
+
+    extern __shared__ char smraw[];
+    T *base = (T *)smem_align(smraw);
+    T *sG = base, *sE = sG + TL::ELEMS, *sZ = sE + TL::ELEMS, *sZV = sZ + TL::ELEMS;
+    T *sXV = sZV + TL::ELEMS, *sXW = sXV + TL::ELEMS;
+
+    TL t(threadIdx.x);
+    typename TL::Reg aV, aW;
+
+    // Forward sweep of V's right-hand side [0; B^]: nonzero only in the last
+    // KB real rows, i.e. blocks J0 and J0+1 (when m is not a multiple of KB).
+    const int J0 = (m - KB) / KB, o = (m - KB) - J0 * KB;
+    if (doV) {
+        // z_{J0}: rows o..KB-1 <- B^ rows 0..KB-1-o ; kept in gV tile J0 (row-major scratch)
+        zero_tile<T, KB>(sZV);
+        __syncthreads();
+        for (int q = threadIdx.x; q < KB * KB; q += NT) {
+            const int r = q / KB, c = q - r * KB;
+            if (r >= o) sZV[r * LD + c] = gBhat[(size_t)part * TS + (r - o) * KB + c];
+        }
+        __syncthreads();
+        store_tile<T, KB>(gV + tb + J0 * TS, sZV);
+        if (o > 0) {
+            // z_{J0+1} = [B^ rows KB-o..KB-1 ; 0] - L_{J0+1} z_{J0}
+            load_tile<T, KB>(sG, gL + tb + (J0 + 1) * TS);
+            zero_tile<T, KB>(sZ);
+            __syncthreads();
+            for (int q = threadIdx.x; q < o * KB; q += NT) {
+                const int r = q / KB, c = q - r * KB;
+                sZ[r * LD + c] = gBhat[(size_t)part * TS + (KB - o + r) * KB + c];
+            }
+            __syncthreads();
+            t.rload(aV, sZ);
+            t.mms(aV, sG, sZV);
+            __syncthreads();
+            t.rstore(sZ, aV);
+            __syncthreads();
+            store_tile<T, KB>(gV + tb + (J0 + 1) * TS, sZ);
+        }
+        __syncthreads();
+    }
+
+    for (int J = N - 1; J >= 0; J--) {
+        load_tile<T, KB>(sG, gG + tb + J * TS);
+        if (J < N - 1) load_tile<T, KB>(sE, gE + tb + J * TS);
+        if (doW) load_tile<T, KB>(sZ, gZ + tb + J * TS);
+        const bool hasZV = doV && (J == J0 || (o > 0 && J == J0 + 1));
+        if (hasZV) load_tile<T, KB>(sZV, gV + tb + J * TS);
+        __syncthreads();
+        // T = Z_J - E_J X_{J+1}
+        if (doV) {
+            if (hasZV)
+                t.rload(aV, sZV);
+            else
+                t.rzero(aV);
+            if (J < N - 1) t.mms(aV, sE, sXV);
+        }
+        if (doW) {
+            t.rload(aW, sZ);
+            if (J < N - 1) t.mms(aW, sE, sXW);
+        }
+        __syncthreads();
+        if (doV) t.rstore(sXV, aV);
+        if (doW) t.rstore(sXW, aW);
+        __syncthreads();
+        // X_J = G_J T
+        if (doV) {
+            t.rzero(aV);
+            t.mma(aV, sG, sXV);
+        }
+        if (doW) {
+            t.rzero(aW);
+            t.mma(aW, sG, sXW);
+        }
+        __syncthreads();
+        if (doV) t.rstore(sXV, aV);
+        if (doW) t.rstore(sXW, aW);
+        __syncthreads();
+        if (doV) store_tile_cm<T, KB>(gV + tb + J * TS, sXV);
+        if (doW) store_tile_cm<T, KB>(gW + tb + J * TS, sXW);
+        __syncthreads();
+    }
+}
+
+// Tips of V and W into the interface blocks of the reduced system (FP64):
+//   P_i = V_i bottom, Q_i = W_{i+1} top, X_i = W_i bottom, Y_i = V_{i+1} top.
+template <class T, int KB>
+__global__ void k_tips(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                       const T *__restrict__ gV, const T *__restrict__ gW, typename HighOf<T>::type *RP,
+                       typename HighOf<T>::type *RQ, typename HighOf<T>::type *RX,
+                       typename HighOf<T>::type *RY)
+{
+    using H = typename HighOf<T>::type;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int i = blockIdx.x; // interface i between partitions i and i+1
+    const int mi = part_start[i + 1] - part_start[i];
+    for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) {
+        const int r = q / KB, c = q - r * KB;
+        // bottom rows of partition i: local row mi - KB + r
+        const int lb = mi - KB + r, Jb = lb / KB, rb = lb - Jb * KB;
+        const size_t ib = ((size_t)blk_off[i] + Jb) * TS + (size_t)c * KB + rb;
+        // top rows of partition i+1: local row r (block 0)
+        const size_t it = (size_t)blk_off[i + 1] * TS + (size_t)c * KB + r;
+        RP[(size_t)i * TS + q] = sc_cvt<H, T>(gV[ib]);
+        RQ[(size_t)i * TS + q] = sc_cvt<H, T>(gW[it]);
+        RX[(size_t)i * TS + q] = i > 0 ? sc_cvt<H, T>(gW[ib]) : sc_zero<H>();
+        RY[(size_t)i * TS + q] = (i + 1 < p - 1) ? sc_cvt<H, T>(gV[it]) : sc_zero<H>();
+    }
+}
+
+template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const int *colind, const void *aij,
+                                          cudaStream_t st)
+{
+    using H = typename HighOf<T>::type;
+    constexpr int NT = NTOf<KB>::value;
+    using S = FactorSmem<T, KB>;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_factor_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::fwd) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_factor_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bwd) !=
+                cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
+    const size_t TS = (size_t)KB * KB;
+    if (cudaMemsetAsync(P->d_Bhat, 0, sizeof(T) * TS * P->p, st) != cudaSuccess) return SPK_ECUDA;
+    k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>(rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off,
+                                                  (T *)P->d_L, (T *)P->d_G, (T *)P->d_E, (T *)P->d_W,
+                                                  (T *)P->d_Bhat, P->d_err);
+    SPK_CHECK_LAUNCH();
+    P->launches++;
+    if (P->p > 1) {
+        k_factor_bwd<T, KB><<<P->p, NT, S::bwd, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L,
+                                                      (const T *)P->d_G, (const T *)P->d_E, (T *)P->d_W,
+                                                      (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
+        SPK_CHECK_LAUNCH();
+        k_tips<T, KB><<<P->n_iface, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_V,
+                                                  (const T *)P->d_W, (H *)P->d_RP, (H *)P->d_RQ, (H *)P->d_RX,
+                                                  (H *)P->d_RY);
+        SPK_CHECK_LAUNCH();
+        P->launches += 2;
+    }
+    return SPK_OK;
+}
+
+template <class T> int dispatch_factor(spk_plan *P, const int *rp, const int *ci, const void *a, cudaStream_t st)
+{
+    switch (P->KB) {
+    case 2: return run_factor<T, 2>(P, rp, ci, a, st);
+    case 4: return run_factor<T, 4>(P, rp, ci, a, st);
+    case 8: return run_factor<T, 8>(P, rp, ci, a, st);
+    case 16: return run_factor<T, 16>(P, rp, ci, a, st);
+    case 32: return run_factor<T, 32>(P, rp, ci, a, st);
+    case 64:
+        if constexpr (sizeof(T) <= 8) return run_factor<T, 64>(P, rp, ci, a, st);
+        else return SPK_EBAND;
+    default: return SPK_EBAND;
+    }
+}
+
+template <class T> size_t smem_for(int KB)
+{
+    switch (KB) {
+    case 2: return FactorSmem<T, 2>::fwd;
+    case 4: return FactorSmem<T, 4>::fwd;
+    case 8: return FactorSmem<T, 8>::fwd;
+    case 16: return FactorSmem<T, 16>::fwd;
+    case 32: return FactorSmem<T, 32>::fwd;
+    case 64:
+        if constexpr (sizeof(T) <= 8) return FactorSmem<T, 64>::fwd;
+        else return 0;
+    default: return 0;
+    }
+}
+
+} // namespace
+
+extern "C" size_t spk_factor_smem(int KB, int is_complex, int mode)
+{
+    if (is_complex) return mode == SPK_MIXED ? smem_for<cfloat>(KB) : smem_for<cdouble>(KB);
+    return mode == SPK_MIXED ? smem_for<float>(KB) : smem_for<double>(KB);
+}
+
+extern "C" int spk_factor(spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (P->is_complex)
+        return P->mode == SPK_MIXED ? dispatch_factor<cfloat>(P, d_rowptr, d_colind, d_aij, st)
+                                    : dispatch_factor<cdouble>(P, d_rowptr, d_colind, d_aij, st);
+    return P->mode == SPK_MIXED ? dispatch_factor<float>(P, d_rowptr, d_colind, d_aij, st)
+                                : dispatch_factor<double>(P, d_rowptr, d_colind, d_aij, st);
+}

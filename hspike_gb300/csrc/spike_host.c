@@ -1,0 +1,816 @@
+/*
+ * spike_host.c -- the C host layer of libspike_gb300.so.
+ *
+ * Implements the reference's C API (OpenMP/spike_interfaces.h:28-72) and the
+ * extensions of spike_gb300.h on top of the thin CUDA C ABI in
+ * spike_internal.h.  It owns everything the reference does on the host in
+ * dspike_core_host (OpenMP/spike_interfaces.c:43-419):
+ *
+ *   argument checks          (the reference only checks nnz < 0, :53-56)
+ *   bandwidth + schedule     (spike_solve_analysis, OpenMP/spike_analysis.c:3-83)
+ *   phase orchestration      factor -> reduced factor -> solve -> retrieve
+ *   iterative refinement     x += SPIKE(b - A x) until ||b - A x|| / ||b||
+ *                            reaches the tolerance (the reference only prints
+ *                            the residual: OpenMP/spike_interfaces.c:405)
+ *
+ * There is no CPU compute path: every numerical step is a kernel on the
+ * current CUDA device, and a missing or failing device is an error.
+ */
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "spike_gb300.h"
+#include "spike_internal.h"
+
+const Error_t SPIKE_SUCCESS = 0;
+const Error_t SPIKE_ERROR = 1;
+
+/* ------------------------------------------------------------------ */
+/* errors                                                               */
+/* ------------------------------------------------------------------ */
+static __thread int t_err_code = 0;
+static __thread char t_err_msg[512] = "";
+
+static Error_t fail(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_err_msg, sizeof t_err_msg, fmt, ap);
+    va_end(ap);
+    t_err_code = code;
+    return SPIKE_ERROR;
+}
+
+static Error_t fail_spk(int code, const char *where)
+{
+    switch (code) {
+    case SPK_ECUDA: return fail(SPIKE_ERR_CUDA, "%s: CUDA error: %s", where, spk_cuda_error_string());
+    case SPK_EMEM: return fail(SPIKE_ERR_MEMORY, "%s: device allocation failed (%s)", where, spk_cuda_error_string());
+    case SPK_EBAND: return fail(SPIKE_ERR_BANDWIDTH, "%s: bandwidth not supported in this precision", where);
+    case SPK_EPIVOT: return fail(SPIKE_ERR_PIVOT, "%s: zero or non-finite pivot", where);
+    default: return fail(code, "%s: error %d", where, code);
+    }
+}
+
+static Error_t succeed(void)
+{
+    t_err_code = SPIKE_ERR_NONE;
+    t_err_msg[0] = 0;
+    return SPIKE_SUCCESS;
+}
+
+int spike_last_error_code(void) { return t_err_code; }
+const char *spike_last_error(void) { return t_err_msg; }
+
+#define TRY(expr)                                                                                               \
+    do {                                                                                                        \
+        int rc_ = (expr);                                                                                       \
+        if (rc_ != SPK_OK) return rc_;                                                                          \
+    } while (0)
+
+/* ------------------------------------------------------------------ */
+/* contexts                                                             */
+/* ------------------------------------------------------------------ */
+#define RHS_CHUNK 64 /* right-hand sides per internal solve pass */
+
+struct spike_context_s {
+    int device;
+    void *own_stream, *stream;
+    /* options */
+    int mode, partitions, max_refine, red_refine;
+    double tol;
+    /* cached plan for the reference-API and device-pointer calls */
+    spk_plan *plan;
+    int *d_scratch; /* 4 ints for the analysis kernel */
+    /* staging buffers, grown on demand */
+    void *d_rowptr, *d_colind, *d_aij, *d_b, *d_x, *d_r, *d_stage;
+    size_t c_rowptr, c_colind, c_aij, c_b, c_x, c_r, c_stage;
+    spike_info_t info;
+};
+
+struct spike_factor_s {
+    spike_context_t ctx;
+    spk_plan *plan;
+    int is_complex;
+    int n;
+    long long nnz;
+    int owns;
+    const int *d_rowptr, *d_colind;
+    const void *d_aij;
+    void *o_rowptr, *o_colind, *o_aij; /* owned copies */
+    void *d_b, *d_x, *d_r;
+    size_t c_b, c_x, c_r;
+    int released;
+};
+
+static __thread spike_context_t t_default = NULL;
+
+static int ensure(void **p, size_t *cap, size_t need)
+{
+    if (need <= *cap && *p) return SPK_OK;
+    spk_free(*p);
+    *p = NULL;
+    *cap = 0;
+    TRY(spk_malloc(p, need));
+    *cap = need;
+    return SPK_OK;
+}
+
+static void plan_destroy(spk_plan *P);
+
+Error_t spike_context_create(spike_context_t *out)
+{
+    if (!out) return fail(SPIKE_ERR_ARGUMENT, "spike_context_create: NULL output");
+    *out = NULL;
+    if (spk_device_count() <= 0) return fail(SPIKE_ERR_NO_DEVICE, "no CUDA device is visible");
+    spike_context_t c = (spike_context_t)calloc(1, sizeof *c);
+    if (!c) return fail(SPIKE_ERR_MEMORY, "host allocation failed");
+    c->device = spk_current_device();
+    if (spk_stream_create(&c->own_stream) != SPK_OK) {
+        free(c);
+        return fail_spk(SPK_ECUDA, "spike_context_create");
+    }
+    c->stream = c->own_stream;
+    c->mode = SPK_MIXED;
+    c->partitions = 0;
+    c->max_refine = 3;
+    c->red_refine = 0;
+    c->tol = 1e-12;
+    if (spk_malloc((void **)&c->d_scratch, 4 * sizeof(int)) != SPK_OK) {
+        spk_stream_destroy(c->own_stream);
+        free(c);
+        return fail_spk(SPK_EMEM, "spike_context_create");
+    }
+    *out = c;
+    return succeed();
+}
+
+Error_t spike_context_destroy(spike_context_t c)
+{
+    if (!c) return fail(SPIKE_ERR_ARGUMENT, "spike_context_destroy: NULL context");
+    if (c->stream) spk_stream_sync(c->stream);
+    plan_destroy(c->plan);
+    spk_free(c->d_scratch);
+    spk_free(c->d_rowptr);
+    spk_free(c->d_colind);
+    spk_free(c->d_aij);
+    spk_free(c->d_b);
+    spk_free(c->d_x);
+    spk_free(c->d_r);
+    spk_free(c->d_stage);
+    spk_stream_destroy(c->own_stream);
+    if (t_default == c) t_default = NULL;
+    free(c);
+    return succeed();
+}
+
+static spike_context_t get_ctx(spike_context_t c)
+{
+    if (c) return c;
+    if (!t_default && spike_context_create(&t_default) != SPIKE_SUCCESS) return NULL;
+    return t_default;
+}
+
+Error_t spike_context_set_stream(spike_context_t c, void *s)
+{
+    c = get_ctx(c);
+    if (!c) return SPIKE_ERROR;
+    spk_stream_sync(c->stream);
+    c->stream = s ? s : c->own_stream;
+    return succeed();
+}
+
+Error_t spike_set_option(spike_context_t c, int opt, double v)
+{
+    c = get_ctx(c);
+    if (!c) return SPIKE_ERROR;
+    switch (opt) {
+    case SPIKE_OPT_PRECISION:
+        if (v != SPIKE_PRECISION_MIXED && v != SPIKE_PRECISION_FP64)
+            return fail(SPIKE_ERR_ARGUMENT, "precision must be SPIKE_PRECISION_MIXED or SPIKE_PRECISION_FP64");
+        c->mode = (v == SPIKE_PRECISION_FP64) ? SPK_PLAIN : SPK_MIXED;
+        break;
+    case SPIKE_OPT_PARTITIONS:
+        if (v < 0 || v > 1 << 24) return fail(SPIKE_ERR_ARGUMENT, "partitions must be in [0, 2^24]");
+        c->partitions = (int)v;
+        break;
+    case SPIKE_OPT_MAX_REFINE:
+        if (v < 0 || v > 100) return fail(SPIKE_ERR_ARGUMENT, "max refine sweeps must be in [0, 100]");
+        c->max_refine = (int)v;
+        break;
+    case SPIKE_OPT_TOLERANCE:
+        if (!(v >= 0)) return fail(SPIKE_ERR_ARGUMENT, "tolerance must be >= 0");
+        c->tol = v;
+        break;
+    case SPIKE_OPT_REDUCED_REFINE:
+        if (v < 0 || v > 20) return fail(SPIKE_ERR_ARGUMENT, "reduced refine sweeps must be in [0, 20]");
+        c->red_refine = (int)v;
+        break;
+    default: return fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
+    }
+    return succeed();
+}
+
+Error_t spike_get_option(spike_context_t c, int opt, double *v)
+{
+    c = get_ctx(c);
+    if (!c || !v) return c ? fail(SPIKE_ERR_ARGUMENT, "NULL output") : SPIKE_ERROR;
+    switch (opt) {
+    case SPIKE_OPT_PRECISION: *v = c->mode == SPK_PLAIN ? SPIKE_PRECISION_FP64 : SPIKE_PRECISION_MIXED; break;
+    case SPIKE_OPT_PARTITIONS: *v = c->partitions; break;
+    case SPIKE_OPT_MAX_REFINE: *v = c->max_refine; break;
+    case SPIKE_OPT_TOLERANCE: *v = c->tol; break;
+    case SPIKE_OPT_REDUCED_REFINE: *v = c->red_refine; break;
+    default: return fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
+    }
+    return succeed();
+}
+
+Error_t spike_get_info(spike_context_t c, spike_info_t *info)
+{
+    c = get_ctx(c);
+    if (!c || !info) return c ? fail(SPIKE_ERR_ARGUMENT, "NULL output") : SPIKE_ERROR;
+    *info = c->info;
+    return succeed();
+}
+
+/* ------------------------------------------------------------------ */
+/* plan: schedule + device workspace                                    */
+/* ------------------------------------------------------------------ */
+static int choose_block(int k)
+{
+    const int sizes[] = {2, 4, 8, 16, 32, 64};
+    for (int i = 0; i < 6; i++)
+        if (k <= sizes[i]) return sizes[i];
+    return 0;
+}
+
+/* Partition count.  The reference fixes p = 4 (OpenMP/spike_analysis.c:168)
+ * and bounds it by p_max = n / (2 (ku + kl)) (:153).  Here every partition
+ * must hold at least two tiles (2 KB rows) so that its top and bottom tips
+ * are distinct; a requested p is clamped to that, an automatic p fills the
+ * GPU: two CTAs per SM for the large tiles, more for the small ones. */
+static int choose_partitions(int n, int KB, int requested)
+{
+    long long pmax = n / (2LL * KB);
+    if (pmax < 1) pmax = 1;
+    long long p = requested;
+    if (p <= 0) {
+        int sms = spk_sm_count();
+        if (sms <= 0) sms = 152;
+        const int per_sm = KB >= 32 ? 2 : KB == 16 ? 8 : 16;
+        p = (long long)sms * per_sm;
+    }
+    if (p > pmax) p = pmax;
+    if (p < 1) p = 1;
+    return (int)p;
+}
+
+static void plan_destroy(spk_plan *P)
+{
+    if (!P) return;
+    void *ptrs[] = {P->d_part_start, P->d_blk_off, P->d_blk_part, P->d_L, P->d_G, P->d_E, P->d_V, P->d_W,
+                    P->d_Bhat, P->d_RP, P->d_RQ, P->d_RX, P->d_RY, P->d_crP, P->d_crQ, P->d_crX, P->d_crY,
+                    P->d_crM, P->d_crg, P->d_z, P->d_y, P->d_g, P->d_u, P->d_rr, P->d_du, P->d_err, P->d_norms};
+    for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) spk_free(ptrs[i]);
+    free(P->part_start);
+    free(P->blk_off);
+    free(P->cr_count);
+    free(P->cr_off);
+    free(P->cr_moff);
+    free(P);
+}
+
+static int palloc(spk_plan *P, void **p, size_t bytes)
+{
+    TRY(spk_malloc(p, bytes));
+    P->bytes += bytes;
+    return SPK_OK;
+}
+
+static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int mode, int partitions,
+                       int nrhs_max, void *stream, spk_plan **out)
+{
+    *out = NULL;
+    const int k = ku > kl ? ku : kl;
+    const int KB = choose_block(k < 1 ? 1 : k);
+    if (!KB || spk_factor_smem(KB, is_complex, mode) == 0) return SPK_EBAND;
+    spk_plan *P = (spk_plan *)calloc(1, sizeof *P);
+    if (!P) return SPK_EMEM;
+    P->n = n;
+    P->nnz = nnz;
+    P->ku = ku;
+    P->kl = kl;
+    P->KB = KB;
+    P->is_complex = is_complex;
+    P->mode = mode;
+    P->nrhs_max = nrhs_max;
+    const int p = choose_partitions(n, KB, partitions);
+    P->p = p;
+    P->n_iface = p - 1;
+    P->part_start = (int *)malloc(sizeof(int) * (p + 1));
+    P->blk_off = (int *)malloc(sizeof(int) * (p + 1));
+    if (!P->part_start || !P->blk_off) {
+        plan_destroy(P);
+        return SPK_EMEM;
+    }
+    /* spike_solve_analysis: regular partitions, remainder in the last one */
+    const int nreg = n / p;
+    for (int i = 0; i < p; i++) P->part_start[i] = i * nreg;
+    P->part_start[p] = n;
+    P->blk_off[0] = 0;
+    for (int i = 0; i < p; i++) {
+        const int m = P->part_start[i + 1] - P->part_start[i];
+        P->blk_off[i + 1] = P->blk_off[i] + (m + KB - 1) / KB;
+    }
+    P->total_blocks = P->blk_off[p];
+    P->NP = (long long)P->total_blocks * KB;
+
+    /* cyclic-reduction levels of the reduced system */
+    int levels = 0;
+    for (int c = P->n_iface; c > 1; c = (c + 1) / 2) levels++;
+    P->cr_levels = levels;
+    P->cr_count = (int *)malloc(sizeof(int) * (levels + 1));
+    P->cr_off = (long long *)malloc(sizeof(long long) * (levels + 2));
+    P->cr_moff = (long long *)malloc(sizeof(long long) * (levels + 2));
+    if (!P->cr_count || !P->cr_off || !P->cr_moff) {
+        plan_destroy(P);
+        return SPK_EMEM;
+    }
+    long long tiles = 0, mtiles = 0;
+    int c = P->n_iface > 0 ? P->n_iface : 1;
+    for (int l = 0; l <= levels; l++) {
+        P->cr_count[l] = c;
+        P->cr_off[l] = tiles;
+        P->cr_moff[l] = mtiles;
+        tiles += c;
+        mtiles += (l < levels) ? c / 2 : 1;
+        c = (c + 1) / 2;
+    }
+    P->cr_off[levels + 1] = tiles;
+    P->cr_moff[levels + 1] = mtiles;
+    P->crg_stride = tiles * 2 * KB;
+
+    const size_t fs = (is_complex ? 2 : 1) * (mode == SPK_MIXED ? 4 : 8); /* factor scalar bytes */
+    const size_t hs = (is_complex ? 2 : 1) * 8;                           /* FP64 scalar bytes */
+    const size_t TS = (size_t)KB * KB;
+    const size_t nif = P->n_iface > 0 ? (size_t)P->n_iface : 1;
+    int rc = SPK_OK;
+#define PA(ptr, bytes)                                                                                          \
+    if (rc == SPK_OK) rc = palloc(P, (void **)&(ptr), (bytes))
+    PA(P->d_part_start, sizeof(int) * (p + 1));
+    PA(P->d_blk_off, sizeof(int) * (p + 1));
+    PA(P->d_blk_part, sizeof(int) * P->total_blocks);
+    PA(P->d_L, fs * TS * P->total_blocks);
+    PA(P->d_G, fs * TS * P->total_blocks);
+    PA(P->d_E, fs * TS * P->total_blocks);
+    PA(P->d_W, fs * TS * P->total_blocks);
+    PA(P->d_V, fs * TS * P->total_blocks);
+    PA(P->d_Bhat, fs * TS * p);
+    PA(P->d_RP, hs * TS * nif);
+    PA(P->d_RQ, hs * TS * nif);
+    PA(P->d_RX, hs * TS * nif);
+    PA(P->d_RY, hs * TS * nif);
+    PA(P->d_crP, fs * TS * tiles);
+    PA(P->d_crQ, fs * TS * tiles);
+    PA(P->d_crX, fs * TS * tiles);
+    PA(P->d_crY, fs * TS * tiles);
+    PA(P->d_crM, fs * TS * 4 * (mtiles > 0 ? mtiles : 1));
+    PA(P->d_crg, fs * 2 * (size_t)P->crg_stride * nrhs_max);
+    PA(P->d_z, fs * (size_t)P->NP * nrhs_max);
+    PA(P->d_y, fs * (size_t)P->NP * nrhs_max);
+    PA(P->d_g, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_u, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_rr, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_du, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_err, sizeof(unsigned) * 4);
+    PA(P->d_norms, sizeof(double) * 2 * nrhs_max);
+#undef PA
+    if (rc == SPK_OK) {
+        int *bp = (int *)malloc(sizeof(int) * P->total_blocks);
+        if (!bp) rc = SPK_EMEM;
+        for (int i = 0; bp && i < p; i++)
+            for (int b = P->blk_off[i]; b < P->blk_off[i + 1]; b++) bp[b] = i;
+        if (rc == SPK_OK) rc = spk_memcpy_h2d(P->d_part_start, P->part_start, sizeof(int) * (p + 1), stream);
+        if (rc == SPK_OK) rc = spk_memcpy_h2d(P->d_blk_off, P->blk_off, sizeof(int) * (p + 1), stream);
+        if (rc == SPK_OK) rc = spk_memcpy_h2d(P->d_blk_part, bp, sizeof(int) * P->total_blocks, stream);
+        if (rc == SPK_OK) rc = spk_stream_sync(stream);
+        free(bp);
+    }
+    if (rc != SPK_OK) {
+        plan_destroy(P);
+        return rc;
+    }
+    *out = P;
+    return SPK_OK;
+}
+
+static int plan_matches(const spk_plan *P, int n, int ku, int kl, int is_complex, int mode, int partitions, int nrhs)
+{
+    if (!P) return 0;
+    const int k = ku > kl ? ku : kl;
+    const int KB = choose_block(k < 1 ? 1 : k);
+    return P->n == n && P->KB == KB && P->is_complex == is_complex && P->mode == mode &&
+           P->p == choose_partitions(n, KB, partitions) && nrhs <= P->nrhs_max;
+}
+
+/* ------------------------------------------------------------------ */
+/* phases                                                              */
+/* ------------------------------------------------------------------ */
+static int check_device_error(spk_plan *P, void *stream)
+{
+    unsigned e[4] = {0, 0, 0, 0};
+    TRY(spk_memcpy_d2h(e, P->d_err, sizeof e, stream));
+    TRY(spk_stream_sync(stream));
+    if (e[0] & SPK_DEV_ERR_PIVOT) return SPK_EPIVOT;
+    if (e[0] & (SPK_DEV_ERR_BAND | SPK_DEV_ERR_CSR)) return SPK_ECSR;
+    return SPK_OK;
+}
+
+static int factor_phase(spk_plan *P, const int *rp, const int *ci, const void *aij, void *stream)
+{
+    TRY(spk_memset(P->d_err, 0, sizeof(unsigned) * 4, stream));
+    TRY(spk_factor(P, rp, ci, aij, stream));
+    TRY(spk_reduced_factor(P, stream));
+    return check_device_error(P, stream);
+}
+
+typedef struct {
+    int max_refine, red_refine;
+    double tol;
+    double relres_max;
+    int sweeps;
+} refine_opts;
+
+/* x = A^{-1} b for nrhs <= P->nrhs_max columns, refined in FP64. */
+static int solve_phase(spk_plan *P, const int *rp, const int *ci, const void *aij, void *x, const void *b, void *r,
+                       int nrhs, refine_opts *o, void *stream)
+{
+    const int red = o->red_refine > 0 ? o->red_refine : (P->mode == SPK_MIXED ? 2 : 1);
+    double norms[2 * RHS_CHUNK];
+    double bnorm[RHS_CHUNK];
+    TRY(spk_apply(P, b, nrhs, stream));
+    TRY(spk_reduced_solve(P, nrhs, red, stream));
+    TRY(spk_retrieve(P, x, nrhs, 0, stream));
+    for (int sweep = 0;; sweep++) {
+        TRY(spk_residual(P, rp, ci, aij, x, b, r, nrhs, sweep == 0, P->d_norms, stream));
+        TRY(spk_memcpy_d2h(norms, P->d_norms, sizeof(double) * 2 * nrhs, stream));
+        TRY(spk_stream_sync(stream));
+        double worst = 0.0;
+        for (int h = 0; h < nrhs; h++) {
+            if (sweep == 0) bnorm[h] = sqrt(norms[nrhs + h]);
+            const double rel = sqrt(norms[h]) / (bnorm[h] > 0 ? bnorm[h] : 1.0);
+            if (!(rel <= worst)) worst = rel; /* NaN propagates */
+        }
+        o->relres_max = worst;
+        o->sweeps = sweep;
+        if (worst <= o->tol) return SPK_OK;
+        if (sweep >= o->max_refine) return SPK_ECONV;
+        TRY(spk_apply(P, r, nrhs, stream));
+        TRY(spk_reduced_solve(P, nrhs, red, stream));
+        TRY(spk_retrieve(P, x, nrhs, 1, stream));
+    }
+}
+
+/* solve all columns in chunks of P->nrhs_max */
+static int solve_all(spk_plan *P, const int *rp, const int *ci, const void *aij, void *x, const void *b, void *r,
+                     int nrhs, refine_opts *o, void *stream)
+{
+    const size_t hs = (P->is_complex ? 2 : 1) * 8;
+    double worst = 0.0;
+    int sweeps = 0, rc = SPK_OK;
+    for (int h0 = 0; h0 < nrhs; h0 += P->nrhs_max) {
+        const int nr = nrhs - h0 < P->nrhs_max ? nrhs - h0 : P->nrhs_max;
+        refine_opts oc = *o;
+        const size_t off = (size_t)h0 * P->n * hs;
+        rc = solve_phase(P, rp, ci, aij, (char *)x + off, (const char *)b + off, r, nr, &oc, stream);
+        if (!(oc.relres_max <= worst)) worst = oc.relres_max;
+        if (oc.sweeps > sweeps) sweeps = oc.sweeps;
+        if (rc != SPK_OK && rc != SPK_ECONV) return rc;
+        if (rc == SPK_ECONV) break;
+    }
+    o->relres_max = worst;
+    o->sweeps = sweeps;
+    return rc;
+}
+
+static void fill_info(spike_context_t c, const spk_plan *P, const refine_opts *o, long long launches)
+{
+    c->info.relres_max = o->relres_max;
+    c->info.refine_sweeps = o->sweeps;
+    c->info.partitions = P->p;
+    c->info.ku = P->ku;
+    c->info.kl = P->kl;
+    c->info.block = P->KB;
+    c->info.kernel_launches = launches;
+    c->info.device_bytes = P->bytes;
+}
+
+static Error_t finish(int rc, const char *where, const refine_opts *o)
+{
+    if (rc == SPK_OK) return succeed();
+    if (rc == SPK_ECONV)
+        return fail(SPIKE_ERR_CONVERGENCE, "%s: relative residual %.3e above tolerance %.3e after %d sweeps", where,
+                    o->relres_max, o->tol, o->sweeps);
+    if (rc == SPK_ECSR) return fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", where);
+    return fail_spk(rc, where);
+}
+
+/* analysis + plan + factor + solve on device-resident FP64 data */
+static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const int *rp, const int *ci,
+                      const void *aij, void *x, const void *b, int is_complex, refine_opts *o, long long *launches)
+{
+    int info[3];
+    long long l0 = 0;
+    TRY(spk_analyze(n, nnz, rp, ci, c->d_scratch, info, c->stream, &l0));
+    if (info[2]) return SPK_ECSR;
+    const int chunk = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
+    if (!plan_matches(c->plan, n, info[0], info[1], is_complex, c->mode, c->partitions, chunk)) {
+        plan_destroy(c->plan);
+        c->plan = NULL;
+        TRY(plan_create(n, nnz, info[0], info[1], is_complex, c->mode, c->partitions, chunk, c->stream, &c->plan));
+    }
+    spk_plan *P = c->plan;
+    P->nnz = nnz;
+    P->ku = info[0];
+    P->kl = info[1];
+    P->launches = l0;
+    const size_t hs = (is_complex ? 2 : 1) * 8;
+    TRY(ensure(&c->d_r, &c->c_r, hs * (size_t)n * chunk));
+    int rc = factor_phase(P, rp, ci, aij, c->stream);
+    if (rc == SPK_OK) rc = solve_all(P, rp, ci, aij, x, b, c->d_r, nrhs, o, c->stream);
+    *launches = P->launches;
+    fill_info(c, P, o, P->launches);
+    return rc;
+}
+
+static void opts_from(const spike_context_t c, refine_opts *o)
+{
+    o->max_refine = c->max_refine;
+    o->red_refine = c->red_refine;
+    o->tol = c->tol;
+    o->relres_max = 0;
+    o->sweeps = 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* reference API: host arrays                                           */
+/* ------------------------------------------------------------------ */
+static Error_t host_solve(int dtype, const char *name, integer_t n, integer_t nnz, integer_t nrhs,
+                          const integer_t *colind, const integer_t *rowptr, const void *aij, void *x, const void *b)
+{
+    if (n < 0 || nnz < 0 || nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
+    if (n == 0 || nrhs == 0) return succeed();
+    if (!colind || !rowptr || !aij || !x || !b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    spike_context_t c = get_ctx(NULL);
+    if (!c) return SPIKE_ERROR;
+    const int cplx = dtype == SPK_C || dtype == SPK_Z;
+    const int wide = dtype == SPK_S || dtype == SPK_C;
+    const size_t es = (cplx ? 2 : 1) * (wide ? 4 : 8); /* caller element bytes */
+    const size_t hs = (cplx ? 2 : 1) * 8;
+    const size_t nb = (size_t)n * nrhs;
+    refine_opts o;
+    opts_from(c, &o);
+    int rc = SPK_OK;
+    rc = ensure(&c->d_rowptr, &c->c_rowptr, sizeof(int) * ((size_t)n + 1));
+    if (rc == SPK_OK) rc = ensure(&c->d_colind, &c->c_colind, sizeof(int) * (size_t)(nnz ? nnz : 1));
+    if (rc == SPK_OK) rc = ensure(&c->d_aij, &c->c_aij, hs * (size_t)(nnz ? nnz : 1));
+    if (rc == SPK_OK) rc = ensure(&c->d_b, &c->c_b, hs * nb);
+    if (rc == SPK_OK) rc = ensure(&c->d_x, &c->c_x, hs * nb);
+    if (rc == SPK_OK && wide) {
+        const size_t m = (size_t)nnz > nb ? (size_t)nnz : nb;
+        rc = ensure(&c->d_stage, &c->c_stage, es * (m ? m : 1));
+    }
+    if (rc != SPK_OK) return finish(rc, name, &o);
+    long long launches = 0;
+    rc = spk_memcpy_h2d(c->d_rowptr, rowptr, sizeof(int) * ((size_t)n + 1), c->stream);
+    if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(c->d_colind, colind, sizeof(int) * (size_t)nnz, c->stream);
+    if (wide) {
+        if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(c->d_stage, aij, es * (size_t)nnz, c->stream);
+        if (rc == SPK_OK) rc = spk_widen(c->d_stage, c->d_aij, nnz, cplx, c->stream, &launches);
+        if (rc == SPK_OK) rc = spk_memcpy_h2d(c->d_stage, b, es * nb, c->stream);
+        if (rc == SPK_OK) rc = spk_widen(c->d_stage, c->d_b, (long long)nb, cplx, c->stream, &launches);
+    } else {
+        if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(c->d_aij, aij, es * (size_t)nnz, c->stream);
+        if (rc == SPK_OK) rc = spk_memcpy_h2d(c->d_b, b, es * nb, c->stream);
+    }
+    long long l2 = 0;
+    if (rc == SPK_OK)
+        rc = run_device(c, n, nnz, nrhs, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, c->d_x, c->d_b,
+                        cplx, &o, &l2);
+    launches += l2;
+    /* x is written back after a convergence shortfall too (it is the last iterate) */
+    if (rc == SPK_OK || rc == SPK_ECONV) {
+        int rc2 = SPK_OK;
+        if (wide) {
+            rc2 = spk_narrow(c->d_x, c->d_stage, (long long)nb, cplx, c->stream, &launches);
+            if (rc2 == SPK_OK) rc2 = spk_memcpy_d2h(x, c->d_stage, es * nb, c->stream);
+        } else {
+            rc2 = spk_memcpy_d2h(x, c->d_x, es * nb, c->stream);
+        }
+        if (rc2 == SPK_OK) rc2 = spk_stream_sync(c->stream);
+        if (rc2 != SPK_OK) rc = rc2;
+    } else {
+        spk_stream_sync(c->stream);
+    }
+    c->info.kernel_launches = launches;
+    return finish(rc, name, &o);
+}
+
+Error_t sspike_core_host(const integer_t n, const integer_t nnz, const integer_t nrhs, integer_t *colind,
+                         integer_t *rowptr, float *aij, float *xij, float *bij)
+{
+    return host_solve(SPK_S, "sspike_core_host", n, nnz, nrhs, colind, rowptr, aij, xij, bij);
+}
+Error_t dspike_core_host(const integer_t n, const integer_t nnz, const integer_t nrhs, integer_t *colind,
+                         integer_t *rowptr, double *aij, double *xij, double *bij)
+{
+    return host_solve(SPK_D, "dspike_core_host", n, nnz, nrhs, colind, rowptr, aij, xij, bij);
+}
+Error_t cspike_core_host(const integer_t n, const integer_t nnz, const integer_t nrhs, integer_t *colind,
+                         integer_t *rowptr, complex8 *aij, complex8 *xij, complex8 *bij)
+{
+    return host_solve(SPK_C, "cspike_core_host", n, nnz, nrhs, colind, rowptr, aij, xij, bij);
+}
+Error_t zspike_core_host(const integer_t n, const integer_t nnz, const integer_t nrhs, integer_t *colind,
+                         integer_t *rowptr, complex16 *aij, complex16 *xij, complex16 *bij)
+{
+    return host_solve(SPK_Z, "zspike_core_host", n, nnz, nrhs, colind, rowptr, aij, xij, bij);
+}
+Error_t dspike_core_host_blocking(const integer_t n, const integer_t nnz, const integer_t nrhs, integer_t *colind,
+                                  integer_t *rowptr, double *aij, double *xij, double *bij)
+{
+    return host_solve(SPK_D, "dspike_core_host_blocking", n, nnz, nrhs, colind, rowptr, aij, xij, bij);
+}
+
+/* ------------------------------------------------------------------ */
+/* device-pointer API                                                   */
+/* ------------------------------------------------------------------ */
+static Error_t device_solve(spike_context_t c, int cplx, const char *name, integer_t n, integer_t nnz, integer_t nrhs,
+                            const integer_t *ci, const integer_t *rp, const void *aij, void *x, const void *b)
+{
+    if (n < 0 || nnz < 0 || nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
+    if (n == 0 || nrhs == 0) return succeed();
+    if (!ci || !rp || !aij || !x || !b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    c = get_ctx(c);
+    if (!c) return SPIKE_ERROR;
+    refine_opts o;
+    opts_from(c, &o);
+    long long launches = 0;
+    int rc = run_device(c, n, nnz, nrhs, rp, ci, aij, x, b, cplx, &o, &launches);
+    if (rc != SPK_OK) spk_stream_sync(c->stream);
+    return finish(rc, name, &o);
+}
+
+Error_t spike_dsolve_device(spike_context_t c, integer_t n, integer_t nnz, integer_t nrhs, const integer_t *d_colind,
+                            const integer_t *d_rowptr, const double *d_aij, double *d_x, const double *d_b)
+{
+    return device_solve(c, 0, "spike_dsolve_device", n, nnz, nrhs, d_colind, d_rowptr, d_aij, d_x, d_b);
+}
+Error_t spike_zsolve_device(spike_context_t c, integer_t n, integer_t nnz, integer_t nrhs, const integer_t *d_colind,
+                            const integer_t *d_rowptr, const complex16 *d_aij, complex16 *d_x, const complex16 *d_b)
+{
+    return device_solve(c, 1, "spike_zsolve_device", n, nnz, nrhs, d_colind, d_rowptr, d_aij, d_x, d_b);
+}
+
+/* ------------------------------------------------------------------ */
+/* factor handles                                                       */
+/* ------------------------------------------------------------------ */
+static Error_t factor_common(spike_context_t c, int cplx, const char *name, integer_t n, integer_t nnz,
+                             const integer_t *ci, const integer_t *rp, const void *aij, int host, spike_factor_t *out)
+{
+    if (!out) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL output", name);
+    *out = NULL;
+    if (n <= 0 || nnz < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n must be > 0 and nnz >= 0", name);
+    if (!ci || !rp || !aij) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    c = get_ctx(c);
+    if (!c) return SPIKE_ERROR;
+    spike_factor_t f = (spike_factor_t)calloc(1, sizeof *f);
+    if (!f) return fail(SPIKE_ERR_MEMORY, "%s: host allocation failed", name);
+    f->ctx = c;
+    f->is_complex = cplx;
+    f->n = n;
+    f->nnz = nnz;
+    const size_t hs = (cplx ? 2 : 1) * 8;
+    int rc = SPK_OK;
+    refine_opts o;
+    opts_from(c, &o);
+    if (host) {
+        f->owns = 1;
+        rc = spk_malloc(&f->o_rowptr, sizeof(int) * ((size_t)n + 1));
+        if (rc == SPK_OK) rc = spk_malloc(&f->o_colind, sizeof(int) * (size_t)(nnz ? nnz : 1));
+        if (rc == SPK_OK) rc = spk_malloc(&f->o_aij, hs * (size_t)(nnz ? nnz : 1));
+        if (rc == SPK_OK) rc = spk_memcpy_h2d(f->o_rowptr, rp, sizeof(int) * ((size_t)n + 1), c->stream);
+        if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(f->o_colind, ci, sizeof(int) * (size_t)nnz, c->stream);
+        if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(f->o_aij, aij, hs * (size_t)nnz, c->stream);
+        f->d_rowptr = (const int *)f->o_rowptr;
+        f->d_colind = (const int *)f->o_colind;
+        f->d_aij = f->o_aij;
+    } else {
+        f->d_rowptr = rp;
+        f->d_colind = ci;
+        f->d_aij = aij;
+    }
+    int info[3];
+    long long l0 = 0;
+    if (rc == SPK_OK) rc = spk_analyze(n, nnz, f->d_rowptr, f->d_colind, c->d_scratch, info, c->stream, &l0);
+    if (rc == SPK_OK && info[2]) rc = SPK_ECSR;
+    if (rc == SPK_OK)
+        rc = plan_create(n, nnz, info[0], info[1], cplx, c->mode, c->partitions, RHS_CHUNK, c->stream, &f->plan);
+    if (rc == SPK_OK) {
+        f->plan->launches = l0;
+        rc = factor_phase(f->plan, f->d_rowptr, f->d_colind, f->d_aij, c->stream);
+    }
+    if (rc != SPK_OK) {
+        spk_stream_sync(c->stream);
+        spike_factor_release(f);
+        return finish(rc, name, &o);
+    }
+    *out = f;
+    return succeed();
+}
+
+Error_t spike_dfactor(spike_context_t c, integer_t n, integer_t nnz, const integer_t *colind, const integer_t *rowptr,
+                      const double *aij, spike_factor_t *f)
+{
+    return factor_common(c, 0, "spike_dfactor", n, nnz, colind, rowptr, aij, 1, f);
+}
+Error_t spike_zfactor(spike_context_t c, integer_t n, integer_t nnz, const integer_t *colind, const integer_t *rowptr,
+                      const complex16 *aij, spike_factor_t *f)
+{
+    return factor_common(c, 1, "spike_zfactor", n, nnz, colind, rowptr, aij, 1, f);
+}
+Error_t spike_dfactor_device(spike_context_t c, integer_t n, integer_t nnz, const integer_t *d_colind,
+                             const integer_t *d_rowptr, const double *d_aij, spike_factor_t *f)
+{
+    return factor_common(c, 0, "spike_dfactor_device", n, nnz, d_colind, d_rowptr, d_aij, 0, f);
+}
+
+static Error_t solve_factored(spike_factor_t f, int cplx, const char *name, integer_t nrhs, void *x, const void *b,
+                              int host)
+{
+    if (!f || f->released) return fail(SPIKE_ERR_HANDLE, "%s: invalid factor handle", name);
+    if (f->is_complex != cplx) return fail(SPIKE_ERR_ARGUMENT, "%s: handle holds another value type", name);
+    if (nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: nrhs must be >= 0", name);
+    if (nrhs == 0) return succeed();
+    if (!x || !b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    spike_context_t c = f->ctx;
+    spk_plan *P = f->plan;
+    const size_t hs = (cplx ? 2 : 1) * 8;
+    const size_t nb = (size_t)f->n * nrhs;
+    refine_opts o;
+    opts_from(c, &o);
+    P->launches = 0;
+    int rc = ensure(&f->d_r, &f->c_r, hs * (size_t)f->n * P->nrhs_max);
+    void *dx = x;
+    const void *db = b;
+    if (host) {
+        if (rc == SPK_OK) rc = ensure(&f->d_b, &f->c_b, hs * nb);
+        if (rc == SPK_OK) rc = ensure(&f->d_x, &f->c_x, hs * nb);
+        if (rc == SPK_OK) rc = spk_memcpy_h2d(f->d_b, b, hs * nb, c->stream);
+        dx = f->d_x;
+        db = f->d_b;
+    }
+    if (rc == SPK_OK) rc = solve_all(P, f->d_rowptr, f->d_colind, f->d_aij, dx, db, f->d_r, nrhs, &o, c->stream);
+    if (host && (rc == SPK_OK || rc == SPK_ECONV)) {
+        int rc2 = spk_memcpy_d2h(x, f->d_x, hs * nb, c->stream);
+        if (rc2 == SPK_OK) rc2 = spk_stream_sync(c->stream);
+        if (rc2 != SPK_OK) rc = rc2;
+    } else {
+        spk_stream_sync(c->stream);
+    }
+    fill_info(c, P, &o, P->launches);
+    return finish(rc, name, &o);
+}
+
+Error_t spike_dsolve_factored(spike_factor_t f, integer_t nrhs, double *x, const double *b)
+{
+    return solve_factored(f, 0, "spike_dsolve_factored", nrhs, x, b, 1);
+}
+Error_t spike_zsolve_factored(spike_factor_t f, integer_t nrhs, complex16 *x, const complex16 *b)
+{
+    return solve_factored(f, 1, "spike_zsolve_factored", nrhs, x, b, 1);
+}
+Error_t spike_dsolve_factored_device(spike_factor_t f, integer_t nrhs, double *d_x, const double *d_b)
+{
+    return solve_factored(f, 0, "spike_dsolve_factored_device", nrhs, d_x, d_b, 0);
+}
+
+Error_t spike_factor_release(spike_factor_t f)
+{
+    if (!f || f->released) return fail(SPIKE_ERR_HANDLE, "spike_factor_release: invalid factor handle");
+    if (f->ctx && f->ctx->stream) spk_stream_sync(f->ctx->stream);
+    plan_destroy(f->plan);
+    spk_free(f->o_rowptr);
+    spk_free(f->o_colind);
+    spk_free(f->o_aij);
+    spk_free(f->d_b);
+    spk_free(f->d_x);
+    spk_free(f->d_r);
+    f->released = 1;
+    free(f);
+    return succeed();
+}

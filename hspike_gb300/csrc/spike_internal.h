@@ -1,0 +1,145 @@
+/*
+ * spike_internal.h -- the thin C ABI between the C host layer (spike_host.c)
+ * and the CUDA layer (spike_*.cu).  Plain C types only.
+ *
+ * Vocabulary (the reference's, OpenMP/spike_analysis.h:38-53 and
+ * OpenMP/spike_interfaces.c):
+ *   partition i   rows [part_start[i], part_start[i+1]) of A, m_i rows
+ *   block         KB consecutive rows of a partition; KB >= max(ku, kl) is the
+ *                 tile size, so A_i is block tridiagonal with KB x KB blocks
+ *                 D_J (diagonal), E_J = A(J, J+1), F_J = A(J+1, J)
+ *   padded rows   a partition is padded with identity rows up to N_i * KB
+ *   spikes        V_i = A_i^{-1} B_i, W_i = A_i^{-1} C_i
+ *   tips          top = first KB rows, bottom = last KB real rows
+ *   interface i   unknowns (b_i, t_{i+1}): bottom tip of partition i and top
+ *                 tip of partition i+1; the reduced system has p-1 interfaces
+ */
+#ifndef SPIKE_GB300_INTERNAL_H
+#define SPIKE_GB300_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* value type of the caller's arrays */
+enum spk_dtype { SPK_S = 0, SPK_D = 1, SPK_C = 2, SPK_Z = 3 };
+/* factor precision: FP32/complex64 factors with FP64 refinement, or FP64 */
+enum spk_mode { SPK_MIXED = 0, SPK_PLAIN = 1 };
+
+/* error detail codes (spike_last_error_code) */
+enum spk_err {
+    SPK_OK = 0,
+    SPK_EARG = 1,       /* bad argument */
+    SPK_ECSR = 2,       /* invalid CSR: out-of-range or unsorted/duplicate column */
+    SPK_EBAND = 3,      /* bandwidth above what the kernels support */
+    SPK_ECUDA = 4,      /* a CUDA runtime call failed */
+    SPK_EMEM = 5,       /* device or host allocation failed */
+    SPK_EPIVOT = 6,     /* zero or non-finite pivot in a diagonal block */
+    SPK_ECONV = 7,      /* refinement did not reach the tolerance */
+    SPK_ENODEV = 8,     /* no CUDA device */
+    SPK_EHANDLE = 9     /* bad or released handle */
+};
+
+/* device error word bits, written by kernels with atomicOr */
+#define SPK_DEV_ERR_PIVOT 1u
+#define SPK_DEV_ERR_BAND 2u
+#define SPK_DEV_ERR_CSR 4u
+
+typedef struct spk_plan {
+    /* problem */
+    int n, nrhs_max, ku, kl, KB, p;
+    int is_complex, mode;
+    long long nnz;
+    /* schedule (host copies) */
+    int *part_start; /* p+1 */
+    int *blk_off;    /* p+1, prefix sum of blocks per partition */
+    int total_blocks;
+    long long NP; /* padded rows = total_blocks * KB */
+    int n_iface;  /* p - 1 */
+    /* device copies of the schedule */
+    int *d_part_start, *d_blk_off;
+    int *d_blk_part; /* total_blocks: partition of each block */
+    /* factor-precision arrays, [total_blocks][KB][KB] (row-major tiles) */
+    void *d_L, *d_G, *d_E, *d_V, *d_W; /* V, W tiles are column-major */
+    void *d_Bhat;                      /* [p][KB][KB] */
+    /* reduced system: level-0 quadrant blocks in FP64 (or complex128) */
+    void *d_RP, *d_RQ, *d_RX, *d_RY; /* [n_iface][KB][KB] */
+    /* cyclic reduction factors in factor precision */
+    int cr_levels;
+    int *cr_count;    /* blocks at each level (host), cr_levels+1 entries */
+    long long *cr_off; /* offset (in tiles) of each level's block arrays */
+    long long *cr_moff; /* offset (in tiles) of each level's odd-block M arrays */
+    void *d_crP, *d_crQ, *d_crX, *d_crY; /* all levels, factor precision */
+    void *d_crM;                         /* 4 tiles per odd block: M00 M01 M10 M11 */
+    void *d_crg;                         /* per-level reduced RHS work, factor precision */
+    long long crg_stride;                /* elements per RHS column of d_crg */
+    /* right-hand-side work (per solve) */
+    void *d_z, *d_y;       /* factor precision, NP x nrhs_max */
+    void *d_g, *d_u, *d_rr; /* FP64 reduced RHS, solution, reduced residual: n_iface*2KB x nrhs_max */
+    void *d_du;            /* FP64 reduced correction */
+    unsigned int *d_err;   /* device error word */
+    double *d_norms;       /* 2*nrhs_max: ||r||^2 then ||b||^2 per column */
+    /* bookkeeping */
+    long long launches; /* kernel launches issued for this plan */
+    size_t bytes;       /* device bytes held */
+} spk_plan;
+
+/* ---- device / memory (spike_util.cu) ---- */
+int spk_device_count(void);
+int spk_current_device(void);
+int spk_sm_count(void);
+int spk_malloc(void **p, size_t bytes);
+void spk_free(void *p);
+int spk_host_register(void *p, size_t bytes);
+int spk_host_unregister(void *p);
+int spk_stream_create(void **stream);
+void spk_stream_destroy(void *stream);
+int spk_stream_sync(void *stream);
+int spk_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
+int spk_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int spk_memcpy_d2d(void *dst, const void *src, size_t bytes, void *stream);
+int spk_memset(void *dst, int v, size_t bytes, void *stream);
+const char *spk_cuda_error_string(void);
+
+/* ---- analysis, conversion, residual (spike_util.cu) ---- */
+/* bandwidth and CSR validation on the device; out[0] = ku, out[1] = kl,
+ * out[2] = error flags (SPK_DEV_ERR_CSR).  d_scratch: 4 device ints.
+ * Synchronizes the stream. */
+int spk_analyze(int n, long long nnz, const int *d_rowptr, const int *d_colind, int *d_scratch, int *out,
+                void *stream, long long *launches);
+/* widen caller values to FP64 / complex128 (S -> D, C -> Z) and narrow back */
+int spk_widen(const void *src, void *dst, long long count, int is_complex, void *stream, long long *launches);
+int spk_narrow(const void *src, void *dst, long long count, int is_complex, void *stream, long long *launches);
+/* r = b - A x for every column (FP64 / complex128), ||r||^2 per column into
+ * norms[0:nrhs]; when want_bnorm, ||b||^2 into norms[nrhs:2*nrhs]. */
+int spk_residual(const spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij,
+                 const void *d_x, const void *d_b, void *d_r, int nrhs, int want_bnorm, double *d_norms,
+                 void *stream);
+
+/* ---- factorization (spike_factor.cu) ---- */
+/* K2: block LU of every A_i, spikes V_i/W_i, tips into the reduced blocks. */
+int spk_factor(spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij, void *stream);
+/* shared-memory bytes the factor kernels need for this plan (0 = unsupported) */
+size_t spk_factor_smem(int KB, int is_complex, int mode);
+
+/* ---- reduced system (spike_reduced.cu) ---- */
+int spk_reduced_factor(spk_plan *P, void *stream);
+/* u = R^{-1} g for nrhs columns (FP64), with refine_iters FP64 refinement
+ * sweeps around the factor-precision cyclic reduction. */
+int spk_reduced_solve(spk_plan *P, int nrhs, int refine_iters, void *stream);
+
+/* ---- right-hand-side sweeps (spike_apply.cu) ---- */
+/* y_i = A_i^{-1} r_i for every partition (r in FP64 / complex128, caller
+ * layout n x nrhs, ld n), y tips into the reduced RHS d_g. */
+int spk_apply(spk_plan *P, const void *d_r, int nrhs, void *stream);
+/* x += y - V_i t_{i+1} - W_i b_{i-1} (x in FP64 / complex128, ld n). */
+int spk_retrieve(spk_plan *P, void *d_x, int nrhs, int accumulate, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPIKE_GB300_INTERNAL_H */

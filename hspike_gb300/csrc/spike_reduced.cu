@@ -1,0 +1,476 @@
+// spike_reduced.cu -- the reduced system of the SPIKE solve on sm_103a.
+//
+// The reference assembles R as a CSR matrix (matrix_CreateEmptyReducedSystem
+// and matrix_AddTipToReducedMatrix, OpenMP/spike_matrix.c:657-740,1414-1495)
+// and solves it with MKL PARDISO on the host (directSolver_Host_Solve,
+// OpenMP/spike_algebra.c:263-420).  Here R stays on the device in its natural
+// block form.  With one 2KB-vector of unknowns per interface i,
+// u_i = (b_i, t_{i+1}), R is block tridiagonal:
+//
+//     D_i = [[I, P_i], [Q_i, I]]     P_i = V_i bottom tip, Q_i = W_{i+1} top tip
+//     A_i = [[X_i, 0], [0, 0]]       X_i = W_i bottom tip       (couples u_{i-1})
+//     C_i = [[0, 0], [0, Y_i]]       Y_i = V_{i+1} top tip      (couples u_{i+1})
+//
+// Block cyclic reduction keeps that quadrant structure at every level (the
+// products A M C, C M A, A M A, C M C each fill a single KB x KB quadrant), so
+// a level costs ~13 KB^3 multiply-adds per eliminated pair instead of the
+// dense (2KB)^3 form.  The factorization runs in the factor precision
+// (FP32/complex64 in mixed mode, FP64 in plain mode); the solve wraps it in
+// FP64 refinement on R itself, u += CR^{-1}(g - R u), so the reduced solution
+// is FP64-accurate in both modes.
+#include "spike_common.cuh"
+
+namespace {
+
+template <class T, int KB> struct RedSmem {
+    using TL = Tile<T, KB, NTOf<KB>::value>;
+    static constexpr size_t bytes = 5 * sizeof(T) * TL::ELEMS + sizeof(T) * 4 * KB + 64;
+};
+
+template <class T, int KB> __device__ void ld(T *s, const T *g)
+{
+    constexpr int NT = NTOf<KB>::value;
+    for (int q = threadIdx.x; q < KB * KB; q += NT) {
+        const int r = q / KB, c = q - r * KB;
+        s[r * (KB + 1) + c] = g[q];
+    }
+}
+template <class T, int KB, class Reg> __device__ void set_identity(const Tile<T, KB, NTOf<KB>::value> &t, Reg &a)
+{
+#pragma unroll
+    for (int i = 0; i < t.TR; i++)
+#pragma unroll
+        for (int j = 0; j < t.TC; j++) a[i][j] = (t.row(i) == t.col(j)) ? sc_one<T>() : sc_zero<T>();
+}
+
+// level-0 blocks: FP64 -> factor precision
+template <class T>
+__global__ void k_red_cvt(const typename HighOf<T>::type *__restrict__ src, T *dst, long long count)
+{
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < count; q += (long long)gridDim.x * blockDim.x)
+        dst[q] = sc_cvt<T, typename HighOf<T>::type>(src[q]);
+}
+
+// Odd blocks j of a level (or the single top block): M = D_j^{-1} by quadrants
+//   S = I - Q P, M11 = S^{-1}, M10 = -M11 Q, M01 = -P M11, M00 = I - P M10.
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_cr_odd(const T *__restrict__ Pl, const T *__restrict__ Ql, int first, int stride, T *M, unsigned *err)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int j = first + blockIdx.x * stride;
+    T *Mj = M + (size_t)blockIdx.x * 4 * TS;
+    extern __shared__ char smraw[];
+    T *sP = (T *)smem_align(smraw), *sQ = sP + TL::ELEMS, *sH = sQ + TL::ELEMS, *sT = sH + TL::ELEMS;
+    T *buf = sT + 2 * TL::ELEMS;
+    TL t(threadIdx.x);
+    typename TL::Reg a;
+    ld<T, KB>(sP, Pl + (size_t)j * TS);
+    ld<T, KB>(sQ, Ql + (size_t)j * TS);
+    __syncthreads();
+    set_identity<T, KB>(t, a);
+    t.mms(a, sQ, sP);
+    const bool ok = t.inverse(a, buf);
+    if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+    t.rstore(sH, a);
+    t.gstore(Mj + 3 * TS, a);
+    __syncthreads();
+    t.rzero(a);
+    t.mms(a, sH, sQ); // M10
+    t.rstore(sT, a);
+    t.gstore(Mj + 2 * TS, a);
+    t.rzero(a);
+    t.mms(a, sP, sH); // M01
+    t.gstore(Mj + 1 * TS, a);
+    __syncthreads();
+    set_identity<T, KB>(t, a);
+    t.mms(a, sP, sT); // M00 = I - P M10
+    t.gstore(Mj, a);
+}
+
+// acc += sign * L (M R); L, M, R global tiles; uses sA, sB, sC
+template <class T, int KB>
+__device__ void chain3(const Tile<T, KB, NTOf<KB>::value> &t, typename Tile<T, KB, NTOf<KB>::value>::Reg &acc,
+                       const T *L, const T *Mg, const T *R, T *sA, T *sB, T *sC, bool negate)
+{
+    typename Tile<T, KB, NTOf<KB>::value>::Reg tmp;
+    __syncthreads();
+    ld<T, KB>(sA, Mg);
+    ld<T, KB>(sB, R);
+    __syncthreads();
+    t.rzero(tmp);
+    t.mma(tmp, sA, sB);
+    t.rstore(sC, tmp);
+    __syncthreads();
+    ld<T, KB>(sA, L);
+    __syncthreads();
+    if (negate)
+        t.mms(acc, sA, sC);
+    else
+        t.mma(acc, sA, sC);
+}
+
+// Even blocks i of level l produce block i/2 of level l+1:
+//   P' = P_i - X_i M01_{i-1} Y_{i-1}    Q' = Q_i - Y_i M10_{i+1} X_{i+1}
+//   X' = -X_i M00_{i-1} X_{i-1}         Y' = -Y_i M11_{i+1} Y_{i+1}
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_cr_even(const T *__restrict__ Pl, const T *__restrict__ Ql, const T *__restrict__ Xl, const T *__restrict__ Yl,
+              const T *__restrict__ Ml, int cnt, T *Pn, T *Qn, T *Xn, T *Yn)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int i = 2 * blockIdx.x, a_out = blockIdx.x;
+    extern __shared__ char smraw[];
+    T *sA = (T *)smem_align(smraw), *sB = sA + TL::ELEMS, *sC = sB + TL::ELEMS;
+    TL t(threadIdx.x);
+    typename TL::Reg acc;
+    const bool left = i - 1 >= 0, right = i + 1 < cnt;
+    const T *Ml_left = left ? Ml + (size_t)((i - 2) / 2) * 4 * TS : nullptr;  // odd block i-1
+    const T *Ml_right = right ? Ml + (size_t)(i / 2) * 4 * TS : nullptr;      // odd block i+1
+    // P'
+    __syncthreads();
+    ld<T, KB>(sA, Pl + (size_t)i * TS);
+    __syncthreads();
+    t.rload(acc, sA);
+    if (left) chain3<T, KB>(t, acc, Xl + (size_t)i * TS, Ml_left + 1 * TS, Yl + (size_t)(i - 1) * TS, sA, sB, sC, true);
+    t.gstore(Pn + (size_t)a_out * TS, acc);
+    // Q'
+    __syncthreads();
+    ld<T, KB>(sA, Ql + (size_t)i * TS);
+    __syncthreads();
+    t.rload(acc, sA);
+    if (right) chain3<T, KB>(t, acc, Yl + (size_t)i * TS, Ml_right + 2 * TS, Xl + (size_t)(i + 1) * TS, sA, sB, sC, true);
+    t.gstore(Qn + (size_t)a_out * TS, acc);
+    // X'
+    t.rzero(acc);
+    if (left) chain3<T, KB>(t, acc, Xl + (size_t)i * TS, Ml_left + 0 * TS, Xl + (size_t)(i - 1) * TS, sA, sB, sC, true);
+    t.gstore(Xn + (size_t)a_out * TS, acc);
+    // Y'
+    t.rzero(acc);
+    if (right) chain3<T, KB>(t, acc, Yl + (size_t)i * TS, Ml_right + 3 * TS, Yl + (size_t)(i + 1) * TS, sA, sB, sC, true);
+    t.gstore(Yn + (size_t)a_out * TS, acc);
+}
+
+// ---------------------------------------------------------------- solve
+// vectors: level block a holds 2KB rows; element (row q, column h) of block a
+// at level offset off lives at g[h * stride + (off + a) * 2KB + q].
+
+// y[r] = sum_k M[r][k] x[k]  for a KB x KB global tile and nr columns, via shared
+template <class T, int KB>
+__device__ T tile_row_dot(const T *sM, const T *sx, int r, int h, int RCP)
+{
+    T acc = sc_zero<T>();
+    for (int k = 0; k < KB; k++) acc = madd(acc, sM[r * (KB + 1) + k], sx[k * RCP + h]);
+    return acc;
+}
+
+constexpr int RRC = 4; // right-hand sides per reduced-solve CTA (keeps static shared memory < 48 KB)
+
+// forward reduction at level l: even i -> block i/2 of level l+1
+//   g'^0 = g^0_i - X_i (M00 g^0 + M01 g^1)_{i-1}
+//   g'^1 = g^1_i - Y_i (M10 g^0 + M11 g^1)_{i+1}
+template <class T, int KB>
+__global__ void __launch_bounds__(128)
+    k_cr_fwd(const T *__restrict__ Xl, const T *__restrict__ Yl, const T *__restrict__ Ml, int cnt, T *g,
+             long long stride, long long off_l, long long off_n, int nrhs)
+{
+    constexpr size_t TS = (size_t)KB * KB;
+    const int i = 2 * blockIdx.x;
+    const int h0 = blockIdx.y * RRC, nr = min(RRC, nrhs - h0);
+    __shared__ T sM[KB * (KB + 1)];
+    __shared__ T sx[2 * KB * RRC], sw[KB * RRC];
+    const bool left = i - 1 >= 0, right = i + 1 < cnt;
+    T *gi = g + (off_l + i) * 2 * KB, *gn = g + (off_n + blockIdx.x) * 2 * KB;
+    for (int half = 0; half < 2; half++) {
+        const bool has = half == 0 ? left : right;
+        const int nb = half == 0 ? i - 1 : i + 1;
+        if (has) {
+            const T *Mb = Ml + (size_t)(half == 0 ? (i - 2) / 2 : i / 2) * 4 * TS;
+            __syncthreads();
+            for (int q = threadIdx.x; q < 2 * KB * nr; q += blockDim.x) {
+                const int rr = q % (2 * KB), h = q / (2 * KB);
+                sx[rr * RRC + h] = g[(h0 + h) * stride + (off_l + nb) * 2 * KB + rr];
+            }
+            // w = M_{row half}(nb) * x : rows 0..KB-1 of [M00 M01] (half 0) or [M10 M11] (half 1)
+            for (int q = threadIdx.x; q < KB * RRC; q += blockDim.x) sw[q] = sc_zero<T>();
+            for (int part = 0; part < 2; part++) {
+                __syncthreads();
+                const T *Mt = Mb + (size_t)(half * 2 + part) * TS;
+                for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Mt[q];
+                __syncthreads();
+                for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+                    const int r = q / nr, h = q - r * nr;
+                    sw[r * RRC + h] = sw[r * RRC + h] + tile_row_dot<T, KB>(sM, sx + part * KB * RRC, r, h, RRC);
+                }
+            }
+            __syncthreads();
+            // subtract X_i w (half 0) or Y_i w (half 1) from the new block's half
+            const T *Ct = (half == 0 ? Xl : Yl) + (size_t)i * TS;
+            for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Ct[q];
+            __syncthreads();
+            for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+                const int r = q / nr, h = q - r * nr;
+                const T v = gi[(h0 + h) * stride + half * KB + r];
+                gn[(h0 + h) * stride + half * KB + r] = v - tile_row_dot<T, KB>(sM, sw, r, h, RRC);
+            }
+        } else {
+            __syncthreads();
+            for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+                const int r = q / nr, h = q - r * nr;
+                gn[(h0 + h) * stride + half * KB + r] = gi[(h0 + h) * stride + half * KB + r];
+            }
+        }
+    }
+}
+
+// u_j = M_j (g_j - [X_j u^0_{j-1}; Y_j u^1_{j+1}]) for odd j (or the top block,
+// first = 0, with no neighbours), then even blocks copy u from the level above.
+template <class T, int KB>
+__global__ void __launch_bounds__(128)
+    k_cr_bwd(const T *__restrict__ Xl, const T *__restrict__ Yl, const T *__restrict__ Ml, int cnt, const T *g, T *u,
+             long long stride, long long off_l, long long off_n, int nrhs, int top)
+{
+    constexpr size_t TS = (size_t)KB * KB;
+    const int h0 = blockIdx.y * RRC, nr = min(RRC, nrhs - h0);
+    __shared__ T sM[KB * (KB + 1)];
+    __shared__ T sx[2 * KB * RRC], sw[2 * KB * RRC];
+    if (!top && (blockIdx.x & 1) == 0) {
+        // even block: copy from level l+1
+        const int i = blockIdx.x;
+        for (int q = threadIdx.x; q < 2 * KB * nr; q += blockDim.x) {
+            const int rr = q % (2 * KB), h = q / (2 * KB);
+            u[(h0 + h) * stride + (off_l + i) * 2 * KB + rr] = u[(h0 + h) * stride + (off_n + i / 2) * 2 * KB + rr];
+        }
+        return;
+    }
+    const int j = blockIdx.x;
+    const T *Mj = Ml + (size_t)(top ? 0 : (j - 1) / 2) * 4 * TS;
+    for (int q = threadIdx.x; q < 2 * KB * nr; q += blockDim.x) {
+        const int rr = q % (2 * KB), h = q / (2 * KB);
+        sx[rr * RRC + h] = g[(h0 + h) * stride + (off_l + j) * 2 * KB + rr];
+    }
+    if (!top) {
+        for (int half = 0; half < 2; half++) {
+            const int nb = half == 0 ? j - 1 : j + 1;
+            if (nb < 0 || nb >= cnt) continue;
+            __syncthreads();
+            const T *Ct = (half == 0 ? Xl : Yl) + (size_t)j * TS;
+            for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Ct[q];
+            for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+                const int r = q / nr, h = q - r * nr;
+                // even neighbours of an odd block: their values sit in the level above
+                sw[r * RRC + h] = u[(h0 + h) * stride + (off_n + nb / 2) * 2 * KB + half * KB + r];
+            }
+            __syncthreads();
+            for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+                const int r = q / nr, h = q - r * nr;
+                sx[(half * KB + r) * RRC + h] = sx[(half * KB + r) * RRC + h] - tile_row_dot<T, KB>(sM, sw, r, h, RRC);
+            }
+        }
+    }
+    // u_j = M_j x : out rows half 0: M00 x0 + M01 x1; half 1: M10 x0 + M11 x1
+    __syncthreads();
+    for (int q = threadIdx.x; q < 2 * KB * RRC; q += blockDim.x) sw[q] = sc_zero<T>();
+    for (int quad = 0; quad < 4; quad++) {
+        __syncthreads();
+        const T *Mt = Mj + (size_t)quad * TS;
+        for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Mt[q];
+        __syncthreads();
+        const int oh = quad >> 1, ih = quad & 1;
+        for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
+            const int r = q / nr, h = q - r * nr;
+            sw[(oh * KB + r) * RRC + h] = sw[(oh * KB + r) * RRC + h] + tile_row_dot<T, KB>(sM, sx + ih * KB * RRC, r, h, RRC);
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < 2 * KB * nr; q += blockDim.x) {
+        const int rr = q % (2 * KB), h = q / (2 * KB);
+        u[(h0 + h) * stride + (off_l + j) * 2 * KB + rr] = sw[rr * RRC + h];
+    }
+}
+
+// level-0 right-hand side (factor precision) <- FP64 residual of R
+template <class T>
+__global__ void k_red_load(const typename HighOf<T>::type *__restrict__ res, T *g, long long NR, long long stride,
+                           int nrhs)
+{
+    const long long tot = NR * nrhs;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < tot; q += (long long)gridDim.x * blockDim.x) {
+        const long long h = q / NR, r = q - h * NR;
+        g[h * stride + r] = sc_cvt<T, typename HighOf<T>::type>(res[q]);
+    }
+}
+
+// u += du (FP64); first sweep sets u = du
+template <class T>
+__global__ void k_red_accum(const T *__restrict__ du, typename HighOf<T>::type *u, long long NR, long long stride,
+                            int nrhs, int first)
+{
+    using H = typename HighOf<T>::type;
+    const long long tot = NR * nrhs;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < tot; q += (long long)gridDim.x * blockDim.x) {
+        const long long h = q / NR, r = q - h * NR;
+        const H d = sc_cvt<H, T>(du[h * stride + r]);
+        u[q] = first ? d : u[q] + d;
+    }
+}
+
+// res = g - R u in FP64 with the level-0 quadrant blocks, one CTA per interface
+template <class H, int KB>
+__global__ void __launch_bounds__(128)
+    k_red_resid(const H *__restrict__ RP, const H *__restrict__ RQ, const H *__restrict__ RX, const H *__restrict__ RY,
+                const H *__restrict__ g, const H *__restrict__ u, H *res, int nif, int nrhs)
+{
+    constexpr size_t TS = (size_t)KB * KB;
+    const int i = blockIdx.x;
+    const long long NR = (long long)nif * 2 * KB;
+    for (int q = threadIdx.x; q < 2 * KB * nrhs; q += blockDim.x) {
+        const int h = q / (2 * KB), rr = q - h * 2 * KB;
+        const H *uh = u + h * NR;
+        const int r = rr % KB;
+        H acc = g[h * NR + (long long)i * 2 * KB + rr] - uh[(long long)i * 2 * KB + rr];
+        if (rr < KB) { // b-equation: P_i t + X_i b_{i-1}
+            for (int c = 0; c < KB; c++) acc = msub(acc, RP[(size_t)i * TS + r * KB + c], uh[(long long)i * 2 * KB + KB + c]);
+            if (i > 0)
+                for (int c = 0; c < KB; c++) acc = msub(acc, RX[(size_t)i * TS + r * KB + c], uh[(long long)(i - 1) * 2 * KB + c]);
+        } else { // t-equation: Q_i b + Y_i t_{i+2}
+            for (int c = 0; c < KB; c++) acc = msub(acc, RQ[(size_t)i * TS + r * KB + c], uh[(long long)i * 2 * KB + c]);
+            if (i + 1 < nif)
+                for (int c = 0; c < KB; c++)
+                    acc = msub(acc, RY[(size_t)i * TS + r * KB + c], uh[(long long)(i + 1) * 2 * KB + KB + c]);
+        }
+        res[h * NR + (long long)i * 2 * KB + rr] = acc;
+    }
+}
+
+template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
+{
+    using S = RedSmem<T, KB>;
+    constexpr int NT = NTOf<KB>::value;
+    constexpr size_t TS = (size_t)KB * KB;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_cr_odd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes) != cudaSuccess ||
+            cudaFuncSetAttribute(k_cr_even<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes) != cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
+    using H = typename HighOf<T>::type;
+    const long long c0 = (long long)P->n_iface * TS;
+    k_red_cvt<T><<<256, 256, 0, st>>>((const H *)P->d_RP, (T *)P->d_crP, c0);
+    k_red_cvt<T><<<256, 256, 0, st>>>((const H *)P->d_RQ, (T *)P->d_crQ, c0);
+    k_red_cvt<T><<<256, 256, 0, st>>>((const H *)P->d_RX, (T *)P->d_crX, c0);
+    k_red_cvt<T><<<256, 256, 0, st>>>((const H *)P->d_RY, (T *)P->d_crY, c0);
+    SPK_CHECK_LAUNCH();
+    P->launches += 4;
+    T *cP = (T *)P->d_crP, *cQ = (T *)P->d_crQ, *cX = (T *)P->d_crX, *cY = (T *)P->d_crY, *cM = (T *)P->d_crM;
+    for (int l = 0; l < P->cr_levels; l++) {
+        const int cnt = P->cr_count[l];
+        const size_t o = (size_t)P->cr_off[l] * TS, on = (size_t)P->cr_off[l + 1] * TS;
+        T *Ml = cM + (size_t)P->cr_moff[l] * 4 * TS;
+        const int nodd = cnt / 2, neven = (cnt + 1) / 2;
+        if (nodd > 0) {
+            k_cr_odd<T, KB><<<nodd, NT, S::bytes, st>>>(cP + o, cQ + o, 1, 2, Ml, P->d_err);
+            SPK_CHECK_LAUNCH();
+        }
+        k_cr_even<T, KB><<<neven, NT, S::bytes, st>>>(cP + o, cQ + o, cX + o, cY + o, Ml, cnt, cP + on, cQ + on, cX + on,
+                                                      cY + on);
+        SPK_CHECK_LAUNCH();
+        P->launches += 2;
+    }
+    // top: a single block
+    {
+        const int L = P->cr_levels;
+        const size_t o = (size_t)P->cr_off[L] * TS;
+        k_cr_odd<T, KB><<<1, NT, S::bytes, st>>>(cP + o, cQ + o, 0, 1, cM + (size_t)P->cr_moff[L] * 4 * TS, P->d_err);
+        SPK_CHECK_LAUNCH();
+        P->launches++;
+    }
+    return SPK_OK;
+}
+
+template <class T, int KB> int run_red_solve(spk_plan *P, int nrhs, int iters, cudaStream_t st)
+{
+    using H = typename HighOf<T>::type;
+    constexpr size_t TS = (size_t)KB * KB;
+    const long long NR = (long long)P->n_iface * 2 * KB;
+    const long long stride = P->crg_stride;
+    T *cg = (T *)P->d_crg;
+    T *cu = cg + stride * P->nrhs_max;
+    const T *cX = (const T *)P->d_crX, *cY = (const T *)P->d_crY, *cM = (const T *)P->d_crM;
+    const int L = P->cr_levels;
+    const dim3 blk(128);
+    const int hy = (nrhs + RRC - 1) / RRC;
+    for (int it = 0; it < iters; it++) {
+        const H *res = it == 0 ? (const H *)P->d_g : (const H *)P->d_rr;
+        k_red_load<T><<<256, 256, 0, st>>>(res, cg, NR, stride, nrhs);
+        P->launches++;
+        for (int l = 0; l < L; l++) {
+            const int cnt = P->cr_count[l];
+            k_cr_fwd<T, KB><<<dim3((cnt + 1) / 2, hy), blk, 0, st>>>(
+                cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS, cM + (size_t)P->cr_moff[l] * 4 * TS, cnt, cg,
+                stride, P->cr_off[l], P->cr_off[l + 1], nrhs);
+            P->launches++;
+        }
+        k_cr_bwd<T, KB><<<dim3(1, hy), blk, 0, st>>>(nullptr, nullptr, cM + (size_t)P->cr_moff[L] * 4 * TS, 1, cg, cu, stride,
+                                                     P->cr_off[L], 0, nrhs, 1);
+        P->launches++;
+        for (int l = L - 1; l >= 0; l--) {
+            const int cnt = P->cr_count[l];
+            k_cr_bwd<T, KB><<<dim3(cnt, hy), blk, 0, st>>>(cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS,
+                                                           cM + (size_t)P->cr_moff[l] * 4 * TS, cnt, cg, cu, stride,
+                                                           P->cr_off[l], P->cr_off[l + 1], nrhs, 0);
+            P->launches++;
+        }
+        k_red_accum<T><<<256, 256, 0, st>>>(cu, (H *)P->d_u, NR, stride, nrhs, it == 0);
+        P->launches++;
+        if (it + 1 < iters) {
+            k_red_resid<H, KB><<<P->n_iface, 128, 0, st>>>((const H *)P->d_RP, (const H *)P->d_RQ, (const H *)P->d_RX,
+                                                           (const H *)P->d_RY, (const H *)P->d_g, (const H *)P->d_u,
+                                                           (H *)P->d_rr, P->n_iface, nrhs);
+            P->launches++;
+        }
+        SPK_CHECK_LAUNCH();
+    }
+    return SPK_OK;
+}
+
+#define SPK_KB_SWITCH(FN, T, ...)                                                                               \
+    switch (P->KB) {                                                                                            \
+    case 2: return FN<T, 2>(__VA_ARGS__);                                                                       \
+    case 4: return FN<T, 4>(__VA_ARGS__);                                                                       \
+    case 8: return FN<T, 8>(__VA_ARGS__);                                                                       \
+    case 16: return FN<T, 16>(__VA_ARGS__);                                                                     \
+    case 32: return FN<T, 32>(__VA_ARGS__);                                                                     \
+    case 64:                                                                                                    \
+        if constexpr (sizeof(T) <= 8) return FN<T, 64>(__VA_ARGS__);                                            \
+        else return SPK_EBAND;                                                                                  \
+    default: return SPK_EBAND;                                                                                  \
+    }
+
+template <class T> int disp_rf(spk_plan *P, cudaStream_t st) { SPK_KB_SWITCH(run_red_factor, T, P, st) }
+template <class T> int disp_rs(spk_plan *P, int nrhs, int it, cudaStream_t st) { SPK_KB_SWITCH(run_red_solve, T, P, nrhs, it, st) }
+
+} // namespace
+
+extern "C" int spk_reduced_factor(spk_plan *P, void *stream)
+{
+    if (P->n_iface <= 0) return SPK_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (P->is_complex) return P->mode == SPK_MIXED ? disp_rf<cfloat>(P, st) : disp_rf<cdouble>(P, st);
+    return P->mode == SPK_MIXED ? disp_rf<float>(P, st) : disp_rf<double>(P, st);
+}
+
+extern "C" int spk_reduced_solve(spk_plan *P, int nrhs, int refine_iters, void *stream)
+{
+    if (P->n_iface <= 0) return SPK_OK;
+    if (refine_iters < 1) refine_iters = 1;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (P->is_complex)
+        return P->mode == SPK_MIXED ? disp_rs<cfloat>(P, nrhs, refine_iters, st) : disp_rs<cdouble>(P, nrhs, refine_iters, st);
+    return P->mode == SPK_MIXED ? disp_rs<float>(P, nrhs, refine_iters, st) : disp_rs<double>(P, nrhs, refine_iters, st);
+}

@@ -1,0 +1,105 @@
+/*
+ * spike_gb300.h -- additive extensions to the SPIKE C API.
+ *
+ * Nothing here changes spike_interfaces.h; a caller written against the
+ * reference's API needs none of it.  The extensions expose what the
+ * reference keeps internal or compile-time:
+ *
+ *   - options (precision mode, partition count, refinement) that the
+ *     reference fixes in code: p = 4 (OpenMP/spike_analysis.c:168), the
+ *     -D_DATATYPE_ scalar type (OpenMP/spike_datatypes.h:29-84);
+ *   - error detail: the reference aborts (OpenMP/spike_interfaces.c:53-56),
+ *     this library returns SPIKE_ERROR and records why;
+ *   - factor handles: factor once, solve many right-hand sides with the
+ *     factors resident on the device (the reference re-factors every block
+ *     in the retrieval phase, OpenMP/spike_interfaces.c:271-277);
+ *   - device-pointer entry points for callers whose data already sits in HBM;
+ *   - contexts bound to a caller-chosen CUDA stream.
+ *
+ * A NULL context everywhere means the calling host thread's default context
+ * (the one the spike_interfaces.h entry points use).
+ */
+#ifndef SPIKE_GB300_H
+#define SPIKE_GB300_H
+
+#include "spike_interfaces.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct spike_context_s *spike_context_t;
+typedef struct spike_factor_s *spike_factor_t;
+
+/* ---- options (spike_set_option) ---- */
+#define SPIKE_OPT_PRECISION 0      /* SPIKE_PRECISION_MIXED (default) or _FP64 */
+#define SPIKE_OPT_PARTITIONS 1     /* 0 = automatic (default), else p */
+#define SPIKE_OPT_MAX_REFINE 2     /* correction sweeps after the first solve (default 3) */
+#define SPIKE_OPT_TOLERANCE 3      /* relative residual target (default 1e-12) */
+#define SPIKE_OPT_REDUCED_REFINE 4 /* FP64 refinement sweeps on the reduced system (default 2 mixed, 1 FP64) */
+
+#define SPIKE_PRECISION_MIXED 0 /* FP32 / complex64 factors, FP64 residual + update + reduced solve */
+#define SPIKE_PRECISION_FP64 1  /* FP64 / complex128 everywhere */
+
+/* ---- error detail ---- */
+#define SPIKE_ERR_NONE 0
+#define SPIKE_ERR_ARGUMENT 1
+#define SPIKE_ERR_CSR 2        /* out-of-range, unsorted or duplicate column index, bad rowptr */
+#define SPIKE_ERR_BANDWIDTH 3  /* max(ku, kl) above the supported tile size */
+#define SPIKE_ERR_CUDA 4
+#define SPIKE_ERR_MEMORY 5
+#define SPIKE_ERR_PIVOT 6      /* zero or non-finite pivot: A is not diagonally dominant enough */
+#define SPIKE_ERR_CONVERGENCE 7 /* refinement stopped above the tolerance (x holds the last iterate) */
+#define SPIKE_ERR_NO_DEVICE 8
+#define SPIKE_ERR_HANDLE 9
+
+int spike_last_error_code(void);          /* of the calling thread's last call */
+const char *spike_last_error(void);       /* human-readable, thread-local */
+
+/* ---- contexts ---- */
+Error_t spike_context_create(spike_context_t *ctx);          /* on the current CUDA device */
+Error_t spike_context_destroy(spike_context_t ctx);
+/* Run this context's work on a caller-owned cudaStream_t (NULL = own stream). */
+Error_t spike_context_set_stream(spike_context_t ctx, void *cuda_stream);
+Error_t spike_set_option(spike_context_t ctx, int option, double value);
+Error_t spike_get_option(spike_context_t ctx, int option, double *value);
+
+/* Statistics of the context's last solve. */
+typedef struct {
+    double relres_max;        /* max over columns of ||b - A x|| / ||b|| (FP64) */
+    int refine_sweeps;        /* correction sweeps after the first solve */
+    int partitions, ku, kl, block;
+    long long kernel_launches; /* kernels launched by the last call */
+    size_t device_bytes;      /* device memory held by the context's plan */
+} spike_info_t;
+Error_t spike_get_info(spike_context_t ctx, spike_info_t *info);
+
+/* ---- device-pointer solves: every array already in device memory ---- */
+Error_t spike_dsolve_device(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs,
+                            const integer_t *d_colind, const integer_t *d_rowptr, const double *d_aij,
+                            double *d_x, const double *d_b);
+Error_t spike_zsolve_device(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs,
+                            const integer_t *d_colind, const integer_t *d_rowptr, const complex16 *d_aij,
+                            complex16 *d_x, const complex16 *d_b);
+
+/* ---- factor handles ---- */
+/* Host arrays: the handle copies A to the device and owns the copy. */
+Error_t spike_dfactor(spike_context_t ctx, integer_t n, integer_t nnz, const integer_t *colind,
+                      const integer_t *rowptr, const double *aij, spike_factor_t *f);
+Error_t spike_zfactor(spike_context_t ctx, integer_t n, integer_t nnz, const integer_t *colind,
+                      const integer_t *rowptr, const complex16 *aij, spike_factor_t *f);
+/* Device arrays: the handle references them; keep them alive until release. */
+Error_t spike_dfactor_device(spike_context_t ctx, integer_t n, integer_t nnz, const integer_t *d_colind,
+                             const integer_t *d_rowptr, const double *d_aij, spike_factor_t *f);
+/* Solve with resident factors; x, b host (column-major, ld n). */
+Error_t spike_dsolve_factored(spike_factor_t f, integer_t nrhs, double *x, const double *b);
+Error_t spike_zsolve_factored(spike_factor_t f, integer_t nrhs, complex16 *x, const complex16 *b);
+/* Same with device arrays. */
+Error_t spike_dsolve_factored_device(spike_factor_t f, integer_t nrhs, double *d_x, const double *d_b);
+Error_t spike_factor_release(spike_factor_t f);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPIKE_GB300_H */
