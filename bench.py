@@ -1,0 +1,349 @@
+"""Benchmark: SPIKE solves/s on the large-band workload (n = 2,000,000,
+kl = ku = 64, 256 partitions, 1 right-hand side, float64 CSR, dominance 1.5).
+
+One step = one complete solve of A x = b from CSR already in HBM: analysis,
+partition + block LU + spikes, reduced system, right-hand-side sweeps and FP64
+iterative refinement until ||b - A x|| / ||b|| <= 1e-12.  ``value`` is that
+rate for the mixed-precision path (FP32 factors, FP64 residual / update /
+reduced solve); the plain-FP64 rate, nrhs = 16, the end-to-end rate through
+the reference's C entry point ``dspike_core_host`` with host buffers, the
+per-kernel-family device times, clocks and the CPU baseline (the CPU oracle,
+a restatement of the reference path, on a sample of the same workload) ride
+along in the same JSON line.
+
+    python bench.py [--gpus 1] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "solves/s & HBM GB/s at resid≤1e-12, mixed vs plain FP64 on 1 GPU; p50/p99 ms"
+N, K_BAND, P, NRHS, DOM, SEED = 2_000_000, 64, 256, 1, 1.5, 2
+WORKLOAD = (f"large-band real SPIKE: n={N:,} kl=ku={K_BAND} partitions={P} nrhs={NRHS} float64 CSR, "
+            f"dominance {DOM}, off-diagonals U[-1,1], seed {SEED}")
+
+
+def nnz_of(n, k):
+    return (2 * k + 1) * n - k * (k + 1)
+
+
+def alg_bytes(n, k, nrhs):
+    """compulsory bytes of one solve: read CSR once, read b, write x"""
+    nnz = nnz_of(n, k)
+    return 12 * nnz + 4 * (n + 1) + 16 * n * nrhs
+
+
+def alg_flops(n, k, nrhs, applies, residuals):
+    """FP32: block LU + spikes 8 k^2 n, sweeps 4 k n per rhs per application;
+    FP64: residual 2 nnz per rhs per sweep."""
+    f32 = 8.0 * k * k * n + 4.0 * k * n * nrhs * applies
+    f64 = 2.0 * nnz_of(n, k) * nrhs * residuals
+    return f32, f64
+
+
+# --------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        rows = self.rows
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+# --------------------------------------------------------------------- CPU baseline
+def cpu_baseline(parts_sample=None):
+    """Time the CPU oracle (restated reference path, OpenMP over partitions) on
+    a sample of the workload: the first ``parts_sample`` partitions' worth of
+    rows of the same band/dominance, solved with that many partitions, then
+    scaled to the full 256-partition solve (partition work is independent)."""
+    import hspike_gb300 as hs
+    from oracle import oracle
+
+    cores = os.cpu_count() or 1
+    parts_sample = parts_sample or max(8, 2 * cores)
+    m = N // P
+    n_s = parts_sample * m
+    rp, ci, a, xt, b = hs.gen_banded(n_s, K_BAND, K_BAND, DOM, SEED, nrhs=NRHS)
+    t0 = time.perf_counter()
+    x = oracle.spike(rp, ci, a, b, p=parts_sample)
+    dt = time.perf_counter() - t0
+    rel = float(oracle.residual(rp, ci, a, x, b).max())
+    t_full = dt * P / parts_sample
+    return {"value": 1.0 / t_full, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": (f"oracle/spike_oracle.c (restated reference SPIKE, banded partial-pivoting LU inner solver) "
+                       f"on {parts_sample} of the {P} partitions (n={n_s:,}, same band and dominance), "
+                       f"{dt:.2f} s with {cores} OpenMP threads, scaled x{P / parts_sample:.0f}; relres {rel:.1e}"),
+            "sample_seconds": dt}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle.build_oracle import build as build_oracle
+
+    build_oracle()
+    runs = []
+    for _ in range(args.warmup):
+        cpu_baseline()
+    for _ in range(args.steps):
+        runs.append(cpu_baseline())
+    vals = [r["value"] for r in runs]
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "note": "reference C code cannot be built here (MKL / SuperLU_MT "
+                       "absent); its path is timed as the CPU restatement in oracle/"},
+            "cpu_baseline": {k: runs[-1][k] for k in ("unit", "cores", "kind", "sample")} | {"value": v},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------- GPU arm
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
+    ap.add_argument("--skip-extras", action="store_true", help="mixed-precision device timing only")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+
+    import hspike_gb300 as hs
+    from hspike_gb300.build import build
+
+    build()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:  # independent replicas, one per GPU; no data exchange
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- inputs: pinned host buffers (for e2e) and device copies (for value)
+    tdt = {np.int32: torch.int32, np.float64: torch.float64, np.complex128: torch.complex128}
+
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=tdt[np.dtype(dtype).type], pin_memory=True).numpy()
+
+    rp, ci, a, xt, b = hs.gen_banded(N, K_BAND, K_BAND, DOM, SEED + rank, nrhs=NRHS, alloc=pinned)
+    nnz = len(ci)
+    d_rp, d_ci, d_a = (torch.from_numpy(v).to(dev) for v in (rp, ci, a))
+    d_b = torch.from_numpy(b.T.copy()).to(dev).contiguous()  # n x nrhs column-major == nrhs x n row-major
+    d_x = torch.zeros_like(d_b)
+    stream = torch.cuda.current_stream(dev)
+    ctx = hs.Context()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_option(hs.SPIKE_OPT_PARTITIONS, P)
+    ctx.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_MIXED)
+
+    def solve(ctx_, d_x_, d_b_, nrhs):
+        ctx_.solve_device(N, nnz, nrhs, d_ci.data_ptr(), d_rp.data_ptr(), d_a.data_ptr(), d_x_.data_ptr(),
+                          d_b_.data_ptr())
+
+    def timed(ctx_, steps, d_x_, d_b_, nrhs, warmup, clocks=None):
+        for _ in range(warmup):
+            solve(ctx_, d_x_, d_b_, nrhs)
+        barrier()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        launches = 0
+        if clocks:
+            clocks.start()
+        barrier()
+        ev[0].record(stream)
+        for s in range(steps):
+            solve(ctx_, d_x_, d_b_, nrhs)
+            ev[s + 1].record(stream)
+            launches += ctx_.info().kernel_launches
+        barrier()
+        clk = clocks.stop() if clocks else None
+        per = [ev[s].elapsed_time(ev[s + 1]) for s in range(steps)]
+        total = ev[0].elapsed_time(ev[steps])
+        if dist:
+            t = torch.tensor([total], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total = float(t.item())
+        return total, per, launches, clk
+
+    # ---- headline: mixed precision, device-resident inputs
+    clocks = ClockSampler(local)
+    total, per, launches, clk = timed(ctx, args.steps, d_x, d_b, NRHS, args.warmup, clocks)
+    info = ctx.info()
+    x = d_x.cpu().numpy().T
+    err = float(np.linalg.norm(x - xt) / np.linalg.norm(xt))
+    ms = total / args.steps
+    value = world * args.steps / (total / 1000.0)
+    sweeps = info.refine_sweeps
+    out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
+           "dtype": "f32 factors / f64 residual+update+reduced", "data": "synthetic (seeded generator)",
+           "config": {"workload": WORKLOAD, "l2": "inputs (3.1 GB CSR) larger than the 129 MB L2; no flush",
+                      "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+           "hbm_gbs": alg_bytes(N, K_BAND, NRHS) / (ms / 1000.0) / 1e9,
+           "p50_ms": statistics.median(per), "p99_ms": float(np.percentile(per, 99)),
+           "relres_max": info.relres_max, "refine_sweeps": sweeps, "err_vs_xtrue": err,
+           "gpu_launches": launches, "clocks": clk}
+    if rank != 0 and world > 1:
+        dist.barrier()
+        return 0
+
+    if not args.skip_extras:
+        # ---- per-kernel-family device time (CUDA events on the launching stream)
+        ctx.set_option(hs.SPIKE_OPT_PHASE_TIMING, 1)
+        ctx.phase_times(reset=True)
+        for _ in range(3):
+            solve(ctx, d_x, d_b, NRHS)
+        torch.cuda.synchronize()
+        ph = ctx.phase_times(reset=True)
+        ctx.set_option(hs.SPIKE_OPT_PHASE_TIMING, 0)
+        fams = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": 0.0} for k, v in ph.items() if v[1]}
+        tot = sum(v[0] for v in ph.values())
+        for k in fams:
+            fams[k]["share"] = ph[k][0] / tot
+        dom = max(fams, key=lambda k: ph[k][0])
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        hbm_peak = peaks.get("hbm_gbs", 6800.0)
+        # algorithmic bytes per launch of each family (units: CSR rows / vector rows)
+        csr_bytes = 12 * nnz + 4 * (N + 1)
+        fam_bytes = {"factor_fwd": csr_bytes, "residual": csr_bytes + 16 * N * NRHS + 8 * N * NRHS,
+                     "rhs_sweeps": 8 * N * NRHS, "retrieval": 8 * N * NRHS}
+        fam_flops = {"factor_fwd": 8.0 * K_BAND ** 3 * (N / K_BAND), "factor_bwd": 6.0 * K_BAND ** 3 * (N / K_BAND)}
+        dur = fams[dom]["ms_per_launch"] / 1000.0
+        ab = fam_bytes.get(dom, csr_bytes)
+        out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ab / dur / 1e9, "peak": hbm_peak,
+                           "unit": "GB/s", "frac": ab / dur / 1e9 / hbm_peak, "traffic": None,
+                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                           "algorithmic_bytes_per_launch": ab, "ms_per_launch": dur * 1000.0}
+        if dom in fam_flops:
+            out["roofline"]["achieved_fp32_tflops"] = fam_flops[dom] / dur / 1e12
+        out["kernel_families"] = fams
+        f32, f64 = alg_flops(N, K_BAND, NRHS, 1 + sweeps, 1 + sweeps)
+        t_roof = max(alg_bytes(N, K_BAND, NRHS) / (hbm_peak * 1e9), f32 / 80.5e12 + f64 / 1.25e12)
+        out["solve_roofline"] = {"t_roof_ms": t_roof * 1000, "frac": t_roof / (ms / 1000.0),
+                                 "rule": "max(B_alg/BW_hbm, F32/P32 + F64/P64); BW measured, P32 80.5 and P64 1.25 "
+                                         "TFLOP/s nominal GB300 (no measured CUDA-core peaks)",
+                                 "f32_gflop": f32 / 1e9, "f64_gflop": f64 / 1e9}
+
+        # ---- plain FP64 SPIKE (the denominator of the mixed/plain ratio)
+        ctx64 = hs.Context()
+        ctx64.set_stream(stream.cuda_stream)
+        ctx64.set_option(hs.SPIKE_OPT_PARTITIONS, P)
+        ctx64.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_FP64)
+        d_x64 = torch.zeros_like(d_b)
+        t64, per64, _, _ = timed(ctx64, 3, d_x64, d_b, NRHS, 1)
+        i64 = ctx64.info()
+        out["fp64"] = {"value": 3 / (t64 / 1000.0), "unit": "solves/s", "ms_per_step": t64 / 3,
+                       "relres_max": i64.relres_max, "mixed_over_fp64": value / (3 / (t64 / 1000.0))}
+        ctx64.close()
+        del d_x64
+
+        # ---- nrhs = 16
+        gen16 = hs.gen_banded(N, K_BAND, K_BAND, DOM, SEED, nrhs=16)
+        d_b16 = torch.from_numpy(gen16[4].T.copy()).to(dev)
+        d_x16 = torch.zeros_like(d_b16)
+        # same matrix (same seed), 16 right-hand sides
+        t16, per16, _, _ = timed(ctx, 3, d_x16, d_b16, 16, 1)
+        x16 = d_x16.cpu().numpy().T
+        out["nrhs16"] = {"value": 3 / (t16 / 1000.0), "unit": "solves/s", "ms_per_step": t16 / 3,
+                         "hbm_gbs": alg_bytes(N, K_BAND, 16) / (t16 / 3000.0) / 1e9,
+                         "relres_max": ctx.info().relres_max,
+                         "err_vs_xtrue": float(np.linalg.norm(x16 - gen16[3]) / np.linalg.norm(gen16[3]))}
+        del d_b16, d_x16, gen16
+
+    # ---- end to end through the reference's C entry point, host buffers
+    hs.set_option(hs.SPIKE_OPT_PARTITIONS, P)
+    hs.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_MIXED)
+    xh = pinned((N * NRHS,), np.float64).reshape((N, NRHS), order="F")
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(max(1, args.warmup)):
+        hs.dspike_core_host(N, nnz, NRHS, ci, rp, a, xh, b)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        rc = hs.dspike_core_host(N, nnz, NRHS, ci, rp, a, xh, b)
+        if rc != hs.SPIKE_SUCCESS:
+            raise RuntimeError(hs.last_error())
+    te = time.perf_counter() - t0
+    out["e2e"] = {"value": e2e_steps / te, "unit": "solves/s", "ms_per_step": te * 1000 / e2e_steps,
+                  "h2d_bytes_per_step": int(rp.nbytes + ci.nbytes + a.nbytes + b.nbytes),
+                  "d2h_bytes_per_step": int(xh.nbytes), "api": "dspike_core_host (pinned host buffers)",
+                  "err_vs_xtrue": float(np.linalg.norm(xh - xt) / np.linalg.norm(xt))}
+
+    if not args.skip_cpu and rank == 0 and world == 1:
+        out["cpu_baseline"] = cpu_baseline()
+
+    ctx.close()
+    if dist:
+        dist.barrier()
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

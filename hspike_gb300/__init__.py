@@ -31,6 +31,9 @@ SPIKE_OPT_PARTITIONS = 1
 SPIKE_OPT_MAX_REFINE = 2
 SPIKE_OPT_TOLERANCE = 3
 SPIKE_OPT_REDUCED_REFINE = 4
+SPIKE_OPT_PHASE_TIMING = 5
+PHASES = ["analysis", "factor_fwd", "factor_bwd", "reduced_factor", "rhs_sweeps", "reduced_solve", "retrieval",
+          "residual"]
 SPIKE_PRECISION_MIXED = 0
 SPIKE_PRECISION_FP64 = 1
 
@@ -43,6 +46,7 @@ EXPORTS = [
     "spike_context_destroy", "spike_context_set_stream", "spike_set_option", "spike_get_option", "spike_get_info",
     "spike_dsolve_device", "spike_zsolve_device", "spike_dfactor", "spike_zfactor", "spike_dfactor_device",
     "spike_dsolve_factored", "spike_zsolve_factored", "spike_dsolve_factored_device", "spike_factor_release",
+    "spike_get_phase_times",
 ]
 
 
@@ -93,6 +97,7 @@ def load(path: str | None = None):
     for name in ("spike_dsolve_factored", "spike_zsolve_factored", "spike_dsolve_factored_device"):
         getattr(L, name).argtypes = [vp, i, vp, vp]
     L.spike_factor_release.argtypes = [vp]
+    L.spike_get_phase_times.argtypes = [vp, i, vp, vp, i]
     _LIB = L
     return L
 
@@ -214,6 +219,13 @@ class Context:
 
     def info(self) -> Info:
         return get_info(self._h)
+
+    def phase_times(self, reset=True):
+        """{family: (total ms, timed launches)} while SPIKE_OPT_PHASE_TIMING is on."""
+        ms = np.zeros(len(PHASES), np.float64)
+        calls = np.zeros(len(PHASES), np.int64)
+        _check(load().spike_get_phase_times(self._h, len(PHASES), _ptr(ms), _ptr(calls), int(reset)))
+        return {name: (float(ms[i]), int(calls[i])) for i, name in enumerate(PHASES)}
 
     def solve_device(self, n, nnz, nrhs, d_colind: int, d_rowptr: int, d_aij: int, d_x: int, d_b: int,
                      complex_=False):

@@ -334,12 +334,15 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     }
     const size_t TS = (size_t)KB * KB;
     if (cudaMemsetAsync(P->d_Bhat, 0, sizeof(T) * TS * P->p, st) != cudaSuccess) return SPK_ECUDA;
+    spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
     k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>(rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off,
                                                   (T *)P->d_L, (T *)P->d_G, (T *)P->d_E, (T *)P->d_W,
                                                   (T *)P->d_Bhat, P->d_err);
     SPK_CHECK_LAUNCH();
+    spk_phase_end(P, st);
     P->launches++;
     if (P->p > 1) {
+        spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
         k_factor_bwd<T, KB><<<P->p, NT, S::bwd, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L,
                                                       (const T *)P->d_G, (const T *)P->d_E, (T *)P->d_W,
                                                       (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
@@ -348,6 +351,7 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
                                                   (const T *)P->d_W, (H *)P->d_RP, (H *)P->d_RQ, (H *)P->d_RX,
                                                   (H *)P->d_RY);
         SPK_CHECK_LAUNCH();
+        spk_phase_end(P, st);
         P->launches += 2;
     }
     return SPK_OK;

@@ -80,7 +80,7 @@ struct spike_context_s {
     int device;
     void *own_stream, *stream;
     /* options */
-    int mode, partitions, max_refine, red_refine;
+    int mode, partitions, max_refine, red_refine, timing;
     double tol;
     /* cached plan for the reference-API and device-pointer calls */
     spk_plan *plan;
@@ -209,6 +209,9 @@ Error_t spike_set_option(spike_context_t c, int opt, double v)
         if (v < 0 || v > 20) return fail(SPIKE_ERR_ARGUMENT, "reduced refine sweeps must be in [0, 20]");
         c->red_refine = (int)v;
         break;
+    case SPIKE_OPT_PHASE_TIMING:
+        c->timing = v != 0;
+        break;
     default: return fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
     return succeed();
@@ -224,6 +227,7 @@ Error_t spike_get_option(spike_context_t c, int opt, double *v)
     case SPIKE_OPT_MAX_REFINE: *v = c->max_refine; break;
     case SPIKE_OPT_TOLERANCE: *v = c->tol; break;
     case SPIKE_OPT_REDUCED_REFINE: *v = c->red_refine; break;
+    case SPIKE_OPT_PHASE_TIMING: *v = c->timing; break;
     default: return fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
     return succeed();
@@ -234,6 +238,24 @@ Error_t spike_get_info(spike_context_t c, spike_info_t *info)
     c = get_ctx(c);
     if (!c || !info) return c ? fail(SPIKE_ERR_ARGUMENT, "NULL output") : SPIKE_ERROR;
     *info = c->info;
+    return succeed();
+}
+
+Error_t spike_get_phase_times(spike_context_t c, int nphases, double *ms, long long *calls, int reset)
+{
+    c = get_ctx(c);
+    if (!c) return SPIKE_ERROR;
+    if (nphases < 0 || nphases > SPK_NPHASES) return fail(SPIKE_ERR_ARGUMENT, "nphases must be in [0, %d]", SPK_NPHASES);
+    spk_plan *P = c->plan;
+    for (int i = 0; i < nphases; i++) {
+        if (ms) ms[i] = P ? P->phase_ms[i] : 0.0;
+        if (calls) calls[i] = P ? P->phase_calls[i] : 0;
+    }
+    if (reset && P)
+        for (int i = 0; i < SPK_NPHASES; i++) {
+            P->phase_ms[i] = 0.0;
+            P->phase_calls[i] = 0;
+        }
     return succeed();
 }
 
@@ -272,6 +294,7 @@ static int choose_partitions(int n, int KB, int requested)
 static void plan_destroy(spk_plan *P)
 {
     if (!P) return;
+    spk_phase_destroy(P);
     void *ptrs[] = {P->d_part_start, P->d_blk_off, P->d_blk_part, P->d_L, P->d_G, P->d_E, P->d_V, P->d_W,
                     P->d_Bhat, P->d_RP, P->d_RQ, P->d_RX, P->d_RY, P->d_crP, P->d_crQ, P->d_crX, P->d_crY,
                     P->d_crM, P->d_crg, P->d_z, P->d_y, P->d_g, P->d_u, P->d_rr, P->d_du, P->d_err, P->d_norms};
@@ -434,8 +457,25 @@ static int factor_phase(spk_plan *P, const int *rp, const int *ci, const void *a
 {
     TRY(spk_memset(P->d_err, 0, sizeof(unsigned) * 4, stream));
     TRY(spk_factor(P, rp, ci, aij, stream));
+    spk_phase_begin(P, SPK_PH_RED_FACTOR, stream);
     TRY(spk_reduced_factor(P, stream));
+    spk_phase_end(P, stream);
     return check_device_error(P, stream);
+}
+
+/* one SPIKE application: x (+)= A_spike^{-1} r */
+static int spike_apply_once(spk_plan *P, void *x, const void *r, int nrhs, int red, int accumulate, void *stream)
+{
+    spk_phase_begin(P, SPK_PH_APPLY, stream);
+    TRY(spk_apply(P, r, nrhs, stream));
+    spk_phase_end(P, stream);
+    spk_phase_begin(P, SPK_PH_RED_SOLVE, stream);
+    TRY(spk_reduced_solve(P, nrhs, red, stream));
+    spk_phase_end(P, stream);
+    spk_phase_begin(P, SPK_PH_RETRIEVE, stream);
+    TRY(spk_retrieve(P, x, nrhs, accumulate, stream));
+    spk_phase_end(P, stream);
+    return SPK_OK;
 }
 
 typedef struct {
@@ -452,11 +492,11 @@ static int solve_phase(spk_plan *P, const int *rp, const int *ci, const void *ai
     const int red = o->red_refine > 0 ? o->red_refine : (P->mode == SPK_MIXED ? 2 : 1);
     double norms[2 * RHS_CHUNK];
     double bnorm[RHS_CHUNK];
-    TRY(spk_apply(P, b, nrhs, stream));
-    TRY(spk_reduced_solve(P, nrhs, red, stream));
-    TRY(spk_retrieve(P, x, nrhs, 0, stream));
+    TRY(spike_apply_once(P, x, b, nrhs, red, 0, stream));
     for (int sweep = 0;; sweep++) {
+        spk_phase_begin(P, SPK_PH_RESIDUAL, stream);
         TRY(spk_residual(P, rp, ci, aij, x, b, r, nrhs, sweep == 0, P->d_norms, stream));
+        spk_phase_end(P, stream);
         TRY(spk_memcpy_d2h(norms, P->d_norms, sizeof(double) * 2 * nrhs, stream));
         TRY(spk_stream_sync(stream));
         double worst = 0.0;
@@ -469,9 +509,7 @@ static int solve_phase(spk_plan *P, const int *rp, const int *ci, const void *ai
         o->sweeps = sweep;
         if (worst <= o->tol) return SPK_OK;
         if (sweep >= o->max_refine) return SPK_ECONV;
-        TRY(spk_apply(P, r, nrhs, stream));
-        TRY(spk_reduced_solve(P, nrhs, red, stream));
-        TRY(spk_retrieve(P, x, nrhs, 1, stream));
+        TRY(spike_apply_once(P, x, r, nrhs, red, 1, stream));
     }
 }
 
@@ -538,10 +576,12 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
     P->ku = info[0];
     P->kl = info[1];
     P->launches = l0;
+    P->timing = c->timing;
     const size_t hs = (is_complex ? 2 : 1) * 8;
     TRY(ensure(&c->d_r, &c->c_r, hs * (size_t)n * chunk));
     int rc = factor_phase(P, rp, ci, aij, c->stream);
     if (rc == SPK_OK) rc = solve_all(P, rp, ci, aij, x, b, c->d_r, nrhs, o, c->stream);
+    if (P->timing && (rc == SPK_OK || rc == SPK_ECONV) && spk_phase_collect(P) != SPK_OK) rc = SPK_ECUDA;
     *launches = P->launches;
     fill_info(c, P, o, P->launches);
     return rc;

@@ -43,6 +43,20 @@ enum spk_err {
     SPK_EHANDLE = 9     /* bad or released handle */
 };
 
+/* kernel families timed by the phase timer */
+enum spk_phase {
+    SPK_PH_ANALYZE = 0,
+    SPK_PH_FACTOR_FWD = 1, /* k_factor_fwd: CSR scatter + block LU + W forward sweep */
+    SPK_PH_FACTOR_BWD = 2, /* k_factor_bwd + k_tips: spike backward sweeps */
+    SPK_PH_RED_FACTOR = 3, /* cyclic reduction of the reduced system */
+    SPK_PH_APPLY = 4,      /* k_apply + k_ytips: y = A_i^{-1} r */
+    SPK_PH_RED_SOLVE = 5,  /* reduced solve with FP64 refinement */
+    SPK_PH_RETRIEVE = 6,   /* k_retrieve */
+    SPK_PH_RESIDUAL = 7,   /* k_residual: FP64 r = b - A x */
+    SPK_NPHASES = 8
+};
+#define SPK_MAX_EVENTS 64
+
 /* device error word bits, written by kernels with atomicOr */
 #define SPK_DEV_ERR_PIVOT 1u
 #define SPK_DEV_ERR_BAND 2u
@@ -85,7 +99,21 @@ typedef struct spk_plan {
     /* bookkeeping */
     long long launches; /* kernel launches issued for this plan */
     size_t bytes;       /* device bytes held */
+    /* optional per-phase CUDA-event timing (SPIKE_OPT_PHASE_TIMING) */
+    int timing;
+    void *ev;                          /* SPK_MAX_EVENTS cudaEvent_t pairs */
+    int ev_phase[SPK_MAX_EVENTS];
+    int nev;
+    double phase_ms[SPK_NPHASES];
+    long long phase_calls[SPK_NPHASES];
 } spk_plan;
+
+/* phase timing: begin/end record events on the stream; collect (after a
+ * stream synchronize) adds the elapsed times to phase_ms / phase_calls */
+void spk_phase_begin(spk_plan *P, int phase, void *stream);
+void spk_phase_end(spk_plan *P, void *stream);
+int spk_phase_collect(spk_plan *P);
+void spk_phase_destroy(spk_plan *P);
 
 /* ---- device / memory (spike_util.cu) ---- */
 int spk_device_count(void);

@@ -11,6 +11,7 @@
 #include "spike_common.cuh"
 
 #include <stdio.h>
+#include <stdlib.h>
 
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
 
@@ -294,4 +295,50 @@ extern "C" int spk_residual(const spk_plan *P, const int *d_rowptr, const int *d
     if (P->is_complex)
         return residual_g<cdouble>(P, d_rowptr, d_colind, d_aij, d_x, d_b, d_r, nrhs, want_bnorm, d_norms, st);
     return residual_g<double>(P, d_rowptr, d_colind, d_aij, d_x, d_b, d_r, nrhs, want_bnorm, d_norms, st);
+}
+
+// ------------------------------------------------------------ phase timing
+extern "C" void spk_phase_begin(spk_plan *P, int phase, void *stream)
+{
+    if (!P->timing) return;
+    if (!P->ev) {
+        cudaEvent_t *ev = (cudaEvent_t *)calloc(2 * SPK_MAX_EVENTS, sizeof(cudaEvent_t));
+        if (!ev) return;
+        for (int i = 0; i < 2 * SPK_MAX_EVENTS; i++) cudaEventCreate(&ev[i]);
+        P->ev = ev;
+        P->nev = 0;
+    }
+    if (P->nev >= SPK_MAX_EVENTS) spk_phase_collect(P);
+    cudaEvent_t *ev = (cudaEvent_t *)P->ev;
+    P->ev_phase[P->nev] = phase;
+    cudaEventRecord(ev[2 * P->nev], (cudaStream_t)stream);
+}
+extern "C" void spk_phase_end(spk_plan *P, void *stream)
+{
+    if (!P->timing || !P->ev) return;
+    cudaEvent_t *ev = (cudaEvent_t *)P->ev;
+    cudaEventRecord(ev[2 * P->nev + 1], (cudaStream_t)stream);
+    P->nev++;
+}
+extern "C" int spk_phase_collect(spk_plan *P)
+{
+    if (!P->ev) return SPK_OK;
+    cudaEvent_t *ev = (cudaEvent_t *)P->ev;
+    for (int i = 0; i < P->nev; i++) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(ev[2 * i + 1]) != cudaSuccess) return SPK_ECUDA;
+        if (cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]) != cudaSuccess) return SPK_ECUDA;
+        P->phase_ms[P->ev_phase[i]] += ms;
+        P->phase_calls[P->ev_phase[i]]++;
+    }
+    P->nev = 0;
+    return SPK_OK;
+}
+extern "C" void spk_phase_destroy(spk_plan *P)
+{
+    if (!P->ev) return;
+    cudaEvent_t *ev = (cudaEvent_t *)P->ev;
+    for (int i = 0; i < 2 * SPK_MAX_EVENTS; i++) cudaEventDestroy(ev[i]);
+    free(ev);
+    P->ev = NULL;
 }

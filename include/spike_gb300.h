@@ -37,6 +37,7 @@ typedef struct spike_factor_s *spike_factor_t;
 #define SPIKE_OPT_MAX_REFINE 2     /* correction sweeps after the first solve (default 3) */
 #define SPIKE_OPT_TOLERANCE 3      /* relative residual target (default 1e-12) */
 #define SPIKE_OPT_REDUCED_REFINE 4 /* FP64 refinement sweeps on the reduced system (default 2 mixed, 1 FP64) */
+#define SPIKE_OPT_PHASE_TIMING 5   /* 1 = time each kernel family with CUDA events (default 0) */
 
 #define SPIKE_PRECISION_MIXED 0 /* FP32 / complex64 factors, FP64 residual + update + reduced solve */
 #define SPIKE_PRECISION_FP64 1  /* FP64 / complex128 everywhere */
@@ -73,6 +74,16 @@ typedef struct {
     size_t device_bytes;      /* device memory held by the context's plan */
 } spike_info_t;
 Error_t spike_get_info(spike_context_t ctx, spike_info_t *info);
+
+/* Per-kernel-family device time accumulated while SPIKE_OPT_PHASE_TIMING is
+ * on, measured with CUDA events on the context's stream.  Families, in order:
+ *   0 analysis, 1 factor forward (CSR scatter + block LU + W sweep),
+ *   2 factor backward (spike sweeps + tips), 3 reduced factorization,
+ *   4 right-hand-side sweeps, 5 reduced solve, 6 retrieval, 7 FP64 residual.
+ * ms[i] is the summed time and calls[i] the number of timed launches of
+ * family i (nphases <= 8); reset = 1 clears the accumulators afterwards. */
+#define SPIKE_NUM_PHASES 8
+Error_t spike_get_phase_times(spike_context_t ctx, int nphases, double *ms, long long *calls, int reset);
 
 /* ---- device-pointer solves: every array already in device memory ---- */
 Error_t spike_dsolve_device(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs,
