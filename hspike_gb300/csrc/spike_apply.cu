@@ -18,12 +18,13 @@ namespace {
 constexpr int RC = 32; // right-hand-side columns per CTA
 
 // out[r][h] = sign * sum_k M[r][k] v[k][h] (+ base[r][h]), r < KB, h < nr.
-// M: shared tile (LD = KB+1); v, base, out: shared [KB][RC].
+// Mt: shared tile holding M transposed (the factor tiles are column-major in
+// global memory); v, base, out: shared [KB][RC].
 template <class T, int KB, bool HAS_BASE>
-__device__ void tile_mv(T *out, const T *M, const T *v, const T *base, int nr, bool negate)
+__device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, bool negate)
 {
     constexpr int NT = NTOf<KB>::value;
-    constexpr int LD = KB + 1;
+    constexpr int LD = TileLD<T, KB>::value;
     const int O = KB * nr;
     int spl = 1;
     while (spl < 32 && spl * 2 * O <= NT && spl * 2 <= KB) spl *= 2;
@@ -39,7 +40,7 @@ __device__ void tile_mv(T *out, const T *M, const T *v, const T *base, int nr, b
         if (o < O) {
             r = o / nr;
             h = o - r * nr;
-            for (int k = part; k < KB; k += spl) acc = madd(acc, M[r * LD + k], v[k * RC + h]);
+            for (int k = part; k < KB; k += spl) acc = madd(acc, Mt[k * LD + r], v[k * RC + h]);
         }
         for (int off = spl >> 1; off > 0; off >>= 1) {
             if constexpr (sizeof(T) == 4) {
@@ -65,11 +66,7 @@ __device__ void tile_mv(T *out, const T *M, const T *v, const T *base, int nr, b
 
 template <class T, int KB> __device__ void load_tile_s(T *s, const T *g)
 {
-    constexpr int NT = NTOf<KB>::value;
-    for (int q = threadIdx.x; q < KB * KB; q += NT) {
-        const int r = q / KB, c = q - r * KB;
-        s[r * (KB + 1) + c] = g[q];
-    }
+    copy_tile_g2s<T, KB, NTOf<KB>::value>(s, g);
 }
 
 template <class T, int KB>
@@ -81,7 +78,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     using H = typename HighOf<T>::type;
     constexpr int NT = NTOf<KB>::value;
     constexpr size_t TS = (size_t)KB * KB;
-    constexpr int LDT = KB + 1;
+    constexpr int LDT = TileLD<T, KB>::value;
     const int part = blockIdx.x;
     const int h0 = blockIdx.y * RC;
     const int nr = min(RC, nrhs - h0);
@@ -219,7 +216,7 @@ __global__ void __launch_bounds__(256)
 template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
     constexpr int NT = NTOf<KB>::value;
-    const size_t smem = 16 + sizeof(T) * (2 * KB * (KB + 1) + 3 * KB * RC);
+    const size_t smem = 16 + sizeof(T) * (2 * KB * TileLD<T, KB>::value + 3 * KB * RC);
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -3,8 +3,8 @@
 //
 // Every dense block of the block-tridiagonal view of A_i is a KB x KB tile.
 // A CTA of NT threads owns one tile operation at a time; each active thread
-// holds a TR x TC register sub-tile at rows ty + i*TY, columns tx + j*TX
-// (strided so that a warp's shared-memory reads are conflict-free).  Shared
+// holds a contiguous TR x TC register sub-tile, so operand fetches are
+// 8/16-byte vectors.  Shared
 // memory tiles are row-major with stride LD = KB + 1.
 #pragma once
 #include <cuda_runtime.h>
@@ -67,6 +67,19 @@ SPK_HD cdouble sc_recip(cdouble a)
     double s = 1.0 / (a.re * a.re + a.im * a.im);
     return {a.re * s, -a.im * s};
 }
+// correctly rounded reciprocal without the IEEE-division slow path
+__device__ __forceinline__ float sc_frcp(float a) { return __frcp_rn(a); }
+__device__ __forceinline__ double sc_frcp(double a) { return __drcp_rn(a); }
+__device__ __forceinline__ cfloat sc_frcp(cfloat a)
+{
+    const float s = __frcp_rn(fmaf(a.re, a.re, a.im * a.im));
+    return {a.re * s, -a.im * s};
+}
+__device__ __forceinline__ cdouble sc_frcp(cdouble a)
+{
+    const double s = __drcp_rn(fma(a.re, a.re, a.im * a.im));
+    return {a.re * s, -a.im * s};
+}
 SPK_HD double sc_abs2(float a) { return (double)a * a; }
 SPK_HD double sc_abs2(double a) { return a * a; }
 SPK_HD double sc_abs2(cfloat a) { return (double)a.re * a.re + (double)a.im * a.im; }
@@ -97,70 +110,162 @@ template <int KB> struct NTOf {
     static constexpr int value = KB >= 64 ? 256 : KB == 32 ? 128 : KB == 16 ? 64 : 32;
 };
 
+// ------------------------------------------------------------ vector access
+// N contiguous elements (N in {1, 2, 4}) between registers and memory in
+// 8- or 16-byte transactions.  The pointer must be aligned to
+// min(16, N * sizeof(T)) bytes.
+template <class T> __device__ __forceinline__ T from_f2(float x, float y);
+template <> __device__ __forceinline__ double from_f2<double>(float x, float y)
+{
+    return __hiloint2double(__float_as_int(y), __float_as_int(x));
+}
+template <> __device__ __forceinline__ cfloat from_f2<cfloat>(float x, float y) { return {x, y}; }
+__device__ __forceinline__ float2 to_f2(double d)
+{
+    return make_float2(__int_as_float(__double2loint(d)), __int_as_float(__double2hiint(d)));
+}
+__device__ __forceinline__ float2 to_f2(cfloat c) { return make_float2(c.re, c.im); }
+
+template <class T, int N> __device__ __forceinline__ void vld(T (&d)[N], const T *p)
+{
+    if constexpr (sizeof(T) == 4 && N == 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(p);
+        d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+    } else if constexpr (sizeof(T) == 4 && N == 2) {
+        const float2 v = *reinterpret_cast<const float2 *>(p);
+        d[0] = v.x; d[1] = v.y;
+    } else if constexpr (sizeof(T) == 8 && N >= 2) {
+#pragma unroll
+        for (int q = 0; q < N / 2; q++) {
+            const float4 v = reinterpret_cast<const float4 *>(p)[q];
+            d[2 * q] = from_f2<T>(v.x, v.y);
+            d[2 * q + 1] = from_f2<T>(v.z, v.w);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < N; q++) d[q] = p[q];
+    }
+}
+template <class T, int N> __device__ __forceinline__ void vst(T *p, const T (&d)[N])
+{
+    if constexpr (sizeof(T) == 4 && N == 4) {
+        *reinterpret_cast<float4 *>(p) = make_float4(d[0], d[1], d[2], d[3]);
+    } else if constexpr (sizeof(T) == 4 && N == 2) {
+        *reinterpret_cast<float2 *>(p) = make_float2(d[0], d[1]);
+    } else if constexpr (sizeof(T) == 8 && N >= 2) {
+#pragma unroll
+        for (int q = 0; q < N / 2; q++) {
+            const float2 a = to_f2(d[2 * q]), b = to_f2(d[2 * q + 1]);
+            reinterpret_cast<float4 *>(p)[q] = make_float4(a.x, a.y, b.x, b.y);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < N; q++) p[q] = d[q];
+    }
+}
+
+// shared-memory row stride of a KB x KB tile: 16 bytes of padding keeps every
+// row 16-byte aligned and shifts consecutive rows across banks
+template <class T, int KB> struct TileLD {
+    static constexpr int value = KB + (16 / (int)sizeof(T) > 0 ? 16 / (int)sizeof(T) : 1);
+};
+
 // ------------------------------------------------------------ tile geometry
+// Thread (tx, ty) owns the contiguous TR x TC sub-tile at rows ty*TR + i,
+// columns tx*TC + j.  Operand fetches are vectors: a row-major right operand
+// gives TC contiguous elements per k, a left operand stored transposed
+// (column-major, "At") gives TR contiguous elements per k.
 template <class T, int KB, int NT> struct Tile {
     static constexpr int TX = KB < 16 ? KB : 16;
     static constexpr int TY0 = NT / TX;
     static constexpr int TY = TY0 < KB ? TY0 : KB;
     static constexpr int TC = KB / TX;
     static constexpr int TR = KB / TY;
-    static constexpr int LD = KB + 1;        // shared-memory row stride
-    static constexpr int ELEMS = KB * LD;    // shared-memory tile size
-    static constexpr int ACTIVE = TX * TY;   // threads that own a sub-tile
+    static constexpr int LD = TileLD<T, KB>::value; // shared-memory row stride
+    static constexpr int ELEMS = KB * LD;           // shared-memory tile size
+    static constexpr int ACTIVE = TX * TY;          // threads that own a sub-tile
+    // the blocked inverse runs when every thread owns a 4 x 4 sub-tile
+    static constexpr bool BLOCK4 = (TR == 4 && TC == 4);
+    static constexpr int INV_HALF = 8 * KB + 16;   // pivot columns + P^{-1} + pivot rows
+    static constexpr int INV_BUF = BLOCK4 ? 2 * INV_HALF + KB : 4 * KB; // shared scratch elements for inverse()
 
     using Reg = T[TR][TC];
 
     int tx, ty;
     bool act;
-    __device__ Tile(int tid)
+    __device__ __forceinline__ Tile(int tid)
     {
         act = tid < ACTIVE;
         tx = tid % TX;
         ty = tid / TX;
     }
-    __device__ int row(int i) const { return ty + i * TY; }
-    __device__ int col(int j) const { return tx + j * TX; }
+    __device__ __forceinline__ int row(int i) const { return ty * TR + i; }
+    __device__ __forceinline__ int col(int j) const { return tx * TC + j; }
 
-    __device__ void rzero(Reg &a) const
+    __device__ __forceinline__ void rzero(Reg &a) const
     {
 #pragma unroll
         for (int i = 0; i < TR; i++)
 #pragma unroll
             for (int j = 0; j < TC; j++) a[i][j] = sc_zero<T>();
     }
-    // register tile <- shared tile (threads without a sub-tile hold zeros and
-    // never touch shared memory: their row() is past the tile)
-    __device__ void rload(Reg &a, const T *s) const
+    __device__ __forceinline__ void ridentity(Reg &a) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++)
+#pragma unroll
+            for (int j = 0; j < TC; j++) a[i][j] = (row(i) == col(j)) ? sc_one<T>() : sc_zero<T>();
+    }
+    // register tile <- shared tile (threads without a sub-tile hold zeros)
+    __device__ __forceinline__ void rload(Reg &a, const T *s) const
     {
         if (!act) {
             rzero(a);
             return;
         }
 #pragma unroll
-        for (int i = 0; i < TR; i++)
-#pragma unroll
-            for (int j = 0; j < TC; j++) a[i][j] = s[row(i) * LD + col(j)];
+        for (int i = 0; i < TR; i++) vld<T, TC>(a[i], s + row(i) * LD + col(0));
     }
-    // shared tile <- register tile (alpha * a)
-    __device__ void rstore(T *s, const Reg &a) const
+    // shared tile <- register tile
+    __device__ __forceinline__ void rstore(T *s, const Reg &a) const
     {
         if (!act) return;
 #pragma unroll
-        for (int i = 0; i < TR; i++)
+        for (int i = 0; i < TR; i++) vst<T, TC>(s + row(i) * LD + col(0), a[i]);
+    }
+    // shared tile, transposed (column-major: element (r, c) at c*LD + r) <- register tile
+    __device__ __forceinline__ void rstore_t(T *s, const Reg &a) const
+    {
+        if (!act) return;
 #pragma unroll
-            for (int j = 0; j < TC; j++) s[row(i) * LD + col(j)] = a[i][j];
+        for (int j = 0; j < TC; j++) {
+            T c[TR];
+#pragma unroll
+            for (int i = 0; i < TR; i++) c[i] = a[i][j];
+            vst<T, TR>(s + col(j) * LD + row(0), c);
+        }
     }
     // dense global tile (row-major, ld KB) <- register tile
-    __device__ void gstore(T *g, const Reg &a) const
+    __device__ __forceinline__ void gstore(T *g, const Reg &a) const
     {
         if (!act) return;
 #pragma unroll
-        for (int i = 0; i < TR; i++)
-#pragma unroll
-            for (int j = 0; j < TC; j++) g[row(i) * KB + col(j)] = a[i][j];
+        for (int i = 0; i < TR; i++) vst<T, TC>(g + row(i) * KB + col(0), a[i]);
     }
-    // acc += A * B (A, B shared tiles)
-    __device__ void mma(Reg &acc, const T *A, const T *B) const
+    // dense global tile, column-major (element (r, c) at c*KB + r) <- register tile
+    __device__ __forceinline__ void gstore_t(T *g, const Reg &a) const
+    {
+        if (!act) return;
+#pragma unroll
+        for (int j = 0; j < TC; j++) {
+            T c[TR];
+#pragma unroll
+            for (int i = 0; i < TR; i++) c[i] = a[i][j];
+            vst<T, TR>(g + col(j) * KB + row(0), c);
+        }
+    }
+    // acc (+|-)= A * B, A row-major in shared memory (scalar fetches)
+    template <bool SUB> __device__ __forceinline__ void mm_rowA(Reg &acc, const T *A, const T *B) const
     {
         if (!act) return;
 #pragma unroll 4
@@ -168,82 +273,237 @@ template <class T, int KB, int NT> struct Tile {
             T a[TR], b[TC];
 #pragma unroll
             for (int i = 0; i < TR; i++) a[i] = A[row(i) * LD + k];
-#pragma unroll
-            for (int j = 0; j < TC; j++) b[j] = B[k * LD + col(j)];
+            vld<T, TC>(b, B + k * LD + col(0));
 #pragma unroll
             for (int i = 0; i < TR; i++)
 #pragma unroll
-                for (int j = 0; j < TC; j++) acc[i][j] = madd(acc[i][j], a[i], b[j]);
+                for (int j = 0; j < TC; j++) acc[i][j] = SUB ? msub(acc[i][j], a[i], b[j]) : madd(acc[i][j], a[i], b[j]);
         }
     }
-    // acc -= A * B
-    __device__ void mms(Reg &acc, const T *A, const T *B) const
+    // acc (+|-)= A * B with A given transposed (At, column-major): vector fetches
+    template <bool SUB> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
     {
         if (!act) return;
 #pragma unroll 4
         for (int k = 0; k < KB; k++) {
             T a[TR], b[TC];
-#pragma unroll
-            for (int i = 0; i < TR; i++) a[i] = A[row(i) * LD + k];
-#pragma unroll
-            for (int j = 0; j < TC; j++) b[j] = B[k * LD + col(j)];
+            vld<T, TR>(a, At + k * LD + row(0));
+            vld<T, TC>(b, B + k * LD + col(0));
 #pragma unroll
             for (int i = 0; i < TR; i++)
 #pragma unroll
-                for (int j = 0; j < TC; j++) acc[i][j] = msub(acc[i][j], a[i], b[j]);
+                for (int j = 0; j < TC; j++) acc[i][j] = SUB ? msub(acc[i][j], a[i], b[j]) : madd(acc[i][j], a[i], b[j]);
         }
     }
+    __device__ __forceinline__ void mma(Reg &acc, const T *A, const T *B) const { mm_rowA<false>(acc, A, B); }
+    __device__ __forceinline__ void mms(Reg &acc, const T *A, const T *B) const { mm_rowA<true>(acc, A, B); }
+    __device__ __forceinline__ void mma_t(Reg &acc, const T *At, const T *B) const { mm_tA<false>(acc, At, B); }
+    __device__ __forceinline__ void mms_t(Reg &acc, const T *At, const T *B) const { mm_tA<true>(acc, At, B); }
 
     // In-place Gauss-Jordan inverse of the register tile, no pivoting (the
     // diagonal blocks of a diagonally dominant A stay diagonally dominant
-    // under block elimination).  buf: 4*KB scratch elements of shared memory.
-    // All NT threads must call.  Returns false in every thread if a pivot was
-    // zero or not finite.
-    __device__ bool inverse(Reg &s, T *buf) const
+    // under block elimination).  Step j, with p = S[j][j], a = column j and
+    // b = row j:
+    //     S[r][c] <- S[r][c] - a[r] b[c] / p     r != j, c != j
+    //     S[j][c] <- b[c] / p,   S[r][j] <- -a[r] / p,   S[j][j] <- 1 / p
+    // The owners of row j / column j publish them as vectors into a double-
+    // buffered shared scratch, so each pivot costs one barrier; every element
+    // then takes one FMA, and only the owners of row j / column j patch it.
+    // buf: INV_BUF elements of shared memory (16-byte aligned).  All NT
+    // threads must call.  Returns false in every thread if a pivot was zero
+    // or not finite.
+    __device__ __forceinline__ bool inverse(Reg &s, T *buf) const
+    {
+        if constexpr (BLOCK4)
+            return inverse_b4(s, buf);
+        else
+            return inverse_r1(s, buf);
+    }
+
+    // Blocked Gauss-Jordan with 4 x 4 pivot blocks, each the sub-tile of one
+    // thread.  With P the pivot block, U the pivot columns, B the pivot rows,
+    // every element takes the same update
+    //     S <- S - U' V',  U' = U - I (on the pivot rows),  V' = P^{-1} (B + I (on the pivot columns))
+    // which yields P^{-1} on the pivot block, P^{-1} B on the pivot rows,
+    // -U P^{-1} on the pivot columns and S - U P^{-1} B elsewhere.  Rows are
+    // scaled to a unit diagonal first (and the inverse's columns back after),
+    // so the pivot blocks stay O(1) and the I terms cancel nothing large.
+    // Per 4 pivots: the pivot owner inverts P, the pivot-row owners form V',
+    // everyone applies 64 FMAs; two barriers.
+    __device__ __forceinline__ bool inverse_b4(Reg &s, T *buf) const
     {
         bool ok = true;
-        for (int j = 0; j < KB; j++) {
-            T *rb = buf + (j & 1) * 2 * KB;
-            T *cb = rb + KB;
-            if (act) {
-                const int jr = j % TY, ir = j / TY;
-                const int jc = j % TX, ic = j / TX;
-                if (ty == jr) {
+        T *dg = buf + 2 * INV_HALF; // diagonal
+        if (act && tx == ty) {
+            T d[4];
 #pragma unroll
-                    for (int i = 0; i < TR; i++)
-                        if (i == ir)
+            for (int i = 0; i < 4; i++) d[i] = s[i][i];
+            vst<T, 4>(dg + row(0), d);
+        }
+        __syncthreads();
+        T dr[4];
+        if (act) {
+            vld<T, 4>(dr, dg + row(0));
 #pragma unroll
-                            for (int jj = 0; jj < TC; jj++) rb[col(jj)] = s[i][jj];
+            for (int i = 0; i < 4; i++) {
+                if (!sc_finite_nonzero(dr[i])) ok = false;
+                const T rr = sc_frcp(dr[i]);
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) s[i][jj] = s[i][jj] * rr;
+            }
+        }
+        for (int q = 0; q < KB / 4; q++) {
+            T *cbuf = buf + (q & 1) * INV_HALF; // [KB][4] pivot columns U'
+            T *pbuf = cbuf + 4 * KB;            // [4][4] P^{-1}
+            T *vbuf = pbuf + 16;                // [4][KB] V'
+            const bool rown = act && ty == q, cown = act && tx == q;
+            if (cown) {
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    T u[4];
+#pragma unroll
+                    for (int t = 0; t < 4; t++) u[t] = (rown && t == i) ? s[i][t] - sc_one<T>() : s[i][t];
+                    vst<T, 4>(cbuf + row(i) * 4, u);
                 }
-                if (tx == jc) {
+                if (rown) { // pivot owner: P^{-1} by unblocked Gauss-Jordan in registers
+                    T pinv[4][4];
 #pragma unroll
-                    for (int jj = 0; jj < TC; jj++)
-                        if (jj == ic)
+                    for (int a = 0; a < 4; a++)
 #pragma unroll
-                            for (int i = 0; i < TR; i++) cb[row(i)] = s[i][jj];
+                        for (int b = 0; b < 4; b++) pinv[a][b] = s[a][b];
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const T piv = pinv[k][k];
+                        if (!sc_finite_nonzero(piv)) ok = false;
+                        const T pr = sc_frcp(piv);
+#pragma unroll
+                        for (int b = 0; b < 4; b++)
+                            if (b != k) pinv[k][b] = pinv[k][b] * pr;
+#pragma unroll
+                        for (int a = 0; a < 4; a++)
+                            if (a != k) {
+                                const T f = pinv[a][k];
+#pragma unroll
+                                for (int b = 0; b < 4; b++)
+                                    if (b != k) pinv[a][b] = msub(pinv[a][b], f, pinv[k][b]);
+                                pinv[a][k] = -(f * pr);
+                            }
+                        pinv[k][k] = pr;
+                    }
+#pragma unroll
+                    for (int a = 0; a < 4; a++) vst<T, 4>(pbuf + 4 * a, pinv[a]);
+                }
+            }
+            __syncthreads();
+            if (rown) { // V' = P^{-1} (B + I on the pivot columns) for this thread's columns
+                T pi[4][4];
+#pragma unroll
+                for (int a = 0; a < 4; a++) vld<T, 4>(pi[a], pbuf + 4 * a);
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    T v[4];
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        T acc = sc_zero<T>();
+#pragma unroll
+                        for (int a = 0; a < 4; a++) {
+                            const T bb = (cown && a == jj) ? s[a][jj] + sc_one<T>() : s[a][jj];
+                            acc = madd(acc, pi[t][a], bb);
+                        }
+                        v[jj] = acc;
+                    }
+                    vst<T, 4>(vbuf + t * KB + col(0), v);
                 }
             }
             __syncthreads();
             if (act) {
-                T piv = rb[j];
-                if (!sc_finite_nonzero(piv)) ok = false;
-                T p = sc_recip(piv);
-                T rp[TC];
+                T u[4][4], v[4][4];
 #pragma unroll
-                for (int jj = 0; jj < TC; jj++) rp[jj] = rb[col(jj)] * p;
+                for (int i = 0; i < 4; i++) vld<T, 4>(u[i], cbuf + row(i) * 4);
 #pragma unroll
-                for (int i = 0; i < TR; i++) {
-                    const int r = row(i);
-                    const T f = cb[r];
+                for (int t = 0; t < 4; t++) vld<T, 4>(v[t], vbuf + t * KB + col(0));
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        T acc = s[i][jj];
+#pragma unroll
+                        for (int t = 0; t < 4; t++) acc = msub(acc, u[i][t], v[t][jj]);
+                        s[i][jj] = acc;
+                    }
+            }
+        }
+        // columns of the inverse back by the diagonal: S^{-1} = (D^{-1} S)^{-1} D^{-1}
+        if (act) {
+            T dc[4];
+            vld<T, 4>(dc, dg + col(0));
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) {
+                const T rc = sc_frcp(dc[jj]);
+#pragma unroll
+                for (int i = 0; i < 4; i++) s[i][jj] = s[i][jj] * rc;
+            }
+        }
+        __syncthreads();
+        return __syncthreads_and(ok ? 1 : 0) != 0;
+    }
+
+    __device__ __forceinline__ bool inverse_r1(Reg &s, T *buf) const
+    {
+        bool ok = true;
+        for (int j = 0; j < KB; j++) {
+            T *rb = buf + (j & 1) * 2 * KB; // row j
+            T *cb = rb + KB;                // column j
+            const int jr = j / TR, ir = j - jr * TR; // owner row group / slot
+            const int jc = j / TC, ic = j - jc * TC; // owner column group / slot
+            if (act) {
+                if (ty == jr) {
+                    T v[TC];
 #pragma unroll
                     for (int jj = 0; jj < TC; jj++) {
-                        const int c = col(jj);
-                        T v;
-                        if (r == j)
-                            v = (c == j) ? p : rp[jj];
-                        else
-                            v = (c == j) ? -(f * p) : msub(s[i][jj], f, rp[jj]);
-                        s[i][jj] = v;
+                        v[jj] = s[0][jj];
+#pragma unroll
+                        for (int i = 1; i < TR; i++) v[jj] = (i == ir) ? s[i][jj] : v[jj];
+                    }
+                    vst<T, TC>(rb + col(0), v);
+                }
+                if (tx == jc) {
+                    T v[TR];
+#pragma unroll
+                    for (int i = 0; i < TR; i++) {
+                        v[i] = s[i][0];
+#pragma unroll
+                        for (int jj = 1; jj < TC; jj++) v[i] = (jj == ic) ? s[i][jj] : v[i];
+                    }
+                    vst<T, TR>(cb + row(0), v);
+                }
+            }
+            __syncthreads();
+            if (act) {
+                const T piv = cb[j];
+                if (!sc_finite_nonzero(piv)) ok = false;
+                const T pr = sc_frcp(piv);
+                T bv[TC], av[TR];
+                vld<T, TC>(bv, rb + col(0));
+                vld<T, TR>(av, cb + row(0));
+#pragma unroll
+                for (int jj = 0; jj < TC; jj++) bv[jj] = bv[jj] * pr; // b[c] / p
+#pragma unroll
+                for (int i = 0; i < TR; i++)
+#pragma unroll
+                    for (int jj = 0; jj < TC; jj++) s[i][jj] = msub(s[i][jj], av[i], bv[jj]);
+                if (ty == jr) { // row j <- b / p
+#pragma unroll
+                    for (int i = 0; i < TR; i++)
+#pragma unroll
+                        for (int jj = 0; jj < TC; jj++) s[i][jj] = (i == ir) ? bv[jj] : s[i][jj];
+                }
+                if (tx == jc) { // column j <- -a / p, pivot <- 1 / p
+#pragma unroll
+                    for (int i = 0; i < TR; i++) {
+                        const T cv = (row(i) == j) ? pr : -(av[i] * pr);
+#pragma unroll
+                        for (int jj = 0; jj < TC; jj++) s[i][jj] = (jj == ic) ? cv : s[i][jj];
                     }
                 }
             }
@@ -252,6 +512,36 @@ template <class T, int KB, int NT> struct Tile {
         return __syncthreads_and(ok ? 1 : 0) != 0;
     }
 };
+
+// Dense global tile (KB*KB elements, 16-byte aligned) -> shared tile with row
+// stride TileLD (the element order is kept: a column-major global tile lands
+// as a transposed shared tile).  Every thread issues all of its 16-byte loads
+// before its first shared-memory store, so a tile costs one memory round trip.
+template <class T, int KB, int NT> __device__ __forceinline__ void copy_tile_g2s(T *s, const T *g)
+{
+    constexpr int EPC = 16 / sizeof(T) > 0 ? 16 / sizeof(T) : 1; // elements per 16-byte chunk
+    constexpr int CH = KB * KB / EPC;                             // chunks per tile
+    constexpr int PER = (CH + NT - 1) / NT;                       // chunks per thread
+    const uint4 *src = reinterpret_cast<const uint4 *>(g);
+    uint4 buf[PER];
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int c = threadIdx.x + i * NT;
+        if (c < CH) buf[i] = __ldg(src + c);
+    }
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+        const int c = threadIdx.x + i * NT;
+        if (c < CH) {
+            const T *e = reinterpret_cast<const T *>(&buf[i]);
+#pragma unroll
+            for (int k = 0; k < EPC; k++) {
+                const int q = c * EPC + k, r = q / KB, cc = q - r * KB;
+                s[r * TileLD<T, KB>::value + cc] = e[k];
+            }
+        }
+    }
+}
 
 // 16-byte-aligned carve-up of dynamic shared memory
 __device__ __forceinline__ char *smem_align(char *p)

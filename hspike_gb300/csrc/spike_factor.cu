@@ -30,35 +30,58 @@ namespace {
 template <class T, int KB> struct FactorSmem {
     using TL = Tile<T, KB, NTOf<KB>::value>;
     static constexpr size_t tile = sizeof(T) * TL::ELEMS;
-    static constexpr size_t fwd = 6 * tile + sizeof(T) * 4 * KB + 64;
+    static constexpr size_t fwd = 6 * tile + sizeof(T) * TL::INV_BUF + sizeof(int) * (KB + 1) + 64;
     static constexpr size_t bwd = 6 * tile + 64;
 };
 
 // Scatter the CSR rows of block J of partition [s, e) into the shared tiles.
-// F: columns of block J-1, D: block J, En: block J+1, Z: C^ coupling (J == 0,
-// columns s-KB..s-1), Bhat (global, row-major): B^ coupling (columns e..e+KB-1)
+// F: columns of block J-1 (stored transposed: it is the left operand of
+// F G), D: block J, En: block J+1, Z: C^ coupling (J == 0,
+// columns s-KB..s-1), Bhat (global, row-major): B^ coupling (columns e..e+KB-1).
+// The block's entries are one contiguous CSR range: the CTA walks it with
+// coalesced, unrolled loads (several in flight per thread) and finds each
+// entry's row by binary search in the block's row-pointer slice srp[].
 template <class T, class H, int KB>
-__device__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
+__device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
                               const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *Z,
-                              T *gBhat, unsigned *err)
+                              T *gBhat, unsigned *err, int *srp)
 {
     constexpr int NT = NTOf<KB>::value;
-    constexpr int LD = KB + 1;
+    constexpr int LD = TileLD<T, KB>::value;
+    constexpr int U = 4;
     const int m = e - s;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int NW = NT / 32;
-    for (int lr = warp; lr < KB; lr += NW) {
-        const int lrow = J * KB + lr; // partition-local row
-        if (lrow >= m) {
-            if (lane == 0) D[lr * LD + lr] = sc_one<T>();
-            continue;
+    const int lrow0 = J * KB;
+    const int nr = min(KB, m - lrow0); // real rows in the block, >= 1
+    for (int q = threadIdx.x; q <= nr; q += NT) srp[q] = rowptr[s + lrow0 + q];
+    for (int lr = nr + threadIdx.x; lr < KB; lr += NT) D[lr * LD + lr] = sc_one<T>(); // identity padding
+    __syncthreads();
+    const int t0 = srp[0], t1 = srp[nr];
+    for (int base = t0; base < t1; base += U * NT) {
+        int cidx[U];
+        H val[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int t = base + threadIdx.x + u * NT;
+            if (t < t1) {
+                cidx[u] = __ldg(colind + t);
+                val[u] = aij[t];
+            }
         }
-        const int g = s + lrow;
-        const int t0 = rowptr[g], t1 = rowptr[g + 1];
-        for (int t = t0 + lane; t < t1; t += 32) {
-            const int c = colind[t];
-            const T v = sc_cvt<T, H>(aij[t]);
-            const int lc = c - s;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int t = base + threadIdx.x + u * NT;
+            if (t >= t1) continue;
+            int lo = 0, hi = nr; // srp[lo] <= t < srp[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (srp[mid] <= t)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            const int lr = lo, lrow = lrow0 + lr;
+            const T v = sc_cvt<T, H>(val[u]);
+            const int lc = cidx[u] - s;
             if (lc < 0) {
                 const int cc = lc + KB;
                 if (cc >= 0 && lrow < KB) {
@@ -77,7 +100,7 @@ __device__ void scatter_block(const int *__restrict__ rowptr, const int *__restr
                 if (d == 0)
                     D[lr * LD + cc] = v;
                 else if (d == -1)
-                    F[lr * LD + cc] = v;
+                    F[cc * LD + lr] = v;
                 else if (d == 1)
                     En[lr * LD + cc] = v;
                 else
@@ -87,37 +110,34 @@ __device__ void scatter_block(const int *__restrict__ rowptr, const int *__restr
     }
 }
 
-template <class T, int KB> __device__ void zero_tile(T *s)
+template <class T, int KB> __device__ __forceinline__ void zero_tile(T *s)
 {
     constexpr int NT = NTOf<KB>::value;
-    for (int q = threadIdx.x; q < KB * (KB + 1); q += NT) s[q] = sc_zero<T>();
+    for (int q = threadIdx.x; q < KB * TileLD<T, KB>::value; q += NT) s[q] = sc_zero<T>();
 }
 
 // shared tile -> dense global tile (row-major)
-template <class T, int KB> __device__ void store_tile(T *g, const T *s)
+template <class T, int KB> __device__ __forceinline__ void store_tile(T *g, const T *s)
 {
     constexpr int NT = NTOf<KB>::value;
     for (int q = threadIdx.x; q < KB * KB; q += NT) {
         const int r = q / KB, c = q - r * KB;
-        g[q] = s[r * (KB + 1) + c];
+        g[q] = s[r * TileLD<T, KB>::value + c];
     }
 }
 // dense global tile (row-major) -> shared tile
-template <class T, int KB> __device__ void load_tile(T *s, const T *g)
+template <class T, int KB> __device__ __forceinline__ void load_tile(T *s, const T *g)
 {
-    constexpr int NT = NTOf<KB>::value;
-    for (int q = threadIdx.x; q < KB * KB; q += NT) {
-        const int r = q / KB, c = q - r * KB;
-        s[r * (KB + 1) + c] = g[q];
-    }
+    copy_tile_g2s<T, KB, NTOf<KB>::value>(s, g);
 }
-// shared tile -> global tile, column-major (for the retrieval's coalesced reads)
-template <class T, int KB> __device__ void store_tile_cm(T *g, const T *s)
+// shared tile -> global tile, column-major (retrieval reads of V / W; factor
+// tiles that later serve as left operands)
+template <class T, int KB> __device__ __forceinline__ void store_tile_cm(T *g, const T *s)
 {
     constexpr int NT = NTOf<KB>::value;
     for (int q = threadIdx.x; q < KB * KB; q += NT) {
         const int c = q / KB, r = q - c * KB;
-        g[q] = s[r * (KB + 1) + c];
+        g[q] = s[r * TileLD<T, KB>::value + c];
     }
 }
 
@@ -142,6 +162,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     T *sG = base, *sEp = sG + TL::ELEMS, *sEn = sEp + TL::ELEMS;
     T *sF = sEn + TL::ELEMS, *sD = sF + TL::ELEMS, *sZ = sD + TL::ELEMS;
     T *buf = sZ + TL::ELEMS;
+    int *srp = (int *)(buf + TL::INV_BUF);
 
     TL t(threadIdx.x);
     typename TL::Reg acc, accZ;
@@ -154,23 +175,23 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
         if (J == 0) zero_tile<T, KB>(sZ);
         __syncthreads();
         scatter_block<T, H, KB>(rowptr, colind, aij, s, e, J, sF, sD, sEn, (J == 0 && doW) ? sZ : nullptr,
-                                gBhat + (size_t)part * TS, err);
+                                gBhat + (size_t)part * TS, err, srp);
         __syncthreads();
-        store_tile<T, KB>(gE + tb + J * TS, sEn);
+        store_tile_cm<T, KB>(gE + tb + J * TS, sEn); // column-major: the backward sweep's left operand
         if (J > 0) {
             // L_J = F_{J-1} G_{J-1}
             t.rzero(acc);
-            t.mma(acc, sF, sG);
+            t.mma_t(acc, sF, sG);
             __syncthreads();
-            t.rstore(sF, acc); // sF now holds L_J
-            t.gstore(gL + tb + J * TS, acc);
+            t.rstore_t(sF, acc); // sF now holds L_J, transposed
+            t.gstore_t(gL + tb + J * TS, acc);
             __syncthreads();
             // S_J = D_J - L_J E_{J-1};  z_J = -L_J z_{J-1}
             t.rload(acc, sD);
-            t.mms(acc, sF, sEp);
+            t.mms_t(acc, sF, sEp);
             if (doW) {
                 t.rzero(accZ);
-                t.mms(accZ, sF, sZ);
+                t.mms_t(accZ, sF, sZ);
                 __syncthreads();
                 t.rstore(sZ, accZ);
                 t.gstore(gZ + tb + J * TS, accZ);
@@ -182,7 +203,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
         // G_J = S_J^{-1}
         ok = t.inverse(acc, buf) && ok;
         t.rstore(sG, acc);
-        t.gstore(gG + tb + J * TS, acc);
+        t.gstore_t(gG + tb + J * TS, acc); // column-major for the backward sweep
         T *tmp = sEp;
         sEp = sEn;
         sEn = tmp;
@@ -201,7 +222,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     constexpr int NT = NTOf<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
-    constexpr int LD = KB + 1;
+    constexpr int LD = TileLD<T, KB>::value;
     const int part = blockIdx.x;
     const int s = part_start[part], e = part_start[part + 1], m = e - s;
     const int N = blk_off[part + 1] - blk_off[part];
@@ -240,7 +261,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
             }
             __syncthreads();
             t.rload(aV, sZ);
-            t.mms(aV, sG, sZV);
+            t.mms_t(aV, sG, sZV); // sG holds L_{J0+1} transposed
             __syncthreads();
             t.rstore(sZ, aV);
             __syncthreads();
@@ -262,11 +283,11 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
                 t.rload(aV, sZV);
             else
                 t.rzero(aV);
-            if (J < N - 1) t.mms(aV, sE, sXV);
+            if (J < N - 1) t.mms_t(aV, sE, sXV);
         }
         if (doW) {
             t.rload(aW, sZ);
-            if (J < N - 1) t.mms(aW, sE, sXW);
+            if (J < N - 1) t.mms_t(aW, sE, sXW);
         }
         __syncthreads();
         if (doV) t.rstore(sXV, aV);
@@ -275,11 +296,11 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
         // X_J = G_J T
         if (doV) {
             t.rzero(aV);
-            t.mma(aV, sG, sXV);
+            t.mma_t(aV, sG, sXV);
         }
         if (doW) {
             t.rzero(aW);
-            t.mma(aW, sG, sXW);
+            t.mma_t(aW, sG, sXW);
         }
         __syncthreads();
         if (doV) t.rstore(sXV, aV);

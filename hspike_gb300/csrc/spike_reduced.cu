@@ -24,16 +24,12 @@ namespace {
 
 template <class T, int KB> struct RedSmem {
     using TL = Tile<T, KB, NTOf<KB>::value>;
-    static constexpr size_t bytes = 5 * sizeof(T) * TL::ELEMS + sizeof(T) * 4 * KB + 64;
+    static constexpr size_t bytes = 5 * sizeof(T) * TL::ELEMS + sizeof(T) * TL::INV_BUF + 64;
 };
 
 template <class T, int KB> __device__ void ld(T *s, const T *g)
 {
-    constexpr int NT = NTOf<KB>::value;
-    for (int q = threadIdx.x; q < KB * KB; q += NT) {
-        const int r = q / KB, c = q - r * KB;
-        s[r * (KB + 1) + c] = g[q];
-    }
+    copy_tile_g2s<T, KB, NTOf<KB>::value>(s, g);
 }
 template <class T, int KB, class Reg> __device__ void set_identity(const Tile<T, KB, NTOf<KB>::value> &t, Reg &a)
 {
@@ -92,7 +88,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
 
 // acc += sign * L (M R); L, M, R global tiles; uses sA, sB, sC
 template <class T, int KB>
-__device__ void chain3(const Tile<T, KB, NTOf<KB>::value> &t, typename Tile<T, KB, NTOf<KB>::value>::Reg &acc,
+__device__ __forceinline__ void chain3(const Tile<T, KB, NTOf<KB>::value> &t, typename Tile<T, KB, NTOf<KB>::value>::Reg &acc,
                        const T *L, const T *Mg, const T *R, T *sA, T *sB, T *sC, bool negate)
 {
     typename Tile<T, KB, NTOf<KB>::value>::Reg tmp;
@@ -164,7 +160,7 @@ template <class T, int KB>
 __device__ T tile_row_dot(const T *sM, const T *sx, int r, int h, int RCP)
 {
     T acc = sc_zero<T>();
-    for (int k = 0; k < KB; k++) acc = madd(acc, sM[r * (KB + 1) + k], sx[k * RCP + h]);
+    for (int k = 0; k < KB; k++) acc = madd(acc, sM[r * TileLD<T, KB>::value + k], sx[k * RCP + h]);
     return acc;
 }
 
@@ -181,7 +177,7 @@ __global__ void __launch_bounds__(128)
     constexpr size_t TS = (size_t)KB * KB;
     const int i = 2 * blockIdx.x;
     const int h0 = blockIdx.y * RRC, nr = min(RRC, nrhs - h0);
-    __shared__ T sM[KB * (KB + 1)];
+    __shared__ __align__(16) T sM[KB * TileLD<T, KB>::value];
     __shared__ T sx[2 * KB * RRC], sw[KB * RRC];
     const bool left = i - 1 >= 0, right = i + 1 < cnt;
     T *gi = g + (off_l + i) * 2 * KB, *gn = g + (off_n + blockIdx.x) * 2 * KB;
@@ -200,7 +196,7 @@ __global__ void __launch_bounds__(128)
             for (int part = 0; part < 2; part++) {
                 __syncthreads();
                 const T *Mt = Mb + (size_t)(half * 2 + part) * TS;
-                for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Mt[q];
+                copy_tile_g2s<T, KB, 128>(sM, Mt);
                 __syncthreads();
                 for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
                     const int r = q / nr, h = q - r * nr;
@@ -210,7 +206,7 @@ __global__ void __launch_bounds__(128)
             __syncthreads();
             // subtract X_i w (half 0) or Y_i w (half 1) from the new block's half
             const T *Ct = (half == 0 ? Xl : Yl) + (size_t)i * TS;
-            for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Ct[q];
+            copy_tile_g2s<T, KB, 128>(sM, Ct);
             __syncthreads();
             for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
                 const int r = q / nr, h = q - r * nr;
@@ -236,7 +232,7 @@ __global__ void __launch_bounds__(128)
 {
     constexpr size_t TS = (size_t)KB * KB;
     const int h0 = blockIdx.y * RRC, nr = min(RRC, nrhs - h0);
-    __shared__ T sM[KB * (KB + 1)];
+    __shared__ __align__(16) T sM[KB * TileLD<T, KB>::value];
     __shared__ T sx[2 * KB * RRC], sw[2 * KB * RRC];
     if (!top && (blockIdx.x & 1) == 0) {
         // even block: copy from level l+1
@@ -259,7 +255,7 @@ __global__ void __launch_bounds__(128)
             if (nb < 0 || nb >= cnt) continue;
             __syncthreads();
             const T *Ct = (half == 0 ? Xl : Yl) + (size_t)j * TS;
-            for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Ct[q];
+            copy_tile_g2s<T, KB, 128>(sM, Ct);
             for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
                 const int r = q / nr, h = q - r * nr;
                 // even neighbours of an odd block: their values sit in the level above
@@ -278,7 +274,7 @@ __global__ void __launch_bounds__(128)
     for (int quad = 0; quad < 4; quad++) {
         __syncthreads();
         const T *Mt = Mj + (size_t)quad * TS;
-        for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) sM[(q / KB) * (KB + 1) + q % KB] = Mt[q];
+        copy_tile_g2s<T, KB, 128>(sM, Mt);
         __syncthreads();
         const int oh = quad >> 1, ih = quad & 1;
         for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {

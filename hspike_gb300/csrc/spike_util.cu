@@ -279,11 +279,12 @@ template <class H>
 static int residual_g(const spk_plan *P, const int *rp, const int *ci, const void *a, const void *x, const void *b,
                       void *r, int nrhs, int want_b, double *norms, cudaStream_t st)
 {
+    // few lanes per row: every shuffle step of the row reduction is an FP64
+    // add per lane, and GB300's FP64 pipe is the residual's bottleneck
     const double per_row = P->n > 0 ? (double)P->nnz / P->n : 1.0;
-    if (per_row >= 48) return launch_residual<H, 32>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    if (per_row >= 20) return launch_residual<H, 16>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    if (per_row >= 10) return launch_residual<H, 8>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    return launch_residual<H, 4>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (per_row >= 32) return launch_residual<H, 8>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (per_row >= 8) return launch_residual<H, 4>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    return launch_residual<H, 2>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
 }
 
 extern "C" int spk_residual(const spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij,
