@@ -854,3 +854,172 @@ Error_t spike_factor_release(spike_factor_t f)
     free(f);
     return succeed();
 }
+
+/* ------------------------------------------------------------------ */
+/* solve without device allocation                                      */
+/* ------------------------------------------------------------------ */
+/* Limits of the fixed workspace's schedule (host arrays live on the stack). */
+#define NOALLOC_MAX_PARTS 64
+#define NOALLOC_MAX_BLOCKS 16384
+
+typedef struct {
+    char *base;
+    size_t used, cap;
+} carve_t;
+
+/* 256-byte aligned slice of the fixed workspace; NULL once it is exhausted */
+static void *carve(carve_t *c, size_t bytes)
+{
+    const size_t off = (c->used + 255) & ~(size_t)255;
+    if (off > c->cap || bytes > c->cap - off) {
+        c->used = c->cap + 1;
+        return NULL;
+    }
+    c->used = off + bytes;
+    return c->base + off;
+}
+
+/*
+ * spike_dsolve_device_noalloc: the solve of spike_dsolve_device with every
+ * temporary carved from the library's fixed per-device workspace
+ * (spike_noalloc.cu).  The schedule is built on the stack; the kernels are the
+ * same as the allocating path's, fed with pointers into the workspace.
+ */
+Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, const integer_t *d_colind,
+                                    const integer_t *d_rowptr, const double *d_aij, double *d_x, const double *d_b,
+                                    void *cuda_stream)
+{
+    const char *name = "spike_dsolve_device_noalloc";
+    if (n < 0 || nnz < 0 || nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
+    if (n == 0 || nrhs == 0) return succeed();
+    if (!d_colind || !d_rowptr || !d_aij || !d_x || !d_b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    if (spk_device_count() <= 0) return fail(SPIKE_ERR_NO_DEVICE, "%s: no CUDA device is visible", name);
+    void *ws = NULL;
+    size_t ws_bytes = 0;
+    if (spk_noalloc_scratch(&ws, &ws_bytes) != SPK_OK)
+        return fail(SPIKE_ERR_CUDA, "%s: cannot resolve the fixed workspace on this device", name);
+    void *stream = cuda_stream;
+    carve_t cv = {(char *)ws, 0, ws_bytes};
+
+    /* analysis: bandwidth and CSR checks */
+    int info[3];
+    long long launches = 0;
+    int *d_an = (int *)carve(&cv, 4 * sizeof(int));
+    int rc = spk_analyze(n, nnz, d_rowptr, d_colind, d_an, info, stream, &launches);
+    if (rc != SPK_OK) return fail_spk(rc, name);
+    if (info[2]) return fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", name);
+
+    /* schedule, as plan_create does, with stack arrays */
+    spk_plan P;
+    memset(&P, 0, sizeof P);
+    const int k = info[0] > info[1] ? info[0] : info[1];
+    const int KB = choose_block(k < 1 ? 1 : k);
+    if (!KB || spk_factor_smem(KB, 0, SPK_MIXED) == 0)
+        return fail(SPIKE_ERR_BANDWIDTH, "%s: bandwidth %d above the supported tile size", name, k);
+    int p = choose_partitions(n, KB, 0);
+    if (p > NOALLOC_MAX_PARTS) p = NOALLOC_MAX_PARTS;
+    int part_start[NOALLOC_MAX_PARTS + 1], blk_off[NOALLOC_MAX_PARTS + 1];
+    int cr_count[32];
+    long long cr_off[33], cr_moff[33];
+    const int nreg = n / p;
+    for (int i = 0; i < p; i++) part_start[i] = i * nreg;
+    part_start[p] = n;
+    blk_off[0] = 0;
+    for (int i = 0; i < p; i++) blk_off[i + 1] = blk_off[i] + (part_start[i + 1] - part_start[i] + KB - 1) / KB;
+    if (blk_off[p] > NOALLOC_MAX_BLOCKS)
+        return fail(SPIKE_ERR_MEMORY, "%s: %d row blocks exceed the fixed schedule's %d (system too large for the "
+                    "%u-byte no-allocation workspace)", name, blk_off[p], NOALLOC_MAX_BLOCKS, SPK_NOALLOC_SCRATCH_BYTES);
+    int blk_part[NOALLOC_MAX_BLOCKS];
+    for (int i = 0; i < p; i++)
+        for (int b = blk_off[i]; b < blk_off[i + 1]; b++) blk_part[b] = i;
+    P.n = n;
+    P.nnz = nnz;
+    P.ku = info[0];
+    P.kl = info[1];
+    P.KB = KB;
+    P.p = p;
+    P.n_iface = p - 1;
+    P.is_complex = 0;
+    P.mode = SPK_MIXED;
+    P.nrhs_max = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
+    P.part_start = part_start;
+    P.blk_off = blk_off;
+    P.total_blocks = blk_off[p];
+    P.NP = (long long)P.total_blocks * KB;
+    int levels = 0;
+    for (int c = P.n_iface; c > 1; c = (c + 1) / 2) levels++;
+    P.cr_levels = levels;
+    long long tiles = 0, mtiles = 0;
+    int c = P.n_iface > 0 ? P.n_iface : 1;
+    for (int l = 0; l <= levels; l++) {
+        cr_count[l] = c;
+        cr_off[l] = tiles;
+        cr_moff[l] = mtiles;
+        tiles += c;
+        mtiles += (l < levels) ? c / 2 : 1;
+        c = (c + 1) / 2;
+    }
+    cr_off[levels + 1] = tiles;
+    cr_moff[levels + 1] = mtiles;
+    P.cr_count = cr_count;
+    P.cr_off = cr_off;
+    P.cr_moff = cr_moff;
+    P.crg_stride = tiles * 2 * KB;
+
+    /* carve the workspace */
+    const size_t fs = 4, hs = 8, TS = (size_t)KB * KB;
+    const size_t nif = P.n_iface > 0 ? (size_t)P.n_iface : 1;
+    const int nr = P.nrhs_max;
+#define CV(ptr, bytes) ptr = carve(&cv, (bytes))
+    CV(P.d_part_start, sizeof(int) * (p + 1));
+    CV(P.d_blk_off, sizeof(int) * (p + 1));
+    CV(P.d_blk_part, sizeof(int) * P.total_blocks);
+    CV(P.d_L, fs * TS * P.total_blocks);
+    CV(P.d_G, fs * TS * P.total_blocks);
+    CV(P.d_E, fs * TS * P.total_blocks);
+    CV(P.d_W, fs * TS * P.total_blocks);
+    CV(P.d_V, fs * TS * P.total_blocks);
+    CV(P.d_Bhat, fs * TS * p);
+    CV(P.d_RP, hs * TS * nif);
+    CV(P.d_RQ, hs * TS * nif);
+    CV(P.d_RX, hs * TS * nif);
+    CV(P.d_RY, hs * TS * nif);
+    CV(P.d_crP, fs * TS * tiles);
+    CV(P.d_crQ, fs * TS * tiles);
+    CV(P.d_crX, fs * TS * tiles);
+    CV(P.d_crY, fs * TS * tiles);
+    CV(P.d_crM, fs * TS * 4 * (mtiles > 0 ? mtiles : 1));
+    CV(P.d_crg, fs * 2 * (size_t)P.crg_stride * nr);
+    CV(P.d_z, fs * (size_t)P.NP * nr);
+    CV(P.d_y, fs * (size_t)P.NP * nr);
+    CV(P.d_g, hs * nif * 2 * KB * nr);
+    CV(P.d_u, hs * nif * 2 * KB * nr);
+    CV(P.d_rr, hs * nif * 2 * KB * nr);
+    CV(P.d_du, hs * nif * 2 * KB * nr);
+    CV(P.d_err, sizeof(unsigned) * 4);
+    CV(P.d_norms, sizeof(double) * 2 * nr);
+    void *d_r = carve(&cv, hs * (size_t)n * nr);
+#undef CV
+    if (cv.used > cv.cap)
+        return fail(SPIKE_ERR_MEMORY, "%s: the system needs more than the %u-byte no-allocation workspace "
+                    "(use spike_dsolve_device)", name, SPK_NOALLOC_SCRATCH_BYTES);
+    P.bytes = cv.used;
+
+    rc = spk_memcpy_h2d(P.d_part_start, part_start, sizeof(int) * (p + 1), stream);
+    if (rc == SPK_OK) rc = spk_memcpy_h2d(P.d_blk_off, blk_off, sizeof(int) * (p + 1), stream);
+    if (rc == SPK_OK) rc = spk_memcpy_h2d(P.d_blk_part, blk_part, sizeof(int) * P.total_blocks, stream);
+    P.launches = launches;
+    refine_opts o;
+    o.max_refine = 3;
+    o.red_refine = 0;
+    o.tol = 1e-12;
+    o.relres_max = 0;
+    o.sweeps = 0;
+    if (rc == SPK_OK) rc = factor_phase(&P, d_rowptr, d_colind, d_aij, stream);
+    if (rc == SPK_OK) rc = solve_all(&P, d_rowptr, d_colind, d_aij, d_x, d_b, d_r, nrhs, &o, stream);
+    if (rc != SPK_ECONV) {
+        const int rs = spk_stream_sync(stream);
+        if (rc == SPK_OK) rc = rs;
+    }
+    return finish(rc, name, &o);
+}

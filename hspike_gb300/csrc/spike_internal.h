@@ -115,6 +115,12 @@ void spk_phase_end(spk_plan *P, void *stream);
 int spk_phase_collect(spk_plan *P);
 void spk_phase_destroy(spk_plan *P);
 
+/* ---- fixed workspace of the no-allocation solve (spike_noalloc.cu) ---- */
+#define SPK_NOALLOC_SCRATCH_BYTES (32u << 20) /* 32 MiB per device */
+/* device address of the fixed workspace on the current device (first call
+ * per device resolves it with cudaGetSymbolAddress) */
+int spk_noalloc_scratch(void **ptr, size_t *bytes);
+
 /* ---- device / memory (spike_util.cu) ---- */
 int spk_device_count(void);
 int spk_current_device(void);

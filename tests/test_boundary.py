@@ -25,6 +25,7 @@ def declared_symbols():
     for h in ("spike_interfaces.h", "spike_gb300.h", "spike_datatypes.h"):
         text = open(os.path.join(ROOT, "include", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = "\n".join(line for line in text.splitlines() if not line.lstrip().startswith("#"))
         names |= set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", text))
         names |= set(re.findall(r"extern\s+const\s+\w+\s+(\w+)\s*;", text))
     return names
