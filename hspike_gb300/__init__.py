@@ -33,7 +33,7 @@ SPIKE_OPT_TOLERANCE = 3
 SPIKE_OPT_REDUCED_REFINE = 4
 SPIKE_OPT_PHASE_TIMING = 5
 PHASES = ["analysis", "factor_fwd", "factor_bwd", "reduced_factor", "rhs_sweeps", "reduced_solve", "retrieval",
-          "residual"]
+          "residual", "band_tiles"]
 SPIKE_PRECISION_MIXED = 0
 SPIKE_PRECISION_FP64 = 1
 

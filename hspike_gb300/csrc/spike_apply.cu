@@ -69,6 +69,41 @@ template <class T, int KB> __device__ void load_tile_s(T *s, const T *g)
     copy_tile_g2s<T, KB, NTOf<KB>::value>(s, g);
 }
 
+// right-hand-side rows of block J (FP64 -> factor precision) into registers
+template <class T, class H, int KB, int VPT>
+__device__ __forceinline__ void fetch_r(T (&nxt)[VPT], const H *__restrict__ r, int n, int s, int m, int h0, int nr,
+                                        int J)
+{
+    constexpr int NT = NTOf<KB>::value;
+#pragma unroll
+    for (int v = 0; v < VPT; v++) {
+        const int q = threadIdx.x + v * NT;
+        const int lr = q / RC, h = q - lr * RC, lrow = J * KB + lr;
+        nxt[v] = (q < KB * RC && h < nr && lrow < m) ? sc_cvt<T, H>(r[(size_t)(h0 + h) * n + s + lrow]) : sc_zero<T>();
+    }
+}
+// forward-sweep vector of block J into registers
+template <class T, int KB, int VPT>
+__device__ __forceinline__ void fetch_z(T (&nxt)[VPT], const T *gz, long long NP, long long rb, int h0, int nr, int J)
+{
+    constexpr int NT = NTOf<KB>::value;
+#pragma unroll
+    for (int v = 0; v < VPT; v++) {
+        const int q = threadIdx.x + v * NT;
+        const int lr = q / RC, h = q - lr * RC;
+        nxt[v] = (q < KB * RC && h < nr) ? gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] : sc_zero<T>();
+    }
+}
+template <class T, int KB, int VPT> __device__ __forceinline__ void put_v(const T (&nxt)[VPT], T *sv)
+{
+    constexpr int NT = NTOf<KB>::value;
+#pragma unroll
+    for (int v = 0; v < VPT; v++) {
+        const int q = threadIdx.x + v * NT;
+        if (q < KB * RC) sv[q] = nxt[v];
+    }
+}
+
 template <class T, int KB>
 __global__ void __launch_bounds__(NTOf<KB>::value)
     k_apply(const int *__restrict__ part_start, const int *__restrict__ blk_off, const T *__restrict__ gL,
@@ -79,6 +114,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     constexpr int NT = NTOf<KB>::value;
     constexpr size_t TS = (size_t)KB * KB;
     constexpr int LDT = TileLD<T, KB>::value;
+    constexpr int VPT = (KB * RC + NT - 1) / NT; // vector elements per thread
     const int part = blockIdx.x;
     const int h0 = blockIdx.y * RC;
     const int nr = min(RC, nrhs - h0);
@@ -88,64 +124,77 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     const long long rb = (long long)blk_off[part] * KB; // padded-row base
 
     extern __shared__ char smraw[];
-    T *sM = (T *)smem_align(smraw);
-    T *sM2 = sM + KB * LDT;
-    T *sv = sM2 + KB * LDT; // [KB][RC]
-    T *sp = sv + KB * RC;   // previous block's vector
-    T *sw = sp + KB * RC;   // work vector
+    // double buffers, selected by block parity: M tiles (L or G) then E tiles
+    T *const sM0 = (T *)smem_align(smraw);
+    T *const sE0 = sM0 + 2 * KB * LDT;
+#define SMA(par) (sM0 + ((par) & 1) * KB * LDT)
+#define SEA(par) (sE0 + ((par) & 1) * KB * LDT)
+    T *sv = sE0 + 2 * KB * LDT; // [KB][RC]
+    T *sp = sv + KB * RC;      // previous block's vector
+    T *sw = sp + KB * RC;      // work vector
 
+    // the next block's right-hand-side rows ride in registers while the
+    // current block computes; its tiles stream into the other buffer (cp.async)
+    T nxt[VPT];
     // forward: z_J = r_J - L_J z_{J-1}
+    fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, 0);
+    put_v<T, KB, VPT>(nxt, sv);
+    __syncthreads();
     for (int J = 0; J < N; J++) {
-        for (int q = threadIdx.x; q < KB * nr; q += NT) {
-            const int lr = q / nr, h = q - lr * nr;
-            const int lrow = J * KB + lr;
-            sv[lr * RC + h] = lrow < m ? sc_cvt<T, H>(r[(size_t)(h0 + h) * n + s + lrow]) : sc_zero<T>();
+        if (J + 1 < N) {
+            cp_async_tile<T, KB, NT>(SMA(J + 1), gL + tb + (J + 1) * TS);
+            cp_async_commit();
+            fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, J + 1);
         }
-        if (J > 0) load_tile_s<T, KB>(sM, gL + tb + J * TS);
-        __syncthreads();
-        if (J > 0) {
-            tile_mv<T, KB, true>(sw, sM, sp, sv, nr, true);
-            __syncthreads();
-        } else {
+        if (J > 0)
+            tile_mv<T, KB, true>(sw, SMA(J), sp, sv, nr, true);
+        else
             for (int q = threadIdx.x; q < KB * RC; q += NT) sw[q] = sv[q];
-            __syncthreads();
-        }
+        __syncthreads();
         for (int q = threadIdx.x; q < KB * nr; q += NT) {
             const int lr = q / nr, h = q - lr * nr;
             const T v = sw[lr * RC + h];
             sp[lr * RC + h] = v;
             gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
         }
+        if (J + 1 < N) put_v<T, KB, VPT>(nxt, sv);
+        cp_async_wait_all();
         __syncthreads();
     }
     // backward: y_J = G_J (z_J - E_J y_{J+1})
+    cp_async_tile<T, KB, NT>(SMA(N - 1), gG + tb + (N - 1) * TS);
+    cp_async_commit();
+    fetch_z<T, KB, VPT>(nxt, gz, NP, rb, h0, nr, N - 1);
+    put_v<T, KB, VPT>(nxt, sv);
+    cp_async_wait_all();
+    __syncthreads();
     for (int J = N - 1; J >= 0; J--) {
-        load_tile_s<T, KB>(sM, gG + tb + J * TS);
-        if (J < N - 1) load_tile_s<T, KB>(sM2, gE + tb + J * TS);
-        for (int q = threadIdx.x; q < KB * nr; q += NT) {
-            const int lr = q / nr, h = q - lr * nr;
-            sv[lr * RC + h] = gz[(size_t)(h0 + h) * NP + rb + J * KB + lr];
+        if (J > 0) {
+            cp_async_tile<T, KB, NT>(SMA(J - 1), gG + tb + (J - 1) * TS);
+            cp_async_tile<T, KB, NT>(SEA(J - 1), gE + tb + (J - 1) * TS);
+            cp_async_commit();
+            fetch_z<T, KB, VPT>(nxt, gz, NP, rb, h0, nr, J - 1);
         }
-        __syncthreads();
         if (J < N - 1) {
-            tile_mv<T, KB, true>(sw, sM2, sp, sv, nr, true);
+            tile_mv<T, KB, true>(sw, SEA(J), sp, sv, nr, true);
             __syncthreads();
-            tile_mv<T, KB, false>(sv, sM, sw, nullptr, nr, false);
+            tile_mv<T, KB, false>(sp, SMA(J), sw, nullptr, nr, false);
         } else {
-            tile_mv<T, KB, false>(sw, sM, sv, nullptr, nr, false);
-            __syncthreads();
-            for (int q = threadIdx.x; q < KB * RC; q += NT) sv[q] = sw[q];
+            tile_mv<T, KB, false>(sp, SMA(J), sv, nullptr, nr, false);
         }
         __syncthreads();
         for (int q = threadIdx.x; q < KB * nr; q += NT) {
             const int lr = q / nr, h = q - lr * nr;
-            const T v = sv[lr * RC + h];
-            sp[lr * RC + h] = v;
-            gy[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
+            gy[(size_t)(h0 + h) * NP + rb + J * KB + lr] = sp[lr * RC + h];
         }
+        if (J > 0) put_v<T, KB, VPT>(nxt, sv);
+        cp_async_wait_all();
         __syncthreads();
     }
 }
+
+#undef SMA
+#undef SEA
 
 // g_i = (y_i bottom, y_{i+1} top), FP64 / complex128.
 template <class T, int KB>
@@ -216,7 +265,7 @@ __global__ void __launch_bounds__(256)
 template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
     constexpr int NT = NTOf<KB>::value;
-    const size_t smem = 16 + sizeof(T) * (2 * KB * TileLD<T, KB>::value + 3 * KB * RC);
+    const size_t smem = 16 + sizeof(T) * (4 * KB * TileLD<T, KB>::value + 3 * KB * RC);
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)

@@ -4,8 +4,7 @@
 // Every dense block of the block-tridiagonal view of A_i is a KB x KB tile.
 // A CTA of NT threads owns one tile operation at a time; each active thread
 // holds a contiguous TR x TC register sub-tile, so operand fetches are
-// 8/16-byte vectors.  Shared
-// memory tiles are row-major with stride LD = KB + 1.
+// 8/16-byte vectors.  Shared tiles have row stride TileLD (KB + 16 bytes).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -80,6 +79,23 @@ __device__ __forceinline__ cdouble sc_frcp(cdouble a)
     const double s = __drcp_rn(fma(a.re, a.re, a.im * a.im));
     return {a.re * s, -a.im * s};
 }
+// reciprocal for the factor-precision inverse: FP32 uses the hardware
+// approximation refined by one Newton step (within 1 ulp; the refinement
+// absorbs it), FP64 the correctly rounded one.
+__device__ __forceinline__ float sc_rcp_fast(float a)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+    const float e = fmaf(-a, r, 1.0f);
+    return fmaf(r, e, r);
+}
+__device__ __forceinline__ double sc_rcp_fast(double a) { return __drcp_rn(a); }
+__device__ __forceinline__ cfloat sc_rcp_fast(cfloat a)
+{
+    const float s = sc_rcp_fast(fmaf(a.re, a.re, a.im * a.im));
+    return {a.re * s, -a.im * s};
+}
+__device__ __forceinline__ cdouble sc_rcp_fast(cdouble a) { return sc_frcp(a); }
 SPK_HD double sc_abs2(float a) { return (double)a * a; }
 SPK_HD double sc_abs2(double a) { return a * a; }
 SPK_HD double sc_abs2(cfloat a) { return (double)a.re * a.re + (double)a.im * a.im; }
@@ -186,7 +202,7 @@ template <class T, int KB, int NT> struct Tile {
     static constexpr int ACTIVE = TX * TY;          // threads that own a sub-tile
     // the blocked inverse runs when every thread owns a 4 x 4 sub-tile
     static constexpr bool BLOCK4 = (TR == 4 && TC == 4);
-    static constexpr int INV_HALF = 8 * KB + 16;   // pivot columns + P^{-1} + pivot rows
+    static constexpr int INV_HALF = 12 * KB + 16;  // pivot columns + P^{-1} + V' + pivot rows
     static constexpr int INV_BUF = BLOCK4 ? 2 * INV_HALF + KB : 4 * KB; // shared scratch elements for inverse()
 
     using Reg = T[TR][TC];
@@ -328,8 +344,8 @@ template <class T, int KB, int NT> struct Tile {
     // -U P^{-1} on the pivot columns and S - U P^{-1} B elsewhere.  Rows are
     // scaled to a unit diagonal first (and the inverse's columns back after),
     // so the pivot blocks stay O(1) and the I terms cancel nothing large.
-    // Per 4 pivots: the pivot owner inverts P, the pivot-row owners form V',
-    // everyone applies 64 FMAs; two barriers.
+    // Per 4 pivots: the pivot owner inverts P, every thread forms one element
+    // of V', everyone applies 64 FMAs; two barriers.
     __device__ __forceinline__ bool inverse_b4(Reg &s, T *buf) const
     {
         bool ok = true;
@@ -347,7 +363,7 @@ template <class T, int KB, int NT> struct Tile {
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 if (!sc_finite_nonzero(dr[i])) ok = false;
-                const T rr = sc_frcp(dr[i]);
+                const T rr = sc_rcp_fast(dr[i]);
 #pragma unroll
                 for (int jj = 0; jj < 4; jj++) s[i][jj] = s[i][jj] * rr;
             }
@@ -356,7 +372,17 @@ template <class T, int KB, int NT> struct Tile {
             T *cbuf = buf + (q & 1) * INV_HALF; // [KB][4] pivot columns U'
             T *pbuf = cbuf + 4 * KB;            // [4][4] P^{-1}
             T *vbuf = pbuf + 16;                // [4][KB] V'
+            T *rbuf = vbuf + 4 * KB;            // [4][KB] pivot rows B + I
             const bool rown = act && ty == q, cown = act && tx == q;
+            if (rown) {
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    T bb[4];
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) bb[jj] = (cown && a == jj) ? s[a][jj] + sc_one<T>() : s[a][jj];
+                    vst<T, 4>(rbuf + a * KB + col(0), bb);
+                }
+            }
             if (cown) {
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
@@ -375,7 +401,7 @@ template <class T, int KB, int NT> struct Tile {
                     for (int k = 0; k < 4; k++) {
                         const T piv = pinv[k][k];
                         if (!sc_finite_nonzero(piv)) ok = false;
-                        const T pr = sc_frcp(piv);
+                        const T pr = sc_rcp_fast(piv);
 #pragma unroll
                         for (int b = 0; b < 4; b++)
                             if (b != k) pinv[k][b] = pinv[k][b] * pr;
@@ -395,25 +421,13 @@ template <class T, int KB, int NT> struct Tile {
                 }
             }
             __syncthreads();
-            if (rown) { // V' = P^{-1} (B + I on the pivot columns) for this thread's columns
-                T pi[4][4];
+            // V' = P^{-1} (B + I on the pivot columns), one element per thread
+            for (int e = threadIdx.x; e < 4 * KB; e += NT) {
+                const int tt = e / KB, c = e - tt * KB;
+                T acc = sc_zero<T>();
 #pragma unroll
-                for (int a = 0; a < 4; a++) vld<T, 4>(pi[a], pbuf + 4 * a);
-#pragma unroll
-                for (int t = 0; t < 4; t++) {
-                    T v[4];
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++) {
-                        T acc = sc_zero<T>();
-#pragma unroll
-                        for (int a = 0; a < 4; a++) {
-                            const T bb = (cown && a == jj) ? s[a][jj] + sc_one<T>() : s[a][jj];
-                            acc = madd(acc, pi[t][a], bb);
-                        }
-                        v[jj] = acc;
-                    }
-                    vst<T, 4>(vbuf + t * KB + col(0), v);
-                }
+                for (int a = 0; a < 4; a++) acc = madd(acc, pbuf[4 * tt + a], rbuf[a * KB + c]);
+                vbuf[tt * KB + c] = acc;
             }
             __syncthreads();
             if (act) {
@@ -439,7 +453,7 @@ template <class T, int KB, int NT> struct Tile {
             vld<T, 4>(dc, dg + col(0));
 #pragma unroll
             for (int jj = 0; jj < 4; jj++) {
-                const T rc = sc_frcp(dc[jj]);
+                const T rc = sc_rcp_fast(dc[jj]);
 #pragma unroll
                 for (int i = 0; i < 4; i++) s[i][jj] = s[i][jj] * rc;
             }
@@ -541,6 +555,57 @@ template <class T, int KB, int NT> __device__ __forceinline__ void copy_tile_g2s
             }
         }
     }
+}
+
+// ------------------------------------------------------------ async copies
+// cp.async (global -> shared, 16 bytes, bypassing registers and L1); used to
+// fetch the next block's tiles while the current block computes.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Dense global tile -> shared tile (row stride TileLD), asynchronously.  Tiles
+// whose rows are shorter than 16 bytes (FP32 with KB = 2) are copied
+// synchronously instead.  The caller commits, waits and synchronizes.
+template <class T, int KB, int NT> __device__ __forceinline__ void cp_async_tile(T *s, const T *g)
+{
+    if constexpr (KB * sizeof(T) < 16) {
+        copy_tile_g2s<T, KB, NT>(s, g);
+    } else {
+        constexpr int EPC = 16 / sizeof(T) > 0 ? 16 / sizeof(T) : 1;
+        constexpr int CH = KB * KB / EPC;
+        constexpr int LD = TileLD<T, KB>::value;
+        for (int c = threadIdx.x; c < CH; c += NT) {
+            const int q = c * EPC, r = q / KB, cc = q - r * KB;
+            cp_async16(s + r * LD + cc, g + q);
+        }
+    }
+}
+
+// FP64 -> FP32, round to nearest even, with integer instructions: GB300's FP64
+// pipe (which executes the F2F conversion) is ~60x narrower than its integer
+// pipe.  Normal results only; zero, subnormal, overflow, inf and NaN take the
+// hardware conversion.  Bit-identical to (float)x.
+__device__ __forceinline__ float f64_to_f32(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+    if (e <= 0 || e >= 255) return (float)x;
+    const unsigned r = ((hi & 0xfffffu) << 3) | (lo >> 29); // 23 mantissa bits
+    const unsigned rem = lo & 0x1fffffffu;                  // 29 dropped bits
+    const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (r & 1u));
+    // a carry out of the mantissa bumps the exponent (to inf at the top), as it should
+    return __uint_as_float(((hi & 0x80000000u) | ((unsigned)e << 23)) + r + up);
+}
+template <class T, class H> __device__ __forceinline__ T cvt_fast(H v) { return sc_cvt<T, H>(v); }
+template <> __device__ __forceinline__ float cvt_fast<float, double>(double v) { return f64_to_f32(v); }
+template <> __device__ __forceinline__ cfloat cvt_fast<cfloat, cdouble>(cdouble v)
+{
+    return {f64_to_f32(v.re), f64_to_f32(v.im)};
 }
 
 // 16-byte-aligned carve-up of dynamic shared memory

@@ -8,12 +8,13 @@
 // column, then scattered the tips into R (OpenMP/spike_matrix.c:1414).
 //
 // Here one CTA owns one partition and walks it as a block-tridiagonal matrix
-// with KB x KB blocks (KB >= max(ku, kl)), reading its CSR rows exactly once:
+// with KB x KB blocks (KB >= max(ku, kl)); the CSR is read exactly once:
 //
-//   k_factor_fwd   (K1 + K2) scatter CSR rows of block J into D_J, E_J, F_{J-1}
-//                  L_J = F_{J-1} G_{J-1},  S_J = D_J - L_J E_{J-1},
+//   k_band_tiles   (K1) CSR rows of every block -> dense factor-precision tiles
+//                  D_J, F_{J-1}^T, E_J, C^, B^; one CTA per block, in parallel.
+//   k_factor_fwd   (K2) L_J = F_{J-1} G_{J-1},  S_J = D_J - L_J E_{J-1},
 //                  G_J = S_J^{-1} (Gauss-Jordan), and the forward sweep of the
-//                  W spike z_J = -L_J z_{J-1} (z_0 = C^_i).  Stores L, G, E, z.
+//                  W spike z_J = -L_J z_{J-1} (z_0 = C^_i).  Stores L, G, z.
 //   k_factor_bwd   (K3) backward sweep X_J = G_J (Z_J - E_J X_{J+1}) for
 //                  [V | W] (V's right-hand side B^_i lives in the last rows
 //                  only), storing the full spikes for explicit retrieval.
@@ -30,25 +31,26 @@ namespace {
 template <class T, int KB> struct FactorSmem {
     using TL = Tile<T, KB, NTOf<KB>::value>;
     static constexpr size_t tile = sizeof(T) * TL::ELEMS;
-    static constexpr size_t fwd = 6 * tile + sizeof(T) * TL::INV_BUF + sizeof(int) * (KB + 1) + 64;
+    static constexpr size_t fwd = 6 * tile + sizeof(T) * TL::INV_BUF + 64;
+    static constexpr size_t band = 3 * sizeof(T) * KB * (KB + 1) + sizeof(int) * (KB + 1) + 64;
     static constexpr size_t bwd = 6 * tile + 64;
 };
 
 // Scatter the CSR rows of block J of partition [s, e) into the shared tiles.
 // F: columns of block J-1 (stored transposed: it is the left operand of
-// F G), D: block J, En: block J+1, Z: C^ coupling (J == 0,
-// columns s-KB..s-1), Bhat (global, row-major): B^ coupling (columns e..e+KB-1).
+// F G), D: block J, En: block J+1 (shared tiles, row stride LD); gZ (global,
+// row-major, zeroed by the caller): C^ coupling (J == 0, columns s-KB..s-1);
+// gBhat (global, row-major): B^ coupling (columns e..e+KB-1).
 // The block's entries are one contiguous CSR range: the CTA walks it with
 // coalesced, unrolled loads (several in flight per thread) and finds each
 // entry's row by binary search in the block's row-pointer slice srp[].
-template <class T, class H, int KB>
+template <class T, class H, int KB, int LD>
 __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
-                              const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *Z,
+                              const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *gZ,
                               T *gBhat, unsigned *err, int *srp)
 {
     constexpr int NT = NTOf<KB>::value;
-    constexpr int LD = TileLD<T, KB>::value;
-    constexpr int U = 4;
+    constexpr int U = 8;
     const int m = e - s;
     const int lrow0 = J * KB;
     const int nr = min(KB, m - lrow0); // real rows in the block, >= 1
@@ -80,12 +82,12 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
                     hi = mid;
             }
             const int lr = lo, lrow = lrow0 + lr;
-            const T v = sc_cvt<T, H>(val[u]);
+            const T v = cvt_fast<T, H>(val[u]);
             const int lc = cidx[u] - s;
             if (lc < 0) {
                 const int cc = lc + KB;
                 if (cc >= 0 && lrow < KB) {
-                    if (Z) Z[lr * LD + cc] = v;
+                    if (gZ) gZ[lr * KB + cc] = v;
                 } else
                     atomicOr(err, SPK_DEV_ERR_BAND);
             } else if (lc >= m) {
@@ -110,19 +112,19 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
     }
 }
 
-template <class T, int KB> __device__ __forceinline__ void zero_tile(T *s)
+template <class T, int KB, int LD = TileLD<T, KB>::value> __device__ __forceinline__ void zero_tile(T *s)
 {
     constexpr int NT = NTOf<KB>::value;
-    for (int q = threadIdx.x; q < KB * TileLD<T, KB>::value; q += NT) s[q] = sc_zero<T>();
+    for (int q = threadIdx.x; q < KB * LD; q += NT) s[q] = sc_zero<T>();
 }
 
 // shared tile -> dense global tile (row-major)
-template <class T, int KB> __device__ __forceinline__ void store_tile(T *g, const T *s)
+template <class T, int KB, int LD = TileLD<T, KB>::value> __device__ __forceinline__ void store_tile(T *g, const T *s)
 {
     constexpr int NT = NTOf<KB>::value;
     for (int q = threadIdx.x; q < KB * KB; q += NT) {
         const int r = q / KB, c = q - r * KB;
-        g[q] = s[r * TileLD<T, KB>::value + c];
+        g[q] = s[r * LD + c];
     }
 }
 // dense global tile (row-major) -> shared tile
@@ -132,29 +134,75 @@ template <class T, int KB> __device__ __forceinline__ void load_tile(T *s, const
 }
 // shared tile -> global tile, column-major (retrieval reads of V / W; factor
 // tiles that later serve as left operands)
-template <class T, int KB> __device__ __forceinline__ void store_tile_cm(T *g, const T *s)
+template <class T, int KB, int LD = TileLD<T, KB>::value>
+__device__ __forceinline__ void store_tile_cm(T *g, const T *s)
 {
     constexpr int NT = NTOf<KB>::value;
     for (int q = threadIdx.x; q < KB * KB; q += NT) {
         const int c = q / KB, r = q - c * KB;
-        g[q] = s[r * TileLD<T, KB>::value + c];
+        g[q] = s[r * LD + c];
     }
 }
 
+// K1: one CTA per row block (all partitions at once, fully parallel).  Reads
+// the block's CSR rows once and writes, in factor precision, the tiles the
+// sequential chain consumes: D_J (row-major), F_{J-1}^T and E_J (row-major)
+// into gT, E_J column-major into gE for the backward sweep, C^ into the W
+// spike's first tile (J == 0) and B^ into gBhat (last rows).
 template <class T, int KB>
 __global__ void __launch_bounds__(NTOf<KB>::value)
-    k_factor_fwd(const int *__restrict__ rowptr, const int *__restrict__ colind,
+    k_band_tiles(const int *__restrict__ rowptr, const int *__restrict__ colind,
                  const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
-                 const int *__restrict__ blk_off, T *gL, T *gG, T *gE, T *gZ, T *gBhat, unsigned *err)
+                 const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
+                 unsigned *err)
 {
     using H = typename HighOf<T>::type;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int gb = blockIdx.x;
+    const int part = blk_part[gb];
+    const int J = gb - blk_off[part];
+    const int s = part_start[part], e = part_start[part + 1];
+    const bool zt = J == 0 && part > 0;
+
+    // odd row stride: conflict-free for the row-major and the column-major stores
+    constexpr int LD1 = KB + 1;
+    constexpr int EL1 = KB * LD1;
+    extern __shared__ char smraw[];
+    T *sD = (T *)smem_align(smraw), *sF = sD + EL1, *sE = sF + EL1;
+    int *srp = (int *)(sE + EL1);
+    T *gz = zt ? gZ + (size_t)blk_off[part] * TS : nullptr;
+    zero_tile<T, KB, LD1>(sD);
+    zero_tile<T, KB, LD1>(sF);
+    zero_tile<T, KB, LD1>(sE);
+    if (zt)
+        for (int q = threadIdx.x; q < KB * KB; q += NTOf<KB>::value) gz[q] = sc_zero<T>();
+    __syncthreads();
+    scatter_block<T, H, KB, LD1>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS, err, srp);
+    __syncthreads();
+    T *g = gT + (size_t)gb * 3 * TS;
+    store_tile<T, KB, LD1>(g, sD);
+    store_tile<T, KB, LD1>(g + TS, sF); // the shared image of F^T
+    store_tile<T, KB, LD1>(g + 2 * TS, sE);
+    store_tile_cm<T, KB, LD1>(gE + (size_t)gb * TS, sE);
+}
+
+// K2: the sequential block-LU chain of one partition per CTA.
+//   L_J = F_{J-1} G_{J-1},  S_J = D_J - L_J E_{J-1},  G_J = S_J^{-1},
+//   W forward sweep z_J = -L_J z_{J-1} (z_0 = C^).
+// While G_J is being inverted, the tiles of block J+1 stream from gT into the
+// three shared buffers that block J no longer reads (cp.async), so the chain
+// never waits on memory.
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_factor_fwd(const T *__restrict__ gT, const int *__restrict__ blk_off, T *gL, T *gG, T *gZ, unsigned *err)
+{
     constexpr int NT = NTOf<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
     const int part = blockIdx.x;
-    const int s = part_start[part], e = part_start[part + 1];
     const int N = blk_off[part + 1] - blk_off[part];
     const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * 3 * TS;
     const bool doW = part > 0;
 
     extern __shared__ char smraw[];
@@ -162,22 +210,20 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     T *sG = base, *sEp = sG + TL::ELEMS, *sEn = sEp + TL::ELEMS;
     T *sF = sEn + TL::ELEMS, *sD = sF + TL::ELEMS, *sZ = sD + TL::ELEMS;
     T *buf = sZ + TL::ELEMS;
-    int *srp = (int *)(buf + TL::INV_BUF);
 
     TL t(threadIdx.x);
     typename TL::Reg acc, accZ;
     bool ok = true;
 
+    cp_async_tile<T, KB, NT>(sD, gTp);
+    cp_async_tile<T, KB, NT>(sF, gTp + TS);
+    cp_async_tile<T, KB, NT>(sEn, gTp + 2 * TS);
+    if (doW) cp_async_tile<T, KB, NT>(sZ, gZ + tb); // z_0 = C^
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+
     for (int J = 0; J < N; J++) {
-        zero_tile<T, KB>(sF);
-        zero_tile<T, KB>(sD);
-        zero_tile<T, KB>(sEn);
-        if (J == 0) zero_tile<T, KB>(sZ);
-        __syncthreads();
-        scatter_block<T, H, KB>(rowptr, colind, aij, s, e, J, sF, sD, sEn, (J == 0 && doW) ? sZ : nullptr,
-                                gBhat + (size_t)part * TS, err, srp);
-        __syncthreads();
-        store_tile_cm<T, KB>(gE + tb + J * TS, sEn); // column-major: the backward sweep's left operand
         if (J > 0) {
             // L_J = F_{J-1} G_{J-1}
             t.rzero(acc);
@@ -198,13 +244,21 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
             }
         } else {
             t.rload(acc, sD);
-            if (doW) store_tile<T, KB>(gZ + tb, sZ);
+        }
+        __syncthreads(); // sD, sF, sEp are free from here on
+        if (J + 1 < N) {
+            const T *gn = gTp + (size_t)(J + 1) * 3 * TS;
+            cp_async_tile<T, KB, NT>(sD, gn);
+            cp_async_tile<T, KB, NT>(sF, gn + TS);
+            cp_async_tile<T, KB, NT>(sEp, gn + 2 * TS);
+            cp_async_commit();
         }
         // G_J = S_J^{-1}
         ok = t.inverse(acc, buf) && ok;
+        cp_async_wait_all();
         t.rstore(sG, acc);
         t.gstore_t(gG + tb + J * TS, acc); // column-major for the backward sweep
-        T *tmp = sEp;
+        T *tmp = sEp; // E_J becomes the previous block's coupling, E_{J+1} the current one
         sEp = sEn;
         sEn = tmp;
         __syncthreads();
@@ -271,11 +325,15 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     }
 
     for (int J = N - 1; J >= 0; J--) {
-        load_tile<T, KB>(sG, gG + tb + J * TS);
-        if (J < N - 1) load_tile<T, KB>(sE, gE + tb + J * TS);
-        if (doW) load_tile<T, KB>(sZ, gZ + tb + J * TS);
+        // all of the step's tiles in flight at once (one memory round trip)
+        constexpr int NTC = NTOf<KB>::value;
+        cp_async_tile<T, KB, NTC>(sG, gG + tb + J * TS);
+        if (J < N - 1) cp_async_tile<T, KB, NTC>(sE, gE + tb + J * TS);
+        if (doW) cp_async_tile<T, KB, NTC>(sZ, gZ + tb + J * TS);
         const bool hasZV = doV && (J == J0 || (o > 0 && J == J0 + 1));
-        if (hasZV) load_tile<T, KB>(sZV, gV + tb + J * TS);
+        if (hasZV) cp_async_tile<T, KB, NTC>(sZV, gV + tb + J * TS);
+        cp_async_commit();
+        cp_async_wait_all();
         __syncthreads();
         // T = Z_J - E_J X_{J+1}
         if (doV) {
@@ -348,6 +406,8 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     if (!attr) {
         if (cudaFuncSetAttribute(k_factor_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::fwd) !=
                 cudaSuccess ||
+            cudaFuncSetAttribute(k_band_tiles<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::band) !=
+                cudaSuccess ||
             cudaFuncSetAttribute(k_factor_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bwd) !=
                 cudaSuccess)
             return SPK_ECUDA;
@@ -355,13 +415,18 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     }
     const size_t TS = (size_t)KB * KB;
     if (cudaMemsetAsync(P->d_Bhat, 0, sizeof(T) * TS * P->p, st) != cudaSuccess) return SPK_ECUDA;
-    spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
-    k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>(rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off,
-                                                  (T *)P->d_L, (T *)P->d_G, (T *)P->d_E, (T *)P->d_W,
-                                                  (T *)P->d_Bhat, P->d_err);
+    spk_phase_begin(P, SPK_PH_BAND_TILES, st);
+    k_band_tiles<T, KB><<<P->total_blocks, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start,
+                                                              P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
+                                                              (T *)P->d_W, (T *)P->d_Bhat, P->d_err);
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
-    P->launches++;
+    spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
+    k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L, (T *)P->d_G,
+                                                  (T *)P->d_W, P->d_err);
+    SPK_CHECK_LAUNCH();
+    spk_phase_end(P, st);
+    P->launches += 2;
     if (P->p > 1) {
         spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
         k_factor_bwd<T, KB><<<P->p, NT, S::bwd, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L,

@@ -296,7 +296,7 @@ static void plan_destroy(spk_plan *P)
     if (!P) return;
     spk_phase_destroy(P);
     void *ptrs[] = {P->d_part_start, P->d_blk_off, P->d_blk_part, P->d_L, P->d_G, P->d_E, P->d_V, P->d_W,
-                    P->d_Bhat, P->d_RP, P->d_RQ, P->d_RX, P->d_RY, P->d_crP, P->d_crQ, P->d_crX, P->d_crY,
+                    P->d_Bhat, P->d_T, P->d_RP, P->d_RQ, P->d_RX, P->d_RY, P->d_crP, P->d_crQ, P->d_crX, P->d_crY,
                     P->d_crM, P->d_crg, P->d_z, P->d_y, P->d_g, P->d_u, P->d_rr, P->d_du, P->d_err, P->d_norms};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) spk_free(ptrs[i]);
     free(P->part_start);
@@ -393,6 +393,7 @@ static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int
     PA(P->d_W, fs * TS * P->total_blocks);
     PA(P->d_V, fs * TS * P->total_blocks);
     PA(P->d_Bhat, fs * TS * p);
+    PA(P->d_T, fs * TS * 3 * P->total_blocks);
     PA(P->d_RP, hs * TS * nif);
     PA(P->d_RQ, hs * TS * nif);
     PA(P->d_RX, hs * TS * nif);
@@ -980,6 +981,7 @@ Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, 
     CV(P.d_W, fs * TS * P.total_blocks);
     CV(P.d_V, fs * TS * P.total_blocks);
     CV(P.d_Bhat, fs * TS * p);
+    CV(P.d_T, fs * TS * 3 * P.total_blocks);
     CV(P.d_RP, hs * TS * nif);
     CV(P.d_RQ, hs * TS * nif);
     CV(P.d_RX, hs * TS * nif);

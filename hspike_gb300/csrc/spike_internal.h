@@ -53,7 +53,8 @@ enum spk_phase {
     SPK_PH_RED_SOLVE = 5,  /* reduced solve with FP64 refinement */
     SPK_PH_RETRIEVE = 6,   /* k_retrieve */
     SPK_PH_RESIDUAL = 7,   /* k_residual: FP64 r = b - A x */
-    SPK_NPHASES = 8
+    SPK_PH_BAND_TILES = 8, /* k_band_tiles: CSR -> dense factor-precision tiles */
+    SPK_NPHASES = 9
 };
 #define SPK_MAX_EVENTS 64
 
@@ -79,6 +80,7 @@ typedef struct spk_plan {
     /* factor-precision arrays, [total_blocks][KB][KB] (row-major tiles) */
     void *d_L, *d_G, *d_E, *d_V, *d_W; /* V, W tiles are column-major */
     void *d_Bhat;                      /* [p][KB][KB] */
+    void *d_T;                         /* [total_blocks][3][KB][KB]: D, F^T, E per block (row-major) */
     /* reduced system: level-0 quadrant blocks in FP64 (or complex128) */
     void *d_RP, *d_RQ, *d_RX, *d_RY; /* [n_iface][KB][KB] */
     /* cyclic reduction factors in factor precision */

@@ -77,12 +77,13 @@ Error_t spike_get_info(spike_context_t ctx, spike_info_t *info);
 
 /* Per-kernel-family device time accumulated while SPIKE_OPT_PHASE_TIMING is
  * on, measured with CUDA events on the context's stream.  Families, in order:
- *   0 analysis, 1 factor forward (CSR scatter + block LU + W sweep),
+ *   0 analysis, 1 factor forward (block LU + W sweep),
  *   2 factor backward (spike sweeps + tips), 3 reduced factorization,
- *   4 right-hand-side sweeps, 5 reduced solve, 6 retrieval, 7 FP64 residual.
+ *   4 right-hand-side sweeps, 5 reduced solve, 6 retrieval, 7 FP64 residual,
+ *   8 band tiles (CSR -> dense tiles).
  * ms[i] is the summed time and calls[i] the number of timed launches of
- * family i (nphases <= 8); reset = 1 clears the accumulators afterwards. */
-#define SPIKE_NUM_PHASES 8
+ * family i (nphases <= 9); reset = 1 clears the accumulators afterwards. */
+#define SPIKE_NUM_PHASES 9
 Error_t spike_get_phase_times(spike_context_t ctx, int nphases, double *ms, long long *calls, int reset);
 
 /* ---- device-pointer solves: every array already in device memory ---- */
