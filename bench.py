@@ -35,6 +35,12 @@ WORKLOAD = (f"large-band real SPIKE: n={N:,} kl=ku={K_BAND} partitions={P} nrhs=
             f"dominance {DOM}, off-diagonals U[-1,1], seed {SEED}")
 
 
+# DRAM bytes (read + write) per row block of each kernel, from one ncu capture of
+# `bench.py --n 600000 --partitions 300` (profiles/ncu_kernels_n600k_k64.md);
+# traffic per launch = this x the launch's row blocks.
+TRAFFIC_PER_BLOCK = {"factor_fwd": 93_130, "factor_bwd": 77_680, "band_tiles": 158_640, "rhs_sweeps": 49_440}
+
+
 def nnz_of(n, k):
     return (2 * k + 1) * n - k * (k + 1)
 
@@ -148,12 +154,109 @@ def reference_arm(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "note": "reference C code cannot be built here (MKL / SuperLU_MT "
+            "config": {"workload": WORKLOAD if (n, p) == (N, P) else WORKLOAD.replace(f"n={N:,}", f"n={n:,}").replace(
+                          f"partitions={P}", f"partitions={p}"), "note": "reference C code cannot be built here (MKL / SuperLU_MT "
                        "absent); its path is timed as the CPU restatement in oracle/"},
             "cpu_baseline": {k: runs[-1][k] for k in ("unit", "cores", "kind", "sample")} | {"value": v},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# --------------------------------------------------------------------- peaks
+def sgemm_tflops(torch, dev):
+    """FP32 CUDA-core peak as measured here: cuBLAS SGEMM 8192^3 with TF32 off,
+    best of 5 (the FP32 analogue of the measured bf16 figure)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    a = torch.randn(8192, 8192, device=dev)
+    b = torch.randn(8192, 8192, device=dev)
+    c = torch.empty(8192, 8192, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b, out=c)
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b, c
+    return 2.0 * 8192 ** 3 / (best / 1000.0) / 1e12
+
+
+# --------------------------------------------------------------------- batched leg
+def batched_leg(torch, dev, hs, count, steps, warmup, autotune=True):
+    """The batched-uneven workload: `count` independent systems (n log-uniform
+    in [1,000, 65,536], k in {1,2,3,8,32}, nrhs in {1,4}, dominance U[1.1,2.0],
+    seed 4), solved by one graph launch per step; mixed precision and plain
+    FP64, each with its autotuned schedule.  Device-resident inputs; each step
+    is spike_batch_run (graph launch + convergence check)."""
+    from hspike_gb300 import workloads as W
+
+    t0 = time.perf_counter()
+    draws = W.batch_draws(count, seed=4)
+    hb = W.gen_batch(draws, seed=4)
+    t = {k: torch.from_numpy(getattr(hb, k)).to(dev) for k in ("rowptr", "colind", "aij", "b")}
+    t["x"] = torch.zeros_like(t["b"])
+    systems = [(n, W.nnz_banded(n, k, k), nrhs, t["colind"].data_ptr() + 4 * int(hb.nz_off[i]),
+                t["rowptr"].data_ptr() + 4 * int(hb.rp_off[i]), t["aij"].data_ptr() + 8 * int(hb.nz_off[i]),
+                t["x"].data_ptr() + 8 * int(hb.v_off[i]), t["b"].data_ptr() + 8 * int(hb.v_off[i]))
+               for i, (n, k, nrhs, _) in enumerate(draws)]
+    gen_s = time.perf_counter() - t0
+    B = W.batch_bytes(draws)
+    out = {"workload": f"{count} independent real banded systems, n log-uniform [1000, 65536] (sum "
+                       f"{sum(d[0] for d in draws):,}), k in {{1,2,3,8,32}}, nrhs in {{1,4}}, dominance U[1.1,2.0], "
+                       f"seed 4", "algorithmic_bytes": B, "setup_s": gen_s}
+    stream = torch.cuda.current_stream(dev)
+    for name, prec in (("mixed", hs.SPIKE_PRECISION_MIXED), ("fp64", hs.SPIKE_PRECISION_FP64)):
+        ctx = hs.Context()
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_option(hs.SPIKE_OPT_PRECISION, prec)
+        c0 = time.perf_counter()
+        bt = hs.Batch(systems, ctx, autotune=autotune)
+        create_s = time.perf_counter() - c0
+        for _ in range(warmup):
+            bt.run()
+        k = steps if name == "mixed" else max(1, min(steps, 3))
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(k + 1)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for s in range(k):
+            bt.run()
+            ev[s + 1].record(stream)
+        torch.cuda.synchronize()
+        per = [ev[s].elapsed_time(ev[s + 1]) for s in range(k)]
+        ms = ev[0].elapsed_time(ev[k]) / k
+        inf = bt.info()
+        rr = bt.relres()
+        # error against x_true on a sample of systems
+        errs = []
+        for i in range(0, count, max(1, count // 64)):
+            n, kk, nrhs, _ = draws[i]
+            o = int(hb.v_off[i])
+            x = t["x"][o:o + n * nrhs].cpu().numpy()
+            xt = hb.x_true[o:o + n * nrhs]
+            errs.append(float(np.linalg.norm(x - xt) / np.linalg.norm(xt)))
+        out[name] = {"value": count / (ms / 1000.0), "unit": "systems/s", "ms_per_step": ms,
+                     "batches_per_s": 1000.0 / ms, "hbm_gbs": B / (ms / 1000.0) / 1e9,
+                     "p50_ms": statistics.median(per), "p99_ms": float(np.percentile(per, 99)),
+                     "relres_max": float(rr.max()), "err_vs_xtrue_max_sampled": max(errs),
+                     "groups": inf.groups, "graph_kernel_launches": inf.graph_kernel_launches,
+                     "graph_sweeps": inf.graph_sweeps, "extra_sweeps": inf.extra_sweeps,
+                     "create_s": create_s, "tune_device_ms": inf.tune_ms,
+                     "device_gb": inf.device_bytes / 1e9,
+                     "schedule": [{k2: g[k2] for k2 in ("block", "nrhs", "systems", "partitions",
+                                                         "rows_per_partition", "graph_sweeps")}
+                                  for g in bt.groups()]}
+        bt.destroy()
+        ctx.close()
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    del t
+    torch.cuda.empty_cache()
+    return out
 
 
 # --------------------------------------------------------------------- GPU arm
@@ -165,6 +268,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
     ap.add_argument("--skip-extras", action="store_true", help="mixed-precision device timing only")
+    ap.add_argument("--skip-e2e", action="store_true", help="omit the host-buffer end-to-end leg")
+    ap.add_argument("--n", type=int, default=N, help="rows (smaller cases for profiler captures)")
+    ap.add_argument("--partitions", type=int, default=P)
+    ap.add_argument("--batch", type=int, default=4096, help="systems in the batched leg (0 = skip it)")
+    ap.add_argument("--batch-only", action="store_true", help="run only the batched leg (profiler captures)")
+    ap.add_argument("--no-autotune", action="store_true", help="batched leg: schedules by rule")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -175,6 +284,13 @@ def main():
     from hspike_gb300.build import build
 
     build()
+    n, p = args.n, args.partitions
+    if args.batch_only:
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        torch.cuda.set_device(dev)
+        res = batched_leg(torch, dev, hs, args.batch, max(1, args.steps), args.warmup, not args.no_autotune)
+        print(json.dumps({"batched": res}), flush=True)
+        return 0
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -197,7 +313,7 @@ def main():
     def pinned(shape, dtype):
         return torch.empty(shape, dtype=tdt[np.dtype(dtype).type], pin_memory=True).numpy()
 
-    rp, ci, a, xt, b = hs.gen_banded(N, K_BAND, K_BAND, DOM, SEED + rank, nrhs=NRHS, alloc=pinned)
+    rp, ci, a, xt, b = hs.gen_banded(n, K_BAND, K_BAND, DOM, SEED + rank, nrhs=NRHS, alloc=pinned)
     nnz = len(ci)
     d_rp, d_ci, d_a = (torch.from_numpy(v).to(dev) for v in (rp, ci, a))
     d_b = torch.from_numpy(b.T.copy()).to(dev).contiguous()  # n x nrhs column-major == nrhs x n row-major
@@ -205,11 +321,11 @@ def main():
     stream = torch.cuda.current_stream(dev)
     ctx = hs.Context()
     ctx.set_stream(stream.cuda_stream)
-    ctx.set_option(hs.SPIKE_OPT_PARTITIONS, P)
+    ctx.set_option(hs.SPIKE_OPT_PARTITIONS, p)
     ctx.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_MIXED)
 
     def solve(ctx_, d_x_, d_b_, nrhs):
-        ctx_.solve_device(N, nnz, nrhs, d_ci.data_ptr(), d_rp.data_ptr(), d_a.data_ptr(), d_x_.data_ptr(),
+        ctx_.solve_device(n, nnz, nrhs, d_ci.data_ptr(), d_rp.data_ptr(), d_a.data_ptr(), d_x_.data_ptr(),
                           d_b_.data_ptr())
 
     def timed(ctx_, steps, d_x_, d_b_, nrhs, warmup, clocks=None):
@@ -249,9 +365,10 @@ def main():
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
            "dtype": "f32 factors / f64 residual+update+reduced", "data": "synthetic (seeded generator)",
-           "config": {"workload": WORKLOAD, "l2": "inputs (3.1 GB CSR) larger than the 129 MB L2; no flush",
+           "config": {"workload": WORKLOAD if (n, p) == (N, P) else WORKLOAD.replace(f"n={N:,}", f"n={n:,}").replace(
+                          f"partitions={P}", f"partitions={p}"), "l2": "inputs (3.1 GB CSR) larger than the 129 MB L2; no flush",
                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-           "hbm_gbs": alg_bytes(N, K_BAND, NRHS) / (ms / 1000.0) / 1e9,
+           "hbm_gbs": alg_bytes(n, K_BAND, NRHS) / (ms / 1000.0) / 1e9,
            "p50_ms": statistics.median(per), "p99_ms": float(np.percentile(per, 99)),
            "relres_max": info.relres_max, "refine_sweeps": sweeps, "err_vs_xtrue": err,
            "gpu_launches": launches, "clocks": clk}
@@ -276,31 +393,67 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
             os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
-        # algorithmic bytes per launch of each family (units: CSR rows / vector rows)
-        csr_bytes = 12 * nnz + 4 * (N + 1)
-        fam_bytes = {"factor_fwd": csr_bytes, "residual": csr_bytes + 16 * N * NRHS + 8 * N * NRHS,
-                     "rhs_sweeps": 8 * N * NRHS, "retrieval": 8 * N * NRHS}
-        fam_flops = {"factor_fwd": 8.0 * K_BAND ** 3 * (N / K_BAND), "factor_bwd": 6.0 * K_BAND ** 3 * (N / K_BAND)}
+        p32 = sgemm_tflops(torch, dev)
+        KB = info.block
+        nreg = n // p
+        blocks = (p - 1) * (-(-nreg // KB)) + (-(-(n - (p - 1) * nreg) // KB))
+        k = K_BAND
+        csr_bytes = 12 * nnz + 4 * (n + 1)
+        # per family: (bound, algorithmic work per launch, executed work per launch, units)
+        #   factor_fwd: block LU (2 k^2 n) + the W spike's forward sweep (2 k^2 n); it executes
+        #               8 KB^3 per row block (two tile products, the tile inverse, the sweep)
+        #   factor_bwd: the rest of the spikes (4 k^2 n); executes 8 KB^3 per row block
+        #   band_tiles: reads the CSR once, writes three factor-precision tiles per block
+        #   residual:   reads the CSR, x and b, writes r (FP64)
+        #   rhs_sweeps: reads the L / G / E tiles once per application
+        work = {"factor_fwd": ("fp32", 4.0 * k * k * n, 8.0 * KB ** 3 * blocks),
+                "factor_bwd": ("fp32", 4.0 * k * k * n, 8.0 * KB ** 3 * blocks),
+                "band_tiles": ("hbm", csr_bytes, csr_bytes + 4 * 4 * KB * KB * blocks),
+                "residual": ("hbm", csr_bytes + 24 * n * NRHS, csr_bytes + 24 * n * NRHS),
+                "rhs_sweeps": ("hbm", 3 * 4 * KB * KB * blocks, 3 * 4 * KB * KB * blocks)}
         dur = fams[dom]["ms_per_launch"] / 1000.0
-        ab = fam_bytes.get(dom, csr_bytes)
-        out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ab / dur / 1e9, "peak": hbm_peak,
-                           "unit": "GB/s", "frac": ab / dur / 1e9 / hbm_peak, "traffic": None,
-                           "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
-                           "algorithmic_bytes_per_launch": ab, "ms_per_launch": dur * 1000.0}
-        if dom in fam_flops:
-            out["roofline"]["achieved_fp32_tflops"] = fam_flops[dom] / dur / 1e12
+        bound, alg, exe = work.get(dom, ("hbm", csr_bytes, csr_bytes))
+        traffic = TRAFFIC_PER_BLOCK.get(dom)
+        if bound == "fp32":
+            out["roofline"] = {"bound": "fp32", "kernel": dom, "achieved": alg / dur / 1e12, "peak": p32,
+                               "unit": "TFLOP/s", "frac": alg / dur / 1e12 / p32,
+                               "traffic": traffic * blocks if traffic else None,
+                               "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured in this run (FP32 CUDA "
+                                              "cores: the factors are FP32 by design, no tensor-core path)",
+                               "algorithmic_tflop_per_launch": alg / 1e12, "executed_tflop_per_launch": exe / 1e12,
+                               "executed_frac": exe / dur / 1e12 / p32, "ms_per_launch": dur * 1000.0,
+                               "traffic_source": "ncu dram__bytes_read+write per row block of this kernel "
+                                                 "(n=600,000 capture) x row blocks"}
+        else:
+            out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": alg / dur / 1e9, "peak": hbm_peak,
+                               "unit": "GB/s", "frac": alg / dur / 1e9 / hbm_peak,
+                               "traffic": traffic * blocks if traffic else None,
+                               "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback",
+                               "ms_per_launch": dur * 1000.0}
+        for fam, (bd, al, ex) in work.items():
+            if fam in fams:
+                d = fams[fam]["ms_per_launch"] / 1000.0
+                fams[fam]["bound"] = bd
+                if bd == "fp32":
+                    fams[fam]["alg_tflops"] = al / d / 1e12
+                    fams[fam]["frac_of_sgemm"] = al / d / 1e12 / p32
+                    fams[fam]["executed_tflops"] = ex / d / 1e12
+                else:
+                    fams[fam]["alg_gbs"] = al / d / 1e9
+                    fams[fam]["frac_of_hbm"] = al / d / 1e9 / hbm_peak
         out["kernel_families"] = fams
-        f32, f64 = alg_flops(N, K_BAND, NRHS, 1 + sweeps, 1 + sweeps)
-        t_roof = max(alg_bytes(N, K_BAND, NRHS) / (hbm_peak * 1e9), f32 / 80.5e12 + f64 / 1.25e12)
+        f32, f64 = alg_flops(n, K_BAND, NRHS, 1 + sweeps, 1 + sweeps)
+        t_roof = max(alg_bytes(n, K_BAND, NRHS) / (hbm_peak * 1e9), f32 / (p32 * 1e12) + f64 / 1.25e12)
         out["solve_roofline"] = {"t_roof_ms": t_roof * 1000, "frac": t_roof / (ms / 1000.0),
-                                 "rule": "max(B_alg/BW_hbm, F32/P32 + F64/P64); BW measured, P32 80.5 and P64 1.25 "
-                                         "TFLOP/s nominal GB300 (no measured CUDA-core peaks)",
-                                 "f32_gflop": f32 / 1e9, "f64_gflop": f64 / 1e9}
+                                 "hbm_frac": alg_bytes(n, K_BAND, NRHS) / (hbm_peak * 1e9) / (ms / 1000.0),
+                                 "rule": "max(B_alg/BW_hbm, F32/P32 + F64/P64); BW measured (MEASURED_PEAKS.json), "
+                                         "P32 measured SGEMM, P64 1.25 TFLOP/s nominal GB300 FP64",
+                                 "p32_tflops": p32, "f32_gflop": f32 / 1e9, "f64_gflop": f64 / 1e9}
 
         # ---- plain FP64 SPIKE (the denominator of the mixed/plain ratio)
         ctx64 = hs.Context()
         ctx64.set_stream(stream.cuda_stream)
-        ctx64.set_option(hs.SPIKE_OPT_PARTITIONS, P)
+        ctx64.set_option(hs.SPIKE_OPT_PARTITIONS, p)
         ctx64.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_FP64)
         d_x64 = torch.zeros_like(d_b)
         t64, per64, _, _ = timed(ctx64, 3, d_x64, d_b, NRHS, 1)
@@ -311,36 +464,41 @@ def main():
         del d_x64
 
         # ---- nrhs = 16
-        gen16 = hs.gen_banded(N, K_BAND, K_BAND, DOM, SEED, nrhs=16)
+        gen16 = hs.gen_banded(n, K_BAND, K_BAND, DOM, SEED, nrhs=16)
         d_b16 = torch.from_numpy(gen16[4].T.copy()).to(dev)
         d_x16 = torch.zeros_like(d_b16)
         # same matrix (same seed), 16 right-hand sides
         t16, per16, _, _ = timed(ctx, 3, d_x16, d_b16, 16, 1)
         x16 = d_x16.cpu().numpy().T
         out["nrhs16"] = {"value": 3 / (t16 / 1000.0), "unit": "solves/s", "ms_per_step": t16 / 3,
-                         "hbm_gbs": alg_bytes(N, K_BAND, 16) / (t16 / 3000.0) / 1e9,
+                         "hbm_gbs": alg_bytes(n, K_BAND, 16) / (t16 / 3000.0) / 1e9,
                          "relres_max": ctx.info().relres_max,
                          "err_vs_xtrue": float(np.linalg.norm(x16 - gen16[3]) / np.linalg.norm(gen16[3]))}
         del d_b16, d_x16, gen16
 
+    if args.batch > 0 and not args.skip_extras:
+        out["batched"] = batched_leg(torch, dev, hs, args.batch, max(3, min(args.steps, 10)), 3,
+                                     not args.no_autotune)
+
     # ---- end to end through the reference's C entry point, host buffers
-    hs.set_option(hs.SPIKE_OPT_PARTITIONS, P)
-    hs.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_MIXED)
-    xh = pinned((N * NRHS,), np.float64).reshape((N, NRHS), order="F")
-    e2e_steps = max(1, min(args.steps, 5))
-    for _ in range(max(1, args.warmup)):
-        hs.dspike_core_host(N, nnz, NRHS, ci, rp, a, xh, b)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        rc = hs.dspike_core_host(N, nnz, NRHS, ci, rp, a, xh, b)
-        if rc != hs.SPIKE_SUCCESS:
-            raise RuntimeError(hs.last_error())
-    te = time.perf_counter() - t0
-    out["e2e"] = {"value": e2e_steps / te, "unit": "solves/s", "ms_per_step": te * 1000 / e2e_steps,
-                  "h2d_bytes_per_step": int(rp.nbytes + ci.nbytes + a.nbytes + b.nbytes),
-                  "d2h_bytes_per_step": int(xh.nbytes), "api": "dspike_core_host (pinned host buffers)",
-                  "err_vs_xtrue": float(np.linalg.norm(xh - xt) / np.linalg.norm(xt))}
+    if not args.skip_e2e:
+        hs.set_option(hs.SPIKE_OPT_PARTITIONS, p)
+        hs.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_MIXED)
+        xh = pinned((n * NRHS,), np.float64).reshape((n, NRHS), order="F")
+        e2e_steps = max(1, min(args.steps, 5))
+        for _ in range(max(1, args.warmup)):
+            hs.dspike_core_host(n, nnz, NRHS, ci, rp, a, xh, b)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            rc = hs.dspike_core_host(n, nnz, NRHS, ci, rp, a, xh, b)
+            if rc != hs.SPIKE_SUCCESS:
+                raise RuntimeError(hs.last_error())
+        te = time.perf_counter() - t0
+        out["e2e"] = {"value": e2e_steps / te, "unit": "solves/s", "ms_per_step": te * 1000 / e2e_steps,
+                      "h2d_bytes_per_step": int(rp.nbytes + ci.nbytes + a.nbytes + b.nbytes),
+                      "d2h_bytes_per_step": int(xh.nbytes), "api": "dspike_core_host (pinned host buffers)",
+                      "err_vs_xtrue": float(np.linalg.norm(xh - xt) / np.linalg.norm(xt))}
 
     if not args.skip_cpu and rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline((rp, ci, a, b))

@@ -46,8 +46,12 @@ EXPORTS = [
     "spike_context_destroy", "spike_context_set_stream", "spike_set_option", "spike_get_option", "spike_get_info",
     "spike_dsolve_device", "spike_zsolve_device", "spike_dfactor", "spike_zfactor", "spike_dfactor_device",
     "spike_dsolve_factored", "spike_zsolve_factored", "spike_dsolve_factored_device", "spike_factor_release",
-    "spike_get_phase_times",
+    "spike_get_phase_times", "spike_dsolve_device_noalloc", "spike_dbatch_create", "spike_batch_run",
+    "spike_batch_relres", "spike_batch_get_info", "spike_batch_group", "spike_batch_destroy",
+    "spike_batch_partitions",
 ]
+SPIKE_BATCH_AUTOTUNE = 1
+SPIKE_BATCH_NO_GRAPH = 2
 
 
 class SpikeError(RuntimeError):
@@ -61,6 +65,24 @@ class Info(C.Structure):
     _fields_ = [("relres_max", C.c_double), ("refine_sweeps", C.c_int), ("partitions", C.c_int), ("ku", C.c_int),
                 ("kl", C.c_int), ("block", C.c_int), ("kernel_launches", C.c_longlong),
                 ("device_bytes", C.c_size_t)]
+
+
+class DSystem(C.Structure):
+    """spike_dsystem_t: one system of a batch (device pointers)."""
+    _fields_ = [("n", C.c_int), ("nnz", C.c_int), ("nrhs", C.c_int), ("d_colind", C.c_void_p),
+                ("d_rowptr", C.c_void_p), ("d_aij", C.c_void_p), ("d_x", C.c_void_p), ("d_b", C.c_void_p)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("systems", C.c_int), ("groups", C.c_int), ("graph", C.c_int), ("graph_sweeps", C.c_int),
+                ("extra_sweeps", C.c_int), ("relres_max", C.c_double), ("graph_kernel_launches", C.c_longlong),
+                ("device_bytes", C.c_size_t), ("tune_ms", C.c_double)]
+
+
+class BatchGroup(C.Structure):
+    _fields_ = [("block", C.c_int), ("nrhs", C.c_int), ("bandwidth", C.c_int), ("systems", C.c_int),
+                ("partitions", C.c_int), ("rows_per_partition", C.c_int), ("graph_sweeps", C.c_int),
+                ("rows", C.c_longlong), ("nnz", C.c_longlong)]
 
 
 _LIB = None
@@ -98,6 +120,14 @@ def load(path: str | None = None):
         getattr(L, name).argtypes = [vp, i, vp, vp]
     L.spike_factor_release.argtypes = [vp]
     L.spike_get_phase_times.argtypes = [vp, i, vp, vp, i]
+    L.spike_dbatch_create.argtypes = [vp, i, vp, i, C.POINTER(vp)]
+    L.spike_batch_run.argtypes = [vp]
+    L.spike_batch_relres.argtypes = [vp, vp]
+    L.spike_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+    L.spike_batch_group.argtypes = [vp, i, C.POINTER(BatchGroup)]
+    L.spike_batch_destroy.argtypes = [vp]
+    L.spike_batch_partitions.argtypes = [i, i, i]
+    L.spike_batch_partitions.restype = i
     _LIB = L
     return L
 
@@ -278,6 +308,59 @@ class Factor:
             self.release()
         except Exception:
             pass
+
+
+class Batch:
+    """Many independent systems (device arrays) solved by one graph launch.
+
+    ``systems``: sequence of (n, nnz, nrhs, d_colind, d_rowptr, d_aij, d_x, d_b)
+    with integer device addresses; x and b are n x nrhs column-major.
+    """
+
+    def __init__(self, systems, ctx: Context | None = None, autotune=True, graph=True):
+        arr = (DSystem * len(systems))(*[DSystem(*s) for s in systems])
+        flags = (SPIKE_BATCH_AUTOTUNE if autotune else 0) | (0 if graph else SPIKE_BATCH_NO_GRAPH)
+        self.count = len(systems)
+        self._h = C.c_void_p()
+        _check(load().spike_dbatch_create(ctx.handle if ctx else None, len(systems), C.cast(arr, C.c_void_p), flags,
+                                          C.byref(self._h)))
+
+    def run(self):
+        _check(load().spike_batch_run(self._h))
+
+    def relres(self) -> np.ndarray:
+        out = np.zeros(self.count, np.float64)
+        _check(load().spike_batch_relres(self._h, _ptr(out)))
+        return out
+
+    def info(self) -> BatchInfo:
+        inf = BatchInfo()
+        _check(load().spike_batch_get_info(self._h, C.byref(inf)))
+        return inf
+
+    def groups(self) -> list[dict]:
+        out = []
+        for i in range(self.info().groups):
+            g = BatchGroup()
+            _check(load().spike_batch_group(self._h, i, C.byref(g)))
+            out.append({f: getattr(g, f) for f, _ in BatchGroup._fields_})
+        return out
+
+    def destroy(self):
+        if self._h:
+            _check(load().spike_batch_destroy(self._h))
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def batch_partitions(n: int, block: int, rows_per_partition: int) -> int:
+    """The batch partition rule (host only, no device needed)."""
+    return int(load().spike_batch_partitions(n, block, rows_per_partition))
 
 
 # ---------------------------------------------------------------- generator

@@ -13,13 +13,16 @@
 //                :259-396); with the spikes resident this is one parallel pass.
 #include "spike_common.cuh"
 
+#include <algorithm>
+
 namespace {
 
-constexpr int RC = 32; // right-hand-side columns per CTA
+constexpr int RC = 32;      // right-hand-side columns per CTA
+constexpr int RCS = RC + 1; // row stride of the shared [KB][RC] vectors (odd: column-wise writes spread over banks)
 
 // out[r][h] = sign * sum_k M[r][k] v[k][h] (+ base[r][h]), r < KB, h < nr.
 // Mt: shared tile holding M transposed (the factor tiles are column-major in
-// global memory); v, base, out: shared [KB][RC].
+// global memory); v, base, out: shared [KB][RC] vectors with row stride RCS.
 template <class T, int KB, bool HAS_BASE>
 __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, bool negate)
 {
@@ -40,7 +43,7 @@ __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, 
         if (o < O) {
             r = o / nr;
             h = o - r * nr;
-            for (int k = part; k < KB; k += spl) acc = madd(acc, Mt[k * LD + r], v[k * RC + h]);
+            for (int k = part; k < KB; k += spl) acc = madd(acc, Mt[k * LD + r], v[k * RCS + h]);
         }
         for (int off = spl >> 1; off > 0; off >>= 1) {
             if constexpr (sizeof(T) == 4) {
@@ -58,8 +61,8 @@ __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, 
         }
         if (o < O && part == 0) {
             T val = negate ? -acc : acc;
-            if (HAS_BASE) val = base[r * RC + h] + val;
-            out[r * RC + h] = val;
+            if (HAS_BASE) val = base[r * RCS + h] + val;
+            out[r * RCS + h] = val;
         }
     }
 }
@@ -69,6 +72,9 @@ template <class T, int KB> __device__ void load_tile_s(T *s, const T *g)
     copy_tile_g2s<T, KB, NTOf<KB>::value>(s, g);
 }
 
+// Vector elements q < KB * nr of block J: column h = q / KB, row lr = q % KB,
+// so consecutive threads touch consecutive rows of one column (coalesced
+// global accesses) and only the live columns are fetched.
 // right-hand-side rows of block J (FP64 -> factor precision) into registers
 template <class T, class H, int KB, int VPT>
 __device__ __forceinline__ void fetch_r(T (&nxt)[VPT], const H *__restrict__ r, int n, int s, int m, int h0, int nr,
@@ -78,8 +84,10 @@ __device__ __forceinline__ void fetch_r(T (&nxt)[VPT], const H *__restrict__ r, 
 #pragma unroll
     for (int v = 0; v < VPT; v++) {
         const int q = threadIdx.x + v * NT;
-        const int lr = q / RC, h = q - lr * RC, lrow = J * KB + lr;
-        nxt[v] = (q < KB * RC && h < nr && lrow < m) ? sc_cvt<T, H>(r[(size_t)(h0 + h) * n + s + lrow]) : sc_zero<T>();
+        if (q < KB * nr) {
+            const int h = q / KB, lr = q - h * KB, lrow = J * KB + lr;
+            nxt[v] = lrow < m ? sc_cvt<T, H>(r[(size_t)(h0 + h) * n + s + lrow]) : sc_zero<T>();
+        }
     }
 }
 // forward-sweep vector of block J into registers
@@ -90,17 +98,22 @@ __device__ __forceinline__ void fetch_z(T (&nxt)[VPT], const T *gz, long long NP
 #pragma unroll
     for (int v = 0; v < VPT; v++) {
         const int q = threadIdx.x + v * NT;
-        const int lr = q / RC, h = q - lr * RC;
-        nxt[v] = (q < KB * RC && h < nr) ? gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] : sc_zero<T>();
+        if (q < KB * nr) {
+            const int h = q / KB, lr = q - h * KB;
+            nxt[v] = gz[(size_t)(h0 + h) * NP + rb + J * KB + lr];
+        }
     }
 }
-template <class T, int KB, int VPT> __device__ __forceinline__ void put_v(const T (&nxt)[VPT], T *sv)
+template <class T, int KB, int VPT> __device__ __forceinline__ void put_v(const T (&nxt)[VPT], T *sv, int nr)
 {
     constexpr int NT = NTOf<KB>::value;
 #pragma unroll
     for (int v = 0; v < VPT; v++) {
         const int q = threadIdx.x + v * NT;
-        if (q < KB * RC) sv[q] = nxt[v];
+        if (q < KB * nr) {
+            const int h = q / KB, lr = q - h * KB;
+            sv[lr * RCS + h] = nxt[v];
+        }
     }
 }
 
@@ -129,16 +142,16 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     T *const sE0 = sM0 + 2 * KB * LDT;
 #define SMA(par) (sM0 + ((par) & 1) * KB * LDT)
 #define SEA(par) (sE0 + ((par) & 1) * KB * LDT)
-    T *sv = sE0 + 2 * KB * LDT; // [KB][RC]
-    T *sp = sv + KB * RC;      // previous block's vector
-    T *sw = sp + KB * RC;      // work vector
+    T *sv = sE0 + 2 * KB * LDT; // [KB][RCS]
+    T *sp = sv + KB * RCS;     // previous block's vector
+    T *sw = sp + KB * RCS;     // work vector
 
     // the next block's right-hand-side rows ride in registers while the
     // current block computes; its tiles stream into the other buffer (cp.async)
     T nxt[VPT];
     // forward: z_J = r_J - L_J z_{J-1}
     fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, 0);
-    put_v<T, KB, VPT>(nxt, sv);
+    put_v<T, KB, VPT>(nxt, sv, nr);
     __syncthreads();
     for (int J = 0; J < N; J++) {
         if (J + 1 < N) {
@@ -149,15 +162,15 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
         if (J > 0)
             tile_mv<T, KB, true>(sw, SMA(J), sp, sv, nr, true);
         else
-            for (int q = threadIdx.x; q < KB * RC; q += NT) sw[q] = sv[q];
+            for (int q = threadIdx.x; q < KB * RCS; q += NT) sw[q] = sv[q];
         __syncthreads();
         for (int q = threadIdx.x; q < KB * nr; q += NT) {
-            const int lr = q / nr, h = q - lr * nr;
-            const T v = sw[lr * RC + h];
-            sp[lr * RC + h] = v;
+            const int h = q / KB, lr = q - h * KB;
+            const T v = sw[lr * RCS + h];
+            sp[lr * RCS + h] = v;
             gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
         }
-        if (J + 1 < N) put_v<T, KB, VPT>(nxt, sv);
+        if (J + 1 < N) put_v<T, KB, VPT>(nxt, sv, nr);
         cp_async_wait_all();
         __syncthreads();
     }
@@ -165,7 +178,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     cp_async_tile<T, KB, NT>(SMA(N - 1), gG + tb + (N - 1) * TS);
     cp_async_commit();
     fetch_z<T, KB, VPT>(nxt, gz, NP, rb, h0, nr, N - 1);
-    put_v<T, KB, VPT>(nxt, sv);
+    put_v<T, KB, VPT>(nxt, sv, nr);
     cp_async_wait_all();
     __syncthreads();
     for (int J = N - 1; J >= 0; J--) {
@@ -184,10 +197,10 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
         }
         __syncthreads();
         for (int q = threadIdx.x; q < KB * nr; q += NT) {
-            const int lr = q / nr, h = q - lr * nr;
-            gy[(size_t)(h0 + h) * NP + rb + J * KB + lr] = sp[lr * RC + h];
+            const int h = q / KB, lr = q - h * KB;
+            gy[(size_t)(h0 + h) * NP + rb + J * KB + lr] = sp[lr * RCS + h];
         }
-        if (J > 0) put_v<T, KB, VPT>(nxt, sv);
+        if (J > 0) put_v<T, KB, VPT>(nxt, sv, nr);
         cp_async_wait_all();
         __syncthreads();
     }
@@ -209,10 +222,10 @@ __global__ void k_ytips(const int *__restrict__ part_start, const int *__restric
         const int h = q / (2 * KB), rr = q - h * 2 * KB;
         long long prow;
         if (rr < KB)
-            prow = (long long)blk_off[i] * KB + (mi - KB + rr);
+            prow = mi - KB + rr < 0 ? -1 : (long long)blk_off[i] * KB + (mi - KB + rr); // no bottom tip: see k_tips
         else
             prow = (long long)blk_off[i + 1] * KB + (rr - KB);
-        g[h * NR + (long long)i * 2 * KB + rr] = sc_cvt<H, T>(gy[(size_t)h * NP + prow]);
+        g[h * NR + (long long)i * 2 * KB + rr] = prow < 0 ? sc_zero<H>() : cvt_fast<H, T>(gy[(size_t)h * NP + prow]);
     }
 }
 
@@ -221,26 +234,34 @@ template <class T, int KB>
 __global__ void __launch_bounds__(256)
     k_retrieve(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const int *__restrict__ blk_part,
                const T *__restrict__ gV, const T *__restrict__ gW, const T *__restrict__ gy,
-               const typename HighOf<T>::type *__restrict__ u, long long NP, int n_iface, int n, int nrhs,
-               typename HighOf<T>::type *x, int accumulate)
+               const T *__restrict__ u, long long NP, int n_iface, int n, int nrhs,
+               typename HighOf<T>::type *x, int accumulate, const spk_sysref *__restrict__ sys,
+               const int *__restrict__ part_sys)
 {
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
     const int gb = blockIdx.x; // global block index
     const int part = blk_part[gb];
     const int J = gb - blk_off[part];
-    const int s = part_start[part], m = part_start[part + 1] - s;
+    int s = part_start[part];
+    const int m = part_start[part + 1] - s;
+    if (sys) { // batch group: write the partition's own system, local rows
+        const spk_sysref &S = sys[part_sys[part]];
+        x = (H *)S.x;
+        n = S.n;
+        s -= (int)S.row0;
+    }
     const long long NR = (long long)n_iface * 2 * KB;
     const bool hasV = part < p - 1, hasW = part > 0;
-    __shared__ H st[2 * KB * 8];
+    __shared__ T st[2 * KB * 8]; // interface unknowns in factor precision, converted once
     const int hchunk = 8;
     for (int hb = 0; hb < nrhs; hb += hchunk) {
         const int nr = min(hchunk, nrhs - hb);
         __syncthreads();
         for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
             const int c = q / nr, h = q - c * nr;
-            st[c * hchunk + h] = hasV ? u[(hb + h) * NR + (long long)part * 2 * KB + KB + c] : sc_zero<H>();
-            st[(KB + c) * hchunk + h] = hasW ? u[(hb + h) * NR + (long long)(part - 1) * 2 * KB + c] : sc_zero<H>();
+            st[c * hchunk + h] = hasV ? u[(hb + h) * NR + (long long)part * 2 * KB + KB + c] : sc_zero<T>();
+            st[(KB + c) * hchunk + h] = hasW ? u[(hb + h) * NR + (long long)(part - 1) * 2 * KB + c] : sc_zero<T>();
         }
         __syncthreads();
         for (int q = threadIdx.x; q < KB * nr; q += blockDim.x) {
@@ -250,32 +271,204 @@ __global__ void __launch_bounds__(256)
             T acc = gy[(size_t)(hb + h) * NP + (long long)gb * KB + lr];
             if (hasV)
                 for (int c = 0; c < KB; c++)
-                    acc = msub(acc, gV[(size_t)gb * TS + (size_t)c * KB + lr], sc_cvt<T, H>(st[c * hchunk + h]));
+                    acc = msub(acc, gV[(size_t)gb * TS + (size_t)c * KB + lr], st[c * hchunk + h]);
             if (hasW)
                 for (int c = 0; c < KB; c++)
-                    acc = msub(acc, gW[(size_t)gb * TS + (size_t)c * KB + lr],
-                               sc_cvt<T, H>(st[(KB + c) * hchunk + h]));
+                    acc = msub(acc, gW[(size_t)gb * TS + (size_t)c * KB + lr], st[(KB + c) * hchunk + h]);
             H *xp = x + (size_t)(hb + h) * n + s + lrow;
-            const H d = sc_cvt<H, T>(acc);
+            const H d = cvt_fast<H, T>(acc);
             *xp = accumulate ? *xp + d : d;
         }
+    }
+}
+
+// ------------------------------------------------------------ small bands
+// KB <= 4: one thread per (partition, column) runs both sweeps with its
+// vectors in registers; the L (forward) and G, E (backward) tiles of the next
+// block are staged by cp.async in the thread's own shared-memory slot.  z is
+// kept in gy between the sweeps (each thread rereads only what it wrote).
+template <class T, int KB> struct ChainApply {
+    static constexpr int TS = KB * KB;
+    static constexpr int STAGE = 2 * TS;
+    static constexpr int SLOT = 2 * STAGE * (int)sizeof(T) + 16;
+    static constexpr int NC = chain_threads(SLOT);
+    static constexpr size_t SMEM = (size_t)NC * SLOT;
+};
+
+template <class T, int KB>
+__global__ void __launch_bounds__(ChainApply<T, KB>::NC)
+    k_chain_apply(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                  const T *__restrict__ gL, const T *__restrict__ gG, const T *__restrict__ gE,
+                  const typename HighOf<T>::type *__restrict__ r, int n, int nrhs, long long NP, T *gy)
+{
+    using H = typename HighOf<T>::type;
+    using C = ChainApply<T, KB>;
+    constexpr int TS = C::TS;
+    constexpr int CT = TS * (int)sizeof(T) / 16; // 16-byte chunks per tile
+    extern __shared__ __align__(16) char smc[];
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int part = idx / nrhs, h = idx - part * nrhs;
+    if (part >= p) return; // no barriers below
+    T *slot = (T *)(smc + threadIdx.x * C::SLOT);
+    const int s = part_start[part], m = part_start[part + 1] - s;
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *yh = gy + (size_t)h * NP + (size_t)blk_off[part] * KB;
+    const H *rh = r + (size_t)h * n + s;
+
+    // forward: z_J = r_J - L_J z_{J-1}
+    T z[KB];
+#pragma unroll
+    for (int i = 0; i < KB; i++) z[i] = i < m ? sc_cvt<T, H>(rh[i]) : sc_zero<T>();
+    vst<T, KB>(yh, z);
+    if (N > 1) cp_async_chunks(slot + C::STAGE, gL + tb + TS, CT);
+    cp_async_commit();
+    for (int J = 1; J < N; J++) {
+        if (J + 1 < N) cp_async_chunks(slot + ((J + 1) & 1) * C::STAGE, gL + tb + (size_t)(J + 1) * TS, CT);
+        cp_async_commit();
+        T rj[KB];
+#pragma unroll
+        for (int i = 0; i < KB; i++) rj[i] = J * KB + i < m ? sc_cvt<T, H>(rh[J * KB + i]) : sc_zero<T>();
+        cp_async_wait_1();
+        RMat<T, KB> L;
+        rm_ldt(L, slot + (J & 1) * C::STAGE);
+#pragma unroll
+        for (int i = 0; i < KB; i++) {
+            T a = rj[i];
+#pragma unroll
+            for (int c = 0; c < KB; c++) a = msub(a, L.v[i][c], z[c]);
+            rj[i] = a;
+        }
+#pragma unroll
+        for (int i = 0; i < KB; i++) z[i] = rj[i];
+        vst<T, KB>(yh + (size_t)J * KB, z);
+    }
+    // backward: y_J = G_J (z_J - E_J y_{J+1})
+    auto issue = [&](int J) {
+        T *st = slot + (J & 1) * C::STAGE;
+        cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
+        cp_async_chunks(st + TS, gE + tb + (size_t)J * TS, CT);
+    };
+    issue(N - 1);
+    cp_async_commit();
+    T y[KB];
+    for (int J = N - 1; J >= 0; J--) {
+        if (J > 0) issue(J - 1);
+        cp_async_commit();
+        T t[KB];
+        vld<T, KB>(t, yh + (size_t)J * KB); // z_J
+        cp_async_wait_1();
+        const T *sc = slot + (J & 1) * C::STAGE;
+        if (J < N - 1) {
+            RMat<T, KB> E;
+            rm_ldt(E, sc + TS);
+#pragma unroll
+            for (int i = 0; i < KB; i++)
+#pragma unroll
+                for (int c = 0; c < KB; c++) t[i] = msub(t[i], E.v[i][c], y[c]);
+        }
+        RMat<T, KB> G;
+        rm_ldt(G, sc);
+#pragma unroll
+        for (int i = 0; i < KB; i++) {
+            T a = sc_zero<T>();
+#pragma unroll
+            for (int c = 0; c < KB; c++) a = madd(a, G.v[i][c], t[c]);
+            y[i] = a;
+        }
+        vst<T, KB>(yh + (size_t)J * KB, y);
+    }
+    cp_async_wait_all();
+}
+
+// interface unknowns u (FP64 / complex128) -> factor precision
+template <class T>
+__global__ void k_u_narrow(const typename HighOf<T>::type *__restrict__ u, T *ut, long long count)
+{
+    using H = typename HighOf<T>::type;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < count;
+         q += (long long)gridDim.x * blockDim.x)
+        ut[q] = cvt_fast<T, H>(u[q]);
+}
+
+// x (+)= y - V_i t_{i+1} - W_i b_{i-1} for small tiles: one thread per (padded
+// row, column), consecutive threads on consecutive rows (a CTA per row block
+// would leave most of its threads idle).
+template <class T, int KB>
+__global__ void __launch_bounds__(256)
+    k_retrieve_rows(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                    const int *__restrict__ blk_part, const T *__restrict__ gV, const T *__restrict__ gW,
+                    const T *__restrict__ gy, const T *__restrict__ ut, long long NP, int n_iface, int n, int nrhs,
+                    typename HighOf<T>::type *x, int accumulate, const spk_sysref *__restrict__ sys,
+                    const int *__restrict__ part_sys)
+{
+    using H = typename HighOf<T>::type;
+    constexpr size_t TS = (size_t)KB * KB;
+    const long long NR = (long long)n_iface * 2 * KB;
+    const long long tot = NP * nrhs;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < tot;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int h = (int)(q / NP);
+        const long long pr = q - (long long)h * NP;
+        const int gb = (int)(pr / KB), lr = (int)(pr - (long long)gb * KB);
+        const int part = blk_part[gb];
+        const int lrow = (gb - blk_off[part]) * KB + lr;
+        int s = part_start[part];
+        if (lrow >= part_start[part + 1] - s) continue; // identity padding row
+        H *xb = x;
+        int ld = n;
+        if (sys) {
+            const spk_sysref &S = sys[part_sys[part]];
+            xb = (H *)S.x;
+            ld = S.n;
+            s -= (int)S.row0;
+        }
+        T acc = gy[(size_t)h * NP + pr];
+        if (part < p - 1) {
+            const T *t = ut + (size_t)h * NR + (size_t)part * 2 * KB + KB;
+#pragma unroll
+            for (int c = 0; c < KB; c++) acc = msub(acc, gV[(size_t)gb * TS + (size_t)c * KB + lr], t[c]);
+        }
+        if (part > 0) {
+            const T *bw = ut + (size_t)h * NR + (size_t)(part - 1) * 2 * KB;
+#pragma unroll
+            for (int c = 0; c < KB; c++) acc = msub(acc, gW[(size_t)gb * TS + (size_t)c * KB + lr], bw[c]);
+        }
+        H *xp = xb + (size_t)h * ld + s + lrow;
+        const H d = cvt_fast<H, T>(acc);
+        *xp = accumulate ? *xp + d : d;
     }
 }
 
 template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
     constexpr int NT = NTOf<KB>::value;
-    const size_t smem = 16 + sizeof(T) * (4 * KB * TileLD<T, KB>::value + 3 * KB * RC);
+    const size_t smem = 16 + sizeof(T) * (4 * KB * TileLD<T, KB>::value + 3 * KB * RCS);
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return SPK_ECUDA;
         attr = true;
     }
-    dim3 grid(P->p, (nrhs + RC - 1) / RC);
-    k_apply<T, KB><<<grid, NT, smem, st>>>(P->d_part_start, P->d_blk_off, (const T *)P->d_L, (const T *)P->d_G,
-                                           (const T *)P->d_E, (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP,
-                                           (T *)P->d_z, (T *)P->d_y);
+    if constexpr (KB <= 4) {
+        using CA = ChainApply<T, KB>;
+        static bool cattr = false;
+        if (!cattr) {
+            if (cudaFuncSetAttribute(k_chain_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)CA::SMEM) != cudaSuccess)
+                return SPK_ECUDA;
+            cattr = true;
+        }
+        const long long threads = (long long)P->p * nrhs;
+        k_chain_apply<T, KB><<<(int)((threads + CA::NC - 1) / CA::NC), CA::NC, CA::SMEM, st>>>(
+            P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_G, (const T *)P->d_E,
+            (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP, (T *)P->d_y);
+    } else {
+        dim3 grid(P->p, (nrhs + RC - 1) / RC);
+        k_apply<T, KB><<<grid, NT, smem, st>>>(P->d_part_start, P->d_blk_off, (const T *)P->d_L, (const T *)P->d_G,
+                                               (const T *)P->d_E, (const typename HighOf<T>::type *)r, P->n, nrhs,
+                                               P->NP, (T *)P->d_z, (T *)P->d_y);
+    }
     SPK_CHECK_LAUNCH();
     P->launches++;
     if (P->n_iface > 0) {
@@ -289,10 +482,31 @@ template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, c
 
 template <class T, int KB> int run_retrieve(spk_plan *P, void *x, int nrhs, int accumulate, cudaStream_t st)
 {
-    k_retrieve<T, KB><<<P->total_blocks, 256, 0, st>>>(
-        P->d_part_start, P->d_blk_off, P->p, P->d_blk_part, (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y,
-        (const typename HighOf<T>::type *)P->d_u, P->NP, P->n_iface, P->n, nrhs, (typename HighOf<T>::type *)x,
-        accumulate);
+    using H = typename HighOf<T>::type;
+    // the interface unknowns, narrowed once into the (now free) reduced-RHS work array
+    T *ut = (T *)P->d_crg;
+    const long long cnt = (long long)(P->n_iface > 0 ? P->n_iface : 1) * 2 * KB * nrhs;
+    if (P->n_iface > 0) {
+        k_u_narrow<T><<<(int)std::min<long long>((cnt + 255) / 256, 4096), 256, 0, st>>>((const H *)P->d_u, ut, cnt);
+        SPK_CHECK_LAUNCH();
+        P->launches++;
+    }
+    if constexpr (KB <= 16) {
+        int sms = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long tot = P->NP * nrhs;
+        const int grid = (int)std::min<long long>((tot + 255) / 256, (long long)(sms > 0 ? sms : 152) * 8);
+        k_retrieve_rows<T, KB><<<grid, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, P->d_blk_part,
+                                                     (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y, ut,
+                                                     P->NP, P->n_iface, P->n, nrhs, (H *)x, accumulate, P->d_sys,
+                                                     P->d_part_sys);
+    } else {
+        k_retrieve<T, KB><<<P->total_blocks, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, P->d_blk_part,
+                                                           (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y,
+                                                           ut, P->NP, P->n_iface, P->n, nrhs, (H *)x, accumulate,
+                                                           P->d_sys, P->d_part_sys);
+    }
     SPK_CHECK_LAUNCH();
     P->launches++;
     return SPK_OK;

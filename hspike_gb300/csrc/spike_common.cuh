@@ -567,6 +567,119 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+// all but the most recently committed group complete
+__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+// `chunks` 16-byte pieces from global to shared, issued by this thread alone
+__device__ __forceinline__ void cp_async_chunks(void *s, const void *g, int chunks)
+{
+    for (int q = 0; q < chunks; q++) cp_async16((char *)s + 16 * q, (const char *)g + 16 * q);
+}
+
+// ------------------------------------------------------------ tiles in registers
+// Small bands (KB <= 4): a CTA per partition would leave most of its threads
+// idle and spend its time in barriers, so one thread runs one partition's
+// whole chain and owns its KB x KB tiles in registers.
+template <class T, int KB> struct RMat {
+    T v[KB][KB];
+};
+template <class T, int KB> __device__ __forceinline__ void rm_zero(RMat<T, KB> &m)
+{
+#pragma unroll
+    for (int r = 0; r < KB; r++)
+#pragma unroll
+        for (int c = 0; c < KB; c++) m.v[r][c] = sc_zero<T>();
+}
+// row-major source (element (r, c) at r*KB + c)
+template <class T, int KB> __device__ __forceinline__ void rm_ld(RMat<T, KB> &m, const T *p)
+{
+#pragma unroll
+    for (int r = 0; r < KB; r++) vld<T, KB>(m.v[r], p + r * KB);
+}
+// column-major source (element (r, c) at c*KB + r)
+template <class T, int KB> __device__ __forceinline__ void rm_ldt(RMat<T, KB> &m, const T *p)
+{
+#pragma unroll
+    for (int c = 0; c < KB; c++) {
+        T col[KB];
+        vld<T, KB>(col, p + c * KB);
+#pragma unroll
+        for (int r = 0; r < KB; r++) m.v[r][c] = col[r];
+    }
+}
+template <class T, int KB> __device__ __forceinline__ void rm_st(T *p, const RMat<T, KB> &m)
+{
+#pragma unroll
+    for (int r = 0; r < KB; r++) vst<T, KB>(p + r * KB, m.v[r]);
+}
+template <class T, int KB> __device__ __forceinline__ void rm_stt(T *p, const RMat<T, KB> &m)
+{
+#pragma unroll
+    for (int c = 0; c < KB; c++) {
+        T col[KB];
+#pragma unroll
+        for (int r = 0; r < KB; r++) col[r] = m.v[r][c];
+        vst<T, KB>(p + c * KB, col);
+    }
+}
+// C = A B
+template <class T, int KB>
+__device__ __forceinline__ void rm_mul(RMat<T, KB> &C, const RMat<T, KB> &A, const RMat<T, KB> &B)
+{
+#pragma unroll
+    for (int r = 0; r < KB; r++)
+#pragma unroll
+        for (int c = 0; c < KB; c++) {
+            T a = sc_zero<T>();
+#pragma unroll
+            for (int k = 0; k < KB; k++) a = madd(a, A.v[r][k], B.v[k][c]);
+            C.v[r][c] = a;
+        }
+}
+// C -= A B
+template <class T, int KB>
+__device__ __forceinline__ void rm_msub(RMat<T, KB> &C, const RMat<T, KB> &A, const RMat<T, KB> &B)
+{
+#pragma unroll
+    for (int r = 0; r < KB; r++)
+#pragma unroll
+        for (int c = 0; c < KB; c++) {
+            T a = C.v[r][c];
+#pragma unroll
+            for (int k = 0; k < KB; k++) a = msub(a, A.v[r][k], B.v[k][c]);
+            C.v[r][c] = a;
+        }
+}
+// In-place Gauss-Jordan inverse without pivoting (same recurrence as the
+// shared-memory tiles); false on a zero or non-finite pivot.
+template <class T, int KB> __device__ __forceinline__ bool rm_inv(RMat<T, KB> &S)
+{
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < KB; j++) {
+        const T piv = S.v[j][j];
+        if (!sc_finite_nonzero(piv)) ok = false;
+        const T ip = sc_recip(piv);
+#pragma unroll
+        for (int c = 0; c < KB; c++)
+            if (c != j) S.v[j][c] = S.v[j][c] * ip;
+        S.v[j][j] = ip;
+#pragma unroll
+        for (int r = 0; r < KB; r++) {
+            if (r == j) continue;
+            const T a = S.v[r][j];
+#pragma unroll
+            for (int c = 0; c < KB; c++)
+                if (c != j) S.v[r][c] = msub(S.v[r][c], a, S.v[j][c]);
+            S.v[r][j] = -(a * ip);
+        }
+    }
+    return ok;
+}
+// threads per CTA of a chain kernel whose threads each stage `bytes` in shared memory
+__host__ __device__ constexpr int chain_threads(int bytes)
+{
+    return (98304 / bytes) >= 128 ? 128 : (98304 / bytes) >= 64 ? 64 : 32;
+}
 
 // Dense global tile -> shared tile (row stride TileLD), asynchronously.  Tiles
 // whose rows are shorter than 16 bytes (FP32 with KB = 2) are copied
@@ -601,7 +714,22 @@ __device__ __forceinline__ float f64_to_f32(double x)
     // a carry out of the mantissa bumps the exponent (to inf at the top), as it should
     return __uint_as_float(((hi & 0x80000000u) | ((unsigned)e << 23)) + r + up);
 }
+// FP32 -> FP64 (exact) with integer instructions, for the same reason.  Normal
+// inputs only; zero, subnormal, inf and NaN take the hardware conversion.
+__device__ __forceinline__ double f32_to_f64(float x)
+{
+    const unsigned u = __float_as_uint(x);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)x;
+    const unsigned hi = (u & 0x80000000u) | ((e + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
 template <class T, class H> __device__ __forceinline__ T cvt_fast(H v) { return sc_cvt<T, H>(v); }
+template <> __device__ __forceinline__ double cvt_fast<double, float>(float v) { return f32_to_f64(v); }
+template <> __device__ __forceinline__ cdouble cvt_fast<cdouble, cfloat>(cfloat v)
+{
+    return {f32_to_f64(v.re), f32_to_f64(v.im)};
+}
 template <> __device__ __forceinline__ float cvt_fast<float, double>(double v) { return f64_to_f32(v); }
 template <> __device__ __forceinline__ cfloat cvt_fast<cfloat, cdouble>(cdouble v)
 {

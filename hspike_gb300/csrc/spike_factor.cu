@@ -154,15 +154,23 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     k_band_tiles(const int *__restrict__ rowptr, const int *__restrict__ colind,
                  const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
                  const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
-                 unsigned *err)
+                 unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys)
 {
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
     const int gb = blockIdx.x;
     const int part = blk_part[gb];
     const int J = gb - blk_off[part];
-    const int s = part_start[part], e = part_start[part + 1];
+    int s = part_start[part], e = part_start[part + 1];
     const bool zt = J == 0 && part > 0;
+    if (sys) { // batch group: the partition's own system, in its local rows
+        const spk_sysref &S = sys[part_sys[part]];
+        rowptr = S.rowptr;
+        colind = S.colind;
+        aij = (const H *)S.aij;
+        s -= (int)S.row0;
+        e -= (int)S.row0;
+    }
 
     // odd row stride: conflict-free for the row-major and the column-major stores
     constexpr int LD1 = KB + 1;
@@ -300,7 +308,8 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
         __syncthreads();
         for (int q = threadIdx.x; q < KB * KB; q += NT) {
             const int r = q / KB, c = q - r * KB;
-            if (r >= o) sZV[r * LD + c] = gBhat[(size_t)part * TS + (r - o) * KB + c];
+            // (o < 0: a partition shorter than a tile takes B^'s last m rows)
+            if (r >= o && r - o < KB) sZV[r * LD + c] = gBhat[(size_t)part * TS + (r - o) * KB + c];
         }
         __syncthreads();
         store_tile<T, KB>(gV + tb + J0 * TS, sZV);
@@ -370,6 +379,177 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     }
 }
 
+// ------------------------------------------------------------ small bands
+// KB <= 4: one thread per partition chain, tiles in registers (RMat), the next
+// block's tiles staged by cp.async in the thread's own shared-memory slot (no
+// barriers: a thread only reads what it copied).  Same recurrences and the same
+// global layouts as k_factor_fwd / k_factor_bwd.
+template <class T, int KB> struct ChainFwd {
+    static constexpr int TS = KB * KB;
+    static constexpr int STAGE = 3 * TS;                           // D, F^T, E
+    static constexpr int SLOT = 2 * STAGE * (int)sizeof(T) + 16;   // two stages + pad (odd in 16-byte units)
+    static constexpr int NC = chain_threads(SLOT);
+    static constexpr size_t SMEM = (size_t)NC * SLOT;
+};
+
+template <class T, int KB>
+__global__ void __launch_bounds__(ChainFwd<T, KB>::NC)
+    k_chain_fwd(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gZ, unsigned *err)
+{
+    using C = ChainFwd<T, KB>;
+    constexpr int TS = C::TS;
+    extern __shared__ __align__(16) char smc[];
+    const int part = blockIdx.x * blockDim.x + threadIdx.x;
+    if (part >= p) return; // no barriers below
+    T *slot = (T *)(smc + threadIdx.x * C::SLOT);
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * C::STAGE;
+    const bool doW = part > 0;
+    constexpr int CH = C::STAGE * (int)sizeof(T) / 16;
+    RMat<T, KB> G, Ep, Zp;
+    bool ok = true;
+    if (doW) rm_ld(Zp, gZ + tb); // z_0 = C^
+    cp_async_chunks(slot, gTp, CH);
+    cp_async_commit();
+    for (int J = 0; J < N; J++) {
+        if (J + 1 < N) cp_async_chunks(slot + ((J + 1) & 1) * C::STAGE, gTp + (size_t)(J + 1) * C::STAGE, CH);
+        cp_async_commit();
+        cp_async_wait_1();
+        const T *sc = slot + (J & 1) * C::STAGE;
+        RMat<T, KB> S;
+        rm_ld(S, sc); // D_J
+        if (J > 0) {
+            RMat<T, KB> L;
+            {
+                RMat<T, KB> F;
+                rm_ldt(F, sc + TS); // stored as F^T, row-major
+                rm_mul(L, F, G);    // L_J = F_{J-1} G_{J-1}
+            }
+            rm_stt(gL + tb + (size_t)J * TS, L);
+            rm_msub(S, L, Ep); // S_J = D_J - L_J E_{J-1}
+            if (doW) {
+                RMat<T, KB> Z;
+                rm_zero(Z);
+                rm_msub(Z, L, Zp); // z_J = -L_J z_{J-1}
+                rm_st(gZ + tb + (size_t)J * TS, Z);
+                Zp = Z;
+            }
+        }
+        rm_ld(Ep, sc + 2 * TS); // E_J, for the next block
+        ok = rm_inv(S) && ok;
+        rm_stt(gG + tb + (size_t)J * TS, S);
+        G = S;
+    }
+    if (!ok) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+
+template <class T, int KB> struct ChainBwd {
+    static constexpr int TS = KB * KB;
+    static constexpr int STAGE = 3 * TS;                         // G, E, Z (W) / G, E (V)
+    static constexpr int SLOT = 2 * STAGE * (int)sizeof(T) + 16;
+    static constexpr int NC = chain_threads(SLOT);
+    static constexpr size_t SMEM = (size_t)NC * SLOT;
+};
+
+// X_J = G_J (Z_J - E_J X_{J+1}): one thread per (partition, spike), V then W
+// of a partition on adjacent threads (they share the G / E tiles in L1).
+template <class T, int KB>
+__global__ void __launch_bounds__(ChainBwd<T, KB>::NC)
+    k_chain_bwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
+                const T *__restrict__ gG, const T *__restrict__ gE, const T *__restrict__ gZ,
+                const T *__restrict__ gBhat, T *gV, T *gW)
+{
+    using C = ChainBwd<T, KB>;
+    constexpr int TS = C::TS;
+    extern __shared__ __align__(16) char smc[];
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int part = idx >> 1;
+    const bool isW = idx & 1;
+    if (part >= p || (isW ? part == 0 : part == p - 1)) return; // no barriers below
+    T *slot = (T *)(smc + threadIdx.x * C::SLOT);
+    const int m = part_start[part + 1] - part_start[part];
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *gX = isW ? gW : gV;
+    constexpr int CT = TS * (int)sizeof(T) / 16; // chunks per tile
+    auto issue = [&](int J) {
+        T *st = slot + (J & 1) * C::STAGE;
+        cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
+        cp_async_chunks(st + TS, gE + tb + (size_t)J * TS, CT);
+        if (isW) cp_async_chunks(st + 2 * TS, gZ + tb + (size_t)J * TS, CT);
+    };
+    RMat<T, KB> X; // X_{J+1}
+    rm_zero(X);
+    int J = N - 1;
+    issue(J);
+    cp_async_commit();
+    if (!isW) {
+        // V's right-hand side [0; B^] lives in the last KB real rows: blocks J0
+        // (rows o..KB-1) and J0+1 (rows 0..o-1, when o > 0).  A partition shorter
+        // than a tile (o < 0) takes B^'s last m rows.
+        const int J0 = m >= KB ? (m - KB) / KB : 0;
+        const int o = m - KB - J0 * KB;
+        const T *B = gBhat + (size_t)part * TS;
+        RMat<T, KB> Z0;
+#pragma unroll
+        for (int r = 0; r < KB; r++)
+#pragma unroll
+            for (int c = 0; c < KB; c++)
+                Z0.v[r][c] = (r >= o && r - o < KB) ? B[(r - o) * KB + c] : sc_zero<T>();
+        if (o > 0) {
+            // z_{J0+1} = [B^ rows KB-o..KB-1 ; 0] - L_{J0+1} z_{J0};  X_{N-1} = G_{N-1} z_{N-1}
+            RMat<T, KB> Z1, L1;
+#pragma unroll
+            for (int r = 0; r < KB; r++)
+#pragma unroll
+                for (int c = 0; c < KB; c++) Z1.v[r][c] = r < o ? B[(KB - o + r) * KB + c] : sc_zero<T>();
+            rm_ldt(L1, gL + tb + (size_t)(J0 + 1) * TS);
+            rm_msub(Z1, L1, Z0);
+            if (J > 0) issue(J - 1);
+            cp_async_commit();
+            cp_async_wait_1();
+            RMat<T, KB> Gt;
+            rm_ldt(Gt, slot + (J & 1) * C::STAGE);
+            rm_mul(X, Gt, Z1);
+            rm_stt(gX + tb + (size_t)J * TS, X);
+            J--;
+        }
+        if (J >= 0) {
+            // block J0: X_{J0} = G_{J0} (z_{J0} - E_{J0} X_{J0+1})
+            if (J > 0) issue(J - 1);
+            cp_async_commit();
+            cp_async_wait_1();
+            const T *sc = slot + (J & 1) * C::STAGE;
+            RMat<T, KB> Gt, Et, Tm;
+            rm_ldt(Et, sc + TS);
+            Tm = Z0;
+            if (J < N - 1) rm_msub(Tm, Et, X);
+            rm_ldt(Gt, sc);
+            rm_mul(X, Gt, Tm);
+            rm_stt(gX + tb + (size_t)J * TS, X);
+            J--;
+        }
+    }
+    for (; J >= 0; J--) {
+        if (J > 0) issue(J - 1);
+        cp_async_commit();
+        cp_async_wait_1();
+        const T *sc = slot + (J & 1) * C::STAGE;
+        RMat<T, KB> Gt, Et, Tm;
+        if (isW)
+            rm_ld(Tm, sc + 2 * TS); // z_J (row-major)
+        else
+            rm_zero(Tm);
+        rm_ldt(Et, sc + TS);
+        if (J < N - 1) rm_msub(Tm, Et, X);
+        rm_ldt(Gt, sc);
+        rm_mul(X, Gt, Tm);
+        rm_stt(gX + tb + (size_t)J * TS, X);
+    }
+    cp_async_wait_all();
+}
+
 // Tips of V and W into the interface blocks of the reduced system (FP64):
 //   P_i = V_i bottom, Q_i = W_{i+1} top, X_i = W_i bottom, Y_i = V_{i+1} top.
 template <class T, int KB>
@@ -385,14 +565,17 @@ __global__ void k_tips(const int *__restrict__ part_start, const int *__restrict
     for (int q = threadIdx.x; q < KB * KB; q += blockDim.x) {
         const int r = q / KB, c = q - r * KB;
         // bottom rows of partition i: local row mi - KB + r
+        // (a partition shorter than one tile -- only a batch's one-partition
+        // system, whose spikes are zero -- has no distinct bottom tip)
         const int lb = mi - KB + r, Jb = lb / KB, rb = lb - Jb * KB;
-        const size_t ib = ((size_t)blk_off[i] + Jb) * TS + (size_t)c * KB + rb;
+        const bool hb = lb >= 0;
+        const size_t ib = hb ? ((size_t)blk_off[i] + Jb) * TS + (size_t)c * KB + rb : 0;
         // top rows of partition i+1: local row r (block 0)
         const size_t it = (size_t)blk_off[i + 1] * TS + (size_t)c * KB + r;
-        RP[(size_t)i * TS + q] = sc_cvt<H, T>(gV[ib]);
-        RQ[(size_t)i * TS + q] = sc_cvt<H, T>(gW[it]);
-        RX[(size_t)i * TS + q] = i > 0 ? sc_cvt<H, T>(gW[ib]) : sc_zero<H>();
-        RY[(size_t)i * TS + q] = (i + 1 < p - 1) ? sc_cvt<H, T>(gV[it]) : sc_zero<H>();
+        RP[(size_t)i * TS + q] = hb ? cvt_fast<H, T>(gV[ib]) : sc_zero<H>();
+        RQ[(size_t)i * TS + q] = cvt_fast<H, T>(gW[it]);
+        RX[(size_t)i * TS + q] = (i > 0 && hb) ? cvt_fast<H, T>(gW[ib]) : sc_zero<H>();
+        RY[(size_t)i * TS + q] = (i + 1 < p - 1) ? cvt_fast<H, T>(gV[it]) : sc_zero<H>();
     }
 }
 
@@ -404,6 +587,13 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     using S = FactorSmem<T, KB>;
     static bool attr = false;
     if (!attr) {
+        if constexpr (KB <= 4) {
+            if (cudaFuncSetAttribute(k_chain_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ChainFwd<T, KB>::SMEM) != cudaSuccess ||
+                cudaFuncSetAttribute(k_chain_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ChainBwd<T, KB>::SMEM) != cudaSuccess)
+                return SPK_ECUDA;
+        }
         if (cudaFuncSetAttribute(k_factor_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::fwd) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(k_band_tiles<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::band) !=
@@ -418,20 +608,34 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     spk_phase_begin(P, SPK_PH_BAND_TILES, st);
     k_band_tiles<T, KB><<<P->total_blocks, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start,
                                                               P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
-                                                              (T *)P->d_W, (T *)P->d_Bhat, P->d_err);
+                                                              (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys,
+                                                              P->d_part_sys);
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
     spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
-    k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L, (T *)P->d_G,
-                                                  (T *)P->d_W, P->d_err);
+    if constexpr (KB <= 4) {
+        using CF = ChainFwd<T, KB>;
+        k_chain_fwd<T, KB><<<(P->p + CF::NC - 1) / CF::NC, CF::NC, CF::SMEM, st>>>(
+            (const T *)P->d_T, P->d_blk_off, P->p, (T *)P->d_L, (T *)P->d_G, (T *)P->d_W, P->d_err);
+    } else {
+        k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L, (T *)P->d_G,
+                                                      (T *)P->d_W, P->d_err);
+    }
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
     P->launches += 2;
     if (P->p > 1) {
         spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
-        k_factor_bwd<T, KB><<<P->p, NT, S::bwd, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L,
-                                                      (const T *)P->d_G, (const T *)P->d_E, (T *)P->d_W,
-                                                      (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
+        if constexpr (KB <= 4) {
+            using CB = ChainBwd<T, KB>;
+            k_chain_bwd<T, KB><<<(2 * P->p + CB::NC - 1) / CB::NC, CB::NC, CB::SMEM, st>>>(
+                P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_G, (const T *)P->d_E,
+                (const T *)P->d_W, (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
+        } else {
+            k_factor_bwd<T, KB><<<P->p, NT, S::bwd, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L,
+                                                          (const T *)P->d_G, (const T *)P->d_E, (T *)P->d_W,
+                                                          (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
+        }
         SPK_CHECK_LAUNCH();
         k_tips<T, KB><<<P->n_iface, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_V,
                                                   (const T *)P->d_W, (H *)P->d_RP, (H *)P->d_RQ, (H *)P->d_RX,

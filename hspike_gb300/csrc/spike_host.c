@@ -22,8 +22,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "spike_gb300.h"
-#include "spike_internal.h"
+#include "spike_host_internal.h"
 
 const Error_t SPIKE_SUCCESS = 0;
 const Error_t SPIKE_ERROR = 1;
@@ -34,7 +33,7 @@ const Error_t SPIKE_ERROR = 1;
 static __thread int t_err_code = 0;
 static __thread char t_err_msg[512] = "";
 
-static Error_t fail(int code, const char *fmt, ...)
+Error_t spk_fail(int code, const char *fmt, ...)
 {
     va_list ap;
     va_start(ap, fmt);
@@ -44,18 +43,19 @@ static Error_t fail(int code, const char *fmt, ...)
     return SPIKE_ERROR;
 }
 
-static Error_t fail_spk(int code, const char *where)
+Error_t spk_fail_code(int code, const char *where)
 {
     switch (code) {
-    case SPK_ECUDA: return fail(SPIKE_ERR_CUDA, "%s: CUDA error: %s", where, spk_cuda_error_string());
-    case SPK_EMEM: return fail(SPIKE_ERR_MEMORY, "%s: device allocation failed (%s)", where, spk_cuda_error_string());
-    case SPK_EBAND: return fail(SPIKE_ERR_BANDWIDTH, "%s: bandwidth not supported in this precision", where);
-    case SPK_EPIVOT: return fail(SPIKE_ERR_PIVOT, "%s: zero or non-finite pivot", where);
-    default: return fail(code, "%s: error %d", where, code);
+    case SPK_ECUDA: return spk_fail(SPIKE_ERR_CUDA, "%s: CUDA error: %s", where, spk_cuda_error_string());
+    case SPK_EMEM: return spk_fail(SPIKE_ERR_MEMORY, "%s: device allocation failed (%s)", where, spk_cuda_error_string());
+    case SPK_EBAND: return spk_fail(SPIKE_ERR_BANDWIDTH, "%s: bandwidth not supported in this precision", where);
+    case SPK_EPIVOT: return spk_fail(SPIKE_ERR_PIVOT, "%s: zero or non-finite pivot", where);
+    case SPK_ECSR: return spk_fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", where);
+    default: return spk_fail(code, "%s: error %d", where, code);
     }
 }
 
-static Error_t succeed(void)
+Error_t spk_succeed(void)
 {
     t_err_code = SPIKE_ERR_NONE;
     t_err_msg[0] = 0;
@@ -65,32 +65,9 @@ static Error_t succeed(void)
 int spike_last_error_code(void) { return t_err_code; }
 const char *spike_last_error(void) { return t_err_msg; }
 
-#define TRY(expr)                                                                                               \
-    do {                                                                                                        \
-        int rc_ = (expr);                                                                                       \
-        if (rc_ != SPK_OK) return rc_;                                                                          \
-    } while (0)
-
 /* ------------------------------------------------------------------ */
 /* contexts                                                             */
 /* ------------------------------------------------------------------ */
-#define RHS_CHUNK 64 /* right-hand sides per internal solve pass */
-
-struct spike_context_s {
-    int device;
-    void *own_stream, *stream;
-    /* options */
-    int mode, partitions, max_refine, red_refine, timing;
-    double tol;
-    /* cached plan for the reference-API and device-pointer calls */
-    spk_plan *plan;
-    int *d_scratch; /* 4 ints for the analysis kernel */
-    /* staging buffers, grown on demand */
-    void *d_rowptr, *d_colind, *d_aij, *d_b, *d_x, *d_r, *d_stage;
-    size_t c_rowptr, c_colind, c_aij, c_b, c_x, c_r, c_stage;
-    spike_info_t info;
-};
-
 struct spike_factor_s {
     spike_context_t ctx;
     spk_plan *plan;
@@ -119,19 +96,18 @@ static int ensure(void **p, size_t *cap, size_t need)
     return SPK_OK;
 }
 
-static void plan_destroy(spk_plan *P);
 
 Error_t spike_context_create(spike_context_t *out)
 {
-    if (!out) return fail(SPIKE_ERR_ARGUMENT, "spike_context_create: NULL output");
+    if (!out) return spk_fail(SPIKE_ERR_ARGUMENT, "spike_context_create: NULL output");
     *out = NULL;
-    if (spk_device_count() <= 0) return fail(SPIKE_ERR_NO_DEVICE, "no CUDA device is visible");
+    if (spk_device_count() <= 0) return spk_fail(SPIKE_ERR_NO_DEVICE, "no CUDA device is visible");
     spike_context_t c = (spike_context_t)calloc(1, sizeof *c);
-    if (!c) return fail(SPIKE_ERR_MEMORY, "host allocation failed");
+    if (!c) return spk_fail(SPIKE_ERR_MEMORY, "host allocation failed");
     c->device = spk_current_device();
     if (spk_stream_create(&c->own_stream) != SPK_OK) {
         free(c);
-        return fail_spk(SPK_ECUDA, "spike_context_create");
+        return spk_fail_code(SPK_ECUDA, "spike_context_create");
     }
     c->stream = c->own_stream;
     c->mode = SPK_MIXED;
@@ -142,17 +118,17 @@ Error_t spike_context_create(spike_context_t *out)
     if (spk_malloc((void **)&c->d_scratch, 4 * sizeof(int)) != SPK_OK) {
         spk_stream_destroy(c->own_stream);
         free(c);
-        return fail_spk(SPK_EMEM, "spike_context_create");
+        return spk_fail_code(SPK_EMEM, "spike_context_create");
     }
     *out = c;
-    return succeed();
+    return spk_succeed();
 }
 
 Error_t spike_context_destroy(spike_context_t c)
 {
-    if (!c) return fail(SPIKE_ERR_ARGUMENT, "spike_context_destroy: NULL context");
+    if (!c) return spk_fail(SPIKE_ERR_ARGUMENT, "spike_context_destroy: NULL context");
     if (c->stream) spk_stream_sync(c->stream);
-    plan_destroy(c->plan);
+    spk_plan_destroy(c->plan);
     spk_free(c->d_scratch);
     spk_free(c->d_rowptr);
     spk_free(c->d_colind);
@@ -164,10 +140,10 @@ Error_t spike_context_destroy(spike_context_t c)
     spk_stream_destroy(c->own_stream);
     if (t_default == c) t_default = NULL;
     free(c);
-    return succeed();
+    return spk_succeed();
 }
 
-static spike_context_t get_ctx(spike_context_t c)
+spike_context_t spk_get_ctx(spike_context_t c)
 {
     if (c) return c;
     if (!t_default && spike_context_create(&t_default) != SPIKE_SUCCESS) return NULL;
@@ -176,51 +152,51 @@ static spike_context_t get_ctx(spike_context_t c)
 
 Error_t spike_context_set_stream(spike_context_t c, void *s)
 {
-    c = get_ctx(c);
+    c = spk_get_ctx(c);
     if (!c) return SPIKE_ERROR;
     spk_stream_sync(c->stream);
     c->stream = s ? s : c->own_stream;
-    return succeed();
+    return spk_succeed();
 }
 
 Error_t spike_set_option(spike_context_t c, int opt, double v)
 {
-    c = get_ctx(c);
+    c = spk_get_ctx(c);
     if (!c) return SPIKE_ERROR;
     switch (opt) {
     case SPIKE_OPT_PRECISION:
         if (v != SPIKE_PRECISION_MIXED && v != SPIKE_PRECISION_FP64)
-            return fail(SPIKE_ERR_ARGUMENT, "precision must be SPIKE_PRECISION_MIXED or SPIKE_PRECISION_FP64");
+            return spk_fail(SPIKE_ERR_ARGUMENT, "precision must be SPIKE_PRECISION_MIXED or SPIKE_PRECISION_FP64");
         c->mode = (v == SPIKE_PRECISION_FP64) ? SPK_PLAIN : SPK_MIXED;
         break;
     case SPIKE_OPT_PARTITIONS:
-        if (v < 0 || v > 1 << 24) return fail(SPIKE_ERR_ARGUMENT, "partitions must be in [0, 2^24]");
+        if (v < 0 || v > 1 << 24) return spk_fail(SPIKE_ERR_ARGUMENT, "partitions must be in [0, 2^24]");
         c->partitions = (int)v;
         break;
     case SPIKE_OPT_MAX_REFINE:
-        if (v < 0 || v > 100) return fail(SPIKE_ERR_ARGUMENT, "max refine sweeps must be in [0, 100]");
+        if (v < 0 || v > 100) return spk_fail(SPIKE_ERR_ARGUMENT, "max refine sweeps must be in [0, 100]");
         c->max_refine = (int)v;
         break;
     case SPIKE_OPT_TOLERANCE:
-        if (!(v >= 0)) return fail(SPIKE_ERR_ARGUMENT, "tolerance must be >= 0");
+        if (!(v >= 0)) return spk_fail(SPIKE_ERR_ARGUMENT, "tolerance must be >= 0");
         c->tol = v;
         break;
     case SPIKE_OPT_REDUCED_REFINE:
-        if (v < 0 || v > 20) return fail(SPIKE_ERR_ARGUMENT, "reduced refine sweeps must be in [0, 20]");
+        if (v < 0 || v > 20) return spk_fail(SPIKE_ERR_ARGUMENT, "reduced refine sweeps must be in [0, 20]");
         c->red_refine = (int)v;
         break;
     case SPIKE_OPT_PHASE_TIMING:
         c->timing = v != 0;
         break;
-    default: return fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
+    default: return spk_fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
-    return succeed();
+    return spk_succeed();
 }
 
 Error_t spike_get_option(spike_context_t c, int opt, double *v)
 {
-    c = get_ctx(c);
-    if (!c || !v) return c ? fail(SPIKE_ERR_ARGUMENT, "NULL output") : SPIKE_ERROR;
+    c = spk_get_ctx(c);
+    if (!c || !v) return c ? spk_fail(SPIKE_ERR_ARGUMENT, "NULL output") : SPIKE_ERROR;
     switch (opt) {
     case SPIKE_OPT_PRECISION: *v = c->mode == SPK_PLAIN ? SPIKE_PRECISION_FP64 : SPIKE_PRECISION_MIXED; break;
     case SPIKE_OPT_PARTITIONS: *v = c->partitions; break;
@@ -228,24 +204,24 @@ Error_t spike_get_option(spike_context_t c, int opt, double *v)
     case SPIKE_OPT_TOLERANCE: *v = c->tol; break;
     case SPIKE_OPT_REDUCED_REFINE: *v = c->red_refine; break;
     case SPIKE_OPT_PHASE_TIMING: *v = c->timing; break;
-    default: return fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
+    default: return spk_fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
-    return succeed();
+    return spk_succeed();
 }
 
 Error_t spike_get_info(spike_context_t c, spike_info_t *info)
 {
-    c = get_ctx(c);
-    if (!c || !info) return c ? fail(SPIKE_ERR_ARGUMENT, "NULL output") : SPIKE_ERROR;
+    c = spk_get_ctx(c);
+    if (!c || !info) return c ? spk_fail(SPIKE_ERR_ARGUMENT, "NULL output") : SPIKE_ERROR;
     *info = c->info;
-    return succeed();
+    return spk_succeed();
 }
 
 Error_t spike_get_phase_times(spike_context_t c, int nphases, double *ms, long long *calls, int reset)
 {
-    c = get_ctx(c);
+    c = spk_get_ctx(c);
     if (!c) return SPIKE_ERROR;
-    if (nphases < 0 || nphases > SPK_NPHASES) return fail(SPIKE_ERR_ARGUMENT, "nphases must be in [0, %d]", SPK_NPHASES);
+    if (nphases < 0 || nphases > SPK_NPHASES) return spk_fail(SPIKE_ERR_ARGUMENT, "nphases must be in [0, %d]", SPK_NPHASES);
     spk_plan *P = c->plan;
     for (int i = 0; i < nphases; i++) {
         if (ms) ms[i] = P ? P->phase_ms[i] : 0.0;
@@ -256,13 +232,13 @@ Error_t spike_get_phase_times(spike_context_t c, int nphases, double *ms, long l
             P->phase_ms[i] = 0.0;
             P->phase_calls[i] = 0;
         }
-    return succeed();
+    return spk_succeed();
 }
 
 /* ------------------------------------------------------------------ */
 /* plan: schedule + device workspace                                    */
 /* ------------------------------------------------------------------ */
-static int choose_block(int k)
+int spk_choose_block(int k)
 {
     const int sizes[] = {2, 4, 8, 16, 32, 64};
     for (int i = 0; i < 6; i++)
@@ -291,7 +267,7 @@ static int choose_partitions(int n, int KB, int requested)
     return (int)p;
 }
 
-static void plan_destroy(spk_plan *P)
+void spk_plan_destroy(spk_plan *P)
 {
     if (!P) return;
     spk_phase_destroy(P);
@@ -314,12 +290,10 @@ static int palloc(spk_plan *P, void **p, size_t bytes)
     return SPK_OK;
 }
 
-static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int mode, int partitions,
-                       int nrhs_max, void *stream, spk_plan **out)
+int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex, int mode, int p,
+                   const int *part_start, int nrhs_max, void *stream, spk_plan **out)
 {
     *out = NULL;
-    const int k = ku > kl ? ku : kl;
-    const int KB = choose_block(k < 1 ? 1 : k);
     if (!KB || spk_factor_smem(KB, is_complex, mode) == 0) return SPK_EBAND;
     spk_plan *P = (spk_plan *)calloc(1, sizeof *P);
     if (!P) return SPK_EMEM;
@@ -331,19 +305,15 @@ static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int
     P->is_complex = is_complex;
     P->mode = mode;
     P->nrhs_max = nrhs_max;
-    const int p = choose_partitions(n, KB, partitions);
     P->p = p;
     P->n_iface = p - 1;
     P->part_start = (int *)malloc(sizeof(int) * (p + 1));
     P->blk_off = (int *)malloc(sizeof(int) * (p + 1));
     if (!P->part_start || !P->blk_off) {
-        plan_destroy(P);
+        spk_plan_destroy(P);
         return SPK_EMEM;
     }
-    /* spike_solve_analysis: regular partitions, remainder in the last one */
-    const int nreg = n / p;
-    for (int i = 0; i < p; i++) P->part_start[i] = i * nreg;
-    P->part_start[p] = n;
+    memcpy(P->part_start, part_start, sizeof(int) * (p + 1));
     P->blk_off[0] = 0;
     for (int i = 0; i < p; i++) {
         const int m = P->part_start[i + 1] - P->part_start[i];
@@ -360,7 +330,7 @@ static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int
     P->cr_off = (long long *)malloc(sizeof(long long) * (levels + 2));
     P->cr_moff = (long long *)malloc(sizeof(long long) * (levels + 2));
     if (!P->cr_count || !P->cr_off || !P->cr_moff) {
-        plan_destroy(P);
+        spk_plan_destroy(P);
         return SPK_EMEM;
     }
     long long tiles = 0, mtiles = 0;
@@ -425,18 +395,37 @@ static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int
         free(bp);
     }
     if (rc != SPK_OK) {
-        plan_destroy(P);
+        spk_plan_destroy(P);
         return rc;
     }
     *out = P;
     return SPK_OK;
 }
 
+static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int mode, int partitions,
+                       int nrhs_max, void *stream, spk_plan **out)
+{
+    *out = NULL;
+    const int k = ku > kl ? ku : kl;
+    const int KB = spk_choose_block(k < 1 ? 1 : k);
+    if (!KB || spk_factor_smem(KB, is_complex, mode) == 0) return SPK_EBAND;
+    const int p = choose_partitions(n, KB, partitions);
+    int *ps = (int *)malloc(sizeof(int) * (p + 1));
+    if (!ps) return SPK_EMEM;
+    /* spike_solve_analysis: regular partitions, remainder in the last one */
+    const int nreg = n / p;
+    for (int i = 0; i < p; i++) ps[i] = i * nreg;
+    ps[p] = n;
+    const int rc = spk_plan_build(n, nnz, ku, kl, KB, is_complex, mode, p, ps, nrhs_max, stream, out);
+    free(ps);
+    return rc;
+}
+
 static int plan_matches(const spk_plan *P, int n, int ku, int kl, int is_complex, int mode, int partitions, int nrhs)
 {
     if (!P) return 0;
     const int k = ku > kl ? ku : kl;
-    const int KB = choose_block(k < 1 ? 1 : k);
+    const int KB = spk_choose_block(k < 1 ? 1 : k);
     return P->n == n && P->KB == KB && P->is_complex == is_complex && P->mode == mode &&
            P->p == choose_partitions(n, KB, partitions) && nrhs <= P->nrhs_max;
 }
@@ -550,12 +539,12 @@ static void fill_info(spike_context_t c, const spk_plan *P, const refine_opts *o
 
 static Error_t finish(int rc, const char *where, const refine_opts *o)
 {
-    if (rc == SPK_OK) return succeed();
+    if (rc == SPK_OK) return spk_succeed();
     if (rc == SPK_ECONV)
-        return fail(SPIKE_ERR_CONVERGENCE, "%s: relative residual %.3e above tolerance %.3e after %d sweeps", where,
+        return spk_fail(SPIKE_ERR_CONVERGENCE, "%s: relative residual %.3e above tolerance %.3e after %d sweeps", where,
                     o->relres_max, o->tol, o->sweeps);
-    if (rc == SPK_ECSR) return fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", where);
-    return fail_spk(rc, where);
+    if (rc == SPK_ECSR) return spk_fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", where);
+    return spk_fail_code(rc, where);
 }
 
 /* analysis + plan + factor + solve on device-resident FP64 data */
@@ -568,7 +557,7 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
     if (info[2]) return SPK_ECSR;
     const int chunk = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
     if (!plan_matches(c->plan, n, info[0], info[1], is_complex, c->mode, c->partitions, chunk)) {
-        plan_destroy(c->plan);
+        spk_plan_destroy(c->plan);
         c->plan = NULL;
         TRY(plan_create(n, nnz, info[0], info[1], is_complex, c->mode, c->partitions, chunk, c->stream, &c->plan));
     }
@@ -603,10 +592,10 @@ static void opts_from(const spike_context_t c, refine_opts *o)
 static Error_t host_solve(int dtype, const char *name, integer_t n, integer_t nnz, integer_t nrhs,
                           const integer_t *colind, const integer_t *rowptr, const void *aij, void *x, const void *b)
 {
-    if (n < 0 || nnz < 0 || nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
-    if (n == 0 || nrhs == 0) return succeed();
-    if (!colind || !rowptr || !aij || !x || !b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
-    spike_context_t c = get_ctx(NULL);
+    if (n < 0 || nnz < 0 || nrhs < 0) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
+    if (n == 0 || nrhs == 0) return spk_succeed();
+    if (!colind || !rowptr || !aij || !x || !b) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    spike_context_t c = spk_get_ctx(NULL);
     if (!c) return SPIKE_ERROR;
     const int cplx = dtype == SPK_C || dtype == SPK_Z;
     const int wide = dtype == SPK_S || dtype == SPK_C;
@@ -693,10 +682,10 @@ Error_t dspike_core_host_blocking(const integer_t n, const integer_t nnz, const 
 static Error_t device_solve(spike_context_t c, int cplx, const char *name, integer_t n, integer_t nnz, integer_t nrhs,
                             const integer_t *ci, const integer_t *rp, const void *aij, void *x, const void *b)
 {
-    if (n < 0 || nnz < 0 || nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
-    if (n == 0 || nrhs == 0) return succeed();
-    if (!ci || !rp || !aij || !x || !b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
-    c = get_ctx(c);
+    if (n < 0 || nnz < 0 || nrhs < 0) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
+    if (n == 0 || nrhs == 0) return spk_succeed();
+    if (!ci || !rp || !aij || !x || !b) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    c = spk_get_ctx(c);
     if (!c) return SPIKE_ERROR;
     refine_opts o;
     opts_from(c, &o);
@@ -723,14 +712,14 @@ Error_t spike_zsolve_device(spike_context_t c, integer_t n, integer_t nnz, integ
 static Error_t factor_common(spike_context_t c, int cplx, const char *name, integer_t n, integer_t nnz,
                              const integer_t *ci, const integer_t *rp, const void *aij, int host, spike_factor_t *out)
 {
-    if (!out) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL output", name);
+    if (!out) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL output", name);
     *out = NULL;
-    if (n <= 0 || nnz < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n must be > 0 and nnz >= 0", name);
-    if (!ci || !rp || !aij) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
-    c = get_ctx(c);
+    if (n <= 0 || nnz < 0) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: n must be > 0 and nnz >= 0", name);
+    if (!ci || !rp || !aij) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    c = spk_get_ctx(c);
     if (!c) return SPIKE_ERROR;
     spike_factor_t f = (spike_factor_t)calloc(1, sizeof *f);
-    if (!f) return fail(SPIKE_ERR_MEMORY, "%s: host allocation failed", name);
+    if (!f) return spk_fail(SPIKE_ERR_MEMORY, "%s: host allocation failed", name);
     f->ctx = c;
     f->is_complex = cplx;
     f->n = n;
@@ -771,7 +760,7 @@ static Error_t factor_common(spike_context_t c, int cplx, const char *name, inte
         return finish(rc, name, &o);
     }
     *out = f;
-    return succeed();
+    return spk_succeed();
 }
 
 Error_t spike_dfactor(spike_context_t c, integer_t n, integer_t nnz, const integer_t *colind, const integer_t *rowptr,
@@ -793,11 +782,11 @@ Error_t spike_dfactor_device(spike_context_t c, integer_t n, integer_t nnz, cons
 static Error_t solve_factored(spike_factor_t f, int cplx, const char *name, integer_t nrhs, void *x, const void *b,
                               int host)
 {
-    if (!f || f->released) return fail(SPIKE_ERR_HANDLE, "%s: invalid factor handle", name);
-    if (f->is_complex != cplx) return fail(SPIKE_ERR_ARGUMENT, "%s: handle holds another value type", name);
-    if (nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: nrhs must be >= 0", name);
-    if (nrhs == 0) return succeed();
-    if (!x || !b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    if (!f || f->released) return spk_fail(SPIKE_ERR_HANDLE, "%s: invalid factor handle", name);
+    if (f->is_complex != cplx) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: handle holds another value type", name);
+    if (nrhs < 0) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: nrhs must be >= 0", name);
+    if (nrhs == 0) return spk_succeed();
+    if (!x || !b) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
     spike_context_t c = f->ctx;
     spk_plan *P = f->plan;
     const size_t hs = (cplx ? 2 : 1) * 8;
@@ -842,9 +831,9 @@ Error_t spike_dsolve_factored_device(spike_factor_t f, integer_t nrhs, double *d
 
 Error_t spike_factor_release(spike_factor_t f)
 {
-    if (!f || f->released) return fail(SPIKE_ERR_HANDLE, "spike_factor_release: invalid factor handle");
+    if (!f || f->released) return spk_fail(SPIKE_ERR_HANDLE, "spike_factor_release: invalid factor handle");
     if (f->ctx && f->ctx->stream) spk_stream_sync(f->ctx->stream);
-    plan_destroy(f->plan);
+    spk_plan_destroy(f->plan);
     spk_free(f->o_rowptr);
     spk_free(f->o_colind);
     spk_free(f->o_aij);
@@ -853,7 +842,7 @@ Error_t spike_factor_release(spike_factor_t f)
     spk_free(f->d_r);
     f->released = 1;
     free(f);
-    return succeed();
+    return spk_succeed();
 }
 
 /* ------------------------------------------------------------------ */
@@ -891,14 +880,14 @@ Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, 
                                     void *cuda_stream)
 {
     const char *name = "spike_dsolve_device_noalloc";
-    if (n < 0 || nnz < 0 || nrhs < 0) return fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
-    if (n == 0 || nrhs == 0) return succeed();
-    if (!d_colind || !d_rowptr || !d_aij || !d_x || !d_b) return fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
-    if (spk_device_count() <= 0) return fail(SPIKE_ERR_NO_DEVICE, "%s: no CUDA device is visible", name);
+    if (n < 0 || nnz < 0 || nrhs < 0) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
+    if (n == 0 || nrhs == 0) return spk_succeed();
+    if (!d_colind || !d_rowptr || !d_aij || !d_x || !d_b) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    if (spk_device_count() <= 0) return spk_fail(SPIKE_ERR_NO_DEVICE, "%s: no CUDA device is visible", name);
     void *ws = NULL;
     size_t ws_bytes = 0;
     if (spk_noalloc_scratch(&ws, &ws_bytes) != SPK_OK)
-        return fail(SPIKE_ERR_CUDA, "%s: cannot resolve the fixed workspace on this device", name);
+        return spk_fail(SPIKE_ERR_CUDA, "%s: cannot resolve the fixed workspace on this device", name);
     void *stream = cuda_stream;
     carve_t cv = {(char *)ws, 0, ws_bytes};
 
@@ -907,16 +896,16 @@ Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, 
     long long launches = 0;
     int *d_an = (int *)carve(&cv, 4 * sizeof(int));
     int rc = spk_analyze(n, nnz, d_rowptr, d_colind, d_an, info, stream, &launches);
-    if (rc != SPK_OK) return fail_spk(rc, name);
-    if (info[2]) return fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", name);
+    if (rc != SPK_OK) return spk_fail_code(rc, name);
+    if (info[2]) return spk_fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", name);
 
     /* schedule, as plan_create does, with stack arrays */
     spk_plan P;
     memset(&P, 0, sizeof P);
     const int k = info[0] > info[1] ? info[0] : info[1];
-    const int KB = choose_block(k < 1 ? 1 : k);
+    const int KB = spk_choose_block(k < 1 ? 1 : k);
     if (!KB || spk_factor_smem(KB, 0, SPK_MIXED) == 0)
-        return fail(SPIKE_ERR_BANDWIDTH, "%s: bandwidth %d above the supported tile size", name, k);
+        return spk_fail(SPIKE_ERR_BANDWIDTH, "%s: bandwidth %d above the supported tile size", name, k);
     int p = choose_partitions(n, KB, 0);
     if (p > NOALLOC_MAX_PARTS) p = NOALLOC_MAX_PARTS;
     int part_start[NOALLOC_MAX_PARTS + 1], blk_off[NOALLOC_MAX_PARTS + 1];
@@ -928,7 +917,7 @@ Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, 
     blk_off[0] = 0;
     for (int i = 0; i < p; i++) blk_off[i + 1] = blk_off[i] + (part_start[i + 1] - part_start[i] + KB - 1) / KB;
     if (blk_off[p] > NOALLOC_MAX_BLOCKS)
-        return fail(SPIKE_ERR_MEMORY, "%s: %d row blocks exceed the fixed schedule's %d (system too large for the "
+        return spk_fail(SPIKE_ERR_MEMORY, "%s: %d row blocks exceed the fixed schedule's %d (system too large for the "
                     "%u-byte no-allocation workspace)", name, blk_off[p], NOALLOC_MAX_BLOCKS, SPK_NOALLOC_SCRATCH_BYTES);
     int blk_part[NOALLOC_MAX_BLOCKS];
     for (int i = 0; i < p; i++)
@@ -1003,7 +992,7 @@ Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, 
     void *d_r = carve(&cv, hs * (size_t)n * nr);
 #undef CV
     if (cv.used > cv.cap)
-        return fail(SPIKE_ERR_MEMORY, "%s: the system needs more than the %u-byte no-allocation workspace "
+        return spk_fail(SPIKE_ERR_MEMORY, "%s: the system needs more than the %u-byte no-allocation workspace "
                     "(use spike_dsolve_device)", name, SPK_NOALLOC_SCRATCH_BYTES);
     P.bytes = cv.used;
 

@@ -1,0 +1,54 @@
+/*
+ * spike_host_internal.h -- pieces of the C host layer shared by its
+ * translation units (spike_host.c: the single-system API; spike_batch.c:
+ * batches; spike_serve.c: the request loop).  Everything here is hidden from
+ * the shared library's export table.
+ */
+#ifndef SPIKE_GB300_HOST_INTERNAL_H
+#define SPIKE_GB300_HOST_INTERNAL_H
+
+#include "spike_gb300.h"
+#include "spike_internal.h"
+
+#define SPK_INTERNAL __attribute__((visibility("hidden")))
+
+#define TRY(expr)                                                                                               \
+    do {                                                                                                        \
+        int rc_ = (expr);                                                                                       \
+        if (rc_ != SPK_OK) return rc_;                                                                          \
+    } while (0)
+
+#define RHS_CHUNK 64 /* right-hand sides per internal solve pass */
+
+struct spike_context_s {
+    int device;
+    void *own_stream, *stream;
+    /* options */
+    int mode, partitions, max_refine, red_refine, timing;
+    double tol;
+    /* cached plan for the reference-API and device-pointer calls */
+    spk_plan *plan;
+    int *d_scratch; /* 4 ints for the analysis kernel */
+    /* staging buffers, grown on demand */
+    void *d_rowptr, *d_colind, *d_aij, *d_b, *d_x, *d_r, *d_stage;
+    size_t c_rowptr, c_colind, c_aij, c_b, c_x, c_r, c_stage;
+    spike_info_t info;
+};
+
+/* thread-local error detail (spike_last_error_code / spike_last_error) */
+SPK_INTERNAL Error_t spk_fail(int code, const char *fmt, ...);
+SPK_INTERNAL Error_t spk_fail_code(int spk_code, const char *where);
+SPK_INTERNAL Error_t spk_succeed(void);
+
+/* the context itself, or the calling thread's default one (created on demand) */
+SPK_INTERNAL spike_context_t spk_get_ctx(spike_context_t c);
+
+/* smallest supported tile size >= k (0 when k is above the largest) */
+SPK_INTERNAL int spk_choose_block(int k);
+/* A plan for an explicit schedule: tile size KB, p partitions starting at
+ * part_start[0..p] (part_start[p] = n).  Allocates the device workspace. */
+SPK_INTERNAL int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex, int mode, int p,
+                                const int *part_start, int nrhs_max, void *stream, spk_plan **out);
+SPK_INTERNAL void spk_plan_destroy(spk_plan *P);
+
+#endif /* SPIKE_GB300_HOST_INTERNAL_H */

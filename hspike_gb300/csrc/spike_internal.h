@@ -63,6 +63,20 @@ enum spk_phase {
 #define SPK_DEV_ERR_BAND 2u
 #define SPK_DEV_ERR_CSR 4u
 
+/* One system of a batch as the kernels see it.  A batch group lays its
+ * systems end to end in one row space (system s owns rows [row0, row0 + n));
+ * partitions never straddle two systems, so no coupling crosses a system
+ * boundary and those interfaces decouple in the reduced system.  The kernels
+ * read each system's own CSR, b and x through this table (no packing). */
+typedef struct spk_sysref {
+    const int *rowptr, *colind;
+    const void *aij; /* FP64 / complex128 */
+    void *x;         /* n x nrhs, ld n */
+    const void *b;   /* n x nrhs, ld n */
+    long long row0;  /* first row of the system in the group's row space */
+    int n, pad;
+} spk_sysref;
+
 typedef struct spk_plan {
     /* problem */
     int n, nrhs_max, ku, kl, KB, p;
@@ -97,6 +111,10 @@ typedef struct spk_plan {
     void *d_g, *d_u, *d_rr; /* FP64 reduced RHS, solution, reduced residual: n_iface*2KB x nrhs_max */
     void *d_du;            /* FP64 reduced correction */
     unsigned int *d_err;   /* device error word */
+    /* batch groups only (NULL otherwise): per-system table and the system
+     * of each partition; CSR, b and x are then read through the table */
+    const spk_sysref *d_sys;
+    const int *d_part_sys;
     double *d_norms;       /* 2*nrhs_max: ||r||^2 then ||b||^2 per column */
     /* bookkeeping */
     long long launches; /* kernel launches issued for this plan */
@@ -154,6 +172,30 @@ int spk_narrow(const void *src, void *dst, long long count, int is_complex, void
 int spk_residual(const spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij,
                  const void *d_x, const void *d_b, void *d_r, int nrhs, int want_bnorm, double *d_norms,
                  void *stream);
+
+/* Batch residual in FP64 / complex128 over the systems of a group, one CTA
+ * per chunk of rows of one system (d_chunks: {system, first local row} pairs,
+ * rows_per_chunk rows each).  have_x = 0: r = b (x is zero); 1: r = b - A x.
+ * r: the group's row space, ld n_rows.  norms[s][0:nrhs] += ||r||^2 and
+ * norms[s][nrhs:2 nrhs] += ||b||^2. */
+int spk_residual_batch(const spk_sysref *d_sys, const int *d_chunks, int nchunks, int rows_per_chunk,
+                       int row_len, long long n_rows, int nrhs, int is_complex, int have_x, void *d_r,
+                       double *d_norms, void *stream, long long *launches);
+/* relres[s] = max_h ||r_h|| / ||b_h|| from the norms above; *d_worst =
+ * max over s (as double bits, atomically) */
+int spk_batch_relres(const double *d_norms, int nsys, int nrhs, double *d_relres, unsigned long long *d_worst,
+                     void *stream, long long *launches);
+
+/* ---- CUDA graphs and stream fork/join (spike_util.cu) ---- */
+int spk_capture_begin(void *stream);
+int spk_capture_end(void *stream, void **graph_exec);
+int spk_graph_launch(void *graph_exec, void *stream);
+void spk_graph_destroy(void *graph_exec);
+/* make `child` wait for the work issued so far on `parent` */
+int spk_stream_fork(void *parent, void *child);
+/* timing with an event pair on one stream (ms between begin and end) */
+int spk_timer_begin(void **timer, void *stream);
+int spk_timer_end(void *timer, void *stream, double *ms);
 
 /* ---- factorization (spike_factor.cu) ---- */
 /* K2: block LU of every A_i, spikes V_i/W_i, tips into the reduced blocks. */

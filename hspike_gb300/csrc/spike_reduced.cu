@@ -44,7 +44,7 @@ template <class T>
 __global__ void k_red_cvt(const typename HighOf<T>::type *__restrict__ src, T *dst, long long count)
 {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < count; q += (long long)gridDim.x * blockDim.x)
-        dst[q] = sc_cvt<T, typename HighOf<T>::type>(src[q]);
+        dst[q] = cvt_fast<T, typename HighOf<T>::type>(src[q]);
 }
 
 // Odd blocks j of a level (or the single top block): M = D_j^{-1} by quadrants
@@ -297,7 +297,7 @@ __global__ void k_red_load(const typename HighOf<T>::type *__restrict__ res, T *
     const long long tot = NR * nrhs;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < tot; q += (long long)gridDim.x * blockDim.x) {
         const long long h = q / NR, r = q - h * NR;
-        g[h * stride + r] = sc_cvt<T, typename HighOf<T>::type>(res[q]);
+        g[h * stride + r] = cvt_fast<T, typename HighOf<T>::type>(res[q]);
     }
 }
 
@@ -310,7 +310,7 @@ __global__ void k_red_accum(const T *__restrict__ du, typename HighOf<T>::type *
     const long long tot = NR * nrhs;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < tot; q += (long long)gridDim.x * blockDim.x) {
         const long long h = q / NR, r = q - h * NR;
-        const H d = sc_cvt<H, T>(du[h * stride + r]);
+        const H d = cvt_fast<H, T>(du[h * stride + r]);
         u[q] = first ? d : u[q] + d;
     }
 }

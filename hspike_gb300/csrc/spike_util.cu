@@ -298,6 +298,210 @@ extern "C" int spk_residual(const spk_plan *P, const int *d_rowptr, const int *d
     return residual_g<double>(P, d_rowptr, d_colind, d_aij, d_x, d_b, d_r, nrhs, want_bnorm, d_norms, st);
 }
 
+// ------------------------------------------------------------ batch residual
+// One CTA per chunk of rows of one system; G lanes per row; NH right-hand-side
+// columns per pass over the row's entries (the CSR entries are read once per
+// pass, not once per column).
+template <class H, int G, int NH>
+__global__ void __launch_bounds__(256)
+    k_residual_batch(const spk_sysref *__restrict__ sys, const int2 *__restrict__ chunks, int R, long long n_rows,
+                     int nrhs, int have_x, H *r, double *norms)
+{
+    __shared__ double sr[NH], sb[NH];
+    if (threadIdx.x < NH) sr[threadIdx.x] = sb[threadIdx.x] = 0.0;
+    const int2 ch = chunks[blockIdx.x];
+    const spk_sysref S = sys[ch.x];
+    const int n = S.n, lr0 = ch.y, lr1 = min(n, ch.y + R);
+    const H *__restrict__ a = (const H *)S.aij;
+    const H *__restrict__ x = (const H *)S.x;
+    const H *__restrict__ b = (const H *)S.b;
+    const int sub = threadIdx.x % G;
+    constexpr int RPB = 256 / G; // rows per CTA per pass
+    for (int h0 = 0; h0 < nrhs; h0 += NH) {
+        double lr[NH], lb[NH];
+#pragma unroll
+        for (int j = 0; j < NH; j++) lr[j] = lb[j] = 0.0;
+        __syncthreads();
+        // every lane runs every iteration so the shuffles see the full warp
+        for (int base = lr0; base < lr1; base += RPB) {
+            const int row = base + threadIdx.x / G;
+            const bool valid = row < lr1;
+            H acc[NH];
+#pragma unroll
+            for (int j = 0; j < NH; j++) acc[j] = sc_zero<H>();
+            if (have_x && valid) {
+                const int t0 = S.rowptr[row], t1 = S.rowptr[row + 1];
+                for (int t = t0 + sub; t < t1; t += G) {
+                    const H av = a[t];
+                    const int c = S.colind[t];
+#pragma unroll
+                    for (int j = 0; j < NH; j++)
+                        if (h0 + j < nrhs) acc[j] = madd(acc[j], av, x[(size_t)(h0 + j) * n + c]);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NH; j++)
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) {
+                    if constexpr (sizeof(H) == 8) {
+                        acc[j] = acc[j] + __shfl_xor_sync(0xffffffffu, acc[j], o);
+                    } else {
+                        H other;
+                        other.re = __shfl_xor_sync(0xffffffffu, acc[j].re, o);
+                        other.im = __shfl_xor_sync(0xffffffffu, acc[j].im, o);
+                        acc[j] = acc[j] + other;
+                    }
+                }
+            if (sub == 0 && valid) {
+#pragma unroll
+                for (int j = 0; j < NH; j++) {
+                    if (h0 + j >= nrhs) break;
+                    const H bv = b[(size_t)(h0 + j) * n + row];
+                    const H rv = bv - acc[j];
+                    r[(size_t)(h0 + j) * n_rows + S.row0 + row] = rv;
+                    lr[j] += sc_abs2(rv);
+                    lb[j] += sc_abs2(bv);
+                }
+            }
+        }
+        if (sub == 0)
+#pragma unroll
+            for (int j = 0; j < NH; j++) {
+                if (h0 + j >= nrhs) break;
+                atomicAdd(&sr[j], lr[j]);
+                atomicAdd(&sb[j], lb[j]);
+            }
+        __syncthreads();
+        if (threadIdx.x < NH && h0 + (int)threadIdx.x < nrhs) {
+            double *ns = norms + (size_t)ch.x * 2 * nrhs;
+            atomicAdd(&ns[h0 + threadIdx.x], sr[threadIdx.x]);
+            atomicAdd(&ns[nrhs + h0 + threadIdx.x], sb[threadIdx.x]);
+            sr[threadIdx.x] = sb[threadIdx.x] = 0.0;
+        }
+    }
+}
+
+template <class H, int G>
+static int residual_batch_g(const spk_sysref *d_sys, const int *d_chunks, int nchunks, int R, long long n_rows,
+                            int nrhs, int have_x, void *d_r, double *d_norms, cudaStream_t st)
+{
+    const int2 *ch = (const int2 *)d_chunks;
+    if (nrhs >= 4)
+        k_residual_batch<H, G, 4><<<nchunks, 256, 0, st>>>(d_sys, ch, R, n_rows, nrhs, have_x, (H *)d_r, d_norms);
+    else if (nrhs >= 2)
+        k_residual_batch<H, G, 2><<<nchunks, 256, 0, st>>>(d_sys, ch, R, n_rows, nrhs, have_x, (H *)d_r, d_norms);
+    else
+        k_residual_batch<H, G, 1><<<nchunks, 256, 0, st>>>(d_sys, ch, R, n_rows, nrhs, have_x, (H *)d_r, d_norms);
+    return ck(cudaGetLastError());
+}
+
+extern "C" int spk_residual_batch(const spk_sysref *d_sys, const int *d_chunks, int nchunks, int rows_per_chunk,
+                                  int row_len, long long n_rows, int nrhs, int is_complex, int have_x, void *d_r,
+                                  double *d_norms, void *stream, long long *launches)
+{
+    if (nchunks <= 0) return SPK_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (launches) (*launches)++;
+    const int R = rows_per_chunk;
+    // lanes per row from the rows' length (as in the single-system residual)
+    if (is_complex) {
+        if (row_len >= 32) return residual_batch_g<cdouble, 8>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+        if (row_len >= 8) return residual_batch_g<cdouble, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+        return residual_batch_g<cdouble, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    }
+    if (row_len >= 32) return residual_batch_g<double, 8>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    if (row_len >= 8) return residual_batch_g<double, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    return residual_batch_g<double, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+}
+
+__global__ void k_batch_relres(const double *__restrict__ norms, int nsys, int nrhs, double *relres,
+                               unsigned long long *worst)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    const double *ns = norms + (size_t)s * 2 * nrhs;
+    double w = 0.0;
+    for (int h = 0; h < nrhs; h++) {
+        const double bn = sqrt(ns[nrhs + h]);
+        const double v = sqrt(ns[h]) / (bn > 0.0 ? bn : 1.0);
+        if (!(v <= w)) w = v; // NaN propagates
+    }
+    relres[s] = w;
+    // non-negative doubles (and NaN above +inf) order like their bit patterns
+    atomicMax(worst, (unsigned long long)__double_as_longlong(w));
+}
+
+extern "C" int spk_batch_relres(const double *d_norms, int nsys, int nrhs, double *d_relres,
+                                unsigned long long *d_worst, void *stream, long long *launches)
+{
+    if (nsys <= 0) return SPK_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (ck(cudaMemsetAsync(d_worst, 0, sizeof(unsigned long long), st))) return SPK_ECUDA;
+    k_batch_relres<<<(nsys + 255) / 256, 256, 0, st>>>(d_norms, nsys, nrhs, d_relres, d_worst);
+    if (launches) (*launches)++;
+    return ck(cudaGetLastError());
+}
+
+// ------------------------------------------------------------ graphs, fork/join, timers
+extern "C" int spk_capture_begin(void *stream)
+{
+    return ck(cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal));
+}
+extern "C" int spk_capture_end(void *stream, void **graph_exec)
+{
+    *graph_exec = nullptr;
+    cudaGraph_t g = nullptr;
+    if (ck(cudaStreamEndCapture((cudaStream_t)stream, &g))) return SPK_ECUDA;
+    cudaGraphExec_t e = nullptr;
+    const int r = ck(cudaGraphInstantiate(&e, g, 0));
+    cudaGraphDestroy(g);
+    if (r != SPK_OK) return r;
+    *graph_exec = (void *)e;
+    return SPK_OK;
+}
+extern "C" int spk_graph_launch(void *graph_exec, void *stream)
+{
+    return ck(cudaGraphLaunch((cudaGraphExec_t)graph_exec, (cudaStream_t)stream));
+}
+extern "C" void spk_graph_destroy(void *graph_exec)
+{
+    if (graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)graph_exec);
+}
+extern "C" int spk_stream_fork(void *parent, void *child)
+{
+    cudaEvent_t e;
+    if (ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return SPK_ECUDA;
+    int r = ck(cudaEventRecord(e, (cudaStream_t)parent));
+    if (r == SPK_OK) r = ck(cudaStreamWaitEvent((cudaStream_t)child, e, 0));
+    cudaEventDestroy(e);
+    return r;
+}
+extern "C" int spk_timer_begin(void **timer, void *stream)
+{
+    cudaEvent_t *ev = (cudaEvent_t *)calloc(2, sizeof(cudaEvent_t));
+    *timer = nullptr;
+    if (!ev) return SPK_EMEM;
+    if (ck(cudaEventCreate(&ev[0])) || ck(cudaEventCreate(&ev[1]))) {
+        free(ev);
+        return SPK_ECUDA;
+    }
+    *timer = ev;
+    return ck(cudaEventRecord(ev[0], (cudaStream_t)stream));
+}
+extern "C" int spk_timer_end(void *timer, void *stream, double *ms)
+{
+    cudaEvent_t *ev = (cudaEvent_t *)timer;
+    float f = 0.f;
+    int r = ck(cudaEventRecord(ev[1], (cudaStream_t)stream));
+    if (r == SPK_OK) r = ck(cudaEventSynchronize(ev[1]));
+    if (r == SPK_OK) r = ck(cudaEventElapsedTime(&f, ev[0], ev[1]));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    free(ev);
+    *ms = f;
+    return r;
+}
+
 // ------------------------------------------------------------ phase timing
 extern "C" void spk_phase_begin(spk_plan *P, int phase, void *stream)
 {

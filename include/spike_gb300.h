@@ -136,6 +136,63 @@ Error_t spike_zsolve_factored(spike_factor_t f, integer_t nrhs, complex16 *x, co
 Error_t spike_dsolve_factored_device(spike_factor_t f, integer_t nrhs, double *d_x, const double *d_b);
 Error_t spike_factor_release(spike_factor_t f);
 
+/* ---- batches of independent systems ----
+ * No counterpart in the reference (one system per dspike_core_host call).
+ * Thousands of systems of uneven n, bandwidth and nrhs are solved by one CUDA
+ * graph launch: the systems are grouped by tile size and nrhs, each group is
+ * one SPIKE schedule whose partitions never straddle two systems, and every
+ * group runs on its own stream inside the graph.  Mixed or FP64 precision,
+ * tolerance and refinement limit come from the context. */
+typedef struct spike_batch_s *spike_batch_t;
+typedef struct {
+    integer_t n, nnz, nrhs;           /* nrhs in [1, 32] */
+    const integer_t *d_colind, *d_rowptr; /* device, CSR 0-based, sorted rows */
+    const double *d_aij;                  /* device */
+    double *d_x;                          /* device, n x nrhs column-major (output) */
+    const double *d_b;                    /* device, n x nrhs column-major */
+} spike_dsystem_t;
+
+#define SPIKE_BATCH_AUTOTUNE 1 /* time candidate tile sizes and partition lengths per group */
+#define SPIKE_BATCH_NO_GRAPH 2 /* launch eagerly on every run instead of replaying the graph */
+
+/* Plan a batch: read every pattern (bandwidth, CSR validity), group, choose
+ * the schedules (autotuned with SPIKE_BATCH_AUTOTUNE, else by rule), allocate,
+ * run once (the warm-up fixes how many refinement sweeps the graph holds) and
+ * capture the solve as one graph.  The descriptors are copied; the arrays are
+ * read at every run, so A's values and b may change between runs, the pattern
+ * and the pointers may not. */
+Error_t spike_dbatch_create(spike_context_t ctx, integer_t count, const spike_dsystem_t *systems, int flags,
+                            spike_batch_t *out);
+/* Solve every system: one graph launch after the work already queued on the
+ * context's stream; a group still above the tolerance then gets eager
+ * refinement sweeps up to the context's limit.  Returns after the solve. */
+Error_t spike_batch_run(spike_batch_t batch);
+/* Relative residual max_h ||b_h - A x_h|| / ||b_h|| of every system after the
+ * last run (count entries, in the systems' order). */
+Error_t spike_batch_relres(spike_batch_t batch, double *relres);
+typedef struct {
+    int systems, groups;
+    int graph;                        /* 1 when runs replay a captured graph */
+    int graph_sweeps;                 /* most refinement sweeps any group's graph holds */
+    int extra_sweeps;                 /* eager sweeps the last run added */
+    double relres_max;                /* worst relative residual of the last run */
+    long long graph_kernel_launches;  /* kernels in one graph launch */
+    size_t device_bytes;
+    double tune_ms;                   /* device time spent timing candidates */
+} spike_batch_info_t;
+Error_t spike_batch_get_info(spike_batch_t batch, spike_batch_info_t *info);
+typedef struct {
+    int block, nrhs, bandwidth, systems, partitions, rows_per_partition, graph_sweeps;
+    long long rows, nnz;
+} spike_batch_group_t;
+Error_t spike_batch_group(spike_batch_t batch, integer_t i, spike_batch_group_t *group);
+Error_t spike_batch_destroy(spike_batch_t batch);
+/* The partition rule of a batch (host only): partitions of a system of n
+ * rows with tile size KB at a target of rows_per_partition rows -- the
+ * nearest count, at least 1 and at most n / (2 KB); the partitions then
+ * start at multiples of floor(n / p), the remainder going to the last. */
+integer_t spike_batch_partitions(integer_t n, integer_t KB, integer_t rows_per_partition);
+
 #ifdef __cplusplus
 }
 #endif
