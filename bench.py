@@ -259,6 +259,75 @@ def batched_leg(torch, dev, hs, count, steps, warmup, autotune=True):
     return out
 
 
+# --------------------------------------------------------------------- serving leg
+def serving_leg(hs, count, rate=20_000.0, slots=8, k_max=64):
+    """The serving stream: Poisson arrivals at `rate`/s, per request n
+    log-normal (median 20,000, sigma 1, clipped to [500, 2,000,000]), k uniform
+    in {1..k_max}, nrhs uniform in {1..32}, dominance 1.05, 30 % reusing an
+    earlier request's matrix (its resident factorization) with a fresh
+    right-hand side; `count` requests (the first count arrivals of the stream,
+    seed 5).  A client thread submits each request at its arrival time; the
+    server admits by device footprint.  Latency = completion - arrival."""
+    import threading
+    from hspike_gb300 import workloads as W
+
+    t0 = time.perf_counter()
+    reqs = W.request_stream(rate, 1e9, seed=5, k_max=k_max, max_requests=count)
+    mats = {}
+    rng = np.random.default_rng(55)
+    work = []
+    for q in reqs:
+        if q.seed not in mats:
+            rp, ci, a, xt, b = hs.gen_banded(q.n, q.k, q.k, q.dom, q.seed, nrhs=1)
+            mats[q.seed] = (rp, ci, a)
+        rp, ci, a = mats[q.seed]
+        b = np.asfortranarray(rng.uniform(-1, 1, (q.n, q.nrhs)))
+        work.append((q, rp, ci, a, b))
+    gen_s = time.perf_counter() - t0
+    keys = {q.seed for q in reqs if q.reuse_of >= 0}
+    srv = hs.Server(slots=slots)
+    tickets = [None] * len(work)
+
+    def client():
+        start = srv.clock()
+        for i, (q, rp, ci, a, b) in enumerate(work):
+            ta = start + q.t_arrival
+            while srv.clock() < ta:
+                pass
+            tickets[i] = srv.submit(rp, ci, a, b, factor_key=q.seed if q.seed in keys else -1, bandwidth=q.k,
+                                    arrival=ta)
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    srv.drain()
+    st = srv.stats()
+    errs = 0
+    for i, (t, x) in enumerate(tickets):
+        s_ = srv.wait(t, check=False)
+        errs += s_.error_code != 0
+    # spot-check results against the oracle's FP64 residual
+    from oracle import oracle
+    worst = 0.0
+    for i in range(0, len(work), max(1, len(work) // 16)):
+        q, rp, ci, a, b = work[i]
+        worst = max(worst, float(oracle.residual(rp, ci, a, tickets[i][1], b).max()))
+    span = reqs[-1].t_arrival
+    out = {"workload": f"{len(work)} requests of a Poisson stream at {rate:.0f}/s (arrivals over {span * 1000:.1f} ms): "
+                       f"n log-normal median 20000 sigma 1 clipped [500, 2e6], k U{{1..{k_max}}}, nrhs U{{1..32}}, "
+                       f"dominance 1.05, 30% reuse of a resident factorization, seed 5",
+           "slots": slots, "value": st.throughput, "unit": "solves/s", "p50_ms": st.latency_p50 * 1000,
+           "p99_ms": st.latency_p99 * 1000, "max_ms": st.latency_max * 1000,
+           "mean_queue_wait_ms": st.mean_queue_wait * 1000, "completed": st.completed, "rejected": st.rejected,
+           "failed": st.failed + errs, "factor_hits": st.factor_hits, "factor_misses": st.factor_misses,
+           "peak_running": st.peak_running, "relres_max": st.relres_max, "relres_oracle_sampled": worst,
+           "offered_per_s": rate, "setup_s": gen_s,
+           "note": "offered load far exceeds one GPU: requests queue, latency is mostly queueing; k above 64 "
+                   "(the largest tile) is outside this leg"}
+    srv.close()
+    return out
+
+
 # --------------------------------------------------------------------- GPU arm
 def main():
     ap = argparse.ArgumentParser()
@@ -274,6 +343,8 @@ def main():
     ap.add_argument("--batch", type=int, default=4096, help="systems in the batched leg (0 = skip it)")
     ap.add_argument("--batch-only", action="store_true", help="run only the batched leg (profiler captures)")
     ap.add_argument("--no-autotune", action="store_true", help="batched leg: schedules by rule")
+    ap.add_argument("--serve", type=int, default=400, help="requests in the serving leg (0 = skip it)")
+    ap.add_argument("--serve-only", action="store_true", help="run only the serving leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -285,6 +356,10 @@ def main():
 
     build()
     n, p = args.n, args.partitions
+    if args.serve_only:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"serving": serving_leg(hs, args.serve)}), flush=True)
+        return 0
     if args.batch_only:
         dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
         torch.cuda.set_device(dev)
@@ -479,6 +554,9 @@ def main():
     if args.batch > 0 and not args.skip_extras:
         out["batched"] = batched_leg(torch, dev, hs, args.batch, max(3, min(args.steps, 10)), 3,
                                      not args.no_autotune)
+
+    if args.serve > 0 and not args.skip_extras:
+        out["serving"] = serving_leg(hs, args.serve)
 
     # ---- end to end through the reference's C entry point, host buffers
     if not args.skip_e2e:

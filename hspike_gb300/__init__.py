@@ -8,7 +8,8 @@ callers, tests and the benchmark:
   ``cspike_core_host`` / ``dspike_core_host_blocking`` -- the reference's
   entry points (OpenMP/spike_interfaces.h:28-72), same argument order and
   meaning, numpy arrays in place of pointers, ``Error_t`` returned;
-* ``Context`` / ``Factor`` -- the extensions of ``include/spike_gb300.h``;
+* ``Context`` / ``Factor`` / ``Batch`` / ``Server`` -- the extensions of
+  ``include/spike_gb300.h``;
 * ``solve`` -- convenience wrapper returning x.
 
 There is no Python or CPU compute path: if the library is missing, every call
@@ -48,8 +49,10 @@ EXPORTS = [
     "spike_dsolve_factored", "spike_zsolve_factored", "spike_dsolve_factored_device", "spike_factor_release",
     "spike_get_phase_times", "spike_dsolve_device_noalloc", "spike_dbatch_create", "spike_batch_run",
     "spike_batch_relres", "spike_batch_get_info", "spike_batch_group", "spike_batch_destroy",
-    "spike_batch_partitions",
+    "spike_batch_partitions", "spike_server_create", "spike_server_submit", "spike_server_wait",
+    "spike_server_drain", "spike_server_stats", "spike_server_clock", "spike_server_destroy",
 ]
+SPIKE_OPT_STREAM_ALLOC = 6
 SPIKE_BATCH_AUTOTUNE = 1
 SPIKE_BATCH_NO_GRAPH = 2
 
@@ -83,6 +86,33 @@ class BatchGroup(C.Structure):
     _fields_ = [("block", C.c_int), ("nrhs", C.c_int), ("bandwidth", C.c_int), ("systems", C.c_int),
                 ("partitions", C.c_int), ("rows_per_partition", C.c_int), ("graph_sweeps", C.c_int),
                 ("rows", C.c_longlong), ("nnz", C.c_longlong)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("slots", C.c_int), ("precision", C.c_int), ("tolerance", C.c_double), ("max_refine", C.c_int),
+                ("hbm_budget", C.c_size_t), ("cache_budget", C.c_size_t)]
+
+
+class Request(C.Structure):
+    _fields_ = [("n", C.c_int), ("nnz", C.c_int), ("nrhs", C.c_int), ("colind", C.c_void_p), ("rowptr", C.c_void_p),
+                ("aij", C.c_void_p), ("b", C.c_void_p), ("x", C.c_void_p), ("bandwidth", C.c_int),
+                ("factor_key", C.c_longlong), ("arrival", C.c_double)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("done", C.c_int), ("error_code", C.c_int), ("relres", C.c_double), ("sweeps", C.c_int),
+                ("factor_hit", C.c_int), ("t_arrival", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("footprint", C.c_size_t)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("rejected", C.c_longlong),
+                ("failed", C.c_longlong), ("queued", C.c_longlong), ("factor_hits", C.c_longlong),
+                ("factor_misses", C.c_longlong), ("running", C.c_int), ("peak_running", C.c_int),
+                ("resident_factors", C.c_int), ("device_bytes_running", C.c_size_t),
+                ("device_bytes_cached", C.c_size_t), ("latency_p50", C.c_double), ("latency_p99", C.c_double),
+                ("latency_max", C.c_double), ("mean_queue_wait", C.c_double), ("throughput", C.c_double),
+                ("relres_max", C.c_double)]
 
 
 _LIB = None
@@ -128,6 +158,14 @@ def load(path: str | None = None):
     L.spike_batch_destroy.argtypes = [vp]
     L.spike_batch_partitions.argtypes = [i, i, i]
     L.spike_batch_partitions.restype = i
+    L.spike_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
+    L.spike_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_longlong)]
+    L.spike_server_wait.argtypes = [vp, C.c_longlong, C.POINTER(RequestStatus)]
+    L.spike_server_drain.argtypes = [vp]
+    L.spike_server_stats.argtypes = [vp, C.POINTER(ServerStats)]
+    L.spike_server_clock.argtypes = [vp]
+    L.spike_server_clock.restype = C.c_double
+    L.spike_server_destroy.argtypes = [vp]
     _LIB = L
     return L
 
@@ -354,6 +392,65 @@ class Batch:
     def __del__(self):
         try:
             self.destroy()
+        except Exception:
+            pass
+
+
+class Server:
+    """The request loop of spike_server_*: ``slots`` concurrent requests,
+    admission by device footprint, resident factors under keys."""
+
+    def __init__(self, slots=4, precision=SPIKE_PRECISION_MIXED, tolerance=1e-12, max_refine=3, hbm_budget=0,
+                 cache_budget=0):
+        cfg = ServerConfig(slots, precision, tolerance, max_refine, hbm_budget, cache_budget)
+        self._h = C.c_void_p()
+        self._keep = {}
+        _check(load().spike_server_create(C.byref(cfg), C.byref(self._h)))
+
+    def submit(self, rowptr, colind, aij, b, x=None, factor_key=-1, bandwidth=-1, arrival=-1.0):
+        """Queue A x = b (host arrays; x allocated if not given); returns (ticket, x)."""
+        rowptr = np.ascontiguousarray(rowptr, np.int32)
+        colind = np.ascontiguousarray(colind, np.int32)
+        aij = np.ascontiguousarray(aij, np.float64)
+        n = len(rowptr) - 1
+        b2 = np.asfortranarray(np.asarray(b, np.float64).reshape(n, -1))
+        if x is None:
+            x = np.zeros_like(b2, order="F")
+        req = Request(n, len(colind), b2.shape[1], colind.ctypes.data, rowptr.ctypes.data, aij.ctypes.data,
+                      b2.ctypes.data, x.ctypes.data, bandwidth, factor_key, arrival)
+        t = C.c_longlong()
+        _check(load().spike_server_submit(self._h, C.byref(req), C.byref(t)))
+        self._keep[t.value] = (rowptr, colind, aij, b2, x)
+        return t.value, x
+
+    def wait(self, ticket, check=True) -> RequestStatus:
+        st = RequestStatus()
+        rc = load().spike_server_wait(self._h, ticket, C.byref(st))
+        self._keep.pop(ticket, None)
+        if check:
+            _check(rc)
+        return st
+
+    def drain(self):
+        _check(load().spike_server_drain(self._h))
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(load().spike_server_stats(self._h, C.byref(st)))
+        return st
+
+    def clock(self) -> float:
+        return float(load().spike_server_clock(self._h))
+
+    def close(self):
+        if self._h:
+            _check(load().spike_server_destroy(self._h))
+            self._h = C.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
         except Exception:
             pass
 

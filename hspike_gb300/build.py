@@ -25,7 +25,7 @@ OUT = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["spike_factor.cu", "spike_apply.cu", "spike_reduced.cu", "spike_util.cu", "spike_noalloc.cu"]
-C_SOURCES = ["spike_host.c", "spike_batch.c"]
+C_SOURCES = ["spike_host.c", "spike_batch.c", "spike_serve.c"]
 
 
 def nvcc() -> str:
@@ -82,7 +82,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src.replace(".c", ".o"))
         if _stale(o, [s] + headers):
-            jobs.append(["gcc", "-O2", "-std=gnu11", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter",
+            jobs.append(["gcc", "-O2", "-std=gnu11", "-fPIC", "-pthread", "-Wall", "-Wextra", "-Wno-unused-parameter",
                          *inc, "-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
@@ -95,7 +95,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     so = lib_path()
     if _stale(so, objs):
         tmp = so + ".tmp"
-        _run([nv, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lm"], verbose)
+        _run([nv, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lm", "-lpthread"], verbose)
         os.replace(tmp, so)
     gsrc = os.path.join(CSRC, "spike_gen.c")
     gso = gen_path()

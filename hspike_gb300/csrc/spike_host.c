@@ -80,18 +80,19 @@ struct spike_factor_s {
     void *o_rowptr, *o_colind, *o_aij; /* owned copies */
     void *d_b, *d_x, *d_r;
     size_t c_b, c_x, c_r;
+    void *astream; /* allocation stream (the context's, when stream-ordered) */
     int released;
 };
 
 static __thread spike_context_t t_default = NULL;
 
-static int ensure(void **p, size_t *cap, size_t need)
+static int ensure(void **p, size_t *cap, size_t need, void *astream)
 {
     if (need <= *cap && *p) return SPK_OK;
-    spk_free(*p);
+    spk_free_on(*p, astream);
     *p = NULL;
     *cap = 0;
-    TRY(spk_malloc(p, need));
+    TRY(spk_malloc_on(p, need, astream));
     *cap = need;
     return SPK_OK;
 }
@@ -127,16 +128,17 @@ Error_t spike_context_create(spike_context_t *out)
 Error_t spike_context_destroy(spike_context_t c)
 {
     if (!c) return spk_fail(SPIKE_ERR_ARGUMENT, "spike_context_destroy: NULL context");
-    if (c->stream) spk_stream_sync(c->stream);
+    void *as = spk_ctx_astream(c);
     spk_plan_destroy(c->plan);
     spk_free(c->d_scratch);
-    spk_free(c->d_rowptr);
-    spk_free(c->d_colind);
-    spk_free(c->d_aij);
-    spk_free(c->d_b);
-    spk_free(c->d_x);
-    spk_free(c->d_r);
-    spk_free(c->d_stage);
+    spk_free_on(c->d_rowptr, as);
+    spk_free_on(c->d_colind, as);
+    spk_free_on(c->d_aij, as);
+    spk_free_on(c->d_b, as);
+    spk_free_on(c->d_x, as);
+    spk_free_on(c->d_r, as);
+    spk_free_on(c->d_stage, as);
+    if (c->stream) spk_stream_sync(c->stream);
     spk_stream_destroy(c->own_stream);
     if (t_default == c) t_default = NULL;
     free(c);
@@ -188,6 +190,24 @@ Error_t spike_set_option(spike_context_t c, int opt, double v)
     case SPIKE_OPT_PHASE_TIMING:
         c->timing = v != 0;
         break;
+    case SPIKE_OPT_STREAM_ALLOC:
+        if ((v != 0) != (c->stream_alloc != 0)) {
+            /* workspace changes allocator: release it (it is rebuilt on demand) */
+            spk_stream_sync(c->stream);
+            void *as = spk_ctx_astream(c);
+            spk_plan_destroy(c->plan);
+            c->plan = NULL;
+            void **bufs[] = {&c->d_rowptr, &c->d_colind, &c->d_aij, &c->d_b, &c->d_x, &c->d_r, &c->d_stage};
+            size_t *caps[] = {&c->c_rowptr, &c->c_colind, &c->c_aij, &c->c_b, &c->c_x, &c->c_r, &c->c_stage};
+            for (int i = 0; i < 7; i++) {
+                spk_free_on(*bufs[i], as);
+                *bufs[i] = NULL;
+                *caps[i] = 0;
+            }
+            spk_stream_sync(c->stream);
+        }
+        c->stream_alloc = v != 0;
+        break;
     default: return spk_fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
     return spk_succeed();
@@ -204,6 +224,7 @@ Error_t spike_get_option(spike_context_t c, int opt, double *v)
     case SPIKE_OPT_TOLERANCE: *v = c->tol; break;
     case SPIKE_OPT_REDUCED_REFINE: *v = c->red_refine; break;
     case SPIKE_OPT_PHASE_TIMING: *v = c->timing; break;
+    case SPIKE_OPT_STREAM_ALLOC: *v = c->stream_alloc; break;
     default: return spk_fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
     return spk_succeed();
@@ -274,7 +295,7 @@ void spk_plan_destroy(spk_plan *P)
     void *ptrs[] = {P->d_part_start, P->d_blk_off, P->d_blk_part, P->d_L, P->d_G, P->d_E, P->d_V, P->d_W,
                     P->d_Bhat, P->d_T, P->d_RP, P->d_RQ, P->d_RX, P->d_RY, P->d_crP, P->d_crQ, P->d_crX, P->d_crY,
                     P->d_crM, P->d_crg, P->d_z, P->d_y, P->d_g, P->d_u, P->d_rr, P->d_du, P->d_err, P->d_norms};
-    for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) spk_free(ptrs[i]);
+    for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) spk_free_on(ptrs[i], P->astream);
     free(P->part_start);
     free(P->blk_off);
     free(P->cr_count);
@@ -285,18 +306,19 @@ void spk_plan_destroy(spk_plan *P)
 
 static int palloc(spk_plan *P, void **p, size_t bytes)
 {
-    TRY(spk_malloc(p, bytes));
+    TRY(spk_malloc_on(p, bytes, P->astream));
     P->bytes += bytes;
     return SPK_OK;
 }
 
 int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex, int mode, int p,
-                   const int *part_start, int nrhs_max, void *stream, spk_plan **out)
+                   const int *part_start, int nrhs_max, void *stream, int stream_alloc, spk_plan **out)
 {
     *out = NULL;
     if (!KB || spk_factor_smem(KB, is_complex, mode) == 0) return SPK_EBAND;
     spk_plan *P = (spk_plan *)calloc(1, sizeof *P);
     if (!P) return SPK_EMEM;
+    P->astream = stream_alloc ? stream : NULL;
     P->n = n;
     P->nnz = nnz;
     P->ku = ku;
@@ -403,7 +425,7 @@ int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex,
 }
 
 static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int mode, int partitions,
-                       int nrhs_max, void *stream, spk_plan **out)
+                       int nrhs_max, void *stream, int stream_alloc, spk_plan **out)
 {
     *out = NULL;
     const int k = ku > kl ? ku : kl;
@@ -416,9 +438,46 @@ static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int
     const int nreg = n / p;
     for (int i = 0; i < p; i++) ps[i] = i * nreg;
     ps[p] = n;
-    const int rc = spk_plan_build(n, nnz, ku, kl, KB, is_complex, mode, p, ps, nrhs_max, stream, out);
+    const int rc = spk_plan_build(n, nnz, ku, kl, KB, is_complex, mode, p, ps, nrhs_max, stream, stream_alloc, out);
     free(ps);
     return rc;
+}
+
+/* mirrors spk_plan_build's allocations and the staging of spk_host_solve_ctx */
+size_t spk_solve_footprint(int n, long long nnz, int k, int nrhs, int is_complex, int mode, int partitions)
+{
+    const int KB = spk_choose_block(k < 1 ? 1 : k);
+    if (!KB || n <= 0) return 0;
+    const int p = choose_partitions(n, KB, partitions);
+    const int nreg = n / p;
+    long long blocks = (long long)(p - 1) * ((nreg + KB - 1) / KB) + ((n - (long long)(p - 1) * nreg) + KB - 1) / KB;
+    const long long nif = p > 1 ? p - 1 : 1;
+    long long tiles = 0, mtiles = 0;
+    for (long long c = nif, l = 0;; l++) {
+        tiles += c;
+        if (c <= 1) {
+            mtiles += 1;
+            break;
+        }
+        mtiles += c / 2;
+        c = (c + 1) / 2;
+    }
+    const int chunk = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
+    const size_t fs = (is_complex ? 2 : 1) * (mode == SPK_MIXED ? 4 : 8);
+    const size_t hs = (is_complex ? 2 : 1) * 8;
+    const size_t TS = (size_t)KB * KB;
+    size_t b = 0;
+    b += sizeof(int) * (2 * (size_t)(p + 1) + (size_t)blocks);
+    b += fs * TS * (size_t)blocks * 8 + fs * TS * p;            /* L G E W V + 3 band tiles, B^ */
+    b += hs * TS * (size_t)nif * 4;                               /* RP RQ RX RY */
+    b += fs * TS * (size_t)tiles * 4 + fs * TS * 4 * (size_t)mtiles; /* cyclic reduction */
+    b += fs * 2 * (size_t)tiles * 2 * KB * chunk;                 /* reduced RHS work */
+    b += fs * 2 * (size_t)blocks * KB * chunk;                    /* z, y */
+    b += hs * (size_t)nif * 2 * KB * chunk * 4;                   /* g u rr du */
+    b += 16 + sizeof(double) * 2 * chunk;
+    /* staging of a host-array solve: CSR, b, x, r */
+    b += sizeof(int) * ((size_t)n + 1 + (size_t)nnz) + hs * (size_t)nnz + hs * (size_t)n * (2 * nrhs + chunk);
+    return b;
 }
 
 static int plan_matches(const spk_plan *P, int n, int ku, int kl, int is_complex, int mode, int partitions, int nrhs)
@@ -559,7 +618,8 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
     if (!plan_matches(c->plan, n, info[0], info[1], is_complex, c->mode, c->partitions, chunk)) {
         spk_plan_destroy(c->plan);
         c->plan = NULL;
-        TRY(plan_create(n, nnz, info[0], info[1], is_complex, c->mode, c->partitions, chunk, c->stream, &c->plan));
+        TRY(plan_create(n, nnz, info[0], info[1], is_complex, c->mode, c->partitions, chunk, c->stream, c->stream_alloc,
+                        &c->plan));
     }
     spk_plan *P = c->plan;
     P->nnz = nnz;
@@ -568,7 +628,7 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
     P->launches = l0;
     P->timing = c->timing;
     const size_t hs = (is_complex ? 2 : 1) * 8;
-    TRY(ensure(&c->d_r, &c->c_r, hs * (size_t)n * chunk));
+    TRY(ensure(&c->d_r, &c->c_r, hs * (size_t)n * chunk, spk_ctx_astream(c)));
     int rc = factor_phase(P, rp, ci, aij, c->stream);
     if (rc == SPK_OK) rc = solve_all(P, rp, ci, aij, x, b, c->d_r, nrhs, o, c->stream);
     if (P->timing && (rc == SPK_OK || rc == SPK_ECONV) && spk_phase_collect(P) != SPK_OK) rc = SPK_ECUDA;
@@ -597,6 +657,13 @@ static Error_t host_solve(int dtype, const char *name, integer_t n, integer_t nn
     if (!colind || !rowptr || !aij || !x || !b) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
     spike_context_t c = spk_get_ctx(NULL);
     if (!c) return SPIKE_ERROR;
+    return spk_host_solve_ctx(c, dtype, name, n, nnz, nrhs, colind, rowptr, aij, x, b);
+}
+
+Error_t spk_host_solve_ctx(spike_context_t c, int dtype, const char *name, integer_t n, integer_t nnz, integer_t nrhs,
+                           const integer_t *colind, const integer_t *rowptr, const void *aij, void *x, const void *b)
+{
+    if (n == 0 || nrhs == 0) return spk_succeed();
     const int cplx = dtype == SPK_C || dtype == SPK_Z;
     const int wide = dtype == SPK_S || dtype == SPK_C;
     const size_t es = (cplx ? 2 : 1) * (wide ? 4 : 8); /* caller element bytes */
@@ -605,14 +672,14 @@ static Error_t host_solve(int dtype, const char *name, integer_t n, integer_t nn
     refine_opts o;
     opts_from(c, &o);
     int rc = SPK_OK;
-    rc = ensure(&c->d_rowptr, &c->c_rowptr, sizeof(int) * ((size_t)n + 1));
-    if (rc == SPK_OK) rc = ensure(&c->d_colind, &c->c_colind, sizeof(int) * (size_t)(nnz ? nnz : 1));
-    if (rc == SPK_OK) rc = ensure(&c->d_aij, &c->c_aij, hs * (size_t)(nnz ? nnz : 1));
-    if (rc == SPK_OK) rc = ensure(&c->d_b, &c->c_b, hs * nb);
-    if (rc == SPK_OK) rc = ensure(&c->d_x, &c->c_x, hs * nb);
+    rc = ensure(&c->d_rowptr, &c->c_rowptr, sizeof(int) * ((size_t)n + 1), spk_ctx_astream(c));
+    if (rc == SPK_OK) rc = ensure(&c->d_colind, &c->c_colind, sizeof(int) * (size_t)(nnz ? nnz : 1), spk_ctx_astream(c));
+    if (rc == SPK_OK) rc = ensure(&c->d_aij, &c->c_aij, hs * (size_t)(nnz ? nnz : 1), spk_ctx_astream(c));
+    if (rc == SPK_OK) rc = ensure(&c->d_b, &c->c_b, hs * nb, spk_ctx_astream(c));
+    if (rc == SPK_OK) rc = ensure(&c->d_x, &c->c_x, hs * nb, spk_ctx_astream(c));
     if (rc == SPK_OK && wide) {
         const size_t m = (size_t)nnz > nb ? (size_t)nnz : nb;
-        rc = ensure(&c->d_stage, &c->c_stage, es * (m ? m : 1));
+        rc = ensure(&c->d_stage, &c->c_stage, es * (m ? m : 1), spk_ctx_astream(c));
     }
     if (rc != SPK_OK) return finish(rc, name, &o);
     long long launches = 0;
@@ -721,6 +788,7 @@ static Error_t factor_common(spike_context_t c, int cplx, const char *name, inte
     spike_factor_t f = (spike_factor_t)calloc(1, sizeof *f);
     if (!f) return spk_fail(SPIKE_ERR_MEMORY, "%s: host allocation failed", name);
     f->ctx = c;
+    f->astream = spk_ctx_astream(c);
     f->is_complex = cplx;
     f->n = n;
     f->nnz = nnz;
@@ -730,9 +798,9 @@ static Error_t factor_common(spike_context_t c, int cplx, const char *name, inte
     opts_from(c, &o);
     if (host) {
         f->owns = 1;
-        rc = spk_malloc(&f->o_rowptr, sizeof(int) * ((size_t)n + 1));
-        if (rc == SPK_OK) rc = spk_malloc(&f->o_colind, sizeof(int) * (size_t)(nnz ? nnz : 1));
-        if (rc == SPK_OK) rc = spk_malloc(&f->o_aij, hs * (size_t)(nnz ? nnz : 1));
+        rc = spk_malloc_on(&f->o_rowptr, sizeof(int) * ((size_t)n + 1), f->astream);
+        if (rc == SPK_OK) rc = spk_malloc_on(&f->o_colind, sizeof(int) * (size_t)(nnz ? nnz : 1), f->astream);
+        if (rc == SPK_OK) rc = spk_malloc_on(&f->o_aij, hs * (size_t)(nnz ? nnz : 1), f->astream);
         if (rc == SPK_OK) rc = spk_memcpy_h2d(f->o_rowptr, rp, sizeof(int) * ((size_t)n + 1), c->stream);
         if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(f->o_colind, ci, sizeof(int) * (size_t)nnz, c->stream);
         if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(f->o_aij, aij, hs * (size_t)nnz, c->stream);
@@ -749,7 +817,8 @@ static Error_t factor_common(spike_context_t c, int cplx, const char *name, inte
     if (rc == SPK_OK) rc = spk_analyze(n, nnz, f->d_rowptr, f->d_colind, c->d_scratch, info, c->stream, &l0);
     if (rc == SPK_OK && info[2]) rc = SPK_ECSR;
     if (rc == SPK_OK)
-        rc = plan_create(n, nnz, info[0], info[1], cplx, c->mode, c->partitions, RHS_CHUNK, c->stream, &f->plan);
+        rc = plan_create(n, nnz, info[0], info[1], cplx, c->mode, c->partitions, RHS_CHUNK, c->stream, c->stream_alloc,
+                         &f->plan);
     if (rc == SPK_OK) {
         f->plan->launches = l0;
         rc = factor_phase(f->plan, f->d_rowptr, f->d_colind, f->d_aij, c->stream);
@@ -794,12 +863,12 @@ static Error_t solve_factored(spike_factor_t f, int cplx, const char *name, inte
     refine_opts o;
     opts_from(c, &o);
     P->launches = 0;
-    int rc = ensure(&f->d_r, &f->c_r, hs * (size_t)f->n * P->nrhs_max);
+    int rc = ensure(&f->d_r, &f->c_r, hs * (size_t)f->n * P->nrhs_max, f->astream);
     void *dx = x;
     const void *db = b;
     if (host) {
-        if (rc == SPK_OK) rc = ensure(&f->d_b, &f->c_b, hs * nb);
-        if (rc == SPK_OK) rc = ensure(&f->d_x, &f->c_x, hs * nb);
+        if (rc == SPK_OK) rc = ensure(&f->d_b, &f->c_b, hs * nb, f->astream);
+        if (rc == SPK_OK) rc = ensure(&f->d_x, &f->c_x, hs * nb, f->astream);
         if (rc == SPK_OK) rc = spk_memcpy_h2d(f->d_b, b, hs * nb, c->stream);
         dx = f->d_x;
         db = f->d_b;
@@ -832,14 +901,14 @@ Error_t spike_dsolve_factored_device(spike_factor_t f, integer_t nrhs, double *d
 Error_t spike_factor_release(spike_factor_t f)
 {
     if (!f || f->released) return spk_fail(SPIKE_ERR_HANDLE, "spike_factor_release: invalid factor handle");
-    if (f->ctx && f->ctx->stream) spk_stream_sync(f->ctx->stream);
     spk_plan_destroy(f->plan);
-    spk_free(f->o_rowptr);
-    spk_free(f->o_colind);
-    spk_free(f->o_aij);
-    spk_free(f->d_b);
-    spk_free(f->d_x);
-    spk_free(f->d_r);
+    spk_free_on(f->o_rowptr, f->astream);
+    spk_free_on(f->o_colind, f->astream);
+    spk_free_on(f->o_aij, f->astream);
+    spk_free_on(f->d_b, f->astream);
+    spk_free_on(f->d_x, f->astream);
+    spk_free_on(f->d_r, f->astream);
+    if (f->ctx && f->ctx->stream) spk_stream_sync(f->ctx->stream);
     f->released = 1;
     free(f);
     return spk_succeed();

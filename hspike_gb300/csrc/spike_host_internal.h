@@ -25,6 +25,7 @@ struct spike_context_s {
     void *own_stream, *stream;
     /* options */
     int mode, partitions, max_refine, red_refine, timing;
+    int stream_alloc; /* workspace allocated stream-ordered on `stream` */
     double tol;
     /* cached plan for the reference-API and device-pointer calls */
     spk_plan *plan;
@@ -48,7 +49,18 @@ SPK_INTERNAL int spk_choose_block(int k);
 /* A plan for an explicit schedule: tile size KB, p partitions starting at
  * part_start[0..p] (part_start[p] = n).  Allocates the device workspace. */
 SPK_INTERNAL int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex, int mode, int p,
-                                const int *part_start, int nrhs_max, void *stream, spk_plan **out);
+                                const int *part_start, int nrhs_max, void *stream, int stream_alloc,
+                                spk_plan **out);
+/* device bytes a solve of this shape holds (plan + staging for host arrays),
+ * without allocating; partitions as for spike_set_option (0 = automatic) */
+SPK_INTERNAL size_t spk_solve_footprint(int n, long long nnz, int k, int nrhs, int is_complex, int mode,
+                                        int partitions);
+/* the reference-API solve on an explicit context (host arrays) */
+SPK_INTERNAL Error_t spk_host_solve_ctx(spike_context_t c, int dtype, const char *name, integer_t n, integer_t nnz,
+                                        integer_t nrhs, const integer_t *colind, const integer_t *rowptr,
+                                        const void *aij, void *x, const void *b);
+/* stream for workspace allocations of this context (NULL: synchronous) */
+static inline void *spk_ctx_astream(spike_context_t c) { return c->stream_alloc ? c->stream : NULL; }
 SPK_INTERNAL void spk_plan_destroy(spk_plan *P);
 
 #endif /* SPIKE_GB300_HOST_INTERNAL_H */

@@ -117,6 +117,7 @@ typedef struct spk_plan {
     const int *d_part_sys;
     double *d_norms;       /* 2*nrhs_max: ||r||^2 then ||b||^2 per column */
     /* bookkeeping */
+    void *astream;      /* allocations stream-ordered on this stream (NULL: cudaMalloc) */
     long long launches; /* kernel launches issued for this plan */
     size_t bytes;       /* device bytes held */
     /* optional per-phase CUDA-event timing (SPIKE_OPT_PHASE_TIMING) */
@@ -145,8 +146,13 @@ int spk_noalloc_scratch(void **ptr, size_t *bytes);
 int spk_device_count(void);
 int spk_current_device(void);
 int spk_sm_count(void);
+int spk_set_device(int dev);
+int spk_mem_info(size_t *free_b, size_t *total_b);
 int spk_malloc(void **p, size_t bytes);
 void spk_free(void *p);
+/* stream-ordered when stream != NULL (cudaMallocAsync / cudaFreeAsync) */
+int spk_malloc_on(void **p, size_t bytes, void *stream);
+void spk_free_on(void *p, void *stream);
 int spk_host_register(void *p, size_t bytes);
 int spk_host_unregister(void *p);
 int spk_stream_create(void **stream);

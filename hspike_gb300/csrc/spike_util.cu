@@ -41,6 +41,12 @@ extern "C" int spk_current_device(void)
     if (cudaGetDevice(&d) != cudaSuccess) return -1;
     return d;
 }
+extern "C" int spk_set_device(int dev) { return ck(cudaSetDevice(dev)); }
+extern "C" int spk_mem_info(size_t *free_b, size_t *total_b)
+{
+    *free_b = *total_b = 0;
+    return ck(cudaMemGetInfo(free_b, total_b));
+}
 extern "C" int spk_sm_count(void)
 {
     int d = spk_current_device(), v = 0;
@@ -63,6 +69,42 @@ extern "C" int spk_malloc(void **p, size_t bytes)
 extern "C" void spk_free(void *p)
 {
     if (p) cudaFree(p);
+}
+// Stream-ordered allocation (stream != NULL): no device-wide synchronisation,
+// so contexts on different streams keep overlapping while they allocate.  The
+// device's default pool keeps freed memory for reuse (release threshold raised
+// once per device).
+extern "C" int spk_malloc_on(void **p, size_t bytes, void *stream)
+{
+    if (!stream) return spk_malloc(p, bytes);
+    *p = nullptr;
+    if (bytes == 0) bytes = 256;
+    static int pool_dev[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !pool_dev[dev]) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            unsigned long long thr = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        pool_dev[dev] = 1;
+    }
+    cudaError_t e = cudaMallocAsync(p, bytes, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        g_last_cuda = e;
+        cudaGetLastError();
+        *p = nullptr;
+        return SPK_EMEM;
+    }
+    return SPK_OK;
+}
+extern "C" void spk_free_on(void *p, void *stream)
+{
+    if (!p) return;
+    if (stream)
+        cudaFreeAsync(p, (cudaStream_t)stream);
+    else
+        cudaFree(p);
 }
 extern "C" int spk_host_register(void *p, size_t bytes)
 {

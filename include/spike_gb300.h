@@ -38,6 +38,8 @@ typedef struct spike_factor_s *spike_factor_t;
 #define SPIKE_OPT_TOLERANCE 3      /* relative residual target (default 1e-12) */
 #define SPIKE_OPT_REDUCED_REFINE 4 /* FP64 refinement sweeps on the reduced system (default 2 mixed, 1 FP64) */
 #define SPIKE_OPT_PHASE_TIMING 5   /* 1 = time each kernel family with CUDA events (default 0) */
+#define SPIKE_OPT_STREAM_ALLOC 6   /* 1 = workspace via cudaMallocAsync on the context's stream, so contexts on
+                                      different streams overlap while they allocate (default 0) */
 
 #define SPIKE_PRECISION_MIXED 0 /* FP32 / complex64 factors, FP64 residual + update + reduced solve */
 #define SPIKE_PRECISION_FP64 1  /* FP64 / complex128 everywhere */
@@ -192,6 +194,60 @@ Error_t spike_batch_destroy(spike_batch_t batch);
  * nearest count, at least 1 and at most n / (2 KB); the partitions then
  * start at multiples of floor(n / p), the remainder going to the last. */
 integer_t spike_batch_partitions(integer_t n, integer_t KB, integer_t rows_per_partition);
+
+/* ---- serving: a request loop with continuous batching ----
+ * No counterpart in the reference.  `slots` worker threads, each with its own
+ * context and stream (workspace stream-ordered), take requests from a FIFO as
+ * soon as a slot is free and the request's device footprint fits in the
+ * budget left by running requests; their GPU work overlaps.  Requests with a
+ * factor key keep their factorization resident (LRU cache with its own budget)
+ * and later requests with the same key solve with it.  Host arrays; they must
+ * stay valid until the request is done. */
+typedef struct spike_server_s *spike_server_t;
+typedef struct {
+    int slots;           /* concurrent requests (1..64) */
+    int precision;       /* SPIKE_PRECISION_MIXED or _FP64 */
+    double tolerance;    /* relative residual target (0 = 1e-12) */
+    int max_refine;      /* refinement sweeps (0 = 3) */
+    size_t hbm_budget;   /* device bytes for running requests (0 = 60 % of free memory) */
+    size_t cache_budget; /* device bytes for resident factors (0 = 20 % of free memory) */
+} spike_server_config_t;
+typedef struct {
+    integer_t n, nnz, nrhs;
+    const integer_t *colind, *rowptr;
+    const double *aij;
+    const double *b; /* n x nrhs column-major */
+    double *x;       /* n x nrhs column-major (output) */
+    integer_t bandwidth; /* max(ku, kl) when known, else -1 (scanned from the pattern) */
+    long long factor_key; /* >= 0: keep / reuse the factorization under this key; -1: none */
+    double arrival;      /* arrival time on spike_server_clock, < 0 = at submission */
+} spike_request_t;
+typedef struct {
+    int done, error_code;
+    double relres;
+    int sweeps, factor_hit;
+    double t_arrival, t_admit, t_done; /* spike_server_clock seconds */
+    size_t footprint;                  /* device bytes charged while it ran */
+} spike_request_status_t;
+typedef struct {
+    long long submitted, completed, rejected, failed, queued;
+    long long factor_hits, factor_misses;
+    int running, peak_running, resident_factors;
+    size_t device_bytes_running, device_bytes_cached;
+    double latency_p50, latency_p99, latency_max; /* seconds, arrival to completion */
+    double mean_queue_wait, throughput;           /* seconds; completed per second */
+    double relres_max;
+} spike_server_stats_t;
+Error_t spike_server_create(const spike_server_config_t *cfg, spike_server_t *server);
+/* Queue a request; a request larger than the whole budget (or with a band
+ * above the largest tile) is completed at once with an error. */
+Error_t spike_server_submit(spike_server_t server, const spike_request_t *req, long long *ticket);
+/* Block until the request is done; returns its error, if any. */
+Error_t spike_server_wait(spike_server_t server, long long ticket, spike_request_status_t *status);
+Error_t spike_server_drain(spike_server_t server);
+Error_t spike_server_stats(spike_server_t server, spike_server_stats_t *stats);
+double spike_server_clock(spike_server_t server); /* seconds since creation */
+Error_t spike_server_destroy(spike_server_t server); /* drains first */
 
 #ifdef __cplusplus
 }

@@ -76,3 +76,10 @@ def test_batch_without_device_fails_loudly():
     with pytest.raises(hs.SpikeError) as e:
         hs.Batch([(100, 298, 1, 1, 1, 1, 1, 1)])
     assert e.value.name == "no_device"
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-device path")
+def test_server_without_device_fails_loudly():
+    with pytest.raises(hs.SpikeError) as e:
+        hs.Server(slots=2)
+    assert e.value.name == "no_device"
