@@ -259,6 +259,50 @@ def batched_leg(torch, dev, hs, count, steps, warmup, autotune=True):
     return out
 
 
+# --------------------------------------------------------------------- complex leg
+def complex_leg(torch, dev, hs, steps, warmup, n=4_000_000, k=3, nrhs=4, p=512, dom=1.2, seed=3):
+    """The complex heptadiagonal workload: n = 4,000,000, kl = ku = 3,
+    complex128, re/im off-diagonals U[-1,1], diagonal 1.2 x the row's |sum| x
+    e^{i theta}, nrhs = 4, 512 partitions; complex64 factors + complex128
+    refinement against plain complex128.  Device-resident inputs."""
+    rp, ci, a, xt, b = hs.gen_banded(n, k, k, dom, seed, complex_=True, nrhs=nrhs)
+    nnz = len(ci)
+    d_rp, d_ci, d_a = (torch.from_numpy(v).to(dev) for v in (rp, ci, a))
+    d_b = torch.from_numpy(np.ascontiguousarray(b.T)).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    B = 20 * nnz + 4 * (n + 1) + 32 * n * nrhs
+    out = {"workload": f"complex heptadiagonal: n={n:,} kl=ku={k} complex128, nrhs={nrhs}, {p} partitions, "
+                       f"dominance {dom} x |row sum| x e^(i theta), seed {seed}", "algorithmic_bytes": B}
+    for name, prec in (("mixed", hs.SPIKE_PRECISION_MIXED), ("fp64", hs.SPIKE_PRECISION_FP64)):
+        ctx = hs.Context()
+        ctx.set_stream(stream.cuda_stream)
+        ctx.set_option(hs.SPIKE_OPT_PARTITIONS, p)
+        ctx.set_option(hs.SPIKE_OPT_PRECISION, prec)
+        d_x = torch.zeros_like(d_b)
+        go = lambda: ctx.solve_device(n, nnz, nrhs, d_ci.data_ptr(), d_rp.data_ptr(), d_a.data_ptr(), d_x.data_ptr(),
+                                      d_b.data_ptr(), complex_=True)
+        for _ in range(warmup):
+            go()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        for s_ in range(steps):
+            go()
+            ev[s_ + 1].record(stream)
+        torch.cuda.synchronize()
+        ms = ev[0].elapsed_time(ev[steps]) / steps
+        x = d_x.cpu().numpy().T
+        inf = ctx.info()
+        out[name] = {"value": 1000.0 / ms, "unit": "solves/s", "ms_per_step": ms, "hbm_gbs": B / (ms / 1000) / 1e9,
+                     "hbm_frac": B / (ms / 1000) / 1e9 / 6662.6, "relres_max": inf.relres_max,
+                     "refine_sweeps": inf.refine_sweeps, "block": inf.block,
+                     "err_vs_xtrue": float(np.linalg.norm(x - xt) / np.linalg.norm(xt))}
+        ctx.close()
+        del d_x
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    return out
+
+
 # --------------------------------------------------------------------- serving leg
 def serving_leg(hs, count, rate=20_000.0, slots=8, k_max=64):
     """The serving stream: Poisson arrivals at `rate`/s, per request n
@@ -345,6 +389,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="batched leg: schedules by rule")
     ap.add_argument("--serve", type=int, default=400, help="requests in the serving leg (0 = skip it)")
     ap.add_argument("--serve-only", action="store_true", help="run only the serving leg")
+    ap.add_argument("--complex-only", action="store_true", help="run only the complex leg")
+    ap.add_argument("--skip-complex", action="store_true", help="omit the complex leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -356,6 +402,11 @@ def main():
 
     build()
     n, p = args.n, args.partitions
+    if args.complex_only:
+        dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+        torch.cuda.set_device(dev)
+        print(json.dumps({"complex": complex_leg(torch, dev, hs, max(1, args.steps), args.warmup)}), flush=True)
+        return 0
     if args.serve_only:
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         print(json.dumps({"serving": serving_leg(hs, args.serve)}), flush=True)
@@ -555,6 +606,8 @@ def main():
         out["batched"] = batched_leg(torch, dev, hs, args.batch, max(3, min(args.steps, 10)), 3,
                                      not args.no_autotune)
 
+    if not args.skip_complex and not args.skip_extras:
+        out["complex"] = complex_leg(torch, dev, hs, max(3, min(args.steps, 10)), 3)
     if args.serve > 0 and not args.skip_extras:
         out["serving"] = serving_leg(hs, args.serve)
 

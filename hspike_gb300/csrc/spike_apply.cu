@@ -288,9 +288,14 @@ __global__ void __launch_bounds__(256)
 // block are staged by cp.async in the thread's own shared-memory slot.  z is
 // kept in gy between the sweeps (each thread rereads only what it wrote).
 template <class T, int KB> struct ChainApply {
+    using H = typename HighOf<T>::type;
     static constexpr int TS = KB * KB;
-    static constexpr int STAGE = 2 * TS;
-    static constexpr int SLOT = 2 * STAGE * (int)sizeof(T) + 16;
+    static constexpr int DEPTH = 4;
+    // a ring entry: forward -> L tile + r rows (FP64); backward -> G, E tiles + z rows
+    static constexpr int FWD = TS * (int)sizeof(T) + KB * (int)sizeof(H);
+    static constexpr int BWD = 2 * TS * (int)sizeof(T) + KB * (int)sizeof(T);
+    static constexpr int STAGE = ((FWD > BWD ? FWD : BWD) + 15) / 16 * 16; // bytes
+    static constexpr int SLOT = DEPTH * STAGE + 16;
     static constexpr int NC = chain_threads(SLOT);
     static constexpr size_t SMEM = (size_t)NC * SLOT;
 };
@@ -303,78 +308,103 @@ __global__ void __launch_bounds__(ChainApply<T, KB>::NC)
 {
     using H = typename HighOf<T>::type;
     using C = ChainApply<T, KB>;
-    constexpr int TS = C::TS;
-    constexpr int CT = TS * (int)sizeof(T) / 16; // 16-byte chunks per tile
+    constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int CT = TS * (int)sizeof(T) / 16;                          // 16-byte chunks per tile
+    constexpr int ZE = KB * (int)sizeof(T) >= 16 ? 16 : KB * (int)sizeof(T); // z rows: alignment of a block's rows
     extern __shared__ __align__(16) char smc[];
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int part = idx / nrhs, h = idx - part * nrhs;
     if (part >= p) return; // no barriers below
-    T *slot = (T *)(smc + threadIdx.x * C::SLOT);
+    char *slot = smc + threadIdx.x * C::SLOT;
     const int s = part_start[part], m = part_start[part + 1] - s;
     const int N = blk_off[part + 1] - blk_off[part];
     const size_t tb = (size_t)blk_off[part] * TS;
     T *yh = gy + (size_t)h * NP + (size_t)blk_off[part] * KB;
     const H *rh = r + (size_t)h * n + s;
 
-    // forward: z_J = r_J - L_J z_{J-1}
+    // forward: z_J = r_J - L_J z_{J-1}; ring entry j % D holds L_j and r_j
+    auto issue_f = [&](int j) {
+        if (j < N) {
+            char *st = slot + (j % D) * C::STAGE;
+            if (j > 0) cp_async_chunks(st, gL + tb + (size_t)j * TS, CT);
+            H *rs = (H *)(st + TS * sizeof(T));
+#pragma unroll
+            for (int i = 0; i < KB; i++)
+                if (j * KB + i < m) cp_async_elem<(int)sizeof(H)>(rs + i, rh + j * KB + i);
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int j = 0; j < D - 1; j++) issue_f(j);
     T z[KB];
 #pragma unroll
-    for (int i = 0; i < KB; i++) z[i] = i < m ? sc_cvt<T, H>(rh[i]) : sc_zero<T>();
-    vst<T, KB>(yh, z);
-    if (N > 1) cp_async_chunks(slot + C::STAGE, gL + tb + TS, CT);
-    cp_async_commit();
-    for (int J = 1; J < N; J++) {
-        if (J + 1 < N) cp_async_chunks(slot + ((J + 1) & 1) * C::STAGE, gL + tb + (size_t)(J + 1) * TS, CT);
-        cp_async_commit();
+    for (int i = 0; i < KB; i++) z[i] = sc_zero<T>();
+    for (int J = 0; J < N; J++) {
+        issue_f(J + D - 1);
+        cp_async_wait_n<D - 1>();
+        const char *st = slot + (J % D) * C::STAGE;
+        const H *rs = (const H *)(st + TS * sizeof(T));
         T rj[KB];
 #pragma unroll
-        for (int i = 0; i < KB; i++) rj[i] = J * KB + i < m ? sc_cvt<T, H>(rh[J * KB + i]) : sc_zero<T>();
-        cp_async_wait_1();
-        RMat<T, KB> L;
-        rm_ldt(L, slot + (J & 1) * C::STAGE);
+        for (int i = 0; i < KB; i++) rj[i] = J * KB + i < m ? sc_cvt<T, H>(rs[i]) : sc_zero<T>();
+        if (J > 0) {
+            RMat<T, KB> L;
+            rm_ldt(L, (const T *)st);
 #pragma unroll
-        for (int i = 0; i < KB; i++) {
-            T a = rj[i];
+            for (int i = 0; i < KB; i++)
 #pragma unroll
-            for (int c = 0; c < KB; c++) a = msub(a, L.v[i][c], z[c]);
-            rj[i] = a;
+                for (int c = 0; c < KB; c++) rj[i] = msub(rj[i], L.v[i][c], z[c]);
         }
 #pragma unroll
         for (int i = 0; i < KB; i++) z[i] = rj[i];
         vst<T, KB>(yh + (size_t)J * KB, z);
     }
-    // backward: y_J = G_J (z_J - E_J y_{J+1})
-    auto issue = [&](int J) {
-        T *st = slot + (J & 1) * C::STAGE;
-        cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
-        cp_async_chunks(st + TS, gE + tb + (size_t)J * TS, CT);
-    };
-    issue(N - 1);
-    cp_async_commit();
-    T y[KB];
-    for (int J = N - 1; J >= 0; J--) {
-        if (J > 0) issue(J - 1);
+    cp_async_wait_all();
+    __threadfence_block(); // the z stores above precede the copies below that read them back
+    // backward: y_J = G_J (z_J - E_J y_{J+1}); step i handles block N-1-i.  The
+    // z rows were stored above by this thread (ordinary stores, visible to its
+    // own later asynchronous copies).
+    auto issue_b = [&](int i) {
+        if (i < N) {
+            const int J = N - 1 - i;
+            char *st = slot + (i % D) * C::STAGE;
+            cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
+            cp_async_chunks(st + TS * sizeof(T), gE + tb + (size_t)J * TS, CT);
+            char *zs = st + 2 * TS * sizeof(T);
+#pragma unroll
+            for (int q = 0; q < KB * (int)sizeof(T) / ZE; q++)
+                cp_async_elem<ZE>(zs + q * ZE, (const char *)(yh + (size_t)J * KB) + q * ZE);
+        }
         cp_async_commit();
+    };
+#pragma unroll
+    for (int i = 0; i < D - 1; i++) issue_b(i);
+    T y[KB];
+#pragma unroll
+    for (int i = 0; i < KB; i++) y[i] = sc_zero<T>();
+    for (int i = 0; i < N; i++) {
+        const int J = N - 1 - i;
+        issue_b(i + D - 1);
+        cp_async_wait_n<D - 1>();
+        const char *st = slot + (i % D) * C::STAGE;
         T t[KB];
-        vld<T, KB>(t, yh + (size_t)J * KB); // z_J
-        cp_async_wait_1();
-        const T *sc = slot + (J & 1) * C::STAGE;
+        vld<T, KB>(t, (const T *)(st + 2 * TS * sizeof(T))); // z_J
         if (J < N - 1) {
             RMat<T, KB> E;
-            rm_ldt(E, sc + TS);
+            rm_ldt(E, (const T *)(st + TS * sizeof(T)));
 #pragma unroll
-            for (int i = 0; i < KB; i++)
+            for (int a = 0; a < KB; a++)
 #pragma unroll
-                for (int c = 0; c < KB; c++) t[i] = msub(t[i], E.v[i][c], y[c]);
+                for (int c = 0; c < KB; c++) t[a] = msub(t[a], E.v[a][c], y[c]);
         }
         RMat<T, KB> G;
-        rm_ldt(G, sc);
+        rm_ldt(G, (const T *)st);
 #pragma unroll
-        for (int i = 0; i < KB; i++) {
-            T a = sc_zero<T>();
+        for (int a = 0; a < KB; a++) {
+            T acc = sc_zero<T>();
 #pragma unroll
-            for (int c = 0; c < KB; c++) a = madd(a, G.v[i][c], t[c]);
-            y[i] = a;
+            for (int c = 0; c < KB; c++) acc = madd(acc, G.v[a][c], t[c]);
+            y[a] = acc;
         }
         vst<T, KB>(yh + (size_t)J * KB, y);
     }

@@ -569,6 +569,32 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 // all but the most recently committed group complete
 __device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+// all but the N most recently committed groups complete
+template <int N> __device__ __forceinline__ void cp_async_wait_n()
+{
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+// 8- and 4-byte asynchronous copies (both addresses aligned to the size)
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+// one element of E bytes (4, 8 or 16, naturally aligned)
+template <int E> __device__ __forceinline__ void cp_async_elem(void *smem, const void *gmem)
+{
+    if constexpr (E == 16)
+        cp_async16(smem, gmem);
+    else if constexpr (E == 8)
+        cp_async8(smem, gmem);
+    else
+        cp_async4(smem, gmem);
+}
 // `chunks` 16-byte pieces from global to shared, issued by this thread alone
 __device__ __forceinline__ void cp_async_chunks(void *s, const void *g, int chunks)
 {

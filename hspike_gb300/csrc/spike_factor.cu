@@ -41,73 +41,69 @@ template <class T, int KB> struct FactorSmem {
 // F G), D: block J, En: block J+1 (shared tiles, row stride LD); gZ (global,
 // row-major, zeroed by the caller): C^ coupling (J == 0, columns s-KB..s-1);
 // gBhat (global, row-major): B^ coupling (columns e..e+KB-1).
-// The block's entries are one contiguous CSR range: the CTA walks it with
-// coalesced, unrolled loads (several in flight per thread) and finds each
-// entry's row by binary search in the block's row-pointer slice srp[].
+// One warp per row: the row's entries are contiguous, so the loads are
+// coalesced and every entry's row is known without a search; two 32-entry
+// chunks of a row are in flight per iteration.
+template <class T, class H, int KB, int LD>
+__device__ __forceinline__ void place_entry(int lr, int lrow, int c, H a, int s, int m, int J, T *F, T *D, T *En,
+                                            T *gZ, T *gBhat, unsigned *err)
+{
+    const T v = cvt_fast<T, H>(a);
+    const int lc = c - s;
+    if (lc < 0) {
+        const int cc = lc + KB;
+        if (cc >= 0 && lrow < KB) {
+            if (gZ) gZ[lr * KB + cc] = v;
+        } else
+            atomicOr(err, SPK_DEV_ERR_BAND);
+    } else if (lc >= m) {
+        const int br = lrow - (m - KB), bc = lc - m;
+        if (br >= 0 && bc < KB) {
+            if (gBhat) gBhat[br * KB + bc] = v;
+        } else
+            atomicOr(err, SPK_DEV_ERR_BAND);
+    } else {
+        const int bc = lc / KB, cc = lc - bc * KB;
+        const int d = bc - J;
+        if (d == 0)
+            D[lr * LD + cc] = v;
+        else if (d == -1)
+            F[cc * LD + lr] = v;
+        else if (d == 1)
+            En[lr * LD + cc] = v;
+        else
+            atomicOr(err, SPK_DEV_ERR_BAND);
+    }
+}
+
 template <class T, class H, int KB, int LD>
 __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
                               const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *gZ,
                               T *gBhat, unsigned *err, int *srp)
 {
     constexpr int NT = NTOf<KB>::value;
-    constexpr int U = 8;
+    constexpr int NW = NT / 32;
     const int m = e - s;
     const int lrow0 = J * KB;
     const int nr = min(KB, m - lrow0); // real rows in the block, >= 1
     for (int q = threadIdx.x; q <= nr; q += NT) srp[q] = rowptr[s + lrow0 + q];
     for (int lr = nr + threadIdx.x; lr < KB; lr += NT) D[lr * LD + lr] = sc_one<T>(); // identity padding
     __syncthreads();
-    const int t0 = srp[0], t1 = srp[nr];
-    for (int base = t0; base < t1; base += U * NT) {
-        int cidx[U];
-        H val[U];
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int t = base + threadIdx.x + u * NT;
-            if (t < t1) {
-                cidx[u] = __ldg(colind + t);
-                val[u] = aij[t];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int lr = warp; lr < nr; lr += NW) {
+        const int t1 = srp[lr + 1];
+        for (int t = srp[lr] + lane; t < t1; t += 64) {
+            const bool two = t + 32 < t1;
+            const int c0 = __ldg(colind + t);
+            const H a0 = aij[t];
+            int c1 = 0;
+            H a1 = sc_zero<H>();
+            if (two) {
+                c1 = __ldg(colind + t + 32);
+                a1 = aij[t + 32];
             }
-        }
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            const int t = base + threadIdx.x + u * NT;
-            if (t >= t1) continue;
-            int lo = 0, hi = nr; // srp[lo] <= t < srp[hi]
-            while (hi - lo > 1) {
-                const int mid = (lo + hi) >> 1;
-                if (srp[mid] <= t)
-                    lo = mid;
-                else
-                    hi = mid;
-            }
-            const int lr = lo, lrow = lrow0 + lr;
-            const T v = cvt_fast<T, H>(val[u]);
-            const int lc = cidx[u] - s;
-            if (lc < 0) {
-                const int cc = lc + KB;
-                if (cc >= 0 && lrow < KB) {
-                    if (gZ) gZ[lr * KB + cc] = v;
-                } else
-                    atomicOr(err, SPK_DEV_ERR_BAND);
-            } else if (lc >= m) {
-                const int br = lrow - (m - KB), bc = lc - m;
-                if (br >= 0 && bc < KB) {
-                    if (gBhat) gBhat[br * KB + bc] = v;
-                } else
-                    atomicOr(err, SPK_DEV_ERR_BAND);
-            } else {
-                const int bc = lc / KB, cc = lc - bc * KB;
-                const int d = bc - J;
-                if (d == 0)
-                    D[lr * LD + cc] = v;
-                else if (d == -1)
-                    F[cc * LD + lr] = v;
-                else if (d == 1)
-                    En[lr * LD + cc] = v;
-                else
-                    atomicOr(err, SPK_DEV_ERR_BAND);
-            }
+            place_entry<T, H, KB, LD>(lr, lrow0 + lr, c0, a0, s, m, J, F, D, En, gZ, gBhat, err);
+            if (two) place_entry<T, H, KB, LD>(lr, lrow0 + lr, c1, a1, s, m, J, F, D, En, gZ, gBhat, err);
         }
     }
 }
@@ -386,8 +382,9 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
 // global layouts as k_factor_fwd / k_factor_bwd.
 template <class T, int KB> struct ChainFwd {
     static constexpr int TS = KB * KB;
-    static constexpr int STAGE = 3 * TS;                           // D, F^T, E
-    static constexpr int SLOT = 2 * STAGE * (int)sizeof(T) + 16;   // two stages + pad (odd in 16-byte units)
+    static constexpr int DEPTH = 4;                                 // blocks in flight per chain
+    static constexpr int STAGE = 3 * TS;                            // D, F^T, E
+    static constexpr int SLOT = DEPTH * STAGE * (int)sizeof(T) + 16; // ring + pad (odd in 16-byte units)
     static constexpr int NC = chain_threads(SLOT);
     static constexpr size_t SMEM = (size_t)NC * SLOT;
 };
@@ -397,7 +394,7 @@ __global__ void __launch_bounds__(ChainFwd<T, KB>::NC)
     k_chain_fwd(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gZ, unsigned *err)
 {
     using C = ChainFwd<T, KB>;
-    constexpr int TS = C::TS;
+    constexpr int TS = C::TS, D = C::DEPTH;
     extern __shared__ __align__(16) char smc[];
     const int part = blockIdx.x * blockDim.x + threadIdx.x;
     if (part >= p) return; // no barriers below
@@ -410,13 +407,17 @@ __global__ void __launch_bounds__(ChainFwd<T, KB>::NC)
     RMat<T, KB> G, Ep, Zp;
     bool ok = true;
     if (doW) rm_ld(Zp, gZ + tb); // z_0 = C^
-    cp_async_chunks(slot, gTp, CH);
-    cp_async_commit();
-    for (int J = 0; J < N; J++) {
-        if (J + 1 < N) cp_async_chunks(slot + ((J + 1) & 1) * C::STAGE, gTp + (size_t)(J + 1) * C::STAGE, CH);
+#pragma unroll
+    for (int j = 0; j < D - 1; j++) {
+        if (j < N) cp_async_chunks(slot + j * C::STAGE, gTp + (size_t)j * C::STAGE, CH);
         cp_async_commit();
-        cp_async_wait_1();
-        const T *sc = slot + (J & 1) * C::STAGE;
+    }
+    for (int J = 0; J < N; J++) {
+        const int jn = J + D - 1;
+        if (jn < N) cp_async_chunks(slot + (jn % D) * C::STAGE, gTp + (size_t)jn * C::STAGE, CH);
+        cp_async_commit();
+        cp_async_wait_n<D - 1>();
+        const T *sc = slot + (J % D) * C::STAGE;
         RMat<T, KB> S;
         rm_ld(S, sc); // D_J
         if (J > 0) {
@@ -441,19 +442,22 @@ __global__ void __launch_bounds__(ChainFwd<T, KB>::NC)
         rm_stt(gG + tb + (size_t)J * TS, S);
         G = S;
     }
+    cp_async_wait_all();
     if (!ok) atomicOr(err, SPK_DEV_ERR_PIVOT);
 }
 
 template <class T, int KB> struct ChainBwd {
     static constexpr int TS = KB * KB;
-    static constexpr int STAGE = 3 * TS;                         // G, E, Z (W) / G, E (V)
-    static constexpr int SLOT = 2 * STAGE * (int)sizeof(T) + 16;
+    static constexpr int DEPTH = 4;
+    static constexpr int STAGE = 3 * TS; // G, E, Z (W) / G, E (V)
+    static constexpr int SLOT = DEPTH * STAGE * (int)sizeof(T) + 16;
     static constexpr int NC = chain_threads(SLOT);
     static constexpr size_t SMEM = (size_t)NC * SLOT;
 };
 
 // X_J = G_J (Z_J - E_J X_{J+1}): one thread per (partition, spike), V then W
 // of a partition on adjacent threads (they share the G / E tiles in L1).
+// Blocks are visited from N-1 down; the ring holds the next DEPTH-1 of them.
 template <class T, int KB>
 __global__ void __launch_bounds__(ChainBwd<T, KB>::NC)
     k_chain_bwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
@@ -461,7 +465,7 @@ __global__ void __launch_bounds__(ChainBwd<T, KB>::NC)
                 const T *__restrict__ gBhat, T *gV, T *gW)
 {
     using C = ChainBwd<T, KB>;
-    constexpr int TS = C::TS;
+    constexpr int TS = C::TS, D = C::DEPTH;
     extern __shared__ __align__(16) char smc[];
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int part = idx >> 1;
@@ -473,72 +477,59 @@ __global__ void __launch_bounds__(ChainBwd<T, KB>::NC)
     const size_t tb = (size_t)blk_off[part] * TS;
     T *gX = isW ? gW : gV;
     constexpr int CT = TS * (int)sizeof(T) / 16; // chunks per tile
-    auto issue = [&](int J) {
-        T *st = slot + (J & 1) * C::STAGE;
-        cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
-        cp_async_chunks(st + TS, gE + tb + (size_t)J * TS, CT);
-        if (isW) cp_async_chunks(st + 2 * TS, gZ + tb + (size_t)J * TS, CT);
+    // step i handles block N-1-i; its tiles sit in ring entry i % D
+    auto issue = [&](int i) {
+        if (i < N) {
+            const int J = N - 1 - i;
+            T *st = slot + (i % D) * C::STAGE;
+            cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
+            cp_async_chunks(st + TS, gE + tb + (size_t)J * TS, CT);
+            if (isW) cp_async_chunks(st + 2 * TS, gZ + tb + (size_t)J * TS, CT);
+        }
+        cp_async_commit();
     };
-    RMat<T, KB> X; // X_{J+1}
-    rm_zero(X);
-    int J = N - 1;
-    issue(J);
-    cp_async_commit();
+#pragma unroll
+    for (int i = 0; i < D - 1; i++) issue(i);
+    // V's right-hand side [0; B^] lives in the last KB real rows: blocks J0
+    // (rows o..KB-1) and J0+1 (rows 0..o-1, when o > 0).  A partition shorter
+    // than a tile (o < 0) takes B^'s last m rows.
+    RMat<T, KB> Z0, Z1;
+    rm_zero(Z0);
+    rm_zero(Z1);
+    const int J0 = m >= KB ? (m - KB) / KB : 0;
+    const int o = m - KB - J0 * KB;
     if (!isW) {
-        // V's right-hand side [0; B^] lives in the last KB real rows: blocks J0
-        // (rows o..KB-1) and J0+1 (rows 0..o-1, when o > 0).  A partition shorter
-        // than a tile (o < 0) takes B^'s last m rows.
-        const int J0 = m >= KB ? (m - KB) / KB : 0;
-        const int o = m - KB - J0 * KB;
         const T *B = gBhat + (size_t)part * TS;
-        RMat<T, KB> Z0;
 #pragma unroll
         for (int r = 0; r < KB; r++)
 #pragma unroll
             for (int c = 0; c < KB; c++)
                 Z0.v[r][c] = (r >= o && r - o < KB) ? B[(r - o) * KB + c] : sc_zero<T>();
         if (o > 0) {
-            // z_{J0+1} = [B^ rows KB-o..KB-1 ; 0] - L_{J0+1} z_{J0};  X_{N-1} = G_{N-1} z_{N-1}
-            RMat<T, KB> Z1, L1;
+            // z_{J0+1} = [B^ rows KB-o..KB-1 ; 0] - L_{J0+1} z_{J0}
+            RMat<T, KB> L1;
 #pragma unroll
             for (int r = 0; r < KB; r++)
 #pragma unroll
                 for (int c = 0; c < KB; c++) Z1.v[r][c] = r < o ? B[(KB - o + r) * KB + c] : sc_zero<T>();
             rm_ldt(L1, gL + tb + (size_t)(J0 + 1) * TS);
             rm_msub(Z1, L1, Z0);
-            if (J > 0) issue(J - 1);
-            cp_async_commit();
-            cp_async_wait_1();
-            RMat<T, KB> Gt;
-            rm_ldt(Gt, slot + (J & 1) * C::STAGE);
-            rm_mul(X, Gt, Z1);
-            rm_stt(gX + tb + (size_t)J * TS, X);
-            J--;
-        }
-        if (J >= 0) {
-            // block J0: X_{J0} = G_{J0} (z_{J0} - E_{J0} X_{J0+1})
-            if (J > 0) issue(J - 1);
-            cp_async_commit();
-            cp_async_wait_1();
-            const T *sc = slot + (J & 1) * C::STAGE;
-            RMat<T, KB> Gt, Et, Tm;
-            rm_ldt(Et, sc + TS);
-            Tm = Z0;
-            if (J < N - 1) rm_msub(Tm, Et, X);
-            rm_ldt(Gt, sc);
-            rm_mul(X, Gt, Tm);
-            rm_stt(gX + tb + (size_t)J * TS, X);
-            J--;
         }
     }
-    for (; J >= 0; J--) {
-        if (J > 0) issue(J - 1);
-        cp_async_commit();
-        cp_async_wait_1();
-        const T *sc = slot + (J & 1) * C::STAGE;
+    RMat<T, KB> X; // X_{J+1}
+    rm_zero(X);
+    for (int i = 0; i < N; i++) {
+        const int J = N - 1 - i;
+        issue(i + D - 1);
+        cp_async_wait_n<D - 1>();
+        const T *sc = slot + (i % D) * C::STAGE;
         RMat<T, KB> Gt, Et, Tm;
         if (isW)
             rm_ld(Tm, sc + 2 * TS); // z_J (row-major)
+        else if (J == J0)
+            Tm = Z0;
+        else if (o > 0 && J == J0 + 1)
+            Tm = Z1;
         else
             rm_zero(Tm);
         rm_ldt(Et, sc + TS);
