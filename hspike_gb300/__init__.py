@@ -51,6 +51,7 @@ EXPORTS = [
     "spike_batch_relres", "spike_batch_get_info", "spike_batch_group", "spike_batch_destroy",
     "spike_batch_partitions", "spike_server_create", "spike_server_submit", "spike_server_wait",
     "spike_server_drain", "spike_server_stats", "spike_server_clock", "spike_server_destroy",
+    "spike_rcm_permutation", "spike_permute_csr", "spike_permute_vector", "spike_dsolve_reordered",
 ]
 SPIKE_OPT_STREAM_ALLOC = 6
 SPIKE_BATCH_AUTOTUNE = 1
@@ -166,6 +167,10 @@ def load(path: str | None = None):
     L.spike_server_clock.argtypes = [vp]
     L.spike_server_clock.restype = C.c_double
     L.spike_server_destroy.argtypes = [vp]
+    L.spike_rcm_permutation.argtypes = [i, i, vp, vp, vp]
+    L.spike_permute_csr.argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp]
+    L.spike_permute_vector.argtypes = [i, i, i, vp, vp]
+    L.spike_dsolve_reordered.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, vp]
     _LIB = L
     return L
 
@@ -453,6 +458,52 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def rcm_permutation(rowptr, colind) -> np.ndarray:
+    """Reverse Cuthill-McKee order of the pattern of A + A^T (host, no device)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    n = len(rowptr) - 1
+    perm = np.zeros(max(n, 1), np.int32)
+    _check(load().spike_rcm_permutation(n, len(colind), _ptr(colind), _ptr(rowptr), _ptr(perm)))
+    return perm[:n]
+
+
+def permute_csr(rowptr, colind, aij, perm):
+    """B = A(perm, perm) as (rowptr, colind, aij), rows sorted."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    aij = np.ascontiguousarray(aij, np.float64)
+    perm = np.ascontiguousarray(perm, np.int32)
+    n = len(rowptr) - 1
+    orp, oci, oa = np.zeros(n + 1, np.int32), np.zeros(max(len(colind), 1), np.int32), np.zeros(max(len(aij), 1))
+    _check(load().spike_permute_csr(n, len(colind), _ptr(colind), _ptr(rowptr), _ptr(aij), _ptr(perm), _ptr(oci),
+                                    _ptr(orp), _ptr(oa)))
+    return orp, oci[:len(colind)], oa[:len(aij)]
+
+
+def permute_vector(flag, perm, v):
+    """In place, column by column: flag > 0 -> v = v(perm); else v(perm) = v."""
+    perm = np.ascontiguousarray(perm, np.int32)
+    assert v.dtype == np.float64 and (v.flags.f_contiguous or v.ndim == 1)
+    n = len(perm)
+    _check(load().spike_permute_vector(flag, n, v.size // max(n, 1), _ptr(perm), _ptr(v)))
+    return v
+
+
+def solve_reordered(rowptr, colind, aij, b, ctx: Context | None = None):
+    """x for a general sparse A: RCM + banded solve + back-permutation; returns (x, perm)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    aij = np.ascontiguousarray(aij, np.float64)
+    n = len(rowptr) - 1
+    b2 = np.asfortranarray(np.asarray(b, np.float64).reshape(n, -1))
+    x = np.zeros_like(b2, order="F")
+    perm = np.zeros(n, np.int32)
+    _check(load().spike_dsolve_reordered(ctx.handle if ctx else None, n, len(colind), b2.shape[1], _ptr(colind),
+                                         _ptr(rowptr), _ptr(aij), _ptr(x), _ptr(b2), _ptr(perm)))
+    return (x if np.ndim(b) == 2 else x[:, 0]), perm
 
 
 def batch_partitions(n: int, block: int, rows_per_partition: int) -> int:

@@ -612,7 +612,16 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
 {
     int info[3];
     long long l0 = 0;
-    TRY(spk_analyze(n, nnz, rp, ci, c->d_scratch, info, c->stream, &l0));
+    /* the analysis is timed on the previous call's plan (the plan for this
+     * call depends on its result) */
+    spk_plan *Pa = c->timing ? c->plan : NULL;
+    if (Pa) {
+        Pa->timing = 1;
+        spk_phase_begin(Pa, SPK_PH_ANALYZE, c->stream);
+    }
+    const int arc = spk_analyze(n, nnz, rp, ci, c->d_scratch, info, c->stream, &l0);
+    if (Pa) spk_phase_end(Pa, c->stream);
+    TRY(arc);
     if (info[2]) return SPK_ECSR;
     const int chunk = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
     if (!plan_matches(c->plan, n, info[0], info[1], is_complex, c->mode, c->partitions, chunk)) {

@@ -1,7 +1,7 @@
 // spike_util.cu -- device plumbing, CSR analysis and the FP64 residual.
 //
 //   k_analyze    bandwidth (matrix_ComputeBandwidth, OpenMP/spike_algebra.c
-//                :56-95) plus CSR validation in one pass over colind: rowptr
+//                :56-95) plus CSR validation in one streaming pass over colind: rowptr
 //                monotone and inside [0, nnz], columns inside [0, n) and
 //                strictly increasing within a row.  Rows whose rowptr entries
 //                are out of range are flagged and never dereferenced.
@@ -151,6 +151,11 @@ extern "C" int spk_memset(void *dst, int v, size_t bytes, void *stream)
 }
 
 // ------------------------------------------------------------ analysis
+// Each warp takes a chunk of AN_ROWS rows and streams their entries as one
+// contiguous range (coalesced); a lane tracks the row of its entries by
+// advancing through the chunk's row pointers.  A chunk whose row pointers are
+// out of range or decreasing is flagged and not scanned.
+constexpr int AN_ROWS = 64;
 __global__ void k_analyze(int n, long long nnz, const int *__restrict__ rowptr, const int *__restrict__ colind,
                           int *out)
 {
@@ -159,21 +164,43 @@ __global__ void k_analyze(int n, long long nnz, const int *__restrict__ rowptr, 
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     int ku = 0, kl = 0;
     unsigned flags = 0;
-    for (long long r = warp; r < n; r += nwarps) {
-        const long long t0 = rowptr[r], t1 = rowptr[r + 1];
-        if (t0 < 0 || t1 > nnz || t1 < t0) {
+    for (long long r0 = warp * AN_ROWS; r0 < n; r0 += nwarps * AN_ROWS) {
+        const long long r1 = min((long long)n, r0 + AN_ROWS);
+        bool bad = false;
+        for (long long r = r0 + lane; r < r1; r += 32) {
+            const long long t0 = rowptr[r], t1 = rowptr[r + 1];
+            if (t0 < 0 || t1 > nnz || t1 < t0) bad = true;
+        }
+        if (__any_sync(0xffffffffu, bad)) {
             flags |= SPK_DEV_ERR_CSR;
             continue;
         }
-        for (long long t = t0 + lane; t < t1; t += 32) {
-            const int c = colind[t];
-            if (c < 0 || c >= n) {
-                flags |= SPK_DEV_ERR_CSR;
-                continue;
+        const long long tb = rowptr[r0], te = rowptr[r1];
+        long long row = r0;
+        // four 32-entry pieces per iteration, their loads issued together; an
+        // entry's predecessor is read directly (an L1 hit), so iterations do
+        // not wait on one another
+        for (long long base = tb; base < te; base += 128) {
+            int c[4], pc[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const long long t = base + 32 * u + lane;
+                c[u] = t < te ? colind[t] : 0;
+                pc[u] = (t < te && t > tb) ? colind[t - 1] : 0;
             }
-            if (t > t0 && colind[t - 1] >= c) flags |= SPK_DEV_ERR_CSR;
-            ku = max(ku, c - (int)r);
-            kl = max(kl, (int)r - c);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const long long t = base + 32 * u + lane;
+                if (t >= te) continue;
+                while (rowptr[row + 1] <= t) row++; // stops by r1: t < rowptr[r1]
+                if (c[u] < 0 || c[u] >= n) {
+                    flags |= SPK_DEV_ERR_CSR;
+                    continue;
+                }
+                if (t > rowptr[row] && pc[u] >= c[u]) flags |= SPK_DEV_ERR_CSR;
+                ku = max(ku, c[u] - (int)row);
+                kl = max(kl, (int)row - c[u]);
+            }
         }
     }
     if (warp == 0 && lane == 0 && (rowptr[0] != 0 || rowptr[n] != nnz)) flags |= SPK_DEV_ERR_CSR;
@@ -195,7 +222,7 @@ extern "C" int spk_analyze(int n, long long nnz, const int *d_rowptr, const int 
     cudaStream_t st = (cudaStream_t)stream;
     int r = ck(cudaMemsetAsync(d_out, 0, 4 * sizeof(int), st));
     if (r == SPK_OK && n > 0) {
-        const long long warps_needed = n;
+        const long long warps_needed = (n + AN_ROWS - 1) / AN_ROWS;
         long long blocks = (warps_needed * 32 + 255) / 256;
         if (blocks > 152 * 16) blocks = 152 * 16;
         k_analyze<<<(unsigned)blocks, 256, 0, st>>>(n, nnz, d_rowptr, d_colind, d_out);

@@ -249,6 +249,27 @@ Error_t spike_server_stats(spike_server_t server, spike_server_stats_t *stats);
 double spike_server_clock(spike_server_t server); /* seconds since creation */
 Error_t spike_server_destroy(spike_server_t server); /* drains first */
 
+/* ---- bandwidth-reducing reordering (host) ----
+ * The reference reorders with cuSolverSp's host RCM + csrperm
+ * (cuda_standalone_symrcm, OpenMP/spike_cuda.c:898-971) and permutes vectors
+ * with permute_vector (OpenMP/spike_algebra.c:34-53). */
+/* Reverse Cuthill-McKee order of the pattern of A + A^T: new row i is old row
+ * perm[i]. */
+Error_t spike_rcm_permutation(integer_t n, integer_t nnz, const integer_t *colind, const integer_t *rowptr,
+                              integer_t *perm);
+/* B = A(perm, perm) into caller arrays (same nnz), rows sorted by column. */
+Error_t spike_permute_csr(integer_t n, integer_t nnz, const integer_t *colind, const integer_t *rowptr,
+                          const double *aij, const integer_t *perm, integer_t *out_colind, integer_t *out_rowptr,
+                          double *out_aij);
+/* permute_vector's meaning for nrhs columns: flag > 0 -> v = v(perm),
+ * flag <= 0 -> v(perm) = v. */
+Error_t spike_permute_vector(integer_t flag, integer_t n, integer_t nrhs, const integer_t *perm, double *v);
+/* Solve A x = b for a general sparse A: RCM, permute, banded solve on the
+ * device, permute back.  perm_out (optional, n entries) receives the order. */
+Error_t spike_dsolve_reordered(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs,
+                               const integer_t *colind, const integer_t *rowptr, const double *aij, double *x,
+                               const double *b, integer_t *perm_out);
+
 #ifdef __cplusplus
 }
 #endif
