@@ -149,18 +149,23 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     // the next block's right-hand-side rows ride in registers while the
     // current block computes; its tiles stream into the other buffer (cp.async)
     T nxt[VPT];
-    // forward: z_J = r_J - L_J z_{J-1}
+    // forward: z_J = r_J - L_J z_{J-1}.  It reads only L, so all four tile
+    // buffers form a ring: L_{J+1..J+3} stream in while block J computes.
+#define RING(j) (sM0 + ((j) & 3) * KB * LDT)
+    for (int j = 1; j <= 3; j++) {
+        if (j < N) cp_async_tile<T, KB, NT>(RING(j), gL + tb + (size_t)j * TS);
+        cp_async_commit();
+    }
     fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, 0);
     put_v<T, KB, VPT>(nxt, sv, nr);
+    cp_async_wait_n<2>(); // L_1
     __syncthreads();
     for (int J = 0; J < N; J++) {
-        if (J + 1 < N) {
-            cp_async_tile<T, KB, NT>(SMA(J + 1), gL + tb + (J + 1) * TS);
-            cp_async_commit();
-            fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, J + 1);
-        }
+        if (J + 3 < N) cp_async_tile<T, KB, NT>(RING(J + 3), gL + tb + (size_t)(J + 3) * TS);
+        cp_async_commit();
+        if (J + 1 < N) fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, J + 1);
         if (J > 0)
-            tile_mv<T, KB, true>(sw, SMA(J), sp, sv, nr, true);
+            tile_mv<T, KB, true>(sw, RING(J), sp, sv, nr, true);
         else
             for (int q = threadIdx.x; q < KB * RCS; q += NT) sw[q] = sv[q];
         __syncthreads();
@@ -171,9 +176,11 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
             gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
         }
         if (J + 1 < N) put_v<T, KB, VPT>(nxt, sv, nr);
-        cp_async_wait_all();
+        cp_async_wait_n<2>(); // L_{J+1}
         __syncthreads();
     }
+#undef RING
+    cp_async_wait_all();
     // backward: y_J = G_J (z_J - E_J y_{J+1})
     cp_async_tile<T, KB, NT>(SMA(N - 1), gG + tb + (N - 1) * TS);
     cp_async_commit();

@@ -296,12 +296,19 @@ template <class T, int KB, int NT> struct Tile {
                 for (int j = 0; j < TC; j++) acc[i][j] = SUB ? msub(acc[i][j], a[i], b[j]) : madd(acc[i][j], a[i], b[j]);
         }
     }
-    // acc (+|-)= A * B with A given transposed (At, column-major): vector fetches
-    template <bool SUB> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
+    // acc (+|-)= A * B with A given transposed (At, column-major): vector fetches.
+    // TRI = 1: A is upper triangular, TRI = 2: lower triangular -- the k range
+    // where the warp's rows of A are zero is skipped (warp-uniform bounds, so
+    // only exact zeros are left out and the result is unchanged).
+    template <bool SUB, int TRI = 0> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
     {
         if (!act) return;
+        const int wr0 = ((int)(threadIdx.x & ~31u) / TX) * TR;             // first row of the warp
+        const int wr1 = ((int)(threadIdx.x | 31u) / TX) * TR + TR;         // one past its last row
+        const int k0 = TRI == 1 ? wr0 : 0;
+        const int k1 = TRI == 2 ? (wr1 < KB ? wr1 : KB) : KB;
 #pragma unroll 4
-        for (int k = 0; k < KB; k++) {
+        for (int k = k0; k < k1; k++) {
             T a[TR], b[TC];
             vld<T, TR>(a, At + k * LD + row(0));
             vld<T, TC>(b, B + k * LD + col(0));
@@ -315,6 +322,9 @@ template <class T, int KB, int NT> struct Tile {
     __device__ __forceinline__ void mms(Reg &acc, const T *A, const T *B) const { mm_rowA<true>(acc, A, B); }
     __device__ __forceinline__ void mma_t(Reg &acc, const T *At, const T *B) const { mm_tA<false>(acc, At, B); }
     __device__ __forceinline__ void mms_t(Reg &acc, const T *At, const T *B) const { mm_tA<true>(acc, At, B); }
+    // A upper triangular (acc += A B) / lower triangular (acc -= A B)
+    __device__ __forceinline__ void mma_tu(Reg &acc, const T *At, const T *B) const { mm_tA<false, 1>(acc, At, B); }
+    __device__ __forceinline__ void mms_tl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 2>(acc, At, B); }
 
     // In-place Gauss-Jordan inverse of the register tile, no pivoting (the
     // diagonal blocks of a diagonally dominant A stay diagonally dominant

@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
         if (J > 0) {
             // L_J = F_{J-1} G_{J-1}
             t.rzero(acc);
-            t.mma_t(acc, sF, sG);
+            t.mma_tu(acc, sF, sG); // F_{J-1} = A(J, J-1) is upper triangular (KB >= kl)
             __syncthreads();
             t.rstore_t(sF, acc); // sF now holds L_J, transposed
             t.gstore_t(gL + tb + J * TS, acc);
@@ -346,11 +346,11 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
                 t.rload(aV, sZV);
             else
                 t.rzero(aV);
-            if (J < N - 1) t.mms_t(aV, sE, sXV);
+            if (J < N - 1) t.mms_tl(aV, sE, sXV); // E_J = A(J, J+1) is lower triangular (KB >= ku)
         }
         if (doW) {
             t.rload(aW, sZ);
-            if (J < N - 1) t.mms_t(aW, sE, sXW);
+            if (J < N - 1) t.mms_tl(aW, sE, sXW);
         }
         __syncthreads();
         if (doV) t.rstore(sXV, aV);
