@@ -290,130 +290,110 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------ small bands
-// KB <= 4: one thread per (partition, column) runs both sweeps with its
-// vectors in registers; the L (forward) and G, E (backward) tiles of the next
-// block are staged by cp.async in the thread's own shared-memory slot.  z is
-// kept in gy between the sweeps (each thread rereads only what it wrote).
-template <class T, int KB> struct ChainApply {
+// KB <= 4: KB lanes per (partition, column) chain.  Lane r owns row r of each
+// block's vectors and tiles; z_{J-1} / y_{J+1} / t arrive by shuffles.  A ring
+// entry holds the block's L (forward) or G and E (backward) tiles plus each
+// lane's own right-hand-side or z element; z is kept in gy between the sweeps
+// (each lane rereads only what it wrote).
+template <class T, int KB> struct QuadApply {
     using H = typename HighOf<T>::type;
     static constexpr int TS = KB * KB;
     static constexpr int DEPTH = 4;
-    // a ring entry: forward -> L tile + r rows (FP64); backward -> G, E tiles + z rows
-    static constexpr int FWD = TS * (int)sizeof(T) + KB * (int)sizeof(H);
-    static constexpr int BWD = 2 * TS * (int)sizeof(T) + KB * (int)sizeof(T);
-    static constexpr int STAGE = ((FWD > BWD ? FWD : BWD) + 15) / 16 * 16; // bytes
+    static constexpr int VEC = 2 * TS * (int)sizeof(T); // byte offset of the lanes' elements
+    static constexpr int STAGE = (VEC + KB * (int)sizeof(H) + 15) / 16 * 16;
     static constexpr int SLOT = DEPTH * STAGE + 16;
-    static constexpr int NC = chain_threads(SLOT);
-    static constexpr size_t SMEM = (size_t)NC * SLOT;
+    static constexpr int CPC = chain_threads(SLOT);
+    static constexpr int NT = CPC * KB;
+    static constexpr size_t SMEM = (size_t)CPC * SLOT;
 };
 
 template <class T, int KB>
-__global__ void __launch_bounds__(ChainApply<T, KB>::NC)
-    k_chain_apply(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
-                  const T *__restrict__ gL, const T *__restrict__ gG, const T *__restrict__ gE,
-                  const typename HighOf<T>::type *__restrict__ r, int n, int nrhs, long long NP, T *gy)
+__global__ void __launch_bounds__(QuadApply<T, KB>::NT)
+    k_quad_apply(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                 const T *__restrict__ gL, const T *__restrict__ gG, const T *__restrict__ gE,
+                 const typename HighOf<T>::type *__restrict__ r, int n, int nrhs, long long NP, T *gy)
 {
     using H = typename HighOf<T>::type;
-    using C = ChainApply<T, KB>;
+    using C = QuadApply<T, KB>;
     constexpr int TS = C::TS, D = C::DEPTH;
-    constexpr int CT = TS * (int)sizeof(T) / 16;                          // 16-byte chunks per tile
-    constexpr int ZE = KB * (int)sizeof(T) >= 16 ? 16 : KB * (int)sizeof(T); // z rows: alignment of a block's rows
+    constexpr int CT = TS * (int)sizeof(T) / 16;
     extern __shared__ __align__(16) char smc[];
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int part = idx / nrhs, h = idx - part * nrhs;
-    if (part >= p) return; // no barriers below
-    char *slot = smc + threadIdx.x * C::SLOT;
-    const int s = part_start[part], m = part_start[part + 1] - s;
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int lr = threadIdx.x % KB;
+    const int part = ch / nrhs, h = ch - part * nrhs;
+    if (part >= p) return; // whole segments; no CTA barriers below
+    const unsigned m = seg_mask<KB>();
+    char *slot = smc + (threadIdx.x / KB) * C::SLOT;
+    const int s = part_start[part], mrows = part_start[part + 1] - s;
     const int N = blk_off[part + 1] - blk_off[part];
     const size_t tb = (size_t)blk_off[part] * TS;
     T *yh = gy + (size_t)h * NP + (size_t)blk_off[part] * KB;
     const H *rh = r + (size_t)h * n + s;
 
-    // forward: z_J = r_J - L_J z_{J-1}; ring entry j % D holds L_j and r_j
+    // forward: z_J = r_J - L_J z_{J-1}
     auto issue_f = [&](int j) {
         if (j < N) {
             char *st = slot + (j % D) * C::STAGE;
-            if (j > 0) cp_async_chunks(st, gL + tb + (size_t)j * TS, CT);
-            H *rs = (H *)(st + TS * sizeof(T));
-#pragma unroll
-            for (int i = 0; i < KB; i++)
-                if (j * KB + i < m) cp_async_elem<(int)sizeof(H)>(rs + i, rh + j * KB + i);
+            if (j > 0)
+                for (int q = lr; q < CT; q += KB)
+                    cp_async16(st + 16 * q, (const char *)(gL + tb + (size_t)j * TS) + 16 * q);
+            if (j * KB + lr < mrows) cp_async_elem<(int)sizeof(H)>(st + C::VEC + lr * sizeof(H), rh + j * KB + lr);
         }
         cp_async_commit();
     };
 #pragma unroll
     for (int j = 0; j < D - 1; j++) issue_f(j);
-    T z[KB];
-#pragma unroll
-    for (int i = 0; i < KB; i++) z[i] = sc_zero<T>();
+    T z = sc_zero<T>();
     for (int J = 0; J < N; J++) {
         issue_f(J + D - 1);
         cp_async_wait_n<D - 1>();
+        __syncwarp(m);
         const char *st = slot + (J % D) * C::STAGE;
-        const H *rs = (const H *)(st + TS * sizeof(T));
-        T rj[KB];
-#pragma unroll
-        for (int i = 0; i < KB; i++) rj[i] = J * KB + i < m ? sc_cvt<T, H>(rs[i]) : sc_zero<T>();
+        T v = J * KB + lr < mrows ? sc_cvt<T, H>(*(const H *)(st + C::VEC + lr * sizeof(H))) : sc_zero<T>();
         if (J > 0) {
-            RMat<T, KB> L;
-            rm_ldt(L, (const T *)st);
+            const T *L = (const T *)st;
 #pragma unroll
-            for (int i = 0; i < KB; i++)
-#pragma unroll
-                for (int c = 0; c < KB; c++) rj[i] = msub(rj[i], L.v[i][c], z[c]);
+            for (int c = 0; c < KB; c++) v = msub(v, L[c * KB + lr], seg_shfl<KB>(m, z, c));
         }
-#pragma unroll
-        for (int i = 0; i < KB; i++) z[i] = rj[i];
-        vst<T, KB>(yh + (size_t)J * KB, z);
+        __syncwarp(m); // the ring entry may be refilled from here on
+        z = v;
+        yh[(size_t)J * KB + lr] = z;
     }
     cp_async_wait_all();
     __threadfence_block(); // the z stores above precede the copies below that read them back
-    // backward: y_J = G_J (z_J - E_J y_{J+1}); step i handles block N-1-i.  The
-    // z rows were stored above by this thread (ordinary stores, visible to its
-    // own later asynchronous copies).
+    // backward: y_J = G_J (z_J - E_J y_{J+1}); step i handles block N-1-i
     auto issue_b = [&](int i) {
         if (i < N) {
             const int J = N - 1 - i;
             char *st = slot + (i % D) * C::STAGE;
-            cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
-            cp_async_chunks(st + TS * sizeof(T), gE + tb + (size_t)J * TS, CT);
-            char *zs = st + 2 * TS * sizeof(T);
-#pragma unroll
-            for (int q = 0; q < KB * (int)sizeof(T) / ZE; q++)
-                cp_async_elem<ZE>(zs + q * ZE, (const char *)(yh + (size_t)J * KB) + q * ZE);
+            for (int q = lr; q < CT; q += KB) {
+                cp_async16(st + 16 * q, (const char *)(gG + tb + (size_t)J * TS) + 16 * q);
+                cp_async16(st + TS * sizeof(T) + 16 * q, (const char *)(gE + tb + (size_t)J * TS) + 16 * q);
+            }
+            cp_async_elem<(int)sizeof(T)>(st + C::VEC + lr * sizeof(T), yh + (size_t)J * KB + lr); // own z element
         }
         cp_async_commit();
     };
 #pragma unroll
     for (int i = 0; i < D - 1; i++) issue_b(i);
-    T y[KB];
-#pragma unroll
-    for (int i = 0; i < KB; i++) y[i] = sc_zero<T>();
+    T y = sc_zero<T>();
     for (int i = 0; i < N; i++) {
         const int J = N - 1 - i;
         issue_b(i + D - 1);
         cp_async_wait_n<D - 1>();
+        __syncwarp(m);
         const char *st = slot + (i % D) * C::STAGE;
-        T t[KB];
-        vld<T, KB>(t, (const T *)(st + 2 * TS * sizeof(T))); // z_J
-        if (J < N - 1) {
-            RMat<T, KB> E;
-            rm_ldt(E, (const T *)(st + TS * sizeof(T)));
+        const T *G = (const T *)st, *E = (const T *)(st + TS * sizeof(T));
+        T t = *(const T *)(st + C::VEC + lr * sizeof(T));
+        if (J < N - 1)
 #pragma unroll
-            for (int a = 0; a < KB; a++)
+            for (int c = 0; c < KB; c++) t = msub(t, E[c * KB + lr], seg_shfl<KB>(m, y, c));
+        T acc = sc_zero<T>();
 #pragma unroll
-                for (int c = 0; c < KB; c++) t[a] = msub(t[a], E.v[a][c], y[c]);
-        }
-        RMat<T, KB> G;
-        rm_ldt(G, (const T *)st);
-#pragma unroll
-        for (int a = 0; a < KB; a++) {
-            T acc = sc_zero<T>();
-#pragma unroll
-            for (int c = 0; c < KB; c++) acc = madd(acc, G.v[a][c], t[c]);
-            y[a] = acc;
-        }
-        vst<T, KB>(yh + (size_t)J * KB, y);
+        for (int c = 0; c < KB; c++) acc = madd(acc, G[c * KB + lr], seg_shfl<KB>(m, t, c));
+        __syncwarp(m);
+        y = acc;
+        yh[(size_t)J * KB + lr] = y;
     }
     cp_async_wait_all();
 }
@@ -428,9 +408,9 @@ __global__ void k_u_narrow(const typename HighOf<T>::type *__restrict__ u, T *ut
         ut[q] = cvt_fast<T, H>(u[q]);
 }
 
-// x (+)= y - V_i t_{i+1} - W_i b_{i-1} for small tiles: one thread per (padded
-// row, column), consecutive threads on consecutive rows (a CTA per row block
-// would leave most of its threads idle).
+// x (+)= y - V_i t_{i+1} - W_i b_{i-1} for tiles up to 32 rows: one thread per
+// (padded row, column), consecutive threads on consecutive rows (a CTA per row
+// block would leave most of its threads idle).
 template <class T, int KB>
 __global__ void __launch_bounds__(256)
     k_retrieve_rows(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
@@ -488,16 +468,16 @@ template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, c
         attr = true;
     }
     if constexpr (KB <= 4) {
-        using CA = ChainApply<T, KB>;
+        using CA = QuadApply<T, KB>;
         static bool cattr = false;
         if (!cattr) {
-            if (cudaFuncSetAttribute(k_chain_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            if (cudaFuncSetAttribute(k_quad_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)CA::SMEM) != cudaSuccess)
                 return SPK_ECUDA;
             cattr = true;
         }
-        const long long threads = (long long)P->p * nrhs;
-        k_chain_apply<T, KB><<<(int)((threads + CA::NC - 1) / CA::NC), CA::NC, CA::SMEM, st>>>(
+        const long long chains = (long long)P->p * nrhs;
+        k_quad_apply<T, KB><<<(int)((chains + CA::CPC - 1) / CA::CPC), CA::NT, CA::SMEM, st>>>(
             P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_G, (const T *)P->d_E,
             (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP, (T *)P->d_y);
     } else {
@@ -528,7 +508,7 @@ template <class T, int KB> int run_retrieve(spk_plan *P, void *x, int nrhs, int 
         SPK_CHECK_LAUNCH();
         P->launches++;
     }
-    if constexpr (KB <= 16) {
+    if constexpr (KB <= 32) {
         int sms = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

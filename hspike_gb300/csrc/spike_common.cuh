@@ -611,106 +611,83 @@ __device__ __forceinline__ void cp_async_chunks(void *s, const void *g, int chun
     for (int q = 0; q < chunks; q++) cp_async16((char *)s + 16 * q, (const char *)g + 16 * q);
 }
 
-// ------------------------------------------------------------ tiles in registers
-// Small bands (KB <= 4): a CTA per partition would leave most of its threads
-// idle and spend its time in barriers, so one thread runs one partition's
-// whole chain and owns its KB x KB tiles in registers.
-template <class T, int KB> struct RMat {
-    T v[KB][KB];
-};
-template <class T, int KB> __device__ __forceinline__ void rm_zero(RMat<T, KB> &m)
+// ------------------------------------------------------------ tile rows across lanes
+// A chain of a small band (KB <= 4) runs on KB consecutive lanes of a warp:
+// lane r owns row r of every KB x KB tile, and rows of another lane arrive by
+// shuffles within the KB-lane segment (mask: the segment's lanes only).
+template <int KB> __device__ __forceinline__ unsigned seg_mask()
 {
-#pragma unroll
-    for (int r = 0; r < KB; r++)
-#pragma unroll
-        for (int c = 0; c < KB; c++) m.v[r][c] = sc_zero<T>();
+    const unsigned lane = threadIdx.x & 31u;
+    return (KB == 32 ? 0xffffffffu : ((1u << KB) - 1u)) << (lane & ~(unsigned)(KB - 1));
 }
-// row-major source (element (r, c) at r*KB + c)
-template <class T, int KB> __device__ __forceinline__ void rm_ld(RMat<T, KB> &m, const T *p)
+template <int KB> __device__ __forceinline__ float seg_shfl(unsigned m, float v, int src)
 {
-#pragma unroll
-    for (int r = 0; r < KB; r++) vld<T, KB>(m.v[r], p + r * KB);
+    return __shfl_sync(m, v, src, KB);
 }
-// column-major source (element (r, c) at c*KB + r)
-template <class T, int KB> __device__ __forceinline__ void rm_ldt(RMat<T, KB> &m, const T *p)
+template <int KB> __device__ __forceinline__ double seg_shfl(unsigned m, double v, int src)
 {
-#pragma unroll
-    for (int c = 0; c < KB; c++) {
-        T col[KB];
-        vld<T, KB>(col, p + c * KB);
-#pragma unroll
-        for (int r = 0; r < KB; r++) m.v[r][c] = col[r];
-    }
+    return __shfl_sync(m, v, src, KB);
 }
-template <class T, int KB> __device__ __forceinline__ void rm_st(T *p, const RMat<T, KB> &m)
+template <int KB> __device__ __forceinline__ cfloat seg_shfl(unsigned m, cfloat v, int src)
 {
-#pragma unroll
-    for (int r = 0; r < KB; r++) vst<T, KB>(p + r * KB, m.v[r]);
+    return {__shfl_sync(m, v.re, src, KB), __shfl_sync(m, v.im, src, KB)};
 }
-template <class T, int KB> __device__ __forceinline__ void rm_stt(T *p, const RMat<T, KB> &m)
+template <int KB> __device__ __forceinline__ cdouble seg_shfl(unsigned m, cdouble v, int src)
 {
-#pragma unroll
-    for (int c = 0; c < KB; c++) {
-        T col[KB];
-#pragma unroll
-        for (int r = 0; r < KB; r++) col[r] = m.v[r][c];
-        vst<T, KB>(p + c * KB, col);
-    }
+    return {__shfl_sync(m, v.re, src, KB), __shfl_sync(m, v.im, src, KB)};
 }
-// C = A B
+// out = this lane's row of A B, a: the lane's row of A, b: the lane's row of B
 template <class T, int KB>
-__device__ __forceinline__ void rm_mul(RMat<T, KB> &C, const RMat<T, KB> &A, const RMat<T, KB> &B)
+__device__ __forceinline__ void row_mul(unsigned m, T (&out)[KB], const T (&a)[KB], const T (&b)[KB])
 {
 #pragma unroll
-    for (int r = 0; r < KB; r++)
+    for (int c = 0; c < KB; c++) out[c] = sc_zero<T>();
 #pragma unroll
-        for (int c = 0; c < KB; c++) {
-            T a = sc_zero<T>();
+    for (int k = 0; k < KB; k++)
 #pragma unroll
-            for (int k = 0; k < KB; k++) a = madd(a, A.v[r][k], B.v[k][c]);
-            C.v[r][c] = a;
-        }
+        for (int c = 0; c < KB; c++) out[c] = madd(out[c], a[k], seg_shfl<KB>(m, b[c], k));
 }
-// C -= A B
+// out -= this lane's row of A B
 template <class T, int KB>
-__device__ __forceinline__ void rm_msub(RMat<T, KB> &C, const RMat<T, KB> &A, const RMat<T, KB> &B)
+__device__ __forceinline__ void row_msub(unsigned m, T (&out)[KB], const T (&a)[KB], const T (&b)[KB])
 {
 #pragma unroll
-    for (int r = 0; r < KB; r++)
+    for (int k = 0; k < KB; k++)
 #pragma unroll
-        for (int c = 0; c < KB; c++) {
-            T a = C.v[r][c];
-#pragma unroll
-            for (int k = 0; k < KB; k++) a = msub(a, A.v[r][k], B.v[k][c]);
-            C.v[r][c] = a;
-        }
+        for (int c = 0; c < KB; c++) out[c] = msub(out[c], a[k], seg_shfl<KB>(m, b[c], k));
 }
-// In-place Gauss-Jordan inverse without pivoting (same recurrence as the
-// shared-memory tiles); false on a zero or non-finite pivot.
-template <class T, int KB> __device__ __forceinline__ bool rm_inv(RMat<T, KB> &S)
+// In-place Gauss-Jordan inverse without pivoting of the tile whose row r this
+// lane holds, pivot rows broadcast by shuffle (S[j][c] *= 1/p, S[j][j] = 1/p;
+// S[r][c] -= S[r][j] S[j][c], S[r][j] = -S[r][j]/p).  false on a zero or
+// non-finite pivot (in every lane).
+template <class T, int KB> __device__ __forceinline__ bool row_inv(unsigned m, T (&s)[KB], int r)
 {
     bool ok = true;
 #pragma unroll
     for (int j = 0; j < KB; j++) {
-        const T piv = S.v[j][j];
+        const T piv = seg_shfl<KB>(m, s[j], j);
         if (!sc_finite_nonzero(piv)) ok = false;
         const T ip = sc_recip(piv);
-#pragma unroll
-        for (int c = 0; c < KB; c++)
-            if (c != j) S.v[j][c] = S.v[j][c] * ip;
-        S.v[j][j] = ip;
-#pragma unroll
-        for (int r = 0; r < KB; r++) {
-            if (r == j) continue;
-            const T a = S.v[r][j];
+        if (r == j) {
 #pragma unroll
             for (int c = 0; c < KB; c++)
-                if (c != j) S.v[r][c] = msub(S.v[r][c], a, S.v[j][c]);
-            S.v[r][j] = -(a * ip);
+                if (c != j) s[c] = s[c] * ip;
+            s[j] = ip;
+        }
+        T pr[KB];
+#pragma unroll
+        for (int c = 0; c < KB; c++) pr[c] = seg_shfl<KB>(m, s[c], j);
+        if (r != j) {
+            const T a = s[j];
+#pragma unroll
+            for (int c = 0; c < KB; c++)
+                if (c != j) s[c] = msub(s[c], a, pr[c]);
+            s[j] = -(a * ip);
         }
     }
     return ok;
 }
+
 // threads per CTA of a chain kernel whose threads each stage `bytes` in shared memory
 __host__ __device__ constexpr int chain_threads(int bytes)
 {

@@ -376,115 +376,142 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
 }
 
 // ------------------------------------------------------------ small bands
-// KB <= 4: one thread per partition chain, tiles in registers (RMat), the next
-// block's tiles staged by cp.async in the thread's own shared-memory slot (no
-// barriers: a thread only reads what it copied).  Same recurrences and the same
-// global layouts as k_factor_fwd / k_factor_bwd.
-template <class T, int KB> struct ChainFwd {
+// KB <= 4: a CTA per partition would leave most threads idle and pay a barrier
+// per tile step.  KB lanes run one partition chain instead: lane r owns row r
+// of every tile, the other rows arrive by shuffles (row_mul / row_msub /
+// row_inv), and the chain's next DEPTH-1 blocks stream into its shared-memory
+// ring by cp.async (each lane copies every KB-th 16-byte piece; __syncwarp on
+// the segment publishes them).  Same recurrences and global layouts as
+// k_factor_fwd / k_factor_bwd.
+template <class T, int KB> struct QuadFwd {
     static constexpr int TS = KB * KB;
-    static constexpr int DEPTH = 4;                                 // blocks in flight per chain
-    static constexpr int STAGE = 3 * TS;                            // D, F^T, E
-    static constexpr int SLOT = DEPTH * STAGE * (int)sizeof(T) + 16; // ring + pad (odd in 16-byte units)
-    static constexpr int NC = chain_threads(SLOT);
-    static constexpr size_t SMEM = (size_t)NC * SLOT;
+    static constexpr int DEPTH = 4;
+    static constexpr int STAGE = 3 * TS;                             // D, F^T, E
+    static constexpr int SLOT = DEPTH * STAGE * (int)sizeof(T) + 16; // per chain (odd in 16-byte units)
+    static constexpr int CPC = chain_threads(SLOT);                  // chains per CTA
+    static constexpr int NT = CPC * KB;
+    static constexpr size_t SMEM = (size_t)CPC * SLOT;
 };
 
 template <class T, int KB>
-__global__ void __launch_bounds__(ChainFwd<T, KB>::NC)
-    k_chain_fwd(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gZ, unsigned *err)
+__global__ void __launch_bounds__(QuadFwd<T, KB>::NT)
+    k_quad_fwd(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gZ, unsigned *err)
 {
-    using C = ChainFwd<T, KB>;
+    using C = QuadFwd<T, KB>;
     constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int CH = C::STAGE * (int)sizeof(T) / 16;
     extern __shared__ __align__(16) char smc[];
-    const int part = blockIdx.x * blockDim.x + threadIdx.x;
-    if (part >= p) return; // no barriers below
-    T *slot = (T *)(smc + threadIdx.x * C::SLOT);
+    const int part = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int r = threadIdx.x % KB;
+    if (part >= p) return; // whole segments leave together; no CTA barriers below
+    const unsigned m = seg_mask<KB>();
+    T *slot = (T *)(smc + (threadIdx.x / KB) * C::SLOT);
     const int N = blk_off[part + 1] - blk_off[part];
     const size_t tb = (size_t)blk_off[part] * TS;
     const T *gTp = gT + (size_t)blk_off[part] * C::STAGE;
     const bool doW = part > 0;
-    constexpr int CH = C::STAGE * (int)sizeof(T) / 16;
-    RMat<T, KB> G, Ep, Zp;
-    bool ok = true;
-    if (doW) rm_ld(Zp, gZ + tb); // z_0 = C^
+    auto issue = [&](int j) {
+        if (j < N)
+            for (int q = r; q < CH; q += KB)
+                cp_async16((char *)(slot + (j % D) * C::STAGE) + 16 * q,
+                           (const char *)(gTp + (size_t)j * C::STAGE) + 16 * q);
+        cp_async_commit();
+    };
+    T g[KB], ep[KB], zp[KB];
 #pragma unroll
-    for (int j = 0; j < D - 1; j++) {
-        if (j < N) cp_async_chunks(slot + j * C::STAGE, gTp + (size_t)j * C::STAGE, CH);
-        cp_async_commit();
+    for (int c = 0; c < KB; c++) {
+        g[c] = ep[c] = sc_zero<T>();
+        zp[c] = doW ? gZ[tb + r * KB + c] : sc_zero<T>(); // z_0 = C^
     }
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < D - 1; j++) issue(j);
     for (int J = 0; J < N; J++) {
-        const int jn = J + D - 1;
-        if (jn < N) cp_async_chunks(slot + (jn % D) * C::STAGE, gTp + (size_t)jn * C::STAGE, CH);
-        cp_async_commit();
+        issue(J + D - 1);
         cp_async_wait_n<D - 1>();
+        __syncwarp(m);
         const T *sc = slot + (J % D) * C::STAGE;
-        RMat<T, KB> S;
-        rm_ld(S, sc); // D_J
+        T sr[KB];
+#pragma unroll
+        for (int c = 0; c < KB; c++) sr[c] = sc[r * KB + c]; // D_J
         if (J > 0) {
-            RMat<T, KB> L;
-            {
-                RMat<T, KB> F;
-                rm_ldt(F, sc + TS); // stored as F^T, row-major
-                rm_mul(L, F, G);    // L_J = F_{J-1} G_{J-1}
-            }
-            rm_stt(gL + tb + (size_t)J * TS, L);
-            rm_msub(S, L, Ep); // S_J = D_J - L_J E_{J-1}
+            T f[KB], l[KB];
+#pragma unroll
+            for (int c = 0; c < KB; c++) f[c] = sc[TS + c * KB + r]; // row r of F (stored as F^T)
+            row_mul<T, KB>(m, l, f, g);                                // L_J = F_{J-1} G_{J-1}
+#pragma unroll
+            for (int c = 0; c < KB; c++) gL[tb + (size_t)J * TS + c * KB + r] = l[c];
+            row_msub<T, KB>(m, sr, l, ep); // S_J = D_J - L_J E_{J-1}
             if (doW) {
-                RMat<T, KB> Z;
-                rm_zero(Z);
-                rm_msub(Z, L, Zp); // z_J = -L_J z_{J-1}
-                rm_st(gZ + tb + (size_t)J * TS, Z);
-                Zp = Z;
+                T z[KB];
+#pragma unroll
+                for (int c = 0; c < KB; c++) z[c] = sc_zero<T>();
+                row_msub<T, KB>(m, z, l, zp); // z_J = -L_J z_{J-1}
+#pragma unroll
+                for (int c = 0; c < KB; c++) {
+                    gZ[tb + (size_t)J * TS + r * KB + c] = z[c];
+                    zp[c] = z[c];
+                }
             }
         }
-        rm_ld(Ep, sc + 2 * TS); // E_J, for the next block
-        ok = rm_inv(S) && ok;
-        rm_stt(gG + tb + (size_t)J * TS, S);
-        G = S;
+#pragma unroll
+        for (int c = 0; c < KB; c++) ep[c] = sc[2 * TS + r * KB + c]; // E_J, for the next block
+        __syncwarp(m); // the ring entry may be refilled from here on
+        ok = row_inv<T, KB>(m, sr, r) && ok;
+#pragma unroll
+        for (int c = 0; c < KB; c++) {
+            gG[tb + (size_t)J * TS + c * KB + r] = sr[c];
+            g[c] = sr[c];
+        }
     }
     cp_async_wait_all();
-    if (!ok) atomicOr(err, SPK_DEV_ERR_PIVOT);
+    if (!ok && r == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
 }
 
-template <class T, int KB> struct ChainBwd {
+template <class T, int KB> struct QuadBwd {
     static constexpr int TS = KB * KB;
     static constexpr int DEPTH = 4;
     static constexpr int STAGE = 3 * TS; // G, E, Z (W) / G, E (V)
     static constexpr int SLOT = DEPTH * STAGE * (int)sizeof(T) + 16;
-    static constexpr int NC = chain_threads(SLOT);
-    static constexpr size_t SMEM = (size_t)NC * SLOT;
+    static constexpr int CPC = chain_threads(SLOT);
+    static constexpr int NT = CPC * KB;
+    static constexpr size_t SMEM = (size_t)CPC * SLOT;
 };
 
-// X_J = G_J (Z_J - E_J X_{J+1}): one thread per (partition, spike), V then W
-// of a partition on adjacent threads (they share the G / E tiles in L1).
-// Blocks are visited from N-1 down; the ring holds the next DEPTH-1 of them.
+// X_J = G_J (Z_J - E_J X_{J+1}), KB lanes per (partition, spike) chain, V and
+// W of a partition on adjacent segments; blocks visited from N-1 down.
 template <class T, int KB>
-__global__ void __launch_bounds__(ChainBwd<T, KB>::NC)
-    k_chain_bwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
-                const T *__restrict__ gG, const T *__restrict__ gE, const T *__restrict__ gZ,
-                const T *__restrict__ gBhat, T *gV, T *gW)
+__global__ void __launch_bounds__(QuadBwd<T, KB>::NT)
+    k_quad_bwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
+               const T *__restrict__ gG, const T *__restrict__ gE, const T *__restrict__ gZ,
+               const T *__restrict__ gBhat, T *gV, T *gW)
 {
-    using C = ChainBwd<T, KB>;
+    using C = QuadBwd<T, KB>;
     constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int CT = TS * (int)sizeof(T) / 16; // 16-byte pieces per tile
     extern __shared__ __align__(16) char smc[];
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int part = idx >> 1;
-    const bool isW = idx & 1;
-    if (part >= p || (isW ? part == 0 : part == p - 1)) return; // no barriers below
-    T *slot = (T *)(smc + threadIdx.x * C::SLOT);
-    const int m = part_start[part + 1] - part_start[part];
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int r = threadIdx.x % KB;
+    const int part = ch >> 1;
+    const bool isW = ch & 1;
+    if (part >= p || (isW ? part == 0 : part == p - 1)) return; // whole segments; no CTA barriers below
+    const unsigned m = seg_mask<KB>();
+    T *slot = (T *)(smc + (threadIdx.x / KB) * C::SLOT);
+    const int mrows = part_start[part + 1] - part_start[part];
     const int N = blk_off[part + 1] - blk_off[part];
     const size_t tb = (size_t)blk_off[part] * TS;
     T *gX = isW ? gW : gV;
-    constexpr int CT = TS * (int)sizeof(T) / 16; // chunks per tile
     // step i handles block N-1-i; its tiles sit in ring entry i % D
     auto issue = [&](int i) {
         if (i < N) {
             const int J = N - 1 - i;
-            T *st = slot + (i % D) * C::STAGE;
-            cp_async_chunks(st, gG + tb + (size_t)J * TS, CT);
-            cp_async_chunks(st + TS, gE + tb + (size_t)J * TS, CT);
-            if (isW) cp_async_chunks(st + 2 * TS, gZ + tb + (size_t)J * TS, CT);
+            char *st = (char *)(slot + (i % D) * C::STAGE);
+            for (int q = r; q < CT; q += KB) {
+                cp_async16(st + 16 * q, (const char *)(gG + tb + (size_t)J * TS) + 16 * q);
+                cp_async16(st + TS * sizeof(T) + 16 * q, (const char *)(gE + tb + (size_t)J * TS) + 16 * q);
+                if (isW)
+                    cp_async16(st + 2 * TS * sizeof(T) + 16 * q, (const char *)(gZ + tb + (size_t)J * TS) + 16 * q);
+            }
         }
         cp_async_commit();
     };
@@ -493,50 +520,46 @@ __global__ void __launch_bounds__(ChainBwd<T, KB>::NC)
     // V's right-hand side [0; B^] lives in the last KB real rows: blocks J0
     // (rows o..KB-1) and J0+1 (rows 0..o-1, when o > 0).  A partition shorter
     // than a tile (o < 0) takes B^'s last m rows.
-    RMat<T, KB> Z0, Z1;
-    rm_zero(Z0);
-    rm_zero(Z1);
-    const int J0 = m >= KB ? (m - KB) / KB : 0;
-    const int o = m - KB - J0 * KB;
+    T z0[KB], z1[KB];
+    const int J0 = mrows >= KB ? (mrows - KB) / KB : 0;
+    const int o = mrows - KB - J0 * KB;
+#pragma unroll
+    for (int c = 0; c < KB; c++) z0[c] = z1[c] = sc_zero<T>();
     if (!isW) {
         const T *B = gBhat + (size_t)part * TS;
 #pragma unroll
-        for (int r = 0; r < KB; r++)
+        for (int c = 0; c < KB; c++) {
+            z0[c] = (r >= o && r - o < KB) ? B[(r - o) * KB + c] : sc_zero<T>();
+            z1[c] = r < o ? B[(KB - o + r) * KB + c] : sc_zero<T>();
+        }
+        if (o > 0) { // z_{J0+1} -= L_{J0+1} z_{J0}
+            T l1[KB];
 #pragma unroll
-            for (int c = 0; c < KB; c++)
-                Z0.v[r][c] = (r >= o && r - o < KB) ? B[(r - o) * KB + c] : sc_zero<T>();
-        if (o > 0) {
-            // z_{J0+1} = [B^ rows KB-o..KB-1 ; 0] - L_{J0+1} z_{J0}
-            RMat<T, KB> L1;
-#pragma unroll
-            for (int r = 0; r < KB; r++)
-#pragma unroll
-                for (int c = 0; c < KB; c++) Z1.v[r][c] = r < o ? B[(KB - o + r) * KB + c] : sc_zero<T>();
-            rm_ldt(L1, gL + tb + (size_t)(J0 + 1) * TS);
-            rm_msub(Z1, L1, Z0);
+            for (int c = 0; c < KB; c++) l1[c] = gL[tb + (size_t)(J0 + 1) * TS + c * KB + r];
+            row_msub<T, KB>(m, z1, l1, z0);
         }
     }
-    RMat<T, KB> X; // X_{J+1}
-    rm_zero(X);
+    T x[KB]; // row r of X_{J+1}
+#pragma unroll
+    for (int c = 0; c < KB; c++) x[c] = sc_zero<T>();
     for (int i = 0; i < N; i++) {
         const int J = N - 1 - i;
         issue(i + D - 1);
         cp_async_wait_n<D - 1>();
+        __syncwarp(m);
         const T *sc = slot + (i % D) * C::STAGE;
-        RMat<T, KB> Gt, Et, Tm;
-        if (isW)
-            rm_ld(Tm, sc + 2 * TS); // z_J (row-major)
-        else if (J == J0)
-            Tm = Z0;
-        else if (o > 0 && J == J0 + 1)
-            Tm = Z1;
-        else
-            rm_zero(Tm);
-        rm_ldt(Et, sc + TS);
-        if (J < N - 1) rm_msub(Tm, Et, X);
-        rm_ldt(Gt, sc);
-        rm_mul(X, Gt, Tm);
-        rm_stt(gX + tb + (size_t)J * TS, X);
+        T t[KB], e[KB], g[KB];
+#pragma unroll
+        for (int c = 0; c < KB; c++) {
+            t[c] = isW ? sc[2 * TS + r * KB + c] : (J == J0 ? z0[c] : (o > 0 && J == J0 + 1) ? z1[c] : sc_zero<T>());
+            e[c] = sc[TS + c * KB + r]; // row r of E_J (stored column-major)
+            g[c] = sc[c * KB + r];      // row r of G_J (stored column-major)
+        }
+        __syncwarp(m); // the ring entry may be refilled from here on
+        if (J < N - 1) row_msub<T, KB>(m, t, e, x);
+        row_mul<T, KB>(m, x, g, t);
+#pragma unroll
+        for (int c = 0; c < KB; c++) gX[tb + (size_t)J * TS + c * KB + r] = x[c];
     }
     cp_async_wait_all();
 }
@@ -579,10 +602,10 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     static bool attr = false;
     if (!attr) {
         if constexpr (KB <= 4) {
-            if (cudaFuncSetAttribute(k_chain_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ChainFwd<T, KB>::SMEM) != cudaSuccess ||
-                cudaFuncSetAttribute(k_chain_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ChainBwd<T, KB>::SMEM) != cudaSuccess)
+            if (cudaFuncSetAttribute(k_quad_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)QuadFwd<T, KB>::SMEM) != cudaSuccess ||
+                cudaFuncSetAttribute(k_quad_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)QuadBwd<T, KB>::SMEM) != cudaSuccess)
                 return SPK_ECUDA;
         }
         if (cudaFuncSetAttribute(k_factor_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::fwd) !=
@@ -605,8 +628,8 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     spk_phase_end(P, st);
     spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
     if constexpr (KB <= 4) {
-        using CF = ChainFwd<T, KB>;
-        k_chain_fwd<T, KB><<<(P->p + CF::NC - 1) / CF::NC, CF::NC, CF::SMEM, st>>>(
+        using CF = QuadFwd<T, KB>;
+        k_quad_fwd<T, KB><<<(P->p + CF::CPC - 1) / CF::CPC, CF::NT, CF::SMEM, st>>>(
             (const T *)P->d_T, P->d_blk_off, P->p, (T *)P->d_L, (T *)P->d_G, (T *)P->d_W, P->d_err);
     } else {
         k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L, (T *)P->d_G,
@@ -618,8 +641,8 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     if (P->p > 1) {
         spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
         if constexpr (KB <= 4) {
-            using CB = ChainBwd<T, KB>;
-            k_chain_bwd<T, KB><<<(2 * P->p + CB::NC - 1) / CB::NC, CB::NC, CB::SMEM, st>>>(
+            using CB = QuadBwd<T, KB>;
+            k_quad_bwd<T, KB><<<(2 * P->p + CB::CPC - 1) / CB::CPC, CB::NT, CB::SMEM, st>>>(
                 P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_G, (const T *)P->d_E,
                 (const T *)P->d_W, (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
         } else {

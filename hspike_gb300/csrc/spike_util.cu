@@ -263,11 +263,14 @@ extern "C" int spk_narrow(const void *src, void *dst, long long count, int is_co
 }
 
 // ------------------------------------------------------------ residual
-// G lanes per row; per-column squared norms reduced in shared memory and
-// added to norms[] once per CTA.
+// G lanes per row; NH columns per pass over a row's entries (the CSR entries
+// are read once per pass, not once per column); per-column squared norms
+// summed within each warp by shuffles, then once per warp in shared memory
+// (contended FP64 shared atomics retry on the FP64 pipe), then once per CTA
+// into norms[].
 constexpr int RES_MAXH = 32;
 
-template <class H, int G>
+template <class H, int G, int NH>
 __global__ void __launch_bounds__(256)
     k_residual(int n, const int *__restrict__ rowptr, const int *__restrict__ colind, const H *__restrict__ aij,
                const H *__restrict__ x, const H *__restrict__ b, H *r, int h0, int nr, int want_b, double *norms,
@@ -283,43 +286,69 @@ __global__ void __launch_bounds__(256)
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     const int lane = threadIdx.x & 31;
-    double lr[RES_MAXH], lb[RES_MAXH];
-    for (int h = 0; h < nr; h++) lr[h] = lb[h] = 0.0;
-    for (long long base = warp * RPW; base < n; base += nwarps * RPW) {
-        const long long row = base + lane / G;
-        const bool valid = row < n;
-        const int t0 = valid ? rowptr[row] : 0, t1 = valid ? rowptr[row + 1] : 0;
-        for (int h = 0; h < nr; h++) {
-            const H *xh = x + (size_t)(h0 + h) * n;
-            H acc = sc_zero<H>();
-            for (int t = t0 + sub; t < t1; t += G) acc = madd(acc, aij[t], xh[colind[t]]);
+    for (int hb = 0; hb < nr; hb += NH) {
+        double lr[NH], lb[NH];
+        const H *xj[NH]; // this pass's columns of x (a column past nr repeats the last one, unused)
 #pragma unroll
-            for (int o = G / 2; o > 0; o >>= 1) {
-                if constexpr (sizeof(H) == 8) {
-                    acc = acc + __shfl_xor_sync(0xffffffffu, acc, o);
-                } else {
-                    H other;
-                    const unsigned *srcw = (const unsigned *)&acc;
-                    unsigned *dstw = (unsigned *)&other;
+        for (int j = 0; j < NH; j++) {
+            lr[j] = lb[j] = 0.0;
+            xj[j] = x + (size_t)(h0 + min(hb + j, nr - 1)) * n;
+        }
+        for (long long base = warp * RPW; base < n; base += nwarps * RPW) {
+            const long long row = base + lane / G;
+            const bool valid = row < n;
+            const int t0 = valid ? rowptr[row] : 0, t1 = valid ? rowptr[row + 1] : 0;
+            H acc[NH];
 #pragma unroll
-                    for (int w = 0; w < (int)(sizeof(H) / 4); w++) dstw[w] = __shfl_xor_sync(0xffffffffu, srcw[w], o);
-                    acc = acc + other;
+            for (int j = 0; j < NH; j++) acc[j] = sc_zero<H>();
+            for (int t = t0 + sub; t < t1; t += G) {
+                const H av = aij[t];
+                const int c = colind[t];
+#pragma unroll
+                for (int j = 0; j < NH; j++)
+                    if (hb + j < nr) acc[j] = madd(acc[j], av, xj[j][c]);
+            }
+#pragma unroll
+            for (int j = 0; j < NH; j++)
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) {
+                    if constexpr (sizeof(H) == 8) {
+                        acc[j] = acc[j] + __shfl_xor_sync(0xffffffffu, acc[j], o);
+                    } else {
+                        H other;
+                        other.re = __shfl_xor_sync(0xffffffffu, acc[j].re, o);
+                        other.im = __shfl_xor_sync(0xffffffffu, acc[j].im, o);
+                        acc[j] = acc[j] + other;
+                    }
+                }
+            if (sub == 0 && valid) {
+#pragma unroll
+                for (int j = 0; j < NH; j++) {
+                    if (hb + j >= nr) break;
+                    const size_t off = (size_t)(h0 + hb + j) * n + row;
+                    const H bv = b[off];
+                    const H rv = bv - acc[j];
+                    r[off] = rv;
+                    lr[j] += sc_abs2(rv);
+                    if (want_b) lb[j] += sc_abs2(bv);
                 }
             }
-            if (sub == 0 && valid) {
-                const H bv = b[(size_t)(h0 + h) * n + row];
-                const H rv = bv - acc;
-                r[(size_t)(h0 + h) * n + row] = rv;
-                lr[h] += sc_abs2(rv);
-                if (want_b) lb[h] += sc_abs2(bv);
+        }
+#pragma unroll
+        for (int j = 0; j < NH; j++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lr[j] += __shfl_xor_sync(0xffffffffu, lr[j], o);
+                lb[j] += __shfl_xor_sync(0xffffffffu, lb[j], o);
             }
-        }
+        if (lane == 0)
+#pragma unroll
+            for (int j = 0; j < NH; j++) {
+                if (hb + j >= nr) break;
+                atomicAdd(&sr[hb + j], lr[j]);
+                if (want_b) atomicAdd(&sb[hb + j], lb[j]);
+            }
     }
-    if (sub == 0)
-        for (int h = 0; h < nr; h++) {
-            atomicAdd(&sr[h], lr[h]);
-            if (want_b) atomicAdd(&sb[h], lb[h]);
-        }
     __syncthreads();
     for (int h = threadIdx.x; h < nr; h += blockDim.x) {
         atomicAdd(&norms[h0 + h], sr[h]);
@@ -336,8 +365,15 @@ static int launch_residual(const spk_plan *P, const int *rp, const int *ci, cons
     if (blocks > 152 * 8) blocks = 152 * 8;
     for (int h0 = 0; h0 < nrhs; h0 += RES_MAXH) {
         const int nr = nrhs - h0 < RES_MAXH ? nrhs - h0 : RES_MAXH;
-        k_residual<H, G><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x, (const H *)b,
-                                                          (H *)r, h0, nr, want_b, norms, nrhs);
+        if (nr >= 4)
+            k_residual<H, G, 4><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
+                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs);
+        else if (nr >= 2)
+            k_residual<H, G, 2><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
+                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs);
+        else
+            k_residual<H, G, 1><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
+                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs);
         if (cudaGetLastError() != cudaSuccess) return SPK_ECUDA;
         ((spk_plan *)P)->launches++;
     }
@@ -433,7 +469,15 @@ __global__ void __launch_bounds__(256)
                 }
             }
         }
-        if (sub == 0)
+        // warp sums first: one shared atomic per warp and column
+#pragma unroll
+        for (int j = 0; j < NH; j++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lr[j] += __shfl_xor_sync(0xffffffffu, lr[j], o);
+                lb[j] += __shfl_xor_sync(0xffffffffu, lb[j], o);
+            }
+        if ((threadIdx.x & 31) == 0)
 #pragma unroll
             for (int j = 0; j < NH; j++) {
                 if (h0 + j >= nrhs) break;
