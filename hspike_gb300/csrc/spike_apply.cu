@@ -477,7 +477,8 @@ template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, c
             cattr = true;
         }
         const long long chains = (long long)P->p * nrhs;
-        k_quad_apply<T, KB><<<(int)((chains + CA::CPC - 1) / CA::CPC), CA::NT, CA::SMEM, st>>>(
+        const int cpc = chains_per_cta(chains, CA::CPC);
+        k_quad_apply<T, KB><<<(int)((chains + cpc - 1) / cpc), cpc * KB, (size_t)cpc * CA::SLOT, st>>>(
             P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_G, (const T *)P->d_E,
             (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP, (T *)P->d_y);
     } else {

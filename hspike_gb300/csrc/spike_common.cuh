@@ -688,6 +688,23 @@ template <class T, int KB> __device__ __forceinline__ bool row_inv(unsigned m, T
     return ok;
 }
 
+// Chains per CTA at launch: spread the chains over every SM (two CTAs each
+// where there are enough), at most cpc_max per CTA.
+static inline int chains_per_cta(long long chains, int cpc_max)
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    long long c = (chains + 2LL * sms - 1) / (2LL * sms);
+    if (c < 1) c = 1;
+    if (c > cpc_max) c = cpc_max;
+    return (int)c;
+}
+
 // threads per CTA of a chain kernel whose threads each stage `bytes` in shared memory
 __host__ __device__ constexpr int chain_threads(int bytes)
 {

@@ -629,7 +629,8 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
     if constexpr (KB <= 4) {
         using CF = QuadFwd<T, KB>;
-        k_quad_fwd<T, KB><<<(P->p + CF::CPC - 1) / CF::CPC, CF::NT, CF::SMEM, st>>>(
+        const int cpc = chains_per_cta(P->p, CF::CPC);
+        k_quad_fwd<T, KB><<<(P->p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * CF::SLOT, st>>>(
             (const T *)P->d_T, P->d_blk_off, P->p, (T *)P->d_L, (T *)P->d_G, (T *)P->d_W, P->d_err);
     } else {
         k_factor_fwd<T, KB><<<P->p, NT, S::fwd, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L, (T *)P->d_G,
@@ -642,7 +643,8 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
         spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
         if constexpr (KB <= 4) {
             using CB = QuadBwd<T, KB>;
-            k_quad_bwd<T, KB><<<(2 * P->p + CB::CPC - 1) / CB::CPC, CB::NT, CB::SMEM, st>>>(
+            const int cpc = chains_per_cta(2LL * P->p, CB::CPC);
+            k_quad_bwd<T, KB><<<(2 * P->p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * CB::SLOT, st>>>(
                 P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_G, (const T *)P->d_E,
                 (const T *)P->d_W, (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
         } else {
