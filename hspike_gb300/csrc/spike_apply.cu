@@ -86,7 +86,7 @@ __device__ __forceinline__ void fetch_r(T (&nxt)[VPT], const H *__restrict__ r, 
         const int q = threadIdx.x + v * NT;
         if (q < KB * nr) {
             const int h = q / KB, lr = q - h * KB, lrow = J * KB + lr;
-            nxt[v] = lrow < m ? sc_cvt<T, H>(r[(size_t)(h0 + h) * n + s + lrow]) : sc_zero<T>();
+            nxt[v] = lrow < m ? cvt_fast<T, H>(r[(size_t)(h0 + h) * n + s + lrow]) : sc_zero<T>();
         }
     }
 }

@@ -733,11 +733,15 @@ template <class T, int KB, int NT> __device__ __forceinline__ void cp_async_tile
 // pipe (which executes the F2F conversion) is ~60x narrower than its integer
 // pipe.  Normal results only; zero, subnormal, overflow, inf and NaN take the
 // hardware conversion.  Bit-identical to (float)x.
+// The rare cases call out of line so the compiler keeps them a branch: an
+// if-converted hardware conversion would run on the FP64 pipe for every value.
+static __device__ __noinline__ float f64_to_f32_rare(double x) { return (float)x; }
+static __device__ __noinline__ double f32_to_f64_rare(float x) { return (double)x; }
 __device__ __forceinline__ float f64_to_f32(double x)
 {
     const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
     const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-    if (e <= 0 || e >= 255) return (float)x;
+    if (e <= 0 || e >= 255) return f64_to_f32_rare(x);
     const unsigned r = ((hi & 0xfffffu) << 3) | (lo >> 29); // 23 mantissa bits
     const unsigned rem = lo & 0x1fffffffu;                  // 29 dropped bits
     const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (r & 1u));
@@ -750,7 +754,7 @@ __device__ __forceinline__ double f32_to_f64(float x)
 {
     const unsigned u = __float_as_uint(x);
     const unsigned e = (u >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)x;
+    if (e == 0u || e == 0xffu) return f32_to_f64_rare(x);
     const unsigned hi = (u & 0x80000000u) | ((e + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
     return __hiloint2double((int)hi, (int)(u << 29));
 }
