@@ -38,7 +38,7 @@ WORKLOAD = (f"large-band real SPIKE: n={N:,} kl=ku={K_BAND} partitions={P} nrhs=
 # DRAM bytes (read + write) per row block of each kernel, from one ncu capture of
 # `bench.py --n 600000 --partitions 300` (profiles/ncu_kernels_n600k_k64.md);
 # traffic per launch = this x the launch's row blocks.
-TRAFFIC_PER_BLOCK = {"factor_fwd": 93_130, "factor_bwd": 77_680, "band_tiles": 158_640, "rhs_sweeps": 49_440}
+TRAFFIC_PER_BLOCK = {"factor_fwd": 92_920, "factor_bwd": 77_810, "band_tiles": 158_650, "rhs_sweeps": 49_380}
 
 
 def nnz_of(n, k):
