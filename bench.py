@@ -105,7 +105,7 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------- CPU baseline
-def cpu_baseline(system=None):
+def cpu_baseline(system=None, p=P):
     """Time the CPU oracle -- the restated reference path (oracle/spike_oracle.c:
     banded partial-pivoting LU per partition, reduced system on R's band,
     implicit retrieval), OpenMP over partitions on every host core -- on the
@@ -119,12 +119,12 @@ def cpu_baseline(system=None):
     else:
         rp, ci, a, b = system
     t0 = time.perf_counter()
-    x = oracle.spike(rp, ci, a, b, p=P)
+    x = oracle.spike(rp, ci, a, b, p=p)
     dt = time.perf_counter() - t0
     rel = float(oracle.residual(rp, ci, a, x, b).max())
     return {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
             "sample": (f"one full solve of the workload by oracle/spike_oracle.c (restated reference SPIKE, "
-                       f"banded partial-pivoting LU inner solver, {P} partitions) with {cores} OpenMP threads: "
+                       f"banded partial-pivoting LU inner solver, {p} partitions) with {cores} OpenMP threads: "
                        f"{dt:.2f} s, relres {rel:.1e}"),
             "seconds": dt}
 
@@ -140,15 +140,16 @@ def reference_arm(args):
     from hspike_gb300.build import build
 
     build()
-    rp, ci, a, xt, b = hs.gen_banded(N, K_BAND, K_BAND, DOM, SEED, nrhs=NRHS)
+    n, p = args.n, args.partitions
+    rp, ci, a, xt, b = hs.gen_banded(n, K_BAND, K_BAND, DOM, SEED, nrhs=NRHS)
     runs = []
     # each step is one full CPU solve (~2-3 s on 16 cores); cap the count so
     # the whole reference run stays within a few minutes
     steps = max(1, min(args.steps, 10))
     for _ in range(min(args.warmup, 1)):
-        cpu_baseline((rp, ci, a, b))
+        cpu_baseline((rp, ci, a, b), p)
     for _ in range(steps):
-        runs.append(cpu_baseline((rp, ci, a, b)))
+        runs.append(cpu_baseline((rp, ci, a, b), p))
     vals = [r["value"] for r in runs]
     v = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
@@ -632,7 +633,7 @@ def main():
                       "err_vs_xtrue": float(np.linalg.norm(xh - xt) / np.linalg.norm(xt))}
 
     if not args.skip_cpu and rank == 0 and world == 1:
-        out["cpu_baseline"] = cpu_baseline((rp, ci, a, b))
+        out["cpu_baseline"] = cpu_baseline((rp, ci, a, b), p)
 
     ctx.close()
     if dist:

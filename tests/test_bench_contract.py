@@ -1,0 +1,24 @@
+"""bench.py's reference arm, run on a small case of the same band without a GPU.
+
+The reference arm times the CPU restatement of the reference path (oracle/)
+and prints the line the driver reads: impl "reference", the metric, a value,
+cpu_baseline and e2e.  Run here at n = 20,000 so it takes seconds.
+"""
+import json
+import os
+import subprocess
+import sys
+
+from tests.conftest import ROOT
+
+
+def test_reference_arm_prints_its_line():
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "20000", "--partitions",
+           "8", "--steps", "1", "--warmup", "0"]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "solves/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert "n=20,000" in line["config"]["workload"] and "partitions=8" in line["config"]["workload"]
