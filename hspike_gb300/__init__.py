@@ -52,6 +52,11 @@ EXPORTS = [
     "spike_batch_partitions", "spike_server_create", "spike_server_submit", "spike_server_wait",
     "spike_server_drain", "spike_server_stats", "spike_server_clock", "spike_server_destroy",
     "spike_rcm_permutation", "spike_permute_csr", "spike_permute_vector", "spike_dsolve_reordered",
+    "matrix_ComputeBandwidth", "matrix_LoadCSR", "matrix_SaveCSR", "matrix_ExportBinary",
+    "matrix_CreateFromComponents", "matrix_Deallocate", "directSolver_CreateHandler", "directSolver_Configure",
+    "directSolver_Factorize", "directSolver_SolveForRHS", "directSolver_ShowStatistics", "directSolver_Finalize",
+    "directSolver_Solve", "block_CreateEmptyBlock", "block_Deallocate", "block_SaveCSR", "block_loadCSR",
+    "vector_LoadPermutationArray", "vector_LoadRHS",
 ]
 SPIKE_OPT_STREAM_ALLOC = 6
 SPIKE_BATCH_AUTOTUNE = 1
@@ -104,6 +109,25 @@ class RequestStatus(C.Structure):
     _fields_ = [("done", C.c_int), ("error_code", C.c_int), ("relres", C.c_double), ("sweeps", C.c_int),
                 ("factor_hit", C.c_int), ("t_arrival", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
                 ("footprint", C.c_size_t)]
+
+
+class Matrix(C.Structure):
+    """matrix_t of the reference's double build (spike_compat.h)."""
+    _fields_ = [("n", C.c_int), ("nnz", C.c_ulonglong), ("ku", C.c_int), ("kl", C.c_int), ("type", C.c_int),
+                ("colind", C.POINTER(C.c_int)), ("rowptr", C.POINTER(C.c_int)), ("aij", C.POINTER(C.c_double))]
+
+
+class Block(C.Structure):
+    """block_t of the reference's double build (spike_compat.h)."""
+    _fields_ = [("type", C.c_int), ("section", C.c_int), ("n", C.c_int), ("m", C.c_int), ("ku", C.c_int),
+                ("kl", C.c_int), ("aij", C.POINTER(C.c_double))]
+
+
+class DirectSolverHandler(C.Structure):
+    """DirectSolverHander_t (spike_compat.h)."""
+    _fields_ = [("ctx", C.c_void_p), ("factor", C.c_void_p), ("n", C.c_int), ("max_nrhs", C.c_int),
+                ("factor_t", C.c_double), ("solve_t", C.c_double), ("rhs_block_count", C.c_int),
+                ("rhs_column_count", C.c_int)]
 
 
 class ServerStats(C.Structure):
@@ -171,6 +195,36 @@ def load(path: str | None = None):
     L.spike_permute_csr.argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp]
     L.spike_permute_vector.argtypes = [i, i, i, vp, vp]
     L.spike_dsolve_reordered.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, vp]
+    mp, hp = C.POINTER(Matrix), C.POINTER(DirectSolverHandler)
+    L.matrix_ComputeBandwidth.argtypes = [i, vp, vp, vp, ip, ip]
+    L.matrix_LoadCSR.argtypes = [C.c_char_p]
+    L.matrix_LoadCSR.restype = mp
+    L.matrix_SaveCSR.argtypes = [C.c_char_p, mp]
+    L.matrix_SaveCSR.restype = None
+    L.matrix_ExportBinary.argtypes = [mp, C.c_char_p]
+    L.matrix_CreateFromComponents.argtypes = [i, C.c_ulonglong, vp, vp, vp]
+    L.matrix_CreateFromComponents.restype = mp
+    L.matrix_Deallocate.argtypes = [mp]
+    bp = C.POINTER(Block)
+    L.block_CreateEmptyBlock.argtypes = [i, i, i, i, i, i]
+    L.block_CreateEmptyBlock.restype = bp
+    L.block_Deallocate.argtypes = [bp]
+    L.block_SaveCSR.argtypes = [C.c_char_p, bp]
+    L.block_SaveCSR.restype = None
+    L.block_loadCSR.argtypes = [C.c_char_p]
+    L.block_loadCSR.restype = bp
+    L.vector_LoadPermutationArray.argtypes = [i, C.c_char_p]
+    L.vector_LoadPermutationArray.restype = vp
+    L.vector_LoadRHS.argtypes = [i, C.c_char_p]
+    L.vector_LoadRHS.restype = vp
+    L.directSolver_CreateHandler.argtypes = []
+    L.directSolver_CreateHandler.restype = hp
+    L.directSolver_Configure.argtypes = [hp, i]
+    L.directSolver_Factorize.argtypes = [hp, i, i, vp, vp, vp]
+    L.directSolver_SolveForRHS.argtypes = [hp, i, vp, vp]
+    L.directSolver_ShowStatistics.argtypes = [hp]
+    L.directSolver_Finalize.argtypes = [hp]
+    L.directSolver_Solve.argtypes = [i, i, i, vp, vp, vp, vp, vp]
     _LIB = L
     return L
 
@@ -509,6 +563,143 @@ def solve_reordered(rowptr, colind, aij, b, ctx: Context | None = None):
 def batch_partitions(n: int, block: int, rows_per_partition: int) -> int:
     """The batch partition rule (host only, no device needed)."""
     return int(load().spike_batch_partitions(n, block, rows_per_partition))
+
+
+# ------------------------------------------------ reference matrix helpers + plugin
+def compute_bandwidth(rowptr, colind) -> tuple[int, int]:
+    """(ku, kl) by matrix_ComputeBandwidth (host)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    ku, kl = C.c_int(-1), C.c_int(-1)
+    _check(load().matrix_ComputeBandwidth(len(rowptr) - 1, _ptr(colind), _ptr(rowptr), None, C.byref(ku),
+                                          C.byref(kl)))
+    return ku.value, kl.value
+
+
+def load_csr(path: str):
+    """matrix_LoadCSR: returns (rowptr, colind, aij, ku, kl) copied out of the matrix_t."""
+    L = load()
+    M = L.matrix_LoadCSR(os.fsencode(path))
+    if not M:
+        code, msg = last_error()
+        raise SpikeError(code, msg)
+    m = M.contents
+    n, nnz = m.n, int(m.nnz)
+    rowptr = np.ctypeslib.as_array(m.rowptr, (n + 1,)).copy()
+    colind = np.ctypeslib.as_array(m.colind, (nnz,)).copy() if nnz else np.zeros(0, np.int32)
+    aij = np.ctypeslib.as_array(m.aij, (nnz,)).copy() if nnz else np.zeros(0)
+    ku, kl = m.ku, m.kl
+    L.matrix_Deallocate(M)
+    return rowptr, colind, aij, ku, kl
+
+
+def save_csr(path: str, rowptr, colind, aij):
+    """matrix_SaveCSR of a wrapping matrix_t (the arrays stay owned by numpy)."""
+    L = load()
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    aij = np.ascontiguousarray(aij, np.float64)
+    M = Matrix(len(rowptr) - 1, len(colind), 0, 0, 1, colind.ctypes.data_as(C.POINTER(C.c_int)),
+               rowptr.ctypes.data_as(C.POINTER(C.c_int)), aij.ctypes.data_as(C.POINTER(C.c_double)))
+    _check(L.matrix_ExportBinary(C.byref(M), os.fsencode(path)))
+
+
+def save_block(path: str, a, ku=0, kl=0, type_=0, section=3):
+    """block_SaveCSR of a dense column-major n x m block."""
+    L = load()
+    a = np.asfortranarray(np.asarray(a, np.float64).reshape(np.shape(a)[0], -1))
+    B = L.block_CreateEmptyBlock(a.shape[0], a.shape[1], ku, kl, type_, section)
+    if not B:
+        code, msg = last_error()
+        raise SpikeError(code, msg)
+    C.memmove(B.contents.aij, a.ctypes.data, a.nbytes)
+    L.block_SaveCSR(os.fsencode(path), B)
+    code, msg = last_error()
+    L.block_Deallocate(B)
+    if code:
+        raise SpikeError(code, msg)
+
+
+def load_block(path: str):
+    """block_loadCSR: returns (aij n x m column-major, type, section, ku, kl)."""
+    L = load()
+    B = L.block_loadCSR(os.fsencode(path))
+    if not B:
+        code, msg = last_error()
+        raise SpikeError(code, msg)
+    b = B.contents
+    a = np.ctypeslib.as_array(b.aij, (b.n * b.m,)).copy() if b.n * b.m else np.zeros(0)
+    out = (a.reshape((b.n, b.m), order="F"), b.type, b.section, b.ku, b.kl)
+    L.block_Deallocate(B)
+    return out
+
+
+def load_vector(path: str, n: int, permutation=False):
+    """vector_LoadPermutationArray (int32) or vector_LoadRHS (float64): n raw entries."""
+    L = load()
+    f = L.vector_LoadPermutationArray if permutation else L.vector_LoadRHS
+    p = f(n, os.fsencode(path))
+    if not p:
+        code, msg = last_error()
+        raise SpikeError(code, msg)
+    ct = C.c_int if permutation else C.c_double
+    v = np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), (n,)).copy() if n else np.zeros(0, ct)
+    C.CDLL(None).free(C.c_void_p(p))
+    return v
+
+
+class DirectSolver:
+    """The directSolver_* plugin: factor once on the device, solve many times."""
+
+    def __init__(self, max_nrhs: int | None = None):
+        self.L = load()
+        self.h = self.L.directSolver_CreateHandler()
+        if not self.h:
+            code, msg = last_error()
+            raise SpikeError(code, msg)
+        if max_nrhs is not None:
+            _check(self.L.directSolver_Configure(self.h, max_nrhs))
+
+    def factorize(self, rowptr, colind, aij):
+        self._keep = (np.ascontiguousarray(rowptr, np.int32), np.ascontiguousarray(colind, np.int32),
+                      np.ascontiguousarray(aij, np.float64))
+        rp, ci, a = self._keep
+        _check(self.L.directSolver_Factorize(self.h, len(rp) - 1, len(ci), _ptr(ci), _ptr(rp), _ptr(a)))
+
+    def solve(self, b):
+        b = np.asarray(b, np.float64)
+        b2 = np.asfortranarray(b.reshape(self.h.contents.n or len(b), -1))
+        x = np.zeros_like(b2, order="F")
+        _check(self.L.directSolver_SolveForRHS(self.h, b2.shape[1], _ptr(x), _ptr(b2)))
+        return x if np.ndim(b) == 2 else x[:, 0]
+
+    @property
+    def stats(self) -> DirectSolverHandler:
+        return self.h.contents
+
+    def close(self):
+        if self.h:
+            _check(self.L.directSolver_Finalize(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def direct_solve(rowptr, colind, aij, b):
+    """directSolver_Solve: factor + solve + release in one call."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    aij = np.ascontiguousarray(aij, np.float64)
+    n = len(rowptr) - 1
+    b2 = np.asfortranarray(np.asarray(b, np.float64).reshape(n, -1))
+    x = np.zeros_like(b2, order="F")
+    _check(load().directSolver_Solve(n, len(colind), b2.shape[1], _ptr(colind), _ptr(rowptr), _ptr(aij), _ptr(x),
+                                     _ptr(b2)))
+    return x if np.ndim(b) == 2 else x[:, 0]
 
 
 # ---------------------------------------------------------------- generator

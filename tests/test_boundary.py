@@ -22,7 +22,7 @@ from tests.conftest import ROOT, has_gpu
 
 def declared_symbols():
     names = set()
-    for h in ("spike_interfaces.h", "spike_gb300.h", "spike_datatypes.h"):
+    for h in ("spike_interfaces.h", "spike_gb300.h", "spike_datatypes.h", "spike_compat.h"):
         text = open(os.path.join(ROOT, "include", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         text = "\n".join(line for line in text.splitlines() if not line.lstrip().startswith("#"))
