@@ -14,6 +14,7 @@
 #include "spike_common.cuh"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace {
 
@@ -136,32 +137,35 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     const size_t tb = (size_t)blk_off[part] * TS;
     const long long rb = (long long)blk_off[part] * KB; // padded-row base
 
+    // 128-row tiles (66 KB each in FP32) leave room for two tile buffers, not four
+    constexpr int NB = KB >= 128 ? 1 : 2; // backward: buffers per tile kind
+    constexpr int RD = 2 * NB;            // forward: ring depth
     extern __shared__ char smraw[];
-    // double buffers, selected by block parity: M tiles (L or G) then E tiles
+    // backward buffers, selected by block parity when double: M tiles (G) then E tiles
     T *const sM0 = (T *)smem_align(smraw);
-    T *const sE0 = sM0 + 2 * KB * LDT;
-#define SMA(par) (sM0 + ((par) & 1) * KB * LDT)
-#define SEA(par) (sE0 + ((par) & 1) * KB * LDT)
-    T *sv = sE0 + 2 * KB * LDT; // [KB][RCS]
+    T *const sE0 = sM0 + NB * KB * LDT;
+#define SMA(par) (sM0 + ((par) % NB) * KB * LDT)
+#define SEA(par) (sE0 + ((par) % NB) * KB * LDT)
+    T *sv = sM0 + RD * KB * LDT; // [KB][RCS]
     T *sp = sv + KB * RCS;     // previous block's vector
     T *sw = sp + KB * RCS;     // work vector
 
     // the next block's right-hand-side rows ride in registers while the
     // current block computes; its tiles stream into the other buffer (cp.async)
     T nxt[VPT];
-    // forward: z_J = r_J - L_J z_{J-1}.  It reads only L, so all four tile
-    // buffers form a ring: L_{J+1..J+3} stream in while block J computes.
-#define RING(j) (sM0 + ((j) & 3) * KB * LDT)
-    for (int j = 1; j <= 3; j++) {
+    // forward: z_J = r_J - L_J z_{J-1}.  It reads only L, so all the tile
+    // buffers form a ring: L_{J+1..J+RD-1} stream in while block J computes.
+#define RING(j) (sM0 + ((j) % RD) * KB * LDT)
+    for (int j = 1; j < RD; j++) {
         if (j < N) cp_async_tile<T, KB, NT>(RING(j), gL + tb + (size_t)j * TS);
         cp_async_commit();
     }
     fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, 0);
     put_v<T, KB, VPT>(nxt, sv, nr);
-    cp_async_wait_n<2>(); // L_1
+    cp_async_wait_n<RD - 2>(); // L_1
     __syncthreads();
     for (int J = 0; J < N; J++) {
-        if (J + 3 < N) cp_async_tile<T, KB, NT>(RING(J + 3), gL + tb + (size_t)(J + 3) * TS);
+        if (J + RD - 1 < N) cp_async_tile<T, KB, NT>(RING(J + RD - 1), gL + tb + (size_t)(J + RD - 1) * TS);
         cp_async_commit();
         if (J + 1 < N) fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, J + 1);
         if (J > 0)
@@ -176,7 +180,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
             gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
         }
         if (J + 1 < N) put_v<T, KB, VPT>(nxt, sv, nr);
-        cp_async_wait_n<2>(); // L_{J+1}
+        cp_async_wait_n<RD - 2>(); // L_{J+1}
         __syncthreads();
     }
 #undef RING
@@ -189,10 +193,21 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     cp_async_wait_all();
     __syncthreads();
     for (int J = N - 1; J >= 0; J--) {
+        if constexpr (NB == 1) { // single buffers: block J's tiles arrive now
+            if (J < N - 1) {
+                cp_async_tile<T, KB, NT>(SMA(J), gG + tb + J * TS);
+                cp_async_tile<T, KB, NT>(SEA(J), gE + tb + J * TS);
+                cp_async_commit();
+                cp_async_wait_all();
+                __syncthreads();
+            }
+        }
         if (J > 0) {
-            cp_async_tile<T, KB, NT>(SMA(J - 1), gG + tb + (J - 1) * TS);
-            cp_async_tile<T, KB, NT>(SEA(J - 1), gE + tb + (J - 1) * TS);
-            cp_async_commit();
+            if constexpr (NB == 2) {
+                cp_async_tile<T, KB, NT>(SMA(J - 1), gG + tb + (J - 1) * TS);
+                cp_async_tile<T, KB, NT>(SEA(J - 1), gE + tb + (J - 1) * TS);
+                cp_async_commit();
+            }
             fetch_z<T, KB, VPT>(nxt, gz, NP, rb, h0, nr, J - 1);
         }
         if (J < N - 1) {
@@ -460,7 +475,7 @@ __global__ void __launch_bounds__(256)
 template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
     constexpr int NT = NTOf<KB>::value;
-    const size_t smem = 16 + sizeof(T) * (4 * KB * TileLD<T, KB>::value + 3 * KB * RCS);
+    const size_t smem = 16 + sizeof(T) * ((KB >= 128 ? 2 : 4) * KB * TileLD<T, KB>::value + 3 * KB * RCS);
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_apply<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
@@ -539,6 +554,9 @@ template <class T, int KB> int run_retrieve(spk_plan *P, void *x, int nrhs, int 
     case 32: return FN<T, 32>(__VA_ARGS__);                                                                     \
     case 64:                                                                                                    \
         if constexpr (sizeof(T) <= 8) return FN<T, 64>(__VA_ARGS__);                                            \
+        else return SPK_EBAND;                                                                                  \
+    case 128:                                                                                                   \
+        if constexpr (std::is_same<T, float>::value) return FN<T, 128>(__VA_ARGS__);                            \
         else return SPK_EBAND;                                                                                  \
     default: return SPK_EBAND;                                                                                  \
     }

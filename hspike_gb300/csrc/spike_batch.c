@@ -452,7 +452,7 @@ Error_t spike_dbatch_create(spike_context_t ctx, integer_t count, const spike_ds
         if (!KB || spk_factor_smem(KB, 0, ctx->mode) == 0) {
             free(key);
             batch_free(B);
-            return spk_fail(SPIKE_ERR_BANDWIDTH, "%s: system %d: bandwidth %d above the largest tile", W, i, k);
+            return spk_fail(SPIKE_ERR_BANDWIDTH, "%s: system %d: bandwidth %d above the largest tile of this precision", W, i, k);
         }
         key[4 * i] = KB;
         key[4 * i + 1] = B->sys[i].nrhs;

@@ -123,7 +123,7 @@ template <> struct HighOf<cdouble> { using type = cdouble; };
 
 // threads per CTA for a tile size
 template <int KB> struct NTOf {
-    static constexpr int value = KB >= 64 ? 256 : KB == 32 ? 128 : KB == 16 ? 64 : 32;
+    static constexpr int value = KB >= 128 ? 1024 : KB >= 64 ? 256 : KB == 32 ? 128 : KB == 16 ? 64 : 32;
 };
 
 // ------------------------------------------------------------ vector access
@@ -192,7 +192,8 @@ template <class T, int KB> struct TileLD {
 // gives TC contiguous elements per k, a left operand stored transposed
 // (column-major, "At") gives TR contiguous elements per k.
 template <class T, int KB, int NT> struct Tile {
-    static constexpr int TX = KB < 16 ? KB : 16;
+    // 128-row tiles: a 32 x 32 thread grid keeps every sub-tile 4 x 4
+    static constexpr int TX = KB < 16 ? KB : KB >= 128 ? 32 : 16;
     static constexpr int TY0 = NT / TX;
     static constexpr int TY = TY0 < KB ? TY0 : KB;
     static constexpr int TC = KB / TX;
@@ -260,6 +261,16 @@ template <class T, int KB, int NT> struct Tile {
             for (int i = 0; i < TR; i++) c[i] = a[i][j];
             vst<T, TR>(s + col(j) * LD + row(0), c);
         }
+    }
+    // register tile <- dense global tile (row-major, ld KB)
+    __device__ __forceinline__ void gload(Reg &a, const T *g) const
+    {
+        if (!act) {
+            rzero(a);
+            return;
+        }
+#pragma unroll
+        for (int i = 0; i < TR; i++) vld<T, TC>(a[i], g + row(i) * KB + col(0));
     }
     // dense global tile (row-major, ld KB) <- register tile
     __device__ __forceinline__ void gstore(T *g, const Reg &a) const

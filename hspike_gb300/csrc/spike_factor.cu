@@ -26,14 +26,19 @@
 // non-finite pivot sets SPK_DEV_ERR_PIVOT and the host returns SPIKE_ERROR.
 #include "spike_common.cuh"
 
+#include <type_traits>
+
 namespace {
 
 template <class T, int KB> struct FactorSmem {
     using TL = Tile<T, KB, NTOf<KB>::value>;
+    // 128-row tiles (FP32 only): three resident tiles per CTA, see k_factor_fwd_big
+    static constexpr bool BIG = KB >= 128;
     static constexpr size_t tile = sizeof(T) * TL::ELEMS;
-    static constexpr size_t fwd = 6 * tile + sizeof(T) * TL::INV_BUF + 64;
+    static constexpr size_t fwd = (BIG ? 3 : 6) * tile + sizeof(T) * TL::INV_BUF + 64;
     static constexpr size_t band = 3 * sizeof(T) * KB * (KB + 1) + sizeof(int) * (KB + 1) + 64;
-    static constexpr size_t bwd = 6 * tile + 64;
+    static constexpr size_t bwd = (BIG ? 3 : 6) * tile + 64;
+    static constexpr size_t wsweep = 3 * tile + 64;
 };
 
 // Scatter the CSR rows of block J of partition [s, e) into the shared tiles.
@@ -375,6 +380,199 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     }
 }
 
+// ------------------------------------------------------------ 128-row tiles
+// A 128 x 128 FP32 tile takes 66 KB of shared memory, so a CTA (1024 threads,
+// a 4 x 4 sub-tile each) keeps three of them resident instead of six: D_J
+// goes from global memory straight into registers (its loads are issued
+// before the L product and land during it), the W forward sweep runs as its
+// own chain (k_wsweep_big) once the L tiles exist, and the backward sweep
+// gives V and W a CTA each.  Same recurrences and global layouts as
+// k_factor_fwd / k_factor_bwd.
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_factor_fwd_big(const T *__restrict__ gT, const int *__restrict__ blk_off, T *gL, T *gG, unsigned *err)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int part = blockIdx.x;
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * 3 * TS; // per block: D, F^T, E (row-major)
+
+    extern __shared__ char smraw[];
+    T *sG = (T *)smem_align(smraw), *sE = sG + TL::ELEMS, *sF = sE + TL::ELEMS;
+    T *buf = sF + TL::ELEMS;
+
+    TL t(threadIdx.x);
+    typename TL::Reg acc, dreg;
+    bool ok = true;
+
+    cp_async_tile<T, KB, NT>(sE, gTp + 2 * TS); // E_0
+    if (N > 1) cp_async_tile<T, KB, NT>(sF, gTp + 3 * TS + TS);
+    cp_async_commit();
+    t.gload(acc, gTp); // S_0 = D_0
+    for (int J = 0; J < N; J++) {
+        if (J > 0) {
+            t.gload(dreg, gTp + (size_t)J * 3 * TS); // D_J
+            // L_J = F_{J-1} G_{J-1}
+            t.rzero(acc);
+            t.mma_tu(acc, sF, sG); // A(J, J-1) is upper triangular (KB >= kl)
+            __syncthreads();
+            t.rstore_t(sF, acc); // sF now holds L_J, transposed
+            t.gstore_t(gL + tb + J * TS, acc);
+            __syncthreads();
+            // S_J = D_J - L_J E_{J-1}
+#pragma unroll
+            for (int i = 0; i < TL::TR; i++)
+#pragma unroll
+                for (int j = 0; j < TL::TC; j++) acc[i][j] = dreg[i][j];
+            t.mms_t(acc, sF, sE);
+            __syncthreads(); // sF, sE and sG are free from here on
+            cp_async_tile<T, KB, NT>(sE, gTp + (size_t)J * 3 * TS + 2 * TS); // E_J
+            if (J + 1 < N) cp_async_tile<T, KB, NT>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);
+            cp_async_commit();
+        }
+        // G_J = S_J^{-1}
+        ok = t.inverse(acc, buf) && ok;
+        cp_async_wait_all();
+        t.rstore(sG, acc);
+        t.gstore_t(gG + tb + J * TS, acc); // column-major for the backward sweep
+        __syncthreads();
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+
+// W forward sweep z_J = -L_J z_{J-1} (z_0 = C^, written by k_band_tiles) of
+// partition blockIdx.x + 1 (partition 0 has no W spike); the next L tile
+// streams into the second buffer while the current one is applied.
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_wsweep_big(const int *__restrict__ blk_off, const T *__restrict__ gL, T *gZ)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int part = blockIdx.x + 1;
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+
+    extern __shared__ char smraw[];
+    T *sZ = (T *)smem_align(smraw), *sL0 = sZ + TL::ELEMS, *sL1 = sL0 + TL::ELEMS;
+    TL t(threadIdx.x);
+    typename TL::Reg acc;
+
+    cp_async_tile<T, KB, NT>(sZ, gZ + tb);
+    if (N > 1) cp_async_tile<T, KB, NT>(sL1, gL + tb + TS);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    for (int J = 1; J < N; J++) {
+        T *cur = (J & 1) ? sL1 : sL0, *nxt = (J & 1) ? sL0 : sL1;
+        if (J + 1 < N) cp_async_tile<T, KB, NT>(nxt, gL + tb + (size_t)(J + 1) * TS);
+        cp_async_commit();
+        t.rzero(acc);
+        t.mms_t(acc, cur, sZ); // cur holds L_J transposed
+        __syncthreads();
+        t.rstore(sZ, acc);
+        t.gstore(gZ + tb + J * TS, acc);
+        cp_async_wait_all();
+        __syncthreads();
+    }
+}
+
+// Backward sweep X_J = G_J (Z_J - E_J X_{J+1}); blockIdx.y = 0: V of
+// partition blockIdx.x, 1: its W.  Z_J comes from global memory into
+// registers; G_{J-1} and E_{J-1} stream in as soon as G_J / E_J are used.
+// gZ and gW are the same buffer (Z_J is read before X_J overwrites it).
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_factor_bwd_big(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                     const T *__restrict__ gL, const T *__restrict__ gG, const T *__restrict__ gE, const T *gZ,
+                     const T *__restrict__ gBhat, T *gV, T *gW)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    constexpr int LD = TileLD<T, KB>::value;
+    const bool isV = blockIdx.y == 0;
+    const int part = blockIdx.x;
+    if (isV ? part >= p - 1 : part == 0) return; // the whole CTA: no spike to compute
+    const int s = part_start[part], e = part_start[part + 1], m = e - s;
+    const int N = blk_off[part + 1] - blk_off[part];
+    const size_t tb = (size_t)blk_off[part] * TS;
+
+    extern __shared__ char smraw[];
+    T *sG = (T *)smem_align(smraw), *sE = sG + TL::ELEMS, *sX = sE + TL::ELEMS;
+    TL t(threadIdx.x);
+    typename TL::Reg acc;
+
+    // V's right-hand side [0; B^] is nonzero only in the last KB real rows:
+    // blocks J0 and J0+1 (when m is not a multiple of KB).  Their forward-swept
+    // values go to gV tiles J0 / J0+1 (row-major scratch, read back below).
+    const int J0 = (m - KB) / KB, o = (m - KB) - J0 * KB;
+    if (isV) {
+        for (int q = threadIdx.x; q < KB * KB; q += NT) {
+            const int r = q / KB, c = q - r * KB;
+            // (o < 0: a partition shorter than a tile takes B^'s last m rows)
+            sX[r * LD + c] = (r >= o && r - o < KB) ? gBhat[(size_t)part * TS + (r - o) * KB + c] : sc_zero<T>();
+        }
+        if (o > 0) {
+            cp_async_tile<T, KB, NT>(sG, gL + tb + (J0 + 1) * TS); // L_{J0+1}, transposed
+            cp_async_commit();
+            for (int q = threadIdx.x; q < KB * KB; q += NT) {
+                const int r = q / KB, c = q - r * KB;
+                sE[r * LD + c] = r < o ? gBhat[(size_t)part * TS + (KB - o + r) * KB + c] : sc_zero<T>();
+            }
+            cp_async_wait_all();
+        }
+        __syncthreads();
+        store_tile<T, KB>(gV + tb + J0 * TS, sX);
+        if (o > 0) {
+            // z_{J0+1} = [B^ rows KB-o..KB-1 ; 0] - L_{J0+1} z_{J0}
+            t.rload(acc, sE);
+            t.mms_t(acc, sG, sX);
+            t.gstore(gV + tb + (J0 + 1) * TS, acc);
+        }
+        __syncthreads();
+    }
+
+    T *gX = isV ? gV : gW;
+    cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)(N - 1) * TS);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
+    for (int J = N - 1; J >= 0; J--) {
+        // T = Z_J - E_J X_{J+1}
+        if (!isV)
+            t.gload(acc, gZ + tb + J * TS);
+        else if (J == J0 || (o > 0 && J == J0 + 1))
+            t.gload(acc, gV + tb + J * TS);
+        else
+            t.rzero(acc);
+        if (J < N - 1) t.mms_tl(acc, sE, sX); // A(J, J+1) is lower triangular (KB >= ku)
+        __syncthreads();
+        if (J > 0) {
+            cp_async_tile<T, KB, NT>(sE, gE + tb + (size_t)(J - 1) * TS);
+            cp_async_commit();
+        }
+        t.rstore(sX, acc);
+        __syncthreads();
+        // X_J = G_J T
+        t.rzero(acc);
+        t.mma_t(acc, sG, sX);
+        __syncthreads();
+        if (J > 0) {
+            cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)(J - 1) * TS);
+            cp_async_commit();
+        }
+        t.rstore(sX, acc);
+        t.gstore_t(gX + tb + J * TS, acc); // column-major, for the tips and the retrieval
+        cp_async_wait_all();
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------ small bands
 // KB <= 4: a CTA per partition would leave most threads idle and pay a barrier
 // per tile step.  KB lanes run one partition chain instead: lane r owns row r
@@ -601,6 +799,17 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     using S = FactorSmem<T, KB>;
     static bool attr = false;
     if (!attr) {
+        if constexpr (S::BIG) {
+            if (cudaFuncSetAttribute(k_factor_fwd_big<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)S::fwd) != cudaSuccess ||
+                cudaFuncSetAttribute(k_wsweep_big<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)S::wsweep) != cudaSuccess ||
+                cudaFuncSetAttribute(k_factor_bwd_big<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)S::bwd) != cudaSuccess ||
+                cudaFuncSetAttribute(k_band_tiles<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)S::band) != cudaSuccess)
+                return SPK_ECUDA;
+        } else {
         if constexpr (KB <= 4) {
             if (cudaFuncSetAttribute(k_quad_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)QuadFwd<T, KB>::SMEM) != cudaSuccess ||
@@ -615,6 +824,7 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
             cudaFuncSetAttribute(k_factor_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bwd) !=
                 cudaSuccess)
             return SPK_ECUDA;
+        }
         attr = true;
     }
     const size_t TS = (size_t)KB * KB;
@@ -627,7 +837,15 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
     spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
-    if constexpr (KB <= 4) {
+    if constexpr (S::BIG) {
+        k_factor_fwd_big<T, KB><<<P->p, NT, S::fwd, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+                                                          (T *)P->d_G, P->d_err);
+        if (P->p > 1) {
+            SPK_CHECK_LAUNCH();
+            k_wsweep_big<T, KB><<<P->p - 1, NT, S::wsweep, st>>>(P->d_blk_off, (const T *)P->d_L, (T *)P->d_W);
+            P->launches++;
+        }
+    } else if constexpr (KB <= 4) {
         using CF = QuadFwd<T, KB>;
         const int cpc = chains_per_cta(P->p, CF::CPC);
         k_quad_fwd<T, KB><<<(P->p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * CF::SLOT, st>>>(
@@ -641,7 +859,11 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     P->launches += 2;
     if (P->p > 1) {
         spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
-        if constexpr (KB <= 4) {
+        if constexpr (S::BIG) {
+            k_factor_bwd_big<T, KB><<<dim3(P->p, 2), NT, S::bwd, st>>>(
+                P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_G, (const T *)P->d_E,
+                (const T *)P->d_W, (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W);
+        } else if constexpr (KB <= 4) {
             using CB = QuadBwd<T, KB>;
             const int cpc = chains_per_cta(2LL * P->p, CB::CPC);
             k_quad_bwd<T, KB><<<(2 * P->p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * CB::SLOT, st>>>(
@@ -674,6 +896,9 @@ template <class T> int dispatch_factor(spk_plan *P, const int *rp, const int *ci
     case 64:
         if constexpr (sizeof(T) <= 8) return run_factor<T, 64>(P, rp, ci, a, st);
         else return SPK_EBAND;
+    case 128:
+        if constexpr (std::is_same<T, float>::value) return run_factor<T, 128>(P, rp, ci, a, st);
+        else return SPK_EBAND;
     default: return SPK_EBAND;
     }
 }
@@ -688,6 +913,9 @@ template <class T> size_t smem_for(int KB)
     case 32: return FactorSmem<T, 32>::fwd;
     case 64:
         if constexpr (sizeof(T) <= 8) return FactorSmem<T, 64>::fwd;
+        else return 0;
+    case 128: // real mixed precision only (a 128-row FP64 or complex tile does not fit three times)
+        if constexpr (std::is_same<T, float>::value) return FactorSmem<T, 128>::fwd;
         else return 0;
     default: return 0;
     }

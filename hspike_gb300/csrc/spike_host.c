@@ -261,8 +261,8 @@ Error_t spike_get_phase_times(spike_context_t c, int nphases, double *ms, long l
 /* ------------------------------------------------------------------ */
 int spk_choose_block(int k)
 {
-    const int sizes[] = {2, 4, 8, 16, 32, 64};
-    for (int i = 0; i < 6; i++)
+    const int sizes[] = {2, 4, 8, 16, 32, 64, 128};
+    for (int i = 0; i < 7; i++)
         if (k <= sizes[i]) return sizes[i];
     return 0;
 }
@@ -280,7 +280,7 @@ static int choose_partitions(int n, int KB, int requested)
     if (p <= 0) {
         int sms = spk_sm_count();
         if (sms <= 0) sms = 152;
-        const int per_sm = KB >= 32 ? 2 : KB == 16 ? 8 : 16;
+        const int per_sm = KB >= 128 ? 1 : KB >= 32 ? 2 : KB == 16 ? 8 : 16;
         p = (long long)sms * per_sm;
     }
     if (p > pmax) p = pmax;

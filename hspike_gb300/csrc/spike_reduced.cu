@@ -20,11 +20,14 @@
 // is FP64-accurate in both modes.
 #include "spike_common.cuh"
 
+#include <type_traits>
+
 namespace {
 
 template <class T, int KB> struct RedSmem {
     using TL = Tile<T, KB, NTOf<KB>::value>;
-    static constexpr size_t bytes = 5 * sizeof(T) * TL::ELEMS + sizeof(T) * TL::INV_BUF + 64;
+    static constexpr size_t bytes = 3 * sizeof(T) * TL::ELEMS + sizeof(T) * TL::INV_BUF + 64;
+    static constexpr size_t solve = sizeof(T) * KB * TileLD<T, KB>::value + 64; // one tile (k_cr_fwd / k_cr_bwd)
 };
 
 template <class T, int KB> __device__ void ld(T *s, const T *g)
@@ -49,6 +52,7 @@ __global__ void k_red_cvt(const typename HighOf<T>::type *__restrict__ src, T *d
 
 // Odd blocks j of a level (or the single top block): M = D_j^{-1} by quadrants
 //   S = I - Q P, M11 = S^{-1}, M10 = -M11 Q, M01 = -P M11, M00 = I - P M10.
+// Three shared tiles: P, Q (overwritten by M10 once M10 exists) and M11.
 template <class T, int KB>
 __global__ void __launch_bounds__(NTOf<KB>::value)
     k_cr_odd(const T *__restrict__ Pl, const T *__restrict__ Ql, int first, int stride, T *M, unsigned *err)
@@ -59,8 +63,8 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     const int j = first + blockIdx.x * stride;
     T *Mj = M + (size_t)blockIdx.x * 4 * TS;
     extern __shared__ char smraw[];
-    T *sP = (T *)smem_align(smraw), *sQ = sP + TL::ELEMS, *sH = sQ + TL::ELEMS, *sT = sH + TL::ELEMS;
-    T *buf = sT + 2 * TL::ELEMS;
+    T *sP = (T *)smem_align(smraw), *sQ = sP + TL::ELEMS, *sH = sQ + TL::ELEMS;
+    T *buf = sH + TL::ELEMS;
     TL t(threadIdx.x);
     typename TL::Reg a;
     ld<T, KB>(sP, Pl + (size_t)j * TS);
@@ -75,14 +79,15 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     __syncthreads();
     t.rzero(a);
     t.mms(a, sH, sQ); // M10
-    t.rstore(sT, a);
     t.gstore(Mj + 2 * TS, a);
+    __syncthreads(); // every read of Q is done
+    t.rstore(sQ, a);
     t.rzero(a);
     t.mms(a, sP, sH); // M01
     t.gstore(Mj + 1 * TS, a);
     __syncthreads();
     set_identity<T, KB>(t, a);
-    t.mms(a, sP, sT); // M00 = I - P M10
+    t.mms(a, sP, sQ); // M00 = I - P M10
     t.gstore(Mj, a);
 }
 
@@ -177,7 +182,8 @@ __global__ void __launch_bounds__(128)
     constexpr size_t TS = (size_t)KB * KB;
     const int i = 2 * blockIdx.x;
     const int h0 = blockIdx.y * RRC, nr = min(RRC, nrhs - h0);
-    __shared__ __align__(16) T sM[KB * TileLD<T, KB>::value];
+    extern __shared__ char smraw[];
+    T *sM = (T *)smem_align(smraw); // one tile (dynamic: a 128-row tile exceeds the static limit)
     __shared__ T sx[2 * KB * RRC], sw[KB * RRC];
     const bool left = i - 1 >= 0, right = i + 1 < cnt;
     T *gi = g + (off_l + i) * 2 * KB, *gn = g + (off_n + blockIdx.x) * 2 * KB;
@@ -232,7 +238,8 @@ __global__ void __launch_bounds__(128)
 {
     constexpr size_t TS = (size_t)KB * KB;
     const int h0 = blockIdx.y * RRC, nr = min(RRC, nrhs - h0);
-    __shared__ __align__(16) T sM[KB * TileLD<T, KB>::value];
+    extern __shared__ char smraw[];
+    T *sM = (T *)smem_align(smraw); // one tile
     __shared__ T sx[2 * KB * RRC], sw[2 * KB * RRC];
     if (!top && (blockIdx.x & 1) == 0) {
         // even block: copy from level l+1
@@ -401,23 +408,31 @@ template <class T, int KB> int run_red_solve(spk_plan *P, int nrhs, int iters, c
     const int L = P->cr_levels;
     const dim3 blk(128);
     const int hy = (nrhs + RRC - 1) / RRC;
+    constexpr size_t sm = RedSmem<T, KB>::solve;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_cr_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess ||
+            cudaFuncSetAttribute(k_cr_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
     for (int it = 0; it < iters; it++) {
         const H *res = it == 0 ? (const H *)P->d_g : (const H *)P->d_rr;
         k_red_load<T><<<256, 256, 0, st>>>(res, cg, NR, stride, nrhs);
         P->launches++;
         for (int l = 0; l < L; l++) {
             const int cnt = P->cr_count[l];
-            k_cr_fwd<T, KB><<<dim3((cnt + 1) / 2, hy), blk, 0, st>>>(
+            k_cr_fwd<T, KB><<<dim3((cnt + 1) / 2, hy), blk, sm, st>>>(
                 cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS, cM + (size_t)P->cr_moff[l] * 4 * TS, cnt, cg,
                 stride, P->cr_off[l], P->cr_off[l + 1], nrhs);
             P->launches++;
         }
-        k_cr_bwd<T, KB><<<dim3(1, hy), blk, 0, st>>>(nullptr, nullptr, cM + (size_t)P->cr_moff[L] * 4 * TS, 1, cg, cu, stride,
+        k_cr_bwd<T, KB><<<dim3(1, hy), blk, sm, st>>>(nullptr, nullptr, cM + (size_t)P->cr_moff[L] * 4 * TS, 1, cg, cu, stride,
                                                      P->cr_off[L], 0, nrhs, 1);
         P->launches++;
         for (int l = L - 1; l >= 0; l--) {
             const int cnt = P->cr_count[l];
-            k_cr_bwd<T, KB><<<dim3(cnt, hy), blk, 0, st>>>(cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS,
+            k_cr_bwd<T, KB><<<dim3(cnt, hy), blk, sm, st>>>(cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS,
                                                            cM + (size_t)P->cr_moff[l] * 4 * TS, cnt, cg, cu, stride,
                                                            P->cr_off[l], P->cr_off[l + 1], nrhs, 0);
             P->launches++;
@@ -444,6 +459,9 @@ template <class T, int KB> int run_red_solve(spk_plan *P, int nrhs, int iters, c
     case 32: return FN<T, 32>(__VA_ARGS__);                                                                     \
     case 64:                                                                                                    \
         if constexpr (sizeof(T) <= 8) return FN<T, 64>(__VA_ARGS__);                                            \
+        else return SPK_EBAND;                                                                                  \
+    case 128:                                                                                                   \
+        if constexpr (std::is_same<T, float>::value) return FN<T, 128>(__VA_ARGS__);                            \
         else return SPK_EBAND;                                                                                  \
     default: return SPK_EBAND;                                                                                  \
     }

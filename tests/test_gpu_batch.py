@@ -71,6 +71,8 @@ def test_batch_matches_single_solves(precision):
     draws.append((70, 8, 1, 1.3))
     draws.append((20, 32, 1, 1.5))   # shorter than one tile (band clipped to n - 1 = 19)
     draws.append((5000, 0, 2, 1.5))  # diagonal
+    if precision == hs.SPIKE_PRECISION_MIXED:  # 128-row tiles (real mixed precision only)
+        draws += [(3000, 100, 2, 1.5), (9000, 128, 1, 1.3), (200, 90, 1, 1.5)]
     hb = W.gen_batch(draws, seed=11)
     t, systems = _device_batch(hb, torch, dev)
     ctx = hs.Context()
@@ -137,6 +139,19 @@ def test_batch_eager_and_autotuned_agree():
     assert (tuned.relres() <= RES_TOL).all()
     eager.destroy()
     tuned.destroy()
+
+
+def test_batch_band_above_fp64_tiles_is_rejected():
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    hb = W.gen_batch([(1000, 2, 1, 1.5), (2000, 100, 1, 1.5)], seed=15)
+    t, systems = _device_batch(hb, torch, dev)
+    ctx = hs.Context()
+    ctx.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_FP64)
+    with pytest.raises(hs.SpikeError) as e:
+        hs.Batch(systems, ctx, autotune=False)
+    assert e.value.name == "bandwidth" and "system 1" in str(e.value)
+    ctx.close()
 
 
 def test_batch_rejects_invalid_system():

@@ -99,6 +99,39 @@ def test_generated_real(case, mode):
     check(rp, ci, a, b, p, mode, x_true=xt)
 
 
+# bands above 64 use 128-row tiles: real data, mixed precision only
+CASES_128 = [
+    (40000, 100, 100, 1.5, 12, 1),
+    (30011, 128, 128, 1.5, 8, 2),
+    (25000, 65, 90, 1.5, 9, 1),    # ku != kl
+    (20000, 128, 128, 1.5, 6, 33),  # two right-hand-side chunks of 32
+    (9000, 72, 72, 1.5, 1, 1),      # one partition
+]
+
+
+@pytest.mark.parametrize("case", CASES_128, ids=lambda c: f"n{c[0]}_k{c[1]}_{c[2]}_p{c[4]}_r{c[5]}")
+def test_generated_real_128_row_tiles(case):
+    n, ku, kl, dom, p, nrhs = case
+    rp, ci, a, xt, b = hs.gen_banded(n, ku, kl, dom, seed=300 + n, nrhs=nrhs)
+    x, info = check(rp, ci, a, b, p, "mixed", x_true=xt)
+    assert info.block == 128
+
+
+def test_128_row_tiles_auto_partitions_and_factor_reuse():
+    rp, ci, a, xt, b = hs.gen_banded(200_000, 96, 96, 1.5, seed=41, nrhs=2)
+    x = hs.solve(rp, ci, a, b)
+    assert hs.get_info().block == 128 and hs.get_info().partitions > 1
+    assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
+    assert relerr(x, xt) <= 1e-10
+    f = hs.Factor(rp, ci, a)
+    try:
+        for _ in range(2):
+            x2 = f.solve(b)
+            assert oracle.residual(rp, ci, a, x2, b).max() <= RES_TOL
+    finally:
+        f.release()
+
+
 @pytest.mark.parametrize("case", [(5000, 3, 3, 1.2, 8, 4), (8191, 1, 1, 2.0, 5, 1), (12000, 8, 8, 1.5, 6, 2),
                                   (20000, 32, 32, 1.5, 8, 1)],
                          ids=lambda c: f"n{c[0]}_k{c[1]}_p{c[4]}_r{c[5]}")
@@ -232,7 +265,19 @@ def test_invalid_csr_is_rejected():
 
 
 def test_bandwidth_above_tile_is_rejected():
-    rp, ci, a, xt, b = hs.gen_banded(2000, 70, 70, 1.5, seed=18)
+    rp, ci, a, xt, b = hs.gen_banded(2000, 130, 130, 1.5, seed=18)
     x = np.zeros_like(b, order="F")
     assert hs.dspike_core_host(2000, len(ci), 1, ci, rp, a, x, b) == hs.SPIKE_ERROR
+    assert hs.ERR_NAMES[hs.last_error()[0]] == "bandwidth"
+    assert not x.any()
+
+
+def test_128_row_tiles_only_in_real_mixed_precision():
+    rp, ci, a, xt, b = hs.gen_banded(3000, 70, 70, 1.5, seed=19)
+    with pytest.raises(hs.SpikeError) as e:
+        hs.solve(rp, ci, a, b, precision=hs.SPIKE_PRECISION_FP64)
+    assert e.value.name == "bandwidth"
+    rp, ci, a, xt, b = hs.gen_banded(3000, 70, 70, 1.5, seed=19, complex_=True)
+    x = np.zeros_like(b, order="F")
+    assert hs.zspike_core_host(3000, len(ci), 1, ci, rp, a, x, b) == hs.SPIKE_ERROR
     assert hs.ERR_NAMES[hs.last_error()[0]] == "bandwidth"

@@ -32,7 +32,7 @@ def _requests(count=24, seed=31):
             reqs.append((rp, ci, a, b, key))
             continue
         n = int(rng.integers(2_000, 40_000))
-        k = int(rng.integers(1, 65))
+        k = int(rng.integers(1, 129))  # 128-row tiles above 64
         nrhs = int(rng.integers(1, 9))
         rp, ci, a, xt, b = hs.gen_banded(n, k, k, 1.5, seed=1000 + i, nrhs=nrhs)
         key = 1000 + i if rng.uniform() < 0.5 else -1
@@ -101,7 +101,7 @@ def test_admission_follows_the_device_budget():
 
 
 def test_band_above_the_largest_tile_is_rejected():
-    rp, ci, a, xt, b = hs.gen_banded(5000, 80, 80, 1.5, seed=3)
+    rp, ci, a, xt, b = hs.gen_banded(5000, 140, 140, 1.5, seed=3)
     srv = hs.Server(slots=2)
     t, _ = srv.submit(rp, ci, a, b)
     st = srv.wait(t, check=False)
