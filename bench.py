@@ -305,7 +305,7 @@ def complex_leg(torch, dev, hs, steps, warmup, n=4_000_000, k=3, nrhs=4, p=512, 
 
 
 # --------------------------------------------------------------------- serving leg
-def serving_leg(hs, count, rate=20_000.0, slots=8, k_max=64):
+def serving_leg(hs, count, rate=20_000.0, slots=8, k_max=128):
     """The serving stream: Poisson arrivals at `rate`/s, per request n
     log-normal (median 20,000, sigma 1, clipped to [500, 2,000,000]), k uniform
     in {1..k_max}, nrhs uniform in {1..32}, dominance 1.05, 30 % reusing an
@@ -367,8 +367,7 @@ def serving_leg(hs, count, rate=20_000.0, slots=8, k_max=64):
            "failed": st.failed + errs, "factor_hits": st.factor_hits, "factor_misses": st.factor_misses,
            "peak_running": st.peak_running, "relres_max": st.relres_max, "relres_oracle_sampled": worst,
            "offered_per_s": rate, "setup_s": gen_s,
-           "note": "offered load far exceeds one GPU: requests queue, latency is mostly queueing; k above 64 "
-                   "(the largest tile) is outside this leg"}
+           "note": "offered load far exceeds one GPU: requests queue, latency is mostly queueing"}
     srv.close()
     return out
 

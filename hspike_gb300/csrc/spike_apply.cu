@@ -24,7 +24,7 @@ constexpr int RCS = RC + 1; // row stride of the shared [KB][RC] vectors (odd: c
 // out[r][h] = sign * sum_k M[r][k] v[k][h] (+ base[r][h]), r < KB, h < nr.
 // Mt: shared tile holding M transposed (the factor tiles are column-major in
 // global memory); v, base, out: shared [KB][RC] vectors with row stride RCS.
-template <class T, int KB, bool HAS_BASE>
+template <class T, int KB, bool HAS_BASE, int S = RCS>
 __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, bool negate)
 {
     constexpr int NT = NTOf<KB>::value;
@@ -44,7 +44,7 @@ __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, 
         if (o < O) {
             r = o / nr;
             h = o - r * nr;
-            for (int k = part; k < KB; k += spl) acc = madd(acc, Mt[k * LD + r], v[k * RCS + h]);
+            for (int k = part; k < KB; k += spl) acc = madd(acc, Mt[k * LD + r], v[k * S + h]);
         }
         for (int off = spl >> 1; off > 0; off >>= 1) {
             if constexpr (sizeof(T) == 4) {
@@ -62,8 +62,8 @@ __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, 
         }
         if (o < O && part == 0) {
             T val = negate ? -acc : acc;
-            if (HAS_BASE) val = base[r * RCS + h] + val;
-            out[r * RCS + h] = val;
+            if (HAS_BASE) val = base[r * S + h] + val;
+            out[r * S + h] = val;
         }
     }
 }
@@ -105,7 +105,7 @@ __device__ __forceinline__ void fetch_z(T (&nxt)[VPT], const T *gz, long long NP
         }
     }
 }
-template <class T, int KB, int VPT> __device__ __forceinline__ void put_v(const T (&nxt)[VPT], T *sv, int nr)
+template <class T, int KB, int VPT, int S = RCS> __device__ __forceinline__ void put_v(const T (&nxt)[VPT], T *sv, int nr)
 {
     constexpr int NT = NTOf<KB>::value;
 #pragma unroll
@@ -113,7 +113,7 @@ template <class T, int KB, int VPT> __device__ __forceinline__ void put_v(const 
         const int q = threadIdx.x + v * NT;
         if (q < KB * nr) {
             const int h = q / KB, lr = q - h * KB;
-            sv[lr * RCS + h] = nxt[v];
+            sv[lr * S + h] = nxt[v];
         }
     }
 }
@@ -144,8 +144,8 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     // backward buffers, selected by block parity when double: M tiles (G) then E tiles
     T *const sM0 = (T *)smem_align(smraw);
     T *const sE0 = sM0 + NB * KB * LDT;
-#define SMA(par) (sM0 + ((par) % NB) * KB * LDT)
-#define SEA(par) (sE0 + ((par) % NB) * KB * LDT)
+#define SMA(par) (sM0 + ((par) & (NB - 1)) * KB * LDT)
+#define SEA(par) (sE0 + ((par) & (NB - 1)) * KB * LDT)
     T *sv = sM0 + RD * KB * LDT; // [KB][RCS]
     T *sp = sv + KB * RCS;     // previous block's vector
     T *sw = sp + KB * RCS;     // work vector
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     T nxt[VPT];
     // forward: z_J = r_J - L_J z_{J-1}.  It reads only L, so all the tile
     // buffers form a ring: L_{J+1..J+RD-1} stream in while block J computes.
-#define RING(j) (sM0 + ((j) % RD) * KB * LDT)
+#define RING(j) (sM0 + ((j) & (RD - 1)) * KB * LDT)
     for (int j = 1; j < RD; j++) {
         if (j < N) cp_async_tile<T, KB, NT>(RING(j), gL + tb + (size_t)j * TS);
         cp_async_commit();
@@ -230,6 +230,211 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
 
 #undef SMA
 #undef SEA
+
+// ------------------------------------------------------------ two-sided partitions
+// y_i = A_i^{-1} r_i with the two-sided factors of spike_twist.cu (layout
+// there): both halves sweep towards the middle block M, M is solved, and both
+// halves sweep back out.  Sixteen right-hand-side columns per CTA keep two
+// tiles and three vectors within a quarter of the SM's shared memory.
+constexpr int RC2 = 16;
+constexpr int RCS2 = RC2 + 1;
+template <class T, int KB> constexpr size_t tw_apply_smem()
+{
+    return 16 + sizeof(T) * (2 * KB * TileLD<T, KB>::value + 3 * KB * RCS2);
+}
+
+//   top     z_J = r_J - L_J z_{J-1},  J = 0..M-1
+//   bottom  w_J = r_J - U_J w_{J+1},  J = N-1..M   (U_M in gE)
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+    k_tw_apply_fwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, const T *__restrict__ gL,
+                   const T *__restrict__ gE, const typename HighOf<T>::type *__restrict__ r, int n, int nrhs,
+                   long long NP, T *gz)
+{
+    using H = typename HighOf<T>::type;
+    constexpr int NT = NTOf<KB>::value;
+    constexpr size_t TS = (size_t)KB * KB;
+    constexpr int LDT = TileLD<T, KB>::value;
+    constexpr int VPT = (KB * RC2 + NT - 1) / NT;
+    const int part = blockIdx.x;
+    const bool top = blockIdx.y == 0;
+    const int h0 = blockIdx.z * RC2, nr = min(RC2, nrhs - h0);
+    const int s = part_start[part], m = part_start[part + 1] - s;
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const long long rb = (long long)blk_off[part] * KB;
+    const int cnt = top ? M : N - M;
+
+    extern __shared__ char smraw[];
+    T *const t0 = (T *)smem_align(smraw), *const t1 = t0 + KB * LDT;
+    T *sv = t1 + KB * LDT, *sp = sv + KB * RCS2, *sw = sp + KB * RCS2;
+    auto blk = [&](int i) { return top ? i : N - 1 - i; };
+    auto slot = [&](int i) { return (i & 1) ? t1 : t0; };
+    auto ctile = [&](int i) { // coupling tile of step i >= 1
+        const int J = blk(i);
+        return (!top && J == M ? gE : gL) + tb + (size_t)J * TS;
+    };
+
+    T nxt[VPT];
+    fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, blk(0));
+    put_v<T, KB, VPT, RCS2>(nxt, sv, nr);
+    __syncthreads();
+    for (int i = 0; i < cnt; i++) {
+        const int J = blk(i);
+        if (i + 1 < cnt) cp_async_tile<T, KB, NT>(slot(i + 1), ctile(i + 1));
+        cp_async_commit();
+        if (i + 1 < cnt) fetch_r<T, H, KB, VPT>(nxt, r, n, s, m, h0, nr, blk(i + 1));
+        if (i > 0)
+            tile_mv<T, KB, true, RCS2>(sw, slot(i), sp, sv, nr, true);
+        else
+            for (int q = threadIdx.x; q < KB * RCS2; q += NT) sw[q] = sv[q];
+        __syncthreads();
+        for (int q = threadIdx.x; q < KB * nr; q += NT) {
+            const int h = q / KB, lr = q - h * KB;
+            const T v = sw[lr * RCS2 + h];
+            sp[lr * RCS2 + h] = v;
+            gz[(size_t)(h0 + h) * NP + rb + J * KB + lr] = v;
+        }
+        if (i + 1 < cnt) put_v<T, KB, VPT, RCS2>(nxt, sv, nr);
+        cp_async_wait_all();
+        __syncthreads();
+    }
+}
+
+// block M: z_M = w_M - L_M z_{M-1},  y_M = G_M z_M
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_tw_apply_mid(const int *__restrict__ blk_off, const T *__restrict__ gL, const T *__restrict__ gG, int nrhs,
+                   long long NP, const T *__restrict__ gz, T *gy)
+{
+    constexpr int NT = NTOf<KB>::value;
+    constexpr size_t TS = (size_t)KB * KB;
+    constexpr int LDT = TileLD<T, KB>::value;
+    const int part = blockIdx.x;
+    const int h0 = blockIdx.y * RC2, nr = min(RC2, nrhs - h0);
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const long long rb = (long long)blk_off[part] * KB;
+
+    extern __shared__ char smraw[];
+    T *const sT = (T *)smem_align(smraw), *const sT2 = sT + KB * LDT;
+    T *sv = sT2 + KB * LDT, *sp = sv + KB * RCS2, *sw = sp + KB * RCS2;
+    cp_async_tile<T, KB, NT>(sT, gL + tb + (size_t)M * TS);
+    cp_async_tile<T, KB, NT>(sT2, gG + tb + (size_t)M * TS);
+    cp_async_commit();
+    for (int q = threadIdx.x; q < KB * nr; q += NT) {
+        const int h = q / KB, lr = q - h * KB;
+        sv[lr * RCS2 + h] = gz[(size_t)(h0 + h) * NP + rb + M * KB + lr];
+        sp[lr * RCS2 + h] = gz[(size_t)(h0 + h) * NP + rb + (M - 1) * KB + lr];
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    tile_mv<T, KB, true, RCS2>(sw, sT, sp, sv, nr, true);
+    __syncthreads();
+    tile_mv<T, KB, false, RCS2>(sp, sT2, sw, nullptr, nr, false);
+    __syncthreads();
+    for (int q = threadIdx.x; q < KB * nr; q += NT) {
+        const int h = q / KB, lr = q - h * KB;
+        gy[(size_t)(h0 + h) * NP + rb + M * KB + lr] = sp[lr * RCS2 + h];
+    }
+}
+
+//   top     y_J = G_J (z_J - A(J,J+1) y_{J+1}),  J = M-1..0
+//   bottom  y_J = H_J (w_J - A(J,J-1) y_{J-1}),  J = M+1..N-1
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+    k_tw_apply_bwd(const int *__restrict__ blk_off, const T *__restrict__ gG, const T *__restrict__ gE, int nrhs,
+                   long long NP, const T *__restrict__ gz, T *gy)
+{
+    constexpr int NT = NTOf<KB>::value;
+    constexpr size_t TS = (size_t)KB * KB;
+    constexpr int LDT = TileLD<T, KB>::value;
+    constexpr int VPT = (KB * RC2 + NT - 1) / NT;
+    const int part = blockIdx.x;
+    const bool top = blockIdx.y == 0;
+    const int h0 = blockIdx.z * RC2, nr = min(RC2, nrhs - h0);
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const long long rb = (long long)blk_off[part] * KB;
+    const int cnt = top ? M : N - 1 - M;
+
+    extern __shared__ char smraw[];
+    T *const sG = (T *)smem_align(smraw), *const sE = sG + KB * LDT;
+    T *sv = sE + KB * LDT, *sp = sv + KB * RCS2, *sw = sp + KB * RCS2;
+    auto blk = [&](int i) { return top ? M - 1 - i : M + 1 + i; };
+
+    T nxt[VPT];
+    cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)blk(0) * TS);
+    cp_async_tile<T, KB, NT>(sE, gE + tb + (size_t)blk(0) * TS);
+    cp_async_commit();
+    fetch_z<T, KB, VPT>(nxt, gz, NP, rb, h0, nr, blk(0));
+    put_v<T, KB, VPT, RCS2>(nxt, sv, nr);
+    for (int q = threadIdx.x; q < KB * nr; q += NT) {
+        const int h = q / KB, lr = q - h * KB;
+        sp[lr * RCS2 + h] = gy[(size_t)(h0 + h) * NP + rb + M * KB + lr]; // y_M
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    for (int i = 0; i < cnt; i++) {
+        const int J = blk(i);
+        const bool more = i + 1 < cnt;
+        if (more) fetch_z<T, KB, VPT>(nxt, gz, NP, rb, h0, nr, blk(i + 1));
+        tile_mv<T, KB, true, RCS2>(sw, sE, sp, sv, nr, true);
+        __syncthreads();
+        if (more) {
+            cp_async_tile<T, KB, NT>(sE, gE + tb + (size_t)blk(i + 1) * TS);
+            cp_async_commit();
+        }
+        tile_mv<T, KB, false, RCS2>(sp, sG, sw, nullptr, nr, false);
+        __syncthreads();
+        if (more) {
+            cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)blk(i + 1) * TS);
+            cp_async_commit();
+        }
+        for (int q = threadIdx.x; q < KB * nr; q += NT) {
+            const int h = q / KB, lr = q - h * KB;
+            gy[(size_t)(h0 + h) * NP + rb + J * KB + lr] = sp[lr * RCS2 + h];
+        }
+        if (more) put_v<T, KB, VPT, RCS2>(nxt, sv, nr);
+        cp_async_wait_all();
+        __syncthreads();
+    }
+}
+
+template <class T, int KB> int run_tw_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
+{
+    if constexpr (!TwistFits<T, KB>::ok) {
+        return SPK_EBAND;
+    } else {
+        constexpr int NT = NTOf<KB>::value;
+        constexpr size_t smem = tw_apply_smem<T, KB>();
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(k_tw_apply_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_tw_apply_mid<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_tw_apply_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                    cudaSuccess)
+                return SPK_ECUDA;
+            attr = true;
+        }
+        const int hy = (nrhs + RC2 - 1) / RC2;
+        k_tw_apply_fwd<T, KB><<<dim3(P->p, 2, hy), NT, smem, st>>>(
+            P->d_part_start, P->d_blk_off, (const T *)P->d_L, (const T *)P->d_E,
+            (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP, (T *)P->d_z);
+        SPK_CHECK_LAUNCH();
+        k_tw_apply_mid<T, KB><<<dim3(P->p, hy), NT, smem, st>>>(P->d_blk_off, (const T *)P->d_L, (const T *)P->d_G,
+                                                                nrhs, P->NP, (const T *)P->d_z, (T *)P->d_y);
+        SPK_CHECK_LAUNCH();
+        k_tw_apply_bwd<T, KB><<<dim3(P->p, 2, hy), NT, smem, st>>>(P->d_blk_off, (const T *)P->d_G,
+                                                                   (const T *)P->d_E, nrhs, P->NP,
+                                                                   (const T *)P->d_z, (T *)P->d_y);
+        SPK_CHECK_LAUNCH();
+        P->launches += 3;
+        return SPK_OK;
+    }
+}
 
 // g_i = (y_i bottom, y_{i+1} top), FP64 / complex128.
 template <class T, int KB>
@@ -472,7 +677,7 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
+template <class T, int KB> int run_apply_1(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
     constexpr int NT = NTOf<KB>::value;
     const size_t smem = 16 + sizeof(T) * ((KB >= 128 ? 2 : 4) * KB * TileLD<T, KB>::value + 3 * KB * RCS);
@@ -504,6 +709,13 @@ template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, c
     }
     SPK_CHECK_LAUNCH();
     P->launches++;
+    return SPK_OK;
+}
+
+template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
+{
+    const int rc = P->twist ? run_tw_apply<T, KB>(P, r, nrhs, st) : run_apply_1<T, KB>(P, r, nrhs, st);
+    if (rc != SPK_OK) return rc;
     if (P->n_iface > 0) {
         k_ytips<T, KB><<<P->n_iface, 128, 0, st>>>(P->d_part_start, P->d_blk_off, (const T *)P->d_y, P->NP, nrhs,
                                                    P->n_iface, (typename HighOf<T>::type *)P->d_g);

@@ -206,15 +206,37 @@ template <class T, int KB, int NT> struct Tile {
     static constexpr int INV_HALF = 12 * KB + 16;  // pivot columns + P^{-1} + V' + pivot rows
     static constexpr int INV_BUF = BLOCK4 ? 2 * INV_HALF + KB : 4 * KB; // shared scratch elements for inverse()
 
+    // Warp footprint: where the grid allows it, a warp's 32 lanes cover 8
+    // sub-tile columns x 4 sub-tile rows (32 x 16 elements with 4 x 4
+    // sub-tiles), so one k step of a product reads 64 B of the left operand
+    // and 128 B of the right one -- two shared-memory wavefronts per 16 FMAs
+    // per thread, where a 16 x 2 footprint needs three.
+    static constexpr bool SQ = NT % 32 == 0 && ACTIVE == NT && TX % 8 == 0 && TY % 4 == 0;
+    static constexpr int WX = SQ ? 8 : TX;  // sub-tile columns per warp
+    static constexpr int WY = SQ ? 4 : 32 / (TX < 32 ? TX : 32); // sub-tile rows per warp
+
     using Reg = T[TR][TC];
 
     int tx, ty;
+    int wr0, wr1; // rows [wr0, wr1) of the tile are owned by this thread's warp
     bool act;
     __device__ __forceinline__ Tile(int tid)
     {
         act = tid < ACTIVE;
-        tx = tid % TX;
-        ty = tid / TX;
+        if constexpr (SQ) {
+            const int warp = tid >> 5, lane = tid & 31;
+            constexpr int WPR = TX / WX; // warps per row of sub-tiles
+            tx = (warp % WPR) * WX + (lane % WX);
+            ty = (warp / WPR) * WY + (lane / WX);
+            wr0 = (warp / WPR) * WY * TR;
+            wr1 = wr0 + WY * TR;
+        } else {
+            tx = tid % TX;
+            ty = tid / TX;
+            wr0 = ((tid & ~31) / TX) * TR;          // first row of the warp
+            wr1 = ((tid | 31) / TX) * TR + TR;      // one past its last row
+        }
+        if (wr1 > KB) wr1 = KB;
     }
     __device__ __forceinline__ int row(int i) const { return ty * TR + i; }
     __device__ __forceinline__ int col(int j) const { return tx * TC + j; }
@@ -314,10 +336,8 @@ template <class T, int KB, int NT> struct Tile {
     template <bool SUB, int TRI = 0> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
     {
         if (!act) return;
-        const int wr0 = ((int)(threadIdx.x & ~31u) / TX) * TR;             // first row of the warp
-        const int wr1 = ((int)(threadIdx.x | 31u) / TX) * TR + TR;         // one past its last row
         const int k0 = TRI == 1 ? wr0 : 0;
-        const int k1 = TRI == 2 ? (wr1 < KB ? wr1 : KB) : KB;
+        const int k1 = TRI == 2 ? wr1 : KB;
 #pragma unroll 4
         for (int k = k0; k < k1; k++) {
             T a[TR], b[TC];
@@ -336,6 +356,9 @@ template <class T, int KB, int NT> struct Tile {
     // A upper triangular (acc += A B) / lower triangular (acc -= A B)
     __device__ __forceinline__ void mma_tu(Reg &acc, const T *At, const T *B) const { mm_tA<false, 1>(acc, At, B); }
     __device__ __forceinline__ void mms_tl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 2>(acc, At, B); }
+    // A lower triangular (acc += A B) / upper triangular (acc -= A B)
+    __device__ __forceinline__ void mma_tl(Reg &acc, const T *At, const T *B) const { mm_tA<false, 2>(acc, At, B); }
+    __device__ __forceinline__ void mms_tu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 1>(acc, At, B); }
 
     // In-place Gauss-Jordan inverse of the register tile, no pivoting (the
     // diagonal blocks of a diagonally dominant A stay diagonally dominant
@@ -546,6 +569,15 @@ template <class T, int KB, int NT> struct Tile {
         __syncthreads();
         return __syncthreads_and(ok ? 1 : 0) != 0;
     }
+};
+
+// Two-sided partition kernels (spike_twist.cu, and their right-hand-side
+// sweeps in spike_apply.cu): three shared tiles per CTA, the tile inverse's
+// scratch inside one of them, four CTAs per SM.
+template <class T, int KB> struct TwistFits {
+    using TL = Tile<T, KB, NTOf<KB>::value>;
+    static constexpr size_t smem = 3 * sizeof(T) * TL::ELEMS + 64;
+    static constexpr bool ok = KB >= 16 && KB <= 64 && TL::INV_BUF <= TL::ELEMS && 4 * (smem + 1024) <= 228 * 1024;
 };
 
 // Dense global tile (KB*KB elements, 16-byte aligned) -> shared tile with row

@@ -37,8 +37,7 @@ template <class T, int KB> struct FactorSmem {
     static constexpr size_t tile = sizeof(T) * TL::ELEMS;
     static constexpr size_t fwd = (BIG ? 3 : 6) * tile + sizeof(T) * TL::INV_BUF + 64;
     static constexpr size_t band = 3 * sizeof(T) * KB * (KB + 1) + sizeof(int) * (KB + 1) + 64;
-    static constexpr size_t bwd = (BIG ? 3 : 6) * tile + 64;
-    static constexpr size_t wsweep = 3 * tile + 64;
+    static constexpr size_t bwd = (BIG ? 3 : 6) * tile + 64; // (also k_wsweep_big: three tiles)
 };
 
 // Scatter the CSR rows of block J of partition [s, e) into the shared tiles.
@@ -149,19 +148,23 @@ __device__ __forceinline__ void store_tile_cm(T *g, const T *s)
 // the block's CSR rows once and writes, in factor precision, the tiles the
 // sequential chain consumes: D_J (row-major), F_{J-1}^T and E_J (row-major)
 // into gT, E_J column-major into gE for the backward sweep, C^ into the W
-// spike's first tile (J == 0) and B^ into gBhat (last rows).
+// spike's first tile (J == 0) and B^ into gBhat (last rows).  With twist set,
+// blocks past the partition's middle block M = N/2 are stored for the
+// bottom-up chain instead (spike_twist.cu): A(J,J-1) row-major in gT and
+// column-major in gE for J > M, A(J,J+1) column-major in gT for J >= M.
 template <class T, int KB>
 __global__ void __launch_bounds__(NTOf<KB>::value)
     k_band_tiles(const int *__restrict__ rowptr, const int *__restrict__ colind,
                  const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
                  const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
-                 unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys)
+                 unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys, int twist)
 {
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
     const int gb = blockIdx.x;
     const int part = blk_part[gb];
     const int J = gb - blk_off[part];
+    const int M = twist ? (blk_off[part + 1] - blk_off[part]) / 2 : 1 << 30; // middle block
     int s = part_start[part], e = part_start[part + 1];
     const bool zt = J == 0 && part > 0;
     if (sys) { // batch group: the partition's own system, in its local rows
@@ -190,9 +193,17 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     __syncthreads();
     T *g = gT + (size_t)gb * 3 * TS;
     store_tile<T, KB, LD1>(g, sD);
-    store_tile<T, KB, LD1>(g + TS, sF); // the shared image of F^T
-    store_tile<T, KB, LD1>(g + 2 * TS, sE);
-    store_tile_cm<T, KB, LD1>(gE + (size_t)gb * TS, sE);
+    if (J <= M)
+        store_tile<T, KB, LD1>(g + TS, sF); // the shared image of F^T: A(J,J-1) column-major
+    else
+        store_tile_cm<T, KB, LD1>(g + TS, sF); // A(J,J-1) row-major
+    if (J < M) {
+        store_tile<T, KB, LD1>(g + 2 * TS, sE);
+        store_tile_cm<T, KB, LD1>(gE + (size_t)gb * TS, sE);
+    } else {
+        store_tile_cm<T, KB, LD1>(g + 2 * TS, sE); // A(J,J+1) column-major
+        if (J > M) store_tile<T, KB, LD1>(gE + (size_t)gb * TS, sF); // A(J,J-1) column-major
+    }
 }
 
 // K2: the sequential block-LU chain of one partition per CTA.
@@ -803,7 +814,7 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
             if (cudaFuncSetAttribute(k_factor_fwd_big<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)S::fwd) != cudaSuccess ||
                 cudaFuncSetAttribute(k_wsweep_big<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)S::wsweep) != cudaSuccess ||
+                                     (int)S::bwd) != cudaSuccess ||
                 cudaFuncSetAttribute(k_factor_bwd_big<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)S::bwd) != cudaSuccess ||
                 cudaFuncSetAttribute(k_band_tiles<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -833,16 +844,33 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     k_band_tiles<T, KB><<<P->total_blocks, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start,
                                                               P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
                                                               (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys,
-                                                              P->d_part_sys);
+                                                              P->d_part_sys, P->twist);
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
+    if (P->twist) { // two-sided chains (spike_twist.cu)
+        P->launches++;  // k_band_tiles
+        spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
+        int rc = spk_twist_factor(P, 1, st);
+        spk_phase_end(P, st);
+        if (rc != SPK_OK || P->p < 2) return rc;
+        spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
+        rc = spk_twist_factor(P, 0, st);
+        if (rc != SPK_OK) return rc;
+        k_tips<T, KB><<<P->n_iface, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_V,
+                                                  (const T *)P->d_W, (H *)P->d_RP, (H *)P->d_RQ, (H *)P->d_RX,
+                                                  (H *)P->d_RY);
+        SPK_CHECK_LAUNCH();
+        spk_phase_end(P, st);
+        P->launches++;
+        return SPK_OK;
+    }
     spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
     if constexpr (S::BIG) {
         k_factor_fwd_big<T, KB><<<P->p, NT, S::fwd, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
                                                           (T *)P->d_G, P->d_err);
         if (P->p > 1) {
             SPK_CHECK_LAUNCH();
-            k_wsweep_big<T, KB><<<P->p - 1, NT, S::wsweep, st>>>(P->d_blk_off, (const T *)P->d_L, (T *)P->d_W);
+            k_wsweep_big<T, KB><<<P->p - 1, NT, S::bwd, st>>>(P->d_blk_off, (const T *)P->d_L, (T *)P->d_W);
             P->launches++;
         }
     } else if constexpr (KB <= 4) {

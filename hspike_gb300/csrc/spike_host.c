@@ -115,6 +115,7 @@ Error_t spike_context_create(spike_context_t *out)
     c->partitions = 0;
     c->max_refine = 3;
     c->red_refine = 0;
+    c->twist = 1;
     c->tol = 1e-12;
     if (spk_malloc((void **)&c->d_scratch, 4 * sizeof(int)) != SPK_OK) {
         spk_stream_destroy(c->own_stream);
@@ -190,6 +191,9 @@ Error_t spike_set_option(spike_context_t c, int opt, double v)
     case SPIKE_OPT_PHASE_TIMING:
         c->timing = v != 0;
         break;
+    case SPIKE_OPT_TWIST:
+        c->twist = v != 0;
+        break;
     case SPIKE_OPT_STREAM_ALLOC:
         if ((v != 0) != (c->stream_alloc != 0)) {
             /* workspace changes allocator: release it (it is rebuilt on demand) */
@@ -224,6 +228,7 @@ Error_t spike_get_option(spike_context_t c, int opt, double *v)
     case SPIKE_OPT_TOLERANCE: *v = c->tol; break;
     case SPIKE_OPT_REDUCED_REFINE: *v = c->red_refine; break;
     case SPIKE_OPT_PHASE_TIMING: *v = c->timing; break;
+    case SPIKE_OPT_TWIST: *v = c->twist; break;
     case SPIKE_OPT_STREAM_ALLOC: *v = c->stream_alloc; break;
     default: return spk_fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
@@ -343,6 +348,13 @@ int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex,
     }
     P->total_blocks = P->blk_off[p];
     P->NP = (long long)P->total_blocks * KB;
+    /* two-sided partition solves pay off on long partitions (eight blocks or
+     * more each, so that V's and W's right-hand sides sit in opposite halves) */
+    int min_blocks = 1 << 30;
+    for (int i = 0; i < p; i++)
+        if (P->blk_off[i + 1] - P->blk_off[i] < min_blocks) min_blocks = P->blk_off[i + 1] - P->blk_off[i];
+    P->twist_cap = spk_twist_supported(KB, is_complex, mode) && min_blocks >= 8;
+    P->twist = P->twist_cap;
 
     /* cyclic-reduction levels of the reduced system */
     int levels = 0;
@@ -594,6 +606,7 @@ static void fill_info(spike_context_t c, const spk_plan *P, const refine_opts *o
     c->info.block = P->KB;
     c->info.kernel_launches = launches;
     c->info.device_bytes = P->bytes;
+    c->info.twisted = P->twist;
 }
 
 static Error_t finish(int rc, const char *where, const refine_opts *o)
@@ -634,6 +647,7 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
     P->nnz = nnz;
     P->ku = info[0];
     P->kl = info[1];
+    P->twist = P->twist_cap && c->twist;
     P->launches = l0;
     P->timing = c->timing;
     const size_t hs = (is_complex ? 2 : 1) * 8;
@@ -830,6 +844,7 @@ static Error_t factor_common(spike_context_t c, int cplx, const char *name, inte
                          &f->plan);
     if (rc == SPK_OK) {
         f->plan->launches = l0;
+        f->plan->twist = f->plan->twist_cap && c->twist;
         rc = factor_phase(f->plan, f->d_rowptr, f->d_colind, f->d_aij, c->stream);
     }
     if (rc != SPK_OK) {

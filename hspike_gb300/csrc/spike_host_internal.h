@@ -24,7 +24,7 @@ struct spike_context_s {
     int device;
     void *own_stream, *stream;
     /* options */
-    int mode, partitions, max_refine, red_refine, timing;
+    int mode, partitions, max_refine, red_refine, timing, twist;
     int stream_alloc; /* workspace allocated stream-ordered on `stream` */
     double tol;
     /* cached plan for the reference-API and device-pointer calls */

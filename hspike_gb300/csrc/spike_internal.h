@@ -88,6 +88,9 @@ typedef struct spk_plan {
     int total_blocks;
     long long NP; /* padded rows = total_blocks * KB */
     int n_iface;  /* p - 1 */
+    /* two-sided partition solves (spike_twist.cu): every partition is
+     * eliminated from both ends towards its block M = N_i / 2 */
+    int twist, twist_cap; /* in use / possible for this schedule and precision */
     /* device copies of the schedule */
     int *d_part_start, *d_blk_off;
     int *d_blk_part; /* total_blocks: partition of each block */
@@ -208,6 +211,13 @@ int spk_timer_end(void *timer, void *stream, double *ms);
 int spk_factor(spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij, void *stream);
 /* shared-memory bytes the factor kernels need for this plan (0 = unsupported) */
 size_t spk_factor_smem(int KB, int is_complex, int mode);
+
+/* ---- two-sided partition factorization (spike_twist.cu) ---- */
+/* 1 if the two-sided kernels exist for this tile size and precision */
+int spk_twist_supported(int KB, int is_complex, int mode);
+/* forward = 1: both elimination chains, the spikes' forward sweeps and the
+ * middle block; forward = 0: the spikes' back substitution */
+int spk_twist_factor(spk_plan *P, int forward, void *stream);
 
 /* ---- reduced system (spike_reduced.cu) ---- */
 int spk_reduced_factor(spk_plan *P, void *stream);

@@ -1,0 +1,453 @@
+// spike_twist.cu -- two-sided ("twisted") partition factorization on sm_103a.
+//
+// A partition of N row blocks is eliminated from both ends at once: blocks
+// 0..M-1 top-down (block LU, the recurrences of k_factor_fwd), blocks
+// N-1..M+1 bottom-up (block UL), and the two chains meet at block M = N/2,
+// which takes the bottom chain's Schur complement in place of D_M:
+//
+//   top     L_J = A(J,J-1) G_{J-1},  S_J = D_J - L_J A(J-1,J),  G_J = S_J^{-1}
+//   bottom  U_J = A(J,J+1) H_{J+1},  T_J = D_J - U_J A(J+1,J),  H_J = T_J^{-1}
+//   middle  T'_M = D_M - U_M A(M+1,M),  L_M = A(M,M-1) G_{M-1},
+//           G_M = (T'_M - L_M A(M-1,M))^{-1}
+//
+// A solve sweeps both halves towards block M and back out again, so every
+// sequential chain is half as long and a partition keeps two CTAs busy.  The
+// arithmetic per block is the same as the one-sided factorization; the
+// reference factors each A_i with SuperLU (OpenMP/spike_superlu.c:763) and
+// solves its spikes column by column (OpenMP/spike_interfaces.c:143-209).
+// These kernels hold three tiles in shared memory (the tile inverse borrows
+// whichever one is idle) so that four CTAs share an SM; the one-sided kernels
+// hold six.
+//
+//   k_tw_lu     (grid p x 2) the two elimination chains; the bottom one ends
+//               with U_M and T'_M
+//   k_tw_sweep  (grid p x 2) forward sweeps of the spikes' right-hand sides:
+//               W's C^ top-down through L, V's B^ bottom-up through U
+//   k_tw_merge  (grid p)     block M: L_M, G_M and X_M of both spikes
+//   k_tw_bwd    (grid p x 4) back substitution of W and V, top and bottom halves
+//
+// Layout, per block J of a partition (factor precision, KB x KB tiles):
+//   gL     J <= M: L_J;  J > M: U_J                           (column-major)
+//   gG     J <= M: G_J;  J > M: H_J                           (column-major)
+//          (T'_M row-major in gG[M] between k_tw_lu and k_tw_merge)
+//   gE     J < M: A(J,J+1);  J = M: U_M;  J > M: A(J,J-1)     (column-major)
+//   gT     D_J (row-major); A(J,J-1): column-major for J <= M, row-major for
+//          J > M; A(J,J+1): row-major for J < M, column-major for J >= M
+//          (written by k_band_tiles)
+//   gV/gW  row-major forward-sweep scratch, then the column-major spike tiles
+// A column-major tile loaded as-is into shared memory is the transposed
+// ("At") left operand of Tile::mm_tA.
+#include "spike_common.cuh"
+
+#include <type_traits>
+
+namespace {
+
+// global column-major tile -> shared row-major tile (row stride TileLD)
+template <class T, int KB, int NT> __device__ __forceinline__ void load_tile_tr(T *s, const T *g)
+{
+    constexpr int LD = TileLD<T, KB>::value;
+    for (int q = threadIdx.x; q < KB * KB; q += NT) {
+        const int c = q / KB, r = q - c * KB;
+        s[r * LD + c] = g[q];
+    }
+}
+
+template <class TL, class Reg> __device__ __forceinline__ void rcopy(Reg &d, const Reg &s)
+{
+#pragma unroll
+    for (int i = 0; i < TL::TR; i++)
+#pragma unroll
+        for (int j = 0; j < TL::TC; j++) d[i][j] = s[i][j];
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+    k_tw_lu(const T *__restrict__ gT, const int *__restrict__ blk_off, T *gL, T *gG, T *gE, unsigned *err)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int part = blockIdx.x;
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * 3 * TS; // per block: D, A(J,J-1), A(J,J+1)
+
+    extern __shared__ char smraw[];
+    T *s0 = (T *)smem_align(smraw), *s1 = s0 + TL::ELEMS, *s2 = s1 + TL::ELEMS;
+    T *buf = s0; // the inverse's scratch: G_{J-1} / H_{J+1} are consumed before it starts
+    TL t(threadIdx.x);
+    typename TL::Reg acc, dreg;
+    bool ok = true;
+
+    if (blockIdx.y == 0) {
+        // top chain, J = 0..M-1 (M >= 4)
+        T *sG = s0, *sE = s1, *sF = s2;
+        cp_async_tile<T, KB, NT>(sE, gTp + 2 * TS);  // A(0,1), row-major
+        cp_async_tile<T, KB, NT>(sF, gTp + 4 * TS);  // A(1,0), column-major
+        cp_async_commit();
+        t.gload(acc, gTp); // S_0 = D_0
+        for (int J = 0; J < M; J++) {
+            if (J > 0) {
+                t.gload(dreg, gTp + (size_t)J * 3 * TS); // D_J, lands during the L product
+                t.rzero(acc);
+                t.mma_tu(acc, sF, sG); // L_J; A(J,J-1) is upper triangular
+                __syncthreads();
+                t.rstore_t(sF, acc);
+                t.gstore_t(gL + tb + J * TS, acc);
+                __syncthreads();
+                rcopy<TL>(acc, dreg);
+                t.mms_t(acc, sF, sE); // S_J = D_J - L_J A(J-1,J)
+                __syncthreads();
+                cp_async_tile<T, KB, NT>(sE, gTp + (size_t)J * 3 * TS + 2 * TS);
+                if (J + 1 < M) cp_async_tile<T, KB, NT>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);
+                cp_async_commit();
+            }
+            ok = t.inverse(acc, buf) && ok;
+            cp_async_wait_all();
+            t.rstore(sG, acc);
+            t.gstore_t(gG + tb + J * TS, acc);
+            __syncthreads();
+        }
+    } else {
+        // bottom chain, J = N-1..M+1, then U_M and T'_M
+        T *sH = s0, *sY = s1, *sX = s2;
+        cp_async_tile<T, KB, NT>(sY, gTp + (size_t)(N - 2) * 3 * TS + 2 * TS); // A(N-2,N-1), column-major
+        cp_async_tile<T, KB, NT>(sX, gTp + (size_t)(N - 1) * 3 * TS + TS);     // A(N-1,N-2), row-major
+        cp_async_commit();
+        t.gload(acc, gTp + (size_t)(N - 1) * 3 * TS); // T_{N-1} = D_{N-1}
+        for (int J = N - 1; J >= M; J--) {
+            if (J < N - 1) {
+                t.gload(dreg, gTp + (size_t)J * 3 * TS);
+                t.rzero(acc);
+                t.mma_tl(acc, sY, sH); // U_J = A(J,J+1) H_{J+1}; A(J,J+1) is lower triangular
+                __syncthreads();
+                t.rstore_t(sY, acc);
+                t.gstore_t((J == M ? gE : gL) + tb + J * TS, acc);
+                __syncthreads();
+                rcopy<TL>(acc, dreg);
+                t.mms_t(acc, sY, sX); // T_J = D_J - U_J A(J+1,J)
+                if (J == M) {
+                    t.gstore(gG + tb + J * TS, acc); // T'_M for k_tw_merge
+                    break;
+                }
+                __syncthreads();
+                cp_async_tile<T, KB, NT>(sY, gTp + (size_t)(J - 1) * 3 * TS + 2 * TS);
+                cp_async_tile<T, KB, NT>(sX, gTp + (size_t)J * 3 * TS + TS);
+                cp_async_commit();
+            }
+            ok = t.inverse(acc, buf) && ok;
+            cp_async_wait_all();
+            t.rstore(sH, acc);
+            t.gstore_t(gG + tb + J * TS, acc);
+            __syncthreads();
+        }
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+
+// V's right-hand side [0; B^] restricted to block J: B^ fills the last KB
+// real rows of the partition, i.e. rows o..KB-1 of block J0 and rows 0..o-1
+// of block J0+1 (when o > 0).
+template <class T, int KB, class TL>
+__device__ __forceinline__ void bhat_block(const TL &t, typename TL::Reg &a, const T *bh, int J, int J0, int o)
+{
+#pragma unroll
+    for (int i = 0; i < TL::TR; i++)
+#pragma unroll
+        for (int j = 0; j < TL::TC; j++) {
+            const int r = t.row(i), c = t.col(j);
+            T v = sc_zero<T>();
+            if (t.act) {
+                if (J == J0 && r >= o)
+                    v = bh[(r - o) * KB + c];
+                else if (o > 0 && J == J0 + 1 && r < o)
+                    v = bh[(KB - o + r) * KB + c];
+            }
+            a[i][j] = v;
+        }
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+    k_tw_sweep(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
+               const T *__restrict__ gE, const T *__restrict__ gBhat, T *gV, T *gW)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int part = blockIdx.x;
+    const bool top = blockIdx.y == 0;
+    if (top ? part == 0 : part == p - 1) return; // the whole CTA: no such spike
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+
+    extern __shared__ char smraw[];
+    T *sZ = (T *)smem_align(smraw), *sA = sZ + TL::ELEMS, *sB = sA + TL::ELEMS;
+    TL t(threadIdx.x);
+    typename TL::Reg acc;
+
+    if (top) {
+        // W: z_0 = C^ (gW tile 0, from k_band_tiles), z_J = -L_J z_{J-1}, J = 1..M-1
+        cp_async_tile<T, KB, NT>(sZ, gW + tb);
+        cp_async_tile<T, KB, NT>(sB, gL + tb + TS);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        for (int J = 1; J < M; J++) {
+            T *cur = (J & 1) ? sB : sA, *nxt = (J & 1) ? sA : sB;
+            if (J + 1 < M) cp_async_tile<T, KB, NT>(nxt, gL + tb + (size_t)(J + 1) * TS);
+            cp_async_commit();
+            t.rzero(acc);
+            t.mms_t(acc, cur, sZ);
+            __syncthreads();
+            t.rstore(sZ, acc);
+            t.gstore(gW + tb + J * TS, acc);
+            cp_async_wait_all();
+            __syncthreads();
+        }
+    } else {
+        // V: w_J = r_J - U_J w_{J+1}, J = N-1..M (U_M lives in gE)
+        const int m = part_start[part + 1] - part_start[part];
+        const int J0 = (m - KB) / KB, o = (m - KB) - J0 * KB; // m >= 8 KB: o >= 0, J0 > M
+        const T *bh = gBhat + (size_t)part * TS;
+        auto utile = [&](int J) { return (J == M ? gE : gL) + tb + (size_t)J * TS; };
+        cp_async_tile<T, KB, NT>(((N - 2) & 1) ? sB : sA, utile(N - 2));
+        cp_async_commit();
+        bhat_block<T, KB>(t, acc, bh, N - 1, J0, o);
+        t.rstore(sZ, acc);
+        t.gstore(gV + tb + (size_t)(N - 1) * TS, acc);
+        cp_async_wait_all();
+        __syncthreads();
+        for (int J = N - 2; J >= M; J--) {
+            T *cur = (J & 1) ? sB : sA, *nxt = (J & 1) ? sA : sB;
+            if (J - 1 >= M) cp_async_tile<T, KB, NT>(nxt, utile(J - 1));
+            cp_async_commit();
+            bhat_block<T, KB>(t, acc, bh, J, J0, o);
+            t.mms_t(acc, cur, sZ);
+            __syncthreads();
+            t.rstore(sZ, acc);
+            t.gstore(gV + tb + J * TS, acc);
+            cp_async_wait_all();
+            __syncthreads();
+        }
+    }
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+    k_tw_merge(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gV, T *gW,
+               unsigned *err)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int part = blockIdx.x;
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * 3 * TS;
+
+    extern __shared__ char smraw[];
+    T *sA = (T *)smem_align(smraw), *sB = sA + TL::ELEMS, *sC = sB + TL::ELEMS;
+    T *buf = sA; // the inverse's scratch: G_{M-1} is consumed before it starts
+    TL t(threadIdx.x);
+    typename TL::Reg acc;
+
+    cp_async_tile<T, KB, NT>(sC, gTp + (size_t)M * 3 * TS + TS);           // A(M,M-1), column-major
+    cp_async_tile<T, KB, NT>(sB, gTp + (size_t)(M - 1) * 3 * TS + 2 * TS); // A(M-1,M), row-major
+    cp_async_commit();
+    load_tile_tr<T, KB, NT>(sA, gG + tb + (size_t)(M - 1) * TS);            // G_{M-1}, row-major
+    cp_async_wait_all();
+    __syncthreads();
+    t.rzero(acc);
+    t.mma_tu(acc, sC, sA); // L_M
+    __syncthreads();
+    t.rstore_t(sC, acc);
+    t.gstore_t(gL + tb + M * TS, acc);
+    __syncthreads();
+    t.gload(acc, gG + tb + M * TS); // T'_M
+    t.mms_t(acc, sC, sB);           // S_M = T'_M - L_M A(M-1,M)
+    const bool ok = t.inverse(acc, buf);
+    t.rstore_t(sA, acc); // G_M as a left operand
+    t.gstore_t(gG + tb + M * TS, acc);
+    __syncthreads();
+    if (part > 0) {
+        // W: z_M = -L_M z_{M-1} (its bottom half is zero), X_M = G_M z_M
+        cp_async_tile<T, KB, NT>(sB, gW + tb + (size_t)(M - 1) * TS);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        t.rzero(acc);
+        t.mms_t(acc, sC, sB);
+        __syncthreads();
+        t.rstore(sB, acc);
+        __syncthreads();
+        t.rzero(acc);
+        t.mma_t(acc, sA, sB);
+        t.gstore_t(gW + tb + M * TS, acc);
+        __syncthreads();
+    }
+    if (part < p - 1) {
+        // V: z_M = w_M (its top half is zero), X_M = G_M w_M
+        cp_async_tile<T, KB, NT>(sB, gV + tb + (size_t)M * TS);
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+        t.rzero(acc);
+        t.mma_t(acc, sA, sB);
+        t.gstore_t(gV + tb + M * TS, acc);
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+
+// Back substitution from X_M outwards; blockIdx.y: 0 W top, 1 W bottom,
+// 2 V top, 3 V bottom.
+//   top     X_J = G_J (Z_J - A(J,J+1) X_{J+1}),  J = M-1..0
+//   bottom  X_J = H_J (Z_J - A(J,J-1) X_{J-1}),  J = M+1..N-1
+// Z_J is the forward sweep where the spike has one (W's top half, V's bottom
+// half), else zero.
+template <class T, int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+    k_tw_bwd(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE, T *gV,
+             T *gW)
+{
+    constexpr int NT = NTOf<KB>::value;
+    using TL = Tile<T, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int part = blockIdx.x, which = blockIdx.y;
+    const bool isV = which >= 2, top = (which & 1) == 0;
+    if (isV ? part == p - 1 : part == 0) return; // the whole CTA: no such spike
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *gX = isV ? gV : gW;
+    const bool hasZ = isV ? !top : top;
+    const int cnt = top ? M : N - 1 - M;
+
+    extern __shared__ char smraw[];
+    T *sG = (T *)smem_align(smraw), *sE = sG + TL::ELEMS, *sX = sE + TL::ELEMS;
+    TL t(threadIdx.x);
+    typename TL::Reg acc;
+
+    const int J1 = top ? M - 1 : M + 1;
+    cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)J1 * TS);
+    cp_async_tile<T, KB, NT>(sE, gE + tb + (size_t)J1 * TS);
+    cp_async_commit();
+    load_tile_tr<T, KB, NT>(sX, gX + tb + (size_t)M * TS); // X_M, row-major
+    cp_async_wait_all();
+    __syncthreads();
+    for (int i = 0; i < cnt; i++) {
+        const int J = top ? M - 1 - i : M + 1 + i;
+        const int Jn = top ? J - 1 : J + 1;
+        const bool more = i + 1 < cnt;
+        if (hasZ)
+            t.gload(acc, gX + tb + (size_t)J * TS);
+        else
+            t.rzero(acc);
+        if (top)
+            t.mms_tl(acc, sE, sX); // A(J,J+1) lower triangular
+        else
+            t.mms_tu(acc, sE, sX); // A(J,J-1) upper triangular
+        __syncthreads();
+        if (more) {
+            cp_async_tile<T, KB, NT>(sE, gE + tb + (size_t)Jn * TS);
+            cp_async_commit();
+        }
+        t.rstore(sX, acc);
+        __syncthreads();
+        t.rzero(acc);
+        t.mma_t(acc, sG, sX);
+        __syncthreads();
+        if (more) {
+            cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)Jn * TS);
+            cp_async_commit();
+        }
+        t.rstore(sX, acc);
+        t.gstore_t(gX + tb + (size_t)J * TS, acc);
+        cp_async_wait_all();
+        __syncthreads();
+    }
+}
+
+template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd)
+{
+    if constexpr (!TwistFits<T, KB>::ok) {
+        return SPK_EBAND;
+    } else {
+        using C = TwistFits<T, KB>;
+        constexpr int NT = NTOf<KB>::value;
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(k_tw_lu<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_tw_sweep<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_tw_merge<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_tw_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem) !=
+                    cudaSuccess)
+                return SPK_ECUDA;
+            attr = true;
+        }
+        const int p = P->p;
+        if (fwd) {
+            k_tw_lu<T, KB><<<dim3(p, 2), NT, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+                                                               (T *)P->d_G, (T *)P->d_E, P->d_err);
+            SPK_CHECK_LAUNCH();
+            P->launches++;
+            if (p > 1) {
+                k_tw_sweep<T, KB><<<dim3(p, 2), NT, C::smem, st>>>(P->d_part_start, P->d_blk_off, p,
+                                                                      (const T *)P->d_L, (const T *)P->d_E,
+                                                                      (const T *)P->d_Bhat, (T *)P->d_V,
+                                                                      (T *)P->d_W);
+                SPK_CHECK_LAUNCH();
+                P->launches++;
+            }
+            k_tw_merge<T, KB><<<p, NT, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
+                                                         (T *)P->d_G, (T *)P->d_V, (T *)P->d_W, P->d_err);
+            SPK_CHECK_LAUNCH();
+            P->launches++;
+        } else if (p > 1) {
+            k_tw_bwd<T, KB><<<dim3(p, 4), NT, C::smem, st>>>(P->d_blk_off, p, (const T *)P->d_G,
+                                                                (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W);
+            SPK_CHECK_LAUNCH();
+            P->launches++;
+        }
+        return SPK_OK;
+    }
+}
+
+template <class T> int disp_twist(spk_plan *P, cudaStream_t st, bool fwd)
+{
+    switch (P->KB) {
+    case 16: return run_twist<T, 16>(P, st, fwd);
+    case 32: return run_twist<T, 32>(P, st, fwd);
+    case 64: return run_twist<T, 64>(P, st, fwd);
+    default: return SPK_EBAND;
+    }
+}
+
+template <class T> bool twist_ok(int KB)
+{
+    switch (KB) {
+    case 16: return TwistFits<T, 16>::ok;
+    case 32: return TwistFits<T, 32>::ok;
+    case 64: return TwistFits<T, 64>::ok;
+    default: return false;
+    }
+}
+
+} // namespace
+
+extern "C" int spk_twist_supported(int KB, int is_complex, int mode)
+{
+    if (is_complex) return mode == SPK_MIXED ? twist_ok<cfloat>(KB) : twist_ok<cdouble>(KB);
+    return mode == SPK_MIXED ? twist_ok<float>(KB) : twist_ok<double>(KB);
+}
+
+extern "C" int spk_twist_factor(spk_plan *P, int forward, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool f = forward != 0;
+    if (P->is_complex) return P->mode == SPK_MIXED ? disp_twist<cfloat>(P, st, f) : disp_twist<cdouble>(P, st, f);
+    return P->mode == SPK_MIXED ? disp_twist<float>(P, st, f) : disp_twist<double>(P, st, f);
+}

@@ -40,6 +40,9 @@ typedef struct spike_factor_s *spike_factor_t;
 #define SPIKE_OPT_PHASE_TIMING 5   /* 1 = time each kernel family with CUDA events (default 0) */
 #define SPIKE_OPT_STREAM_ALLOC 6   /* 1 = workspace via cudaMallocAsync on the context's stream, so contexts on
                                       different streams overlap while they allocate (default 0) */
+#define SPIKE_OPT_TWIST 7          /* 1 = eliminate each partition from both ends at once where the kernels
+                                      allow it (tiles 16..64 fitting four CTAs per SM, >= 8 blocks per
+                                      partition); 0 = top-down only (default 1) */
 
 #define SPIKE_PRECISION_MIXED 0 /* FP32 / complex64 factors, FP64 residual + update + reduced solve */
 #define SPIKE_PRECISION_FP64 1  /* FP64 / complex128 everywhere */
@@ -74,6 +77,7 @@ typedef struct {
     int partitions, ku, kl, block;
     long long kernel_launches; /* kernels launched by the last call */
     size_t device_bytes;      /* device memory held by the context's plan */
+    int twisted;              /* 1 if the partitions were eliminated from both ends (SPIKE_OPT_TWIST) */
 } spike_info_t;
 Error_t spike_get_info(spike_context_t ctx, spike_info_t *info);
 

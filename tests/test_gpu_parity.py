@@ -117,6 +117,56 @@ def test_generated_real_128_row_tiles(case):
     assert info.block == 128
 
 
+# partitions eliminated from both ends (tiles 16..64, >= 8 blocks per partition)
+CASES_TWIST = [
+    (8 * 64 * 4, 64, 64, 1.5, 4, 1),    # exactly 8 blocks per partition
+    (9 * 64 * 5 + 37, 64, 64, 1.5, 5, 3),  # odd block count, ragged last block
+    (40000, 32, 32, 1.5, 10, 2),
+    (30000, 16, 9, 1.5, 12, 17),        # ku != kl, two right-hand-side chunks
+    (60000, 20, 20, 1.2, 1, 1),         # one partition
+]
+
+
+@pytest.mark.parametrize("case", CASES_TWIST, ids=lambda c: f"n{c[0]}_k{c[1]}_{c[2]}_p{c[4]}_r{c[5]}")
+def test_two_sided_partitions_match_one_sided(case):
+    n, ku, kl, dom, p, nrhs = case
+    rp, ci, a, xt, b = hs.gen_banded(n, ku, kl, dom, seed=500 + n, nrhs=nrhs)
+    x2, info = check(rp, ci, a, b, p, "mixed", x_true=xt)
+    assert info.twisted == 1
+    hs.set_option(hs.SPIKE_OPT_TWIST, 0)
+    try:
+        x1, info1 = check(rp, ci, a, b, p, "mixed", x_true=xt)
+        assert info1.twisted == 0
+    finally:
+        hs.set_option(hs.SPIKE_OPT_TWIST, 1)
+    assert relerr(x2, x1) <= ERR_TOL
+
+
+def test_two_sided_partitions_in_plain_fp64():
+    rp, ci, a, xt, b = hs.gen_banded(50000, 24, 24, 1.5, seed=77, nrhs=2)
+    x, info = check(rp, ci, a, b, 8, "fp64", x_true=xt)
+    assert info.twisted == 1 and info.block == 32
+
+
+def test_two_sided_factor_handle_and_complex():
+    rp, ci, a, xt, b = hs.gen_banded(40000, 12, 12, 1.5, seed=78, complex_=True, nrhs=2)
+    x, info = check(rp, ci, a, b, 8, "mixed", x_true=xt)
+    assert info.twisted == 1
+    rp, ci, a, xt, b = hs.gen_banded(80000, 64, 64, 1.5, seed=79, nrhs=1)
+    hs.set_option(hs.SPIKE_OPT_PARTITIONS, 16)
+    try:
+        f = hs.Factor(rp, ci, a)
+        try:
+            for _ in range(2):
+                x = f.solve(b)
+                assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
+                assert relerr(x, xt) <= 1e-10
+        finally:
+            f.release()
+    finally:
+        hs.set_option(hs.SPIKE_OPT_PARTITIONS, 0)
+
+
 def test_128_row_tiles_auto_partitions_and_factor_reuse():
     rp, ci, a, xt, b = hs.gen_banded(200_000, 96, 96, 1.5, seed=41, nrhs=2)
     x = hs.solve(rp, ci, a, b)
