@@ -46,7 +46,7 @@ template <class T, int KB> struct FactorSmem {
 // row-major, zeroed by the caller): C^ coupling (J == 0, columns s-KB..s-1);
 // gBhat (global, row-major): B^ coupling (columns e..e+KB-1).
 // One warp per row: the row's entries are contiguous, so the loads are
-// coalesced and every entry's row is known without a search; two 32-entry
+// coalesced and every entry's row is known without a search; four 32-entry
 // chunks of a row are in flight per iteration.
 template <class T, class H, int KB, int LD>
 __device__ __forceinline__ void place_entry(int lr, int lrow, int c, H a, int s, int m, int J, T *F, T *D, T *En,
@@ -96,18 +96,19 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int lr = warp; lr < nr; lr += NW) {
         const int t1 = srp[lr + 1];
-        for (int t = srp[lr] + lane; t < t1; t += 64) {
-            const bool two = t + 32 < t1;
-            const int c0 = __ldg(colind + t);
-            const H a0 = aij[t];
-            int c1 = 0;
-            H a1 = sc_zero<H>();
-            if (two) {
-                c1 = __ldg(colind + t + 32);
-                a1 = aij[t + 32];
-            }
-            place_entry<T, H, KB, LD>(lr, lrow0 + lr, c0, a0, s, m, J, F, D, En, gZ, gBhat, err);
-            if (two) place_entry<T, H, KB, LD>(lr, lrow0 + lr, c1, a1, s, m, J, F, D, En, gZ, gBhat, err);
+        for (int t = srp[lr] + lane; t < t1; t += 128) {
+            int c[4];
+            H a[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) // four 32-entry pieces of the row in flight at once
+                if (t + 32 * u < t1) {
+                    c[u] = __ldg(colind + t + 32 * u);
+                    a[u] = aij[t + 32 * u];
+                }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (t + 32 * u < t1)
+                    place_entry<T, H, KB, LD>(lr, lrow0 + lr, c[u], a[u], s, m, J, F, D, En, gZ, gBhat, err);
         }
     }
 }
