@@ -368,6 +368,7 @@ static void batch_free(struct spike_batch_s *B)
     free(B->sys);
     free(B->ku);
     free(B->kl);
+    if (B->ctx) spk_ctx_unref(B->ctx);
     free(B);
 }
 
@@ -425,6 +426,7 @@ Error_t spike_dbatch_create(spike_context_t ctx, integer_t count, const spike_ds
     struct spike_batch_s *B = (struct spike_batch_s *)calloc(1, sizeof *B);
     if (!B) return spk_fail(SPIKE_ERR_MEMORY, "%s: host allocation failed", W);
     B->ctx = ctx;
+    spk_ctx_ref(ctx);
     B->count = count;
     B->flags = flags;
     B->sys = (spike_dsystem_t *)malloc(sizeof(spike_dsystem_t) * count);

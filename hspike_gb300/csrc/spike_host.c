@@ -111,6 +111,7 @@ Error_t spike_context_create(spike_context_t *out)
         return spk_fail_code(SPK_ECUDA, "spike_context_create");
     }
     c->stream = c->own_stream;
+    c->refs = 1;
     c->mode = SPK_MIXED;
     c->partitions = 0;
     c->max_refine = 3;
@@ -126,9 +127,8 @@ Error_t spike_context_create(spike_context_t *out)
     return spk_succeed();
 }
 
-Error_t spike_context_destroy(spike_context_t c)
+static void ctx_free(spike_context_t c)
 {
-    if (!c) return spk_fail(SPIKE_ERR_ARGUMENT, "spike_context_destroy: NULL context");
     void *as = spk_ctx_astream(c);
     spk_plan_destroy(c->plan);
     spk_free(c->d_scratch);
@@ -143,6 +143,19 @@ Error_t spike_context_destroy(spike_context_t c)
     spk_stream_destroy(c->own_stream);
     if (t_default == c) t_default = NULL;
     free(c);
+}
+
+void spk_ctx_ref(spike_context_t c) { __atomic_add_fetch(&c->refs, 1, __ATOMIC_ACQ_REL); }
+
+void spk_ctx_unref(spike_context_t c)
+{
+    if (__atomic_sub_fetch(&c->refs, 1, __ATOMIC_ACQ_REL) == 0) ctx_free(c);
+}
+
+Error_t spike_context_destroy(spike_context_t c)
+{
+    if (!c) return spk_fail(SPIKE_ERR_ARGUMENT, "spike_context_destroy: NULL context");
+    spk_ctx_unref(c);
     return spk_succeed();
 }
 
@@ -811,6 +824,7 @@ static Error_t factor_common(spike_context_t c, int cplx, const char *name, inte
     spike_factor_t f = (spike_factor_t)calloc(1, sizeof *f);
     if (!f) return spk_fail(SPIKE_ERR_MEMORY, "%s: host allocation failed", name);
     f->ctx = c;
+    spk_ctx_ref(c);
     f->astream = spk_ctx_astream(c);
     f->is_complex = cplx;
     f->n = n;
@@ -933,6 +947,7 @@ Error_t spike_factor_release(spike_factor_t f)
     spk_free_on(f->d_x, f->astream);
     spk_free_on(f->d_r, f->astream);
     if (f->ctx && f->ctx->stream) spk_stream_sync(f->ctx->stream);
+    if (f->ctx) spk_ctx_unref(f->ctx);
     f->released = 1;
     free(f);
     return spk_succeed();

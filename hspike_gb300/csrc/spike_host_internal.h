@@ -24,6 +24,7 @@ struct spike_context_s {
     int device;
     void *own_stream, *stream;
     /* options */
+    int refs; /* the creator's reference + one per factor handle or batch using the context */
     int mode, partitions, max_refine, red_refine, timing, twist;
     int stream_alloc; /* workspace allocated stream-ordered on `stream` */
     double tol;
@@ -43,6 +44,11 @@ SPK_INTERNAL Error_t spk_succeed(void);
 
 /* the context itself, or the calling thread's default one (created on demand) */
 SPK_INTERNAL spike_context_t spk_get_ctx(spike_context_t c);
+/* Handles that use a context (factors, batches) hold a reference to it, so
+ * spike_context_destroy before their release only drops the creator's
+ * reference: the context goes when its last handle does. */
+SPK_INTERNAL void spk_ctx_ref(spike_context_t c);
+SPK_INTERNAL void spk_ctx_unref(spike_context_t c);
 
 /* smallest supported tile size >= k (0 when k is above the largest) */
 SPK_INTERNAL int spk_choose_block(int k);

@@ -387,9 +387,9 @@ static int residual_g(const spk_plan *P, const int *rp, const int *ci, const voi
     // few lanes per row: every shuffle step of the row reduction is an FP64
     // add per lane, and GB300's FP64 pipe is the residual's bottleneck
     const double per_row = P->n > 0 ? (double)P->nnz / P->n : 1.0;
-    if (per_row >= 32) return launch_residual<H, 8>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    if (per_row >= 8) return launch_residual<H, 4>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    return launch_residual<H, 2>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (per_row >= 64) return launch_residual<H, 4>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (per_row >= 12) return launch_residual<H, 2>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    return launch_residual<H, 1>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
 }
 
 extern "C" int spk_residual(const spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij,
@@ -424,8 +424,12 @@ __global__ void __launch_bounds__(256)
     constexpr int RPB = 256 / G; // rows per CTA per pass
     for (int h0 = 0; h0 < nrhs; h0 += NH) {
         double lr[NH], lb[NH];
+        const H *xj[NH]; // column pointers, hoisted out of the entry loop (no 64-bit offset per entry)
 #pragma unroll
-        for (int j = 0; j < NH; j++) lr[j] = lb[j] = 0.0;
+        for (int j = 0; j < NH; j++) {
+            lr[j] = lb[j] = 0.0;
+            xj[j] = x + (size_t)(h0 + j < nrhs ? h0 + j : h0) * n;
+        }
         __syncthreads();
         // every lane runs every iteration so the shuffles see the full warp
         for (int base = lr0; base < lr1; base += RPB) {
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(256)
                     const int c = S.colind[t];
 #pragma unroll
                     for (int j = 0; j < NH; j++)
-                        if (h0 + j < nrhs) acc[j] = madd(acc[j], av, x[(size_t)(h0 + j) * n + c]);
+                        if (h0 + j < nrhs) acc[j] = madd(acc[j], av, xj[j][c]);
                 }
             }
 #pragma unroll
@@ -518,13 +522,13 @@ extern "C" int spk_residual_batch(const spk_sysref *d_sys, const int *d_chunks, 
     const int R = rows_per_chunk;
     // lanes per row from the rows' length (as in the single-system residual)
     if (is_complex) {
-        if (row_len >= 32) return residual_batch_g<cdouble, 8>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
-        if (row_len >= 8) return residual_batch_g<cdouble, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
-        return residual_batch_g<cdouble, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+        if (row_len >= 64) return residual_batch_g<cdouble, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+        if (row_len >= 12) return residual_batch_g<cdouble, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+        return residual_batch_g<cdouble, 1>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
     }
-    if (row_len >= 32) return residual_batch_g<double, 8>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
-    if (row_len >= 8) return residual_batch_g<double, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
-    return residual_batch_g<double, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    if (row_len >= 64) return residual_batch_g<double, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    if (row_len >= 12) return residual_batch_g<double, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    return residual_batch_g<double, 1>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
 }
 
 __global__ void k_batch_relres(const double *__restrict__ norms, int nsys, int nrhs, double *relres,

@@ -64,6 +64,9 @@ const char *spike_last_error(void);       /* human-readable, thread-local */
 
 /* ---- contexts ---- */
 Error_t spike_context_create(spike_context_t *ctx);          /* on the current CUDA device */
+/* Factor handles and batches created on a context keep it alive: destroying
+ * the context before releasing them drops the caller's reference only, and
+ * the context goes with the last of them. */
 Error_t spike_context_destroy(spike_context_t ctx);
 /* Run this context's work on a caller-owned cudaStream_t (NULL = own stream). */
 Error_t spike_context_set_stream(spike_context_t ctx, void *cuda_stream);

@@ -154,6 +154,25 @@ def test_batch_band_above_fp64_tiles_is_rejected():
     ctx.close()
 
 
+def test_handles_outlive_their_context():
+    # a factor handle and a batch released after their context is destroyed
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    rp, ci, a, xt, b = hs.gen_banded(20000, 8, 8, 1.5, seed=91)
+    ctx = hs.Context()
+    f = hs.Factor(rp, ci, a, ctx)
+    hb = W.gen_batch([(3000, 3, 1, 1.5), (5000, 8, 2, 1.5)], seed=92)
+    t, systems = _device_batch(hb, torch, dev)
+    bt = hs.Batch(systems, ctx, autotune=False)
+    ctx.close()  # the handles keep the context alive
+    x = f.solve(b)
+    assert np.linalg.norm(x - xt) / np.linalg.norm(xt) <= 1e-9
+    bt.run()
+    assert (bt.relres() <= RES_TOL).all()
+    f.release()
+    bt.destroy()
+
+
 def test_batch_rejects_invalid_system():
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda:0")
