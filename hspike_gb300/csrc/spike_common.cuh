@@ -127,7 +127,7 @@ template <int KB> struct NTOf {
 };
 
 // ------------------------------------------------------------ vector access
-// N contiguous elements (N in {1, 2, 4}) between registers and memory in
+// N contiguous elements (N in {1, 2} or a multiple of 4) between registers and memory in
 // 8- or 16-byte transactions.  The pointer must be aligned to
 // min(16, N * sizeof(T)) bytes.
 template <class T> __device__ __forceinline__ T from_f2(float x, float y);
@@ -144,9 +144,12 @@ __device__ __forceinline__ float2 to_f2(cfloat c) { return make_float2(c.re, c.i
 
 template <class T, int N> __device__ __forceinline__ void vld(T (&d)[N], const T *p)
 {
-    if constexpr (sizeof(T) == 4 && N == 4) {
-        const float4 v = *reinterpret_cast<const float4 *>(p);
-        d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+    if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < N / 4; q++) {
+            const float4 v = reinterpret_cast<const float4 *>(p)[q];
+            d[4 * q] = v.x; d[4 * q + 1] = v.y; d[4 * q + 2] = v.z; d[4 * q + 3] = v.w;
+        }
     } else if constexpr (sizeof(T) == 4 && N == 2) {
         const float2 v = *reinterpret_cast<const float2 *>(p);
         d[0] = v.x; d[1] = v.y;
@@ -164,8 +167,10 @@ template <class T, int N> __device__ __forceinline__ void vld(T (&d)[N], const T
 }
 template <class T, int N> __device__ __forceinline__ void vst(T *p, const T (&d)[N])
 {
-    if constexpr (sizeof(T) == 4 && N == 4) {
-        *reinterpret_cast<float4 *>(p) = make_float4(d[0], d[1], d[2], d[3]);
+    if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < N / 4; q++)
+            reinterpret_cast<float4 *>(p)[q] = make_float4(d[4 * q], d[4 * q + 1], d[4 * q + 2], d[4 * q + 3]);
     } else if constexpr (sizeof(T) == 4 && N == 2) {
         *reinterpret_cast<float2 *>(p) = make_float2(d[0], d[1]);
     } else if constexpr (sizeof(T) == 8 && N >= 2) {
@@ -202,7 +207,10 @@ template <class T, int KB, int NT> struct Tile {
     static constexpr int ELEMS = KB * LD;           // shared-memory tile size
     static constexpr int ACTIVE = TX * TY;          // threads that own a sub-tile
     // the blocked inverse runs when every thread owns a 4 x 4 sub-tile
-    static constexpr bool BLOCK4 = (TR == 4 && TC == 4);
+    // every thread owns 4 columns and a multiple of 4 rows; pivot block q is
+    // columns 4q..4q+3 of thread column tx = q
+    static constexpr bool BLOCK4 = (TC == 4 && TR % 4 == 0 && TR <= 8 && TX == KB / 4);
+    static constexpr int RB = TR / 4; // pivot-block rows per thread
     static constexpr int INV_HALF = 12 * KB + 16;  // pivot columns + P^{-1} + V' + pivot rows
     static constexpr int INV_BUF = BLOCK4 ? 2 * INV_HALF + KB : 4 * KB; // shared scratch elements for inverse()
 
@@ -394,18 +402,24 @@ template <class T, int KB, int NT> struct Tile {
     {
         bool ok = true;
         T *dg = buf + 2 * INV_HALF; // diagonal
-        if (act && tx == ty) {
+        // the thread whose columns tx*4..tx*4+3 cross its rows holds those diagonal entries
+        if (act && (RB == 1 ? tx == ty : (tx * 4) / TR == ty)) {
+            const int o = RB == 1 ? 0 : tx * 4 - ty * TR;
             T d[4];
 #pragma unroll
-            for (int i = 0; i < 4; i++) d[i] = s[i][i];
-            vst<T, 4>(dg + row(0), d);
+            for (int j = 0; j < 4; j++) {
+                d[j] = s[0][j];
+#pragma unroll
+                for (int i = 1; i < TR; i++) d[j] = (i == o + j) ? s[i][j] : d[j];
+            }
+            vst<T, 4>(dg + col(0), d);
         }
         __syncthreads();
-        T dr[4];
         if (act) {
-            vld<T, 4>(dr, dg + row(0));
+            T dr[TR];
+            vld<T, TR>(dr, dg + row(0));
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
+            for (int i = 0; i < TR; i++) {
                 if (!sc_finite_nonzero(dr[i])) ok = false;
                 const T rr = sc_rcp_fast(dr[i]);
 #pragma unroll
@@ -417,51 +431,61 @@ template <class T, int KB, int NT> struct Tile {
             T *pbuf = cbuf + 4 * KB;            // [4][4] P^{-1}
             T *vbuf = pbuf + 16;                // [4][KB] V'
             T *rbuf = vbuf + 4 * KB;            // [4][KB] pivot rows B + I
-            const bool rown = act && ty == q, cown = act && tx == q;
+            const bool rown = act && (RB == 1 ? ty == q : ty == (4 * q) / TR), cown = act && tx == q;
+            const int ro = RB == 1 ? 0 : 4 * (q % RB); // first pivot row within the owner's rows
             if (rown) {
 #pragma unroll
-                for (int a = 0; a < 4; a++) {
-                    T bb[4];
+                for (int rb = 0; rb < RB; rb++)
+                    if (ro == 4 * rb) {
 #pragma unroll
-                    for (int jj = 0; jj < 4; jj++) bb[jj] = (cown && a == jj) ? s[a][jj] + sc_one<T>() : s[a][jj];
-                    vst<T, 4>(rbuf + a * KB + col(0), bb);
-                }
+                        for (int a = 0; a < 4; a++) {
+                            T bb[4];
+#pragma unroll
+                            for (int jj = 0; jj < 4; jj++)
+                                bb[jj] = (cown && a == jj) ? s[4 * rb + a][jj] + sc_one<T>() : s[4 * rb + a][jj];
+                            vst<T, 4>(rbuf + a * KB + col(0), bb);
+                        }
+                    }
             }
             if (cown) {
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
+                for (int i = 0; i < TR; i++) {
                     T u[4];
 #pragma unroll
-                    for (int t = 0; t < 4; t++) u[t] = (rown && t == i) ? s[i][t] - sc_one<T>() : s[i][t];
+                    for (int t = 0; t < 4; t++) u[t] = (rown && i - ro == t) ? s[i][t] - sc_one<T>() : s[i][t];
                     vst<T, 4>(cbuf + row(i) * 4, u);
                 }
                 if (rown) { // pivot owner: P^{-1} by unblocked Gauss-Jordan in registers
-                    T pinv[4][4];
 #pragma unroll
-                    for (int a = 0; a < 4; a++)
+                    for (int rb = 0; rb < RB; rb++)
+                        if (ro == 4 * rb) {
+                            T pinv[4][4];
 #pragma unroll
-                        for (int b = 0; b < 4; b++) pinv[a][b] = s[a][b];
+                            for (int a = 0; a < 4; a++)
 #pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        const T piv = pinv[k][k];
-                        if (!sc_finite_nonzero(piv)) ok = false;
-                        const T pr = sc_rcp_fast(piv);
+                                for (int b = 0; b < 4; b++) pinv[a][b] = s[4 * rb + a][b];
 #pragma unroll
-                        for (int b = 0; b < 4; b++)
-                            if (b != k) pinv[k][b] = pinv[k][b] * pr;
-#pragma unroll
-                        for (int a = 0; a < 4; a++)
-                            if (a != k) {
-                                const T f = pinv[a][k];
+                            for (int k = 0; k < 4; k++) {
+                                const T piv = pinv[k][k];
+                                if (!sc_finite_nonzero(piv)) ok = false;
+                                const T pr = sc_rcp_fast(piv);
 #pragma unroll
                                 for (int b = 0; b < 4; b++)
-                                    if (b != k) pinv[a][b] = msub(pinv[a][b], f, pinv[k][b]);
-                                pinv[a][k] = -(f * pr);
-                            }
-                        pinv[k][k] = pr;
-                    }
+                                    if (b != k) pinv[k][b] = pinv[k][b] * pr;
 #pragma unroll
-                    for (int a = 0; a < 4; a++) vst<T, 4>(pbuf + 4 * a, pinv[a]);
+                                for (int a = 0; a < 4; a++)
+                                    if (a != k) {
+                                        const T f = pinv[a][k];
+#pragma unroll
+                                        for (int b = 0; b < 4; b++)
+                                            if (b != k) pinv[a][b] = msub(pinv[a][b], f, pinv[k][b]);
+                                        pinv[a][k] = -(f * pr);
+                                    }
+                                pinv[k][k] = pr;
+                            }
+#pragma unroll
+                            for (int a = 0; a < 4; a++) vst<T, 4>(pbuf + 4 * a, pinv[a]);
+                        }
                 }
             }
             __syncthreads();
@@ -475,13 +499,13 @@ template <class T, int KB, int NT> struct Tile {
             }
             __syncthreads();
             if (act) {
-                T u[4][4], v[4][4];
+                T u[TR][4], v[4][4];
 #pragma unroll
-                for (int i = 0; i < 4; i++) vld<T, 4>(u[i], cbuf + row(i) * 4);
+                for (int i = 0; i < TR; i++) vld<T, 4>(u[i], cbuf + row(i) * 4);
 #pragma unroll
                 for (int t = 0; t < 4; t++) vld<T, 4>(v[t], vbuf + t * KB + col(0));
 #pragma unroll
-                for (int i = 0; i < 4; i++)
+                for (int i = 0; i < TR; i++)
 #pragma unroll
                     for (int jj = 0; jj < 4; jj++) {
                         T acc = s[i][jj];
@@ -499,7 +523,7 @@ template <class T, int KB, int NT> struct Tile {
             for (int jj = 0; jj < 4; jj++) {
                 const T rc = sc_rcp_fast(dc[jj]);
 #pragma unroll
-                for (int i = 0; i < 4; i++) s[i][jj] = s[i][jj] * rc;
+                for (int i = 0; i < TR; i++) s[i][jj] = s[i][jj] * rc;
             }
         }
         __syncthreads();
@@ -574,6 +598,14 @@ template <class T, int KB, int NT> struct Tile {
 // Two-sided partition kernels (spike_twist.cu, and their right-hand-side
 // sweeps in spike_apply.cu): three shared tiles per CTA, the tile inverse's
 // scratch inside one of them, four CTAs per SM.
+// Threads per CTA of the product-only kernels among them (the spikes' sweeps
+// and back substitution): 128 for 64-row tiles gives every thread an 8 x 4
+// sub-tile, i.e. 1.5 bytes of shared-memory operand traffic per FMA instead
+// of 2.  The kernels with a tile inverse keep 4 x 4 sub-tiles: the inverse's
+// barrier-separated steps want the larger CTA.
+template <int KB> struct TwNT {
+    static constexpr int value = KB == 64 ? 128 : NTOf<KB>::value;
+};
 template <class T, int KB> struct TwistFits {
     using TL = Tile<T, KB, NTOf<KB>::value>;
     static constexpr size_t smem = 3 * sizeof(T) * TL::ELEMS + 64;

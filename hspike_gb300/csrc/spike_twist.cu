@@ -169,11 +169,11 @@ __device__ __forceinline__ void bhat_block(const TL &t, typename TL::Reg &a, con
 }
 
 template <class T, int KB>
-__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+__global__ void __launch_bounds__(TwNT<KB>::value, 4)
     k_tw_sweep(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
                const T *__restrict__ gE, const T *__restrict__ gBhat, T *gV, T *gW)
 {
-    constexpr int NT = NTOf<KB>::value;
+    constexpr int NT = TwNT<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
     const int part = blockIdx.x;
@@ -307,11 +307,11 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
 // Z_J is the forward sweep where the spike has one (W's top half, V's bottom
 // half), else zero.
 template <class T, int KB>
-__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+__global__ void __launch_bounds__(TwNT<KB>::value, 4)
     k_tw_bwd(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE, T *gV,
              T *gW)
 {
-    constexpr int NT = NTOf<KB>::value;
+    constexpr int NT = TwNT<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
     const int part = blockIdx.x, which = blockIdx.y;
@@ -374,7 +374,7 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd)
         return SPK_EBAND;
     } else {
         using C = TwistFits<T, KB>;
-        constexpr int NT = NTOf<KB>::value;
+        constexpr int NT = TwNT<KB>::value;
         static bool attr = false;
         if (!attr) {
             if (cudaFuncSetAttribute(k_tw_lu<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem) !=
@@ -390,7 +390,7 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd)
         }
         const int p = P->p;
         if (fwd) {
-            k_tw_lu<T, KB><<<dim3(p, 2), NT, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+            k_tw_lu<T, KB><<<dim3(p, 2), NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
                                                                (T *)P->d_G, (T *)P->d_E, P->d_err);
             SPK_CHECK_LAUNCH();
             P->launches++;
@@ -402,7 +402,7 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd)
                 SPK_CHECK_LAUNCH();
                 P->launches++;
             }
-            k_tw_merge<T, KB><<<p, NT, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
+            k_tw_merge<T, KB><<<p, NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
                                                          (T *)P->d_G, (T *)P->d_V, (T *)P->d_W, P->d_err);
             SPK_CHECK_LAUNCH();
             P->launches++;
