@@ -55,7 +55,7 @@ EXPORTS = [
     "matrix_ComputeBandwidth", "matrix_LoadCSR", "matrix_SaveCSR", "matrix_ExportBinary",
     "matrix_CreateFromComponents", "matrix_Deallocate", "directSolver_CreateHandler", "directSolver_Configure",
     "directSolver_Factorize", "directSolver_SolveForRHS", "directSolver_ShowStatistics", "directSolver_Finalize",
-    "directSolver_Solve", "block_CreateEmptyBlock", "block_Deallocate", "block_SaveCSR", "block_loadCSR",
+    "spike_dsolve", "spike_zsolve", "directSolver_Solve", "block_CreateEmptyBlock", "block_Deallocate", "block_SaveCSR", "block_loadCSR",
     "vector_LoadPermutationArray", "vector_LoadRHS",
 ]
 SPIKE_OPT_STREAM_ALLOC = 6
@@ -168,7 +168,7 @@ def load(path: str | None = None):
     L.spike_set_option.argtypes = [vp, i, C.c_double]
     L.spike_get_option.argtypes = [vp, i, C.POINTER(C.c_double)]
     L.spike_get_info.argtypes = [vp, C.POINTER(Info)]
-    for name in ("spike_dsolve_device", "spike_zsolve_device"):
+    for name in ("spike_dsolve_device", "spike_zsolve_device", "spike_dsolve", "spike_zsolve"):
         getattr(L, name).argtypes = [vp, i, i, i, vp, vp, vp, vp, vp]
     for name in ("spike_dfactor", "spike_zfactor", "spike_dfactor_device"):
         getattr(L, name).argtypes = [vp, i, i, vp, vp, vp, C.POINTER(vp)]
@@ -313,14 +313,16 @@ def solve(rowptr, colind, aij, b, precision=SPIKE_PRECISION_MIXED, partitions=0,
     aij = np.ascontiguousarray(aij, dt)
     b2 = np.asfortranarray(np.asarray(b, dt).reshape(len(rowptr) - 1, -1))
     x = np.zeros_like(b2, order="F")
+    n, nrhs = b2.shape
     if ctx is not None:
         ctx.set_option(SPIKE_OPT_PRECISION, precision)
         ctx.set_option(SPIKE_OPT_PARTITIONS, partitions)
+        fn = load().spike_zsolve if cplx else load().spike_dsolve
+        rc = fn(ctx.handle, n, len(colind), nrhs, _ptr(colind), _ptr(rowptr), _ptr(aij), _ptr(x), _ptr(b2))
     else:
         set_option(SPIKE_OPT_PRECISION, precision)
         set_option(SPIKE_OPT_PARTITIONS, partitions)
-    n, nrhs = b2.shape
-    rc = _core("z" if cplx else "d", n, len(colind), nrhs, colind, rowptr, aij, x, b2)
+        rc = _core("z" if cplx else "d", n, len(colind), nrhs, colind, rowptr, aij, x, b2)
     _check(rc)
     return x if np.ndim(b) == 2 else x[:, 0]
 

@@ -80,10 +80,15 @@ __device__ __forceinline__ void place_entry(int lr, int lrow, int c, H a, int s,
     }
 }
 
-template <class T, class H, int KB, int LD>
+// VAL: the single-system path skipped its separate analysis pass (the plan
+// was reused), so this pass also validates the CSR -- row pointers in range
+// and non-decreasing, columns in [0, n) and increasing within a row -- and
+// measures the exact bandwidth: err[1] = ku, err[2] = kl.  A row with bad
+// pointers is flagged and not read.
+template <class T, class H, int KB, int LD, bool VAL>
 __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
                               const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *gZ,
-                              T *gBhat, unsigned *err, int *srp)
+                              T *gBhat, unsigned *err, int *srp, int n, long long nnz)
 {
     constexpr int NT = NTOf<KB>::value;
     constexpr int NW = NT / 32;
@@ -94,9 +99,17 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
     for (int lr = nr + threadIdx.x; lr < KB; lr += NT) D[lr * LD + lr] = sc_one<T>(); // identity padding
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int ku = 0, kl = 0;
     for (int lr = warp; lr < nr; lr += NW) {
-        const int t1 = srp[lr + 1];
-        for (int t = srp[lr] + lane; t < t1; t += 128) {
+        const int t0 = srp[lr], t1 = srp[lr + 1];
+        if (VAL && (t0 < 0 || (long long)t1 > nnz || t1 < t0)) {
+            if (lane == 0) atomicOr(err, SPK_DEV_ERR_CSR);
+            continue;
+        }
+        const int grow = s + lrow0 + lr; // the row's index in the system
+        int carry = -1;                  // last column of the previous iteration
+        for (int base = t0; base < t1; base += 128) { // warp-uniform: the shuffles see every lane
+            const int t = base + lane;
             int c[4];
             H a[4];
 #pragma unroll
@@ -105,10 +118,35 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
                     c[u] = __ldg(colind + t + 32 * u);
                     a[u] = aij[t + 32 * u];
                 }
+            if constexpr (VAL) {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int up = __shfl_up_sync(0xffffffffu, c[u], 1);
+                    const int wrap = __shfl_sync(0xffffffffu, u ? c[u > 0 ? u - 1 : 0] : carry, 31);
+                    const int pred = lane ? up : (u ? wrap : carry);
+                    const int tt = t + 32 * u;
+                    if (tt < t1) {
+                        if (c[u] < 0 || c[u] >= n || (tt > t0 && pred >= c[u])) atomicOr(err, SPK_DEV_ERR_CSR);
+                        ku = max(ku, c[u] - grow);
+                        kl = max(kl, grow - c[u]);
+                    }
+                }
+                carry = __shfl_sync(0xffffffffu, c[3], 31); // used only when the next iteration's entries exist
+            }
 #pragma unroll
             for (int u = 0; u < 4; u++)
                 if (t + 32 * u < t1)
                     place_entry<T, H, KB, LD>(lr, lrow0 + lr, c[u], a[u], s, m, J, F, D, En, gZ, gBhat, err);
+        }
+    }
+    if constexpr (VAL) {
+        for (int o = 16; o > 0; o >>= 1) {
+            ku = max(ku, __shfl_xor_sync(0xffffffffu, ku, o));
+            kl = max(kl, __shfl_xor_sync(0xffffffffu, kl, o));
+        }
+        if (lane == 0) {
+            atomicMax(err + 1, (unsigned)ku);
+            atomicMax(err + 2, (unsigned)kl);
         }
     }
 }
@@ -158,7 +196,8 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     k_band_tiles(const int *__restrict__ rowptr, const int *__restrict__ colind,
                  const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
                  const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
-                 unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys, int twist)
+                 unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys, int twist,
+                 int validate, int n, long long nnz)
 {
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
@@ -190,7 +229,16 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     if (zt)
         for (int q = threadIdx.x; q < KB * KB; q += NTOf<KB>::value) gz[q] = sc_zero<T>();
     __syncthreads();
-    scatter_block<T, H, KB, LD1>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS, err, srp);
+    if (validate) {
+        scatter_block<T, H, KB, LD1, true>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
+                                           err, srp, n, nnz);
+        if (threadIdx.x == 0 && ((gb == 0 && rowptr[0] != 0) ||
+                                 (gb == (int)gridDim.x - 1 && (long long)rowptr[n] != nnz)))
+            atomicOr(err, SPK_DEV_ERR_CSR);
+    } else {
+        scatter_block<T, H, KB, LD1, false>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
+                                            err, srp, n, nnz);
+    }
     __syncthreads();
     T *g = gT + (size_t)gb * 3 * TS;
     store_tile<T, KB, LD1>(g, sD);
@@ -845,7 +893,8 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     k_band_tiles<T, KB><<<P->total_blocks, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start,
                                                               P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
                                                               (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys,
-                                                              P->d_part_sys, P->twist);
+                                                              P->d_part_sys, P->twist, P->validate && !P->d_sys,
+                                                              P->n, P->nnz);
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
     if (P->twist) { // two-sided chains (spike_twist.cu)

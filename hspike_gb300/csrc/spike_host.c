@@ -517,24 +517,31 @@ static int plan_matches(const spk_plan *P, int n, int ku, int kl, int is_complex
 /* ------------------------------------------------------------------ */
 /* phases                                                              */
 /* ------------------------------------------------------------------ */
-static int check_device_error(spk_plan *P, void *stream)
+static int check_device_error(spk_plan *P, void *stream, unsigned *e)
 {
-    unsigned e[4] = {0, 0, 0, 0};
-    TRY(spk_memcpy_d2h(e, P->d_err, sizeof e, stream));
+    e[0] = e[1] = e[2] = e[3] = 0;
+    TRY(spk_memcpy_d2h(e, P->d_err, sizeof(unsigned) * 4, stream));
     TRY(spk_stream_sync(stream));
     if (e[0] & SPK_DEV_ERR_PIVOT) return SPK_EPIVOT;
     if (e[0] & (SPK_DEV_ERR_BAND | SPK_DEV_ERR_CSR)) return SPK_ECSR;
     return SPK_OK;
 }
 
-static int factor_phase(spk_plan *P, const int *rp, const int *ci, const void *aij, void *stream)
+/* e (optional): the device error word and, with P->validate, ku and kl */
+static int factor_phase_e(spk_plan *P, const int *rp, const int *ci, const void *aij, void *stream, unsigned *e)
 {
+    unsigned w[4];
     TRY(spk_memset(P->d_err, 0, sizeof(unsigned) * 4, stream));
     TRY(spk_factor(P, rp, ci, aij, stream));
     spk_phase_begin(P, SPK_PH_RED_FACTOR, stream);
     TRY(spk_reduced_factor(P, stream));
     spk_phase_end(P, stream);
-    return check_device_error(P, stream);
+    return check_device_error(P, stream, e ? e : w);
+}
+
+static int factor_phase(spk_plan *P, const int *rp, const int *ci, const void *aij, void *stream)
+{
+    return factor_phase_e(P, rp, ci, aij, stream, NULL);
 }
 
 /* one SPIKE application: x (+)= A_spike^{-1} r */
@@ -638,6 +645,39 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
 {
     int info[3];
     long long l0 = 0;
+    const int chunk0 = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
+    const size_t hs0 = (is_complex ? 2 : 1) * 8;
+    /* A call with the shape of the previous one (n, nnz, precision,
+     * partitions) reuses its plan without the separate analysis pass: the
+     * band-tile pass validates the CSR and measures the bandwidth itself, and
+     * only if the bandwidth class changed (or the CSR is invalid) does the
+     * call fall back to analysis, a new plan and a second factorization. */
+    spk_plan *Q = c->plan;
+    if (Q && Q->n == n && Q->nnz == nnz && Q->is_complex == is_complex && Q->mode == c->mode &&
+        Q->p == choose_partitions(n, Q->KB, c->partitions) && chunk0 <= Q->nrhs_max) {
+        unsigned e[4];
+        Q->twist = Q->twist_cap && c->twist;
+        Q->launches = 0;
+        Q->timing = c->timing;
+        Q->validate = 1;
+        TRY(ensure(&c->d_r, &c->c_r, hs0 * (size_t)n * chunk0, spk_ctx_astream(c)));
+        const int frc = factor_phase_e(Q, rp, ci, aij, c->stream, e);
+        Q->validate = 0;
+        const int ku = (int)e[1], kl = (int)e[2], kmax = ku > kl ? ku : kl;
+        const int same = !(e[0] & (SPK_DEV_ERR_CSR | SPK_DEV_ERR_BAND)) && spk_choose_block(kmax < 1 ? 1 : kmax) == Q->KB;
+        if (same && (frc == SPK_OK || frc == SPK_EPIVOT)) {
+            Q->ku = ku;
+            Q->kl = kl;
+            int rc = frc;
+            if (rc == SPK_OK) rc = solve_all(Q, rp, ci, aij, x, b, c->d_r, nrhs, o, c->stream);
+            if (Q->timing && (rc == SPK_OK || rc == SPK_ECONV) && spk_phase_collect(Q) != SPK_OK) rc = SPK_ECUDA;
+            *launches = Q->launches;
+            fill_info(c, Q, o, Q->launches);
+            return rc;
+        }
+        if (frc != SPK_OK && frc != SPK_ECSR && frc != SPK_EPIVOT) return frc;
+        /* otherwise: the full path below */
+    }
     /* the analysis is timed on the previous call's plan (the plan for this
      * call depends on its result) */
     spk_plan *Pa = c->timing ? c->plan : NULL;
@@ -694,6 +734,29 @@ static Error_t host_solve(int dtype, const char *name, integer_t n, integer_t nn
     spike_context_t c = spk_get_ctx(NULL);
     if (!c) return SPIKE_ERROR;
     return spk_host_solve_ctx(c, dtype, name, n, nnz, nrhs, colind, rowptr, aij, x, b);
+}
+
+static Error_t solve_on(spike_context_t c, int dtype, const char *name, integer_t n, integer_t nnz, integer_t nrhs,
+                        const integer_t *colind, const integer_t *rowptr, const void *aij, void *x, const void *b)
+{
+    if (n < 0 || nnz < 0 || nrhs < 0) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: n, nnz and nrhs must be >= 0", name);
+    if (n == 0 || nrhs == 0) return spk_succeed();
+    if (!colind || !rowptr || !aij || !x || !b) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: NULL array", name);
+    c = spk_get_ctx(c);
+    if (!c) return SPIKE_ERROR;
+    return spk_host_solve_ctx(c, dtype, name, n, nnz, nrhs, colind, rowptr, aij, x, b);
+}
+
+Error_t spike_dsolve(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs, const integer_t *colind,
+                     const integer_t *rowptr, const double *aij, double *x, const double *b)
+{
+    return solve_on(ctx, SPK_D, "spike_dsolve", n, nnz, nrhs, colind, rowptr, aij, x, b);
+}
+
+Error_t spike_zsolve(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs, const integer_t *colind,
+                     const integer_t *rowptr, const void *aij, void *x, const void *b)
+{
+    return solve_on(ctx, SPK_Z, "spike_zsolve", n, nnz, nrhs, colind, rowptr, aij, x, b);
 }
 
 Error_t spk_host_solve_ctx(spike_context_t c, int dtype, const char *name, integer_t n, integer_t nnz, integer_t nrhs,

@@ -91,6 +91,9 @@ typedef struct spk_plan {
     /* two-sided partition solves (spike_twist.cu): every partition is
      * eliminated from both ends towards its block M = N_i / 2 */
     int twist, twist_cap; /* in use / possible for this schedule and precision */
+    /* k_band_tiles also validates the CSR and measures the bandwidth into
+     * d_err[1..2] (set when the separate analysis pass was skipped) */
+    int validate;
     /* device copies of the schedule */
     int *d_part_start, *d_blk_off;
     int *d_blk_part; /* total_blocks: partition of each block */

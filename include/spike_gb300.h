@@ -95,6 +95,14 @@ Error_t spike_get_info(spike_context_t ctx, spike_info_t *info);
 #define SPIKE_NUM_PHASES 9
 Error_t spike_get_phase_times(spike_context_t ctx, int nphases, double *ms, long long *calls, int reset);
 
+/* ---- host-array solves on an explicit context ---- */
+/* dspike_core_host / zspike_core_host on an explicit context (host arrays,
+ * same meaning; NULL = the calling thread's default context). */
+Error_t spike_dsolve(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs, const integer_t *colind,
+                     const integer_t *rowptr, const double *aij, double *x, const double *b);
+Error_t spike_zsolve(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs, const integer_t *colind,
+                     const integer_t *rowptr, const void *aij, void *x, const void *b);
+
 /* ---- device-pointer solves: every array already in device memory ---- */
 Error_t spike_dsolve_device(spike_context_t ctx, integer_t n, integer_t nnz, integer_t nrhs,
                             const integer_t *d_colind, const integer_t *d_rowptr, const double *d_aij,

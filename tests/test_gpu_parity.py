@@ -314,6 +314,51 @@ def test_invalid_csr_is_rejected():
     assert hs.ERR_NAMES[hs.last_error()[0]] == "csr"
 
 
+def test_reused_plan_validates_each_call():
+    # a call with the shape (n, nnz) of the previous one skips the separate
+    # analysis pass: the band-tile pass validates the CSR and measures the
+    # bandwidth, falling back to a new plan when the tile class changed
+    ctx = hs.Context()
+    try:
+        n = 30000
+        rp, ci, a, xt, b = hs.gen_banded(n, 10, 10, 1.5, seed=23)
+        x1 = hs.solve(rp, ci, a, b, ctx=ctx)
+        x2 = hs.solve(rp, ci, a, b, ctx=ctx)
+        assert np.array_equal(x1, x2)
+        assert (ctx.info().ku, ctx.info().kl, ctx.info().block) == (10, 10, 16)
+        # same n and nnz, bandwidth 14: same tile class, the plan is kept
+        ci14 = ci.copy()
+        ci14[rp[1] - 1] = 14  # row 0's last column 10 -> 14 (still sorted)
+        x = hs.solve(rp, ci14, a, b, ctx=ctx)
+        assert (ctx.info().ku, ctx.info().kl, ctx.info().block) == (14, 10, 16)
+        assert oracle.residual(rp, ci14, a, x, b).max() <= RES_TOL
+        # bandwidth 60: another tile class -> a new plan, same answer quality
+        ci60 = ci.copy()
+        ci60[rp[1] - 1] = 60
+        x = hs.solve(rp, ci60, a, b, ctx=ctx)
+        assert (ctx.info().ku, ctx.info().block) == (60, 64)
+        assert oracle.residual(rp, ci60, a, x, b).max() <= RES_TOL
+        hs.solve(rp, ci60, a, b, ctx=ctx)  # reuse that plan
+        # invalid CSR with the reused shape: rejected, not misread
+        for bad_ci, bad_rp in ((ci60.copy(), rp), (ci60.copy(), rp.copy())):
+            if bad_rp is rp:
+                bad_ci[100], bad_ci[101] = bad_ci[101], bad_ci[100]  # unsorted row
+            else:
+                bad_ci[7] = n + 5  # column out of range
+            with pytest.raises(hs.SpikeError) as e:
+                hs.solve(bad_rp, bad_ci, a, b, ctx=ctx)
+            assert e.value.name == "csr"
+        bad_rp = rp.copy()
+        bad_rp[500] = len(ci) + 100  # row pointer past nnz
+        with pytest.raises(hs.SpikeError) as e:
+            hs.solve(bad_rp, ci60, a, b, ctx=ctx)
+        assert e.value.name == "csr"
+        x = hs.solve(rp, ci, a, b, ctx=ctx)  # and back to the first matrix
+        assert relerr(x, x1) <= 1e-12
+    finally:
+        ctx.close()
+
+
 def test_bandwidth_above_tile_is_rejected():
     rp, ci, a, xt, b = hs.gen_banded(2000, 130, 130, 1.5, seed=18)
     x = np.zeros_like(b, order="F")
