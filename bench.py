@@ -35,10 +35,11 @@ WORKLOAD = (f"large-band real SPIKE: n={N:,} kl=ku={K_BAND} partitions={P} nrhs=
             f"dominance {DOM}, off-diagonals U[-1,1], seed {SEED}")
 
 
-# DRAM bytes (read + write) per row block of each kernel, from one ncu capture of
-# `bench.py --n 600000 --partitions 300` (profiles/ncu_kernels_n600k_k64.md);
-# traffic per launch = this x the launch's row blocks.
-TRAFFIC_PER_BLOCK = {"factor_fwd": 92_920, "factor_bwd": 77_810, "band_tiles": 158_650, "rhs_sweeps": 49_380}
+# DRAM bytes (read + write) per row block of each kernel family, from one ncu
+# capture of `bench.py --n 600000 --partitions 300` (same 64-row tiles and
+# partition length, CSR larger than L2); traffic per launch = this x the
+# launch's row blocks.
+TRAFFIC_PER_BLOCK = {"factor_fwd": 103_318, "factor_bwd": 107_729, "band_tiles": 158_175, "rhs_sweeps": 48_796}
 
 
 def nnz_of(n, k):
