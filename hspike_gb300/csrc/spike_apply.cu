@@ -21,14 +21,87 @@ namespace {
 constexpr int RC = 32;      // right-hand-side columns per CTA
 constexpr int RCS = RC + 1; // row stride of the shared [KB][RC] vectors (odd: column-wise writes spread over banks)
 
+template <class T> __device__ __forceinline__ T shfl_xor_any(T v, int off)
+{
+    if constexpr (sizeof(T) == 4) {
+        return __shfl_xor_sync(0xffffffffu, v, off);
+    } else {
+        T other;
+        const unsigned *src = (const unsigned *)&v;
+        unsigned *dst = (unsigned *)&other;
+#pragma unroll
+        for (int w = 0; w < (int)(sizeof(T) / 4); w++) dst[w] = __shfl_xor_sync(0xffffffffu, src[w], off);
+        return other;
+    }
+}
+
 // out[r][h] = sign * sum_k M[r][k] v[k][h] (+ base[r][h]), r < KB, h < nr.
 // Mt: shared tile holding M transposed (the factor tiles are column-major in
 // global memory); v, base, out: shared [KB][RC] vectors with row stride RCS.
+// Four or more columns: each thread accumulates a 4 x 4 block (4 rows of M
+// by one 16-byte load, 4 columns of v) over a slice of k, so a step moves
+// 0.5 shared-memory words per FMA instead of 2; the k slices of a block are
+// summed by shuffles.  Fewer columns: one output per lane group, k split
+// across the group.
 template <class T, int KB, bool HAS_BASE, int S = RCS>
 __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, bool negate)
 {
     constexpr int NT = NTOf<KB>::value;
     constexpr int LD = TileLD<T, KB>::value;
+    // (FP32 arithmetic only: the shuffle sums of the k slices would add FP64
+    // work on GB300's slow FP64 pipe; and only where most threads stay busy)
+    if constexpr (KB >= 8 && (std::is_same<T, float>::value || std::is_same<T, cfloat>::value)) {
+      constexpr int RG = KB / 4; // row groups
+      const int CG = (nr + 3) / 4;
+      if (nr >= 4 && RG * CG * (RG < 8 ? RG : 8) >= NT / 2) {
+        const int units = RG * CG;
+        int spl = 1;
+        while (spl < 8 && spl * 2 * units <= NT && spl * 2 <= RG) spl *= 2;
+        const int tid = threadIdx.x;
+        const int part = tid & (spl - 1);
+        const int groups = NT / spl;
+        const int iters = (units + groups - 1) / groups;
+        for (int it = 0; it < iters; it++) {
+            const int u = it * groups + tid / spl;
+            const bool valid = u < units;
+            const int uu = valid ? u : 0;
+            const int r0 = (uu % RG) * 4, h0 = (uu / RG) * 4;
+            T acc[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[i][c] = sc_zero<T>();
+            for (int k = part; k < KB; k += spl) {
+                T m[4], w[4];
+                vld<T, 4>(m, Mt + k * LD + r0);
+#pragma unroll
+                for (int c = 0; c < 4; c++) w[c] = h0 + c < nr ? v[k * S + h0 + c] : sc_zero<T>();
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[i][c] = madd(acc[i][c], m[i], w[c]);
+            }
+            for (int off = spl >> 1; off > 0; off >>= 1)
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[i][c] = acc[i][c] + shfl_xor_any(acc[i][c], off);
+            if (valid && part == 0) {
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        if (h0 + c < nr) {
+                            const int q = (r0 + i) * S + h0 + c;
+                            T val = negate ? -acc[i][c] : acc[i][c];
+                            if (HAS_BASE) val = base[q] + val;
+                            out[q] = val;
+                        }
+            }
+        }
+        return;
+      }
+    }
     const int O = KB * nr;
     int spl = 1;
     while (spl < 32 && spl * 2 * O <= NT && spl * 2 <= KB) spl *= 2;
