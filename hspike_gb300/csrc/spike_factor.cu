@@ -197,11 +197,11 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
                  const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
                  const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
                  unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys, int twist,
-                 int validate, int n, long long nnz)
+                 int validate, int n, long long nnz, int gb0, int nb_total)
 {
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
-    const int gb = blockIdx.x;
+    const int gb = blockIdx.x + gb0; // this launch covers blocks [gb0, gb0 + gridDim.x)
     const int part = blk_part[gb];
     const int J = gb - blk_off[part];
     const int M = twist ? (blk_off[part + 1] - blk_off[part]) / 2 : 1 << 30; // middle block
@@ -232,8 +232,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     if (validate) {
         scatter_block<T, H, KB, LD1, true>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
                                            err, srp, n, nnz);
-        if (threadIdx.x == 0 && ((gb == 0 && rowptr[0] != 0) ||
-                                 (gb == (int)gridDim.x - 1 && (long long)rowptr[n] != nnz)))
+        if (threadIdx.x == 0 && ((gb == 0 && rowptr[0] != 0) || (gb == nb_total - 1 && (long long)rowptr[n] != nnz)))
             atomicOr(err, SPK_DEV_ERR_CSR);
     } else {
         scatter_block<T, H, KB, LD1, false>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
@@ -851,6 +850,44 @@ __global__ void k_tips(const int *__restrict__ part_start, const int *__restrict
     }
 }
 
+template <class T, int KB> int run_tips(spk_plan *P, cudaStream_t st)
+{
+    using H = typename HighOf<T>::type;
+    if (P->n_iface <= 0) return SPK_OK;
+    k_tips<T, KB><<<P->n_iface, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_V,
+                                              (const T *)P->d_W, (H *)P->d_RP, (H *)P->d_RQ, (H *)P->d_RX,
+                                              (H *)P->d_RY);
+    SPK_CHECK_LAUNCH();
+    P->launches++;
+    return SPK_OK;
+}
+
+// Partitions [part0, part1) of a two-sided plan: their band tiles (the rows'
+// CSR entries must be on the device), both chains, the spikes' sweeps, the
+// middle blocks and the back substitution.  The tips follow once every range
+// is done.  The kernel attributes are set by a full run_factor first.
+template <class T, int KB> int run_factor_range(spk_plan *P, const int *rowptr, const int *colind, const void *aij,
+                                                int part0, int part1, cudaStream_t st)
+{
+    using H = typename HighOf<T>::type;
+    using S = FactorSmem<T, KB>;
+    constexpr int NT = NTOf<KB>::value;
+    if (!P->twist || part0 < 0 || part1 > P->p || part0 >= part1) return SPK_EARG;
+    const size_t TS = (size_t)KB * KB;
+    const int b0 = P->blk_off[part0], b1 = P->blk_off[part1];
+    if (cudaMemsetAsync((T *)P->d_Bhat + (size_t)part0 * TS, 0, sizeof(T) * TS * (part1 - part0), st) != cudaSuccess)
+        return SPK_ECUDA;
+    k_band_tiles<T, KB><<<b1 - b0, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off,
+                                                      P->d_blk_part, (T *)P->d_T, (T *)P->d_E, (T *)P->d_W,
+                                                      (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist,
+                                                      P->validate && !P->d_sys, P->n, P->nnz, b0, P->total_blocks);
+    SPK_CHECK_LAUNCH();
+    P->launches++;
+    int rc = spk_twist_factor(P, 1, part0, part1, st);
+    if (rc == SPK_OK) rc = spk_twist_factor(P, 0, part0, part1, st);
+    return rc;
+}
+
 template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const int *colind, const void *aij,
                                           cudaStream_t st)
 {
@@ -894,25 +931,21 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
                                                               P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
                                                               (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys,
                                                               P->d_part_sys, P->twist, P->validate && !P->d_sys,
-                                                              P->n, P->nnz);
+                                                              P->n, P->nnz, 0, P->total_blocks);
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
     if (P->twist) { // two-sided chains (spike_twist.cu)
         P->launches++;  // k_band_tiles
         spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
-        int rc = spk_twist_factor(P, 1, st);
+        int rc = spk_twist_factor(P, 1, 0, P->p, st);
         spk_phase_end(P, st);
         if (rc != SPK_OK || P->p < 2) return rc;
         spk_phase_begin(P, SPK_PH_FACTOR_BWD, st);
-        rc = spk_twist_factor(P, 0, st);
+        rc = spk_twist_factor(P, 0, 0, P->p, st);
         if (rc != SPK_OK) return rc;
-        k_tips<T, KB><<<P->n_iface, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_V,
-                                                  (const T *)P->d_W, (H *)P->d_RP, (H *)P->d_RQ, (H *)P->d_RX,
-                                                  (H *)P->d_RY);
-        SPK_CHECK_LAUNCH();
+        rc = run_tips<T, KB>(P, st);
         spk_phase_end(P, st);
-        P->launches++;
-        return SPK_OK;
+        return rc;
     }
     spk_phase_begin(P, SPK_PH_FACTOR_FWD, st);
     if constexpr (S::BIG) {
@@ -981,6 +1014,31 @@ template <class T> int dispatch_factor(spk_plan *P, const int *rp, const int *ci
     }
 }
 
+template <class T> int dispatch_range(spk_plan *P, const int *rp, const int *ci, const void *a, int p0, int p1,
+                                     cudaStream_t st)
+{
+    switch (P->KB) {
+    case 16: return run_factor_range<T, 16>(P, rp, ci, a, p0, p1, st);
+    case 32: return run_factor_range<T, 32>(P, rp, ci, a, p0, p1, st);
+    case 64:
+        if constexpr (sizeof(T) <= 8) return run_factor_range<T, 64>(P, rp, ci, a, p0, p1, st);
+        else return SPK_EBAND;
+    default: return SPK_EARG;
+    }
+}
+
+template <class T> int dispatch_tips(spk_plan *P, cudaStream_t st)
+{
+    switch (P->KB) {
+    case 16: return run_tips<T, 16>(P, st);
+    case 32: return run_tips<T, 32>(P, st);
+    case 64:
+        if constexpr (sizeof(T) <= 8) return run_tips<T, 64>(P, st);
+        else return SPK_EBAND;
+    default: return SPK_EARG;
+    }
+}
+
 template <class T> size_t smem_for(int KB)
 {
     switch (KB) {
@@ -1005,6 +1063,24 @@ extern "C" size_t spk_factor_smem(int KB, int is_complex, int mode)
 {
     if (is_complex) return mode == SPK_MIXED ? smem_for<cfloat>(KB) : smem_for<cdouble>(KB);
     return mode == SPK_MIXED ? smem_for<float>(KB) : smem_for<double>(KB);
+}
+
+extern "C" int spk_factor_range(spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij, int part0,
+                                int part1, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (P->is_complex)
+        return P->mode == SPK_MIXED ? dispatch_range<cfloat>(P, d_rowptr, d_colind, d_aij, part0, part1, st)
+                                    : dispatch_range<cdouble>(P, d_rowptr, d_colind, d_aij, part0, part1, st);
+    return P->mode == SPK_MIXED ? dispatch_range<float>(P, d_rowptr, d_colind, d_aij, part0, part1, st)
+                                : dispatch_range<double>(P, d_rowptr, d_colind, d_aij, part0, part1, st);
+}
+
+extern "C" int spk_factor_tips(spk_plan *P, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    if (P->is_complex) return P->mode == SPK_MIXED ? dispatch_tips<cfloat>(P, st) : dispatch_tips<cdouble>(P, st);
+    return P->mode == SPK_MIXED ? dispatch_tips<float>(P, st) : dispatch_tips<double>(P, st);
 }
 
 extern "C" int spk_factor(spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij, void *stream)

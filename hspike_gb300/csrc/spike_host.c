@@ -141,6 +141,9 @@ static void ctx_free(spike_context_t c)
     spk_free_on(c->d_stage, as);
     if (c->stream) spk_stream_sync(c->stream);
     spk_stream_destroy(c->own_stream);
+    if (c->copy_stream) spk_stream_destroy(c->copy_stream);
+    for (int i = 0; i < 4; i++)
+        if (c->range_streams[i]) spk_stream_destroy(c->range_streams[i]);
     if (t_default == c) t_default = NULL;
     free(c);
 }
@@ -759,6 +762,90 @@ Error_t spike_zsolve(spike_context_t ctx, integer_t n, integer_t nnz, integer_t 
     return solve_on(ctx, SPK_Z, "spike_zsolve", n, nnz, nrhs, colind, rowptr, aij, x, b);
 }
 
+/* Host arrays, plan reused (same shape as the previous call on the context)
+ * and two-sided: the matrix goes to the device in partition ranges on a copy
+ * stream, and each range's band tiles and chains start as soon as its rows
+ * have arrived, so the factorization hides behind the copy (host -> device
+ * copies are the larger part of such a call).  Returns SPK_EARG when the
+ * path does not apply; the caller then copies everything and solves. */
+#define PIPE_RANGES 8
+static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, const int *colind, const int *rowptr,
+                          const void *aij, const void *b, int cplx, refine_opts *o, long long *launches)
+{
+    spk_plan *Q = c->plan;
+    const int chunk = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
+    if (!Q || Q->n != n || Q->nnz != nnz || Q->is_complex != cplx || Q->mode != c->mode || !Q->twist_cap || !c->twist ||
+        Q->p != choose_partitions(n, Q->KB, c->partitions) || chunk > Q->nrhs_max || Q->p < PIPE_RANGES ||
+        nnz < (8LL << 20) || c->timing)
+        return SPK_EARG;
+    /* the ranges' entry bounds come from the caller's row pointers */
+    long long tb[PIPE_RANGES + 1];
+    for (int r = 0; r <= PIPE_RANGES; r++) {
+        const int prt = (int)((long long)Q->p * r / PIPE_RANGES);
+        tb[r] = rowptr[Q->part_start[prt]];
+        if (tb[r] < 0 || tb[r] > nnz || (r > 0 && tb[r] < tb[r - 1])) return SPK_EARG;
+    }
+    if (tb[0] != 0 || tb[PIPE_RANGES] != nnz) return SPK_EARG;
+    const size_t hs = (cplx ? 2 : 1) * 8;
+    if (!c->copy_stream) TRY(spk_stream_create(&c->copy_stream));
+    for (int i = 0; i < 4; i++)
+        if (!c->range_streams[i]) TRY(spk_stream_create(&c->range_streams[i]));
+    void *cs = c->copy_stream;
+    TRY(spk_stream_fork(c->stream, cs)); /* after whatever the caller queued on the context's stream */
+    TRY(spk_memcpy_h2d(c->d_rowptr, rowptr, sizeof(int) * ((size_t)n + 1), cs));
+    TRY(spk_memcpy_h2d(c->d_b, b, hs * (size_t)n * nrhs, cs));
+    TRY(ensure(&c->d_r, &c->c_r, hs * (size_t)n * chunk, spk_ctx_astream(c)));
+    Q->twist = 1;
+    Q->launches = 0;
+    Q->timing = 0;
+    Q->validate = 1;
+    int rc = spk_memset(Q->d_err, 0, sizeof(unsigned) * 4, c->stream);
+    if (rc == SPK_OK) rc = spk_stream_fork(c->stream, cs); /* the cleared error word before any range */
+    /* ranges are factored on a few streams at once: one range's chains use a
+     * fraction of the GPU */
+    for (int r = 0; r < PIPE_RANGES && rc == SPK_OK; r++) {
+        const int p0 = (int)((long long)Q->p * r / PIPE_RANGES), p1 = (int)((long long)Q->p * (r + 1) / PIPE_RANGES);
+        const size_t e0 = (size_t)tb[r], ne = (size_t)(tb[r + 1] - tb[r]);
+        void *rs = c->range_streams[r % 4];
+        if (ne) {
+            rc = spk_memcpy_h2d((int *)c->d_colind + e0, colind + e0, sizeof(int) * ne, cs);
+            if (rc == SPK_OK) rc = spk_memcpy_h2d((char *)c->d_aij + hs * e0, (const char *)aij + hs * e0, hs * ne, cs);
+        }
+        if (rc == SPK_OK) rc = spk_stream_fork(cs, rs);
+        if (rc == SPK_OK)
+            rc = spk_factor_range(Q, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, p0, p1, rs);
+    }
+    for (int i = 0; i < 4 && rc == SPK_OK; i++) rc = spk_stream_fork(c->range_streams[i], c->stream);
+    if (rc == SPK_OK) rc = spk_stream_fork(cs, c->stream);
+    if (rc == SPK_OK) rc = spk_factor_tips(Q, c->stream);
+    if (rc == SPK_OK) rc = spk_reduced_factor(Q, c->stream);
+    Q->validate = 0;
+    unsigned e[4] = {0, 0, 0, 0};
+    if (rc == SPK_OK) {
+        const int frc = check_device_error(Q, c->stream, e);
+        const int ku = (int)e[1], kl = (int)e[2], kmax = ku > kl ? ku : kl;
+        const int same =
+            !(e[0] & (SPK_DEV_ERR_CSR | SPK_DEV_ERR_BAND)) && spk_choose_block(kmax < 1 ? 1 : kmax) == Q->KB;
+        if (!same) {
+            /* the whole matrix is on the device now: the general path re-plans */
+            long long l2 = 0;
+            rc = run_device(c, n, nnz, nrhs, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, c->d_x,
+                            c->d_b, cplx, o, &l2);
+            *launches = Q->launches + l2;
+            return rc;
+        }
+        Q->ku = ku;
+        Q->kl = kl;
+        rc = frc;
+    }
+    if (rc == SPK_OK)
+        rc = solve_all(Q, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, c->d_x, c->d_b, c->d_r, nrhs, o,
+                       c->stream);
+    *launches = Q->launches;
+    fill_info(c, Q, o, Q->launches);
+    return rc;
+}
+
 Error_t spk_host_solve_ctx(spike_context_t c, int dtype, const char *name, integer_t n, integer_t nnz, integer_t nrhs,
                            const integer_t *colind, const integer_t *rowptr, const void *aij, void *x, const void *b)
 {
@@ -782,6 +869,23 @@ Error_t spk_host_solve_ctx(spike_context_t c, int dtype, const char *name, integ
     }
     if (rc != SPK_OK) return finish(rc, name, &o);
     long long launches = 0;
+    if (!wide) {
+        long long lp = 0;
+        rc = host_pipelined(c, n, nnz, nrhs, colind, rowptr, aij, b, cplx, &o, &lp);
+        if (rc != SPK_EARG) { /* the pipelined path ran (to success or a real error) */
+            launches += lp;
+            if (rc == SPK_OK || rc == SPK_ECONV) {
+                int rc2 = spk_memcpy_d2h(x, c->d_x, es * nb, c->stream);
+                if (rc2 == SPK_OK) rc2 = spk_stream_sync(c->stream);
+                if (rc2 != SPK_OK) rc = rc2;
+            } else {
+                spk_stream_sync(c->stream);
+            }
+            c->info.kernel_launches = launches;
+            return finish(rc, name, &o);
+        }
+        rc = SPK_OK;
+    }
     rc = spk_memcpy_h2d(c->d_rowptr, rowptr, sizeof(int) * ((size_t)n + 1), c->stream);
     if (rc == SPK_OK && nnz) rc = spk_memcpy_h2d(c->d_colind, colind, sizeof(int) * (size_t)nnz, c->stream);
     if (wide) {

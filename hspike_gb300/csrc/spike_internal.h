@@ -218,9 +218,17 @@ size_t spk_factor_smem(int KB, int is_complex, int mode);
 /* ---- two-sided partition factorization (spike_twist.cu) ---- */
 /* 1 if the two-sided kernels exist for this tile size and precision */
 int spk_twist_supported(int KB, int is_complex, int mode);
-/* forward = 1: both elimination chains, the spikes' forward sweeps and the
- * middle block; forward = 0: the spikes' back substitution */
-int spk_twist_factor(spk_plan *P, int forward, void *stream);
+/* Partitions [part0, part1): forward = 1: both elimination chains, the
+ * spikes' forward sweeps and the middle block; forward = 0: the spikes' back
+ * substitution */
+int spk_twist_factor(spk_plan *P, int forward, int part0, int part1, void *stream);
+/* The factorization of a two-sided plan in pieces, for copies that arrive in
+ * partition ranges: band tiles, chains and back substitution of partitions
+ * [part0, part1) (their CSR rows must be on the device), then, after the
+ * last range, the tips. */
+int spk_factor_range(spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij, int part0, int part1,
+                     void *stream);
+int spk_factor_tips(spk_plan *P, void *stream);
 
 /* ---- reduced system (spike_reduced.cu) ---- */
 int spk_reduced_factor(spk_plan *P, void *stream);

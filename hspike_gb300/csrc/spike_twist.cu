@@ -63,12 +63,12 @@ template <class TL, class Reg> __device__ __forceinline__ void rcopy(Reg &d, con
 
 template <class T, int KB>
 __global__ void __launch_bounds__(NTOf<KB>::value, 4)
-    k_tw_lu(const T *__restrict__ gT, const int *__restrict__ blk_off, T *gL, T *gG, T *gE, unsigned *err)
+    k_tw_lu(const T *__restrict__ gT, const int *__restrict__ blk_off, T *gL, T *gG, T *gE, unsigned *err, int part0)
 {
     constexpr int NT = NTOf<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
-    const int part = blockIdx.x;
+    const int part = blockIdx.x + part0;
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
     const size_t tb = (size_t)blk_off[part] * TS;
     const T *gTp = gT + (size_t)blk_off[part] * 3 * TS; // per block: D, A(J,J-1), A(J,J+1)
@@ -171,12 +171,12 @@ __device__ __forceinline__ void bhat_block(const TL &t, typename TL::Reg &a, con
 template <class T, int KB>
 __global__ void __launch_bounds__(TwNT<KB>::value, 4)
     k_tw_sweep(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
-               const T *__restrict__ gE, const T *__restrict__ gBhat, T *gV, T *gW)
+               const T *__restrict__ gE, const T *__restrict__ gBhat, T *gV, T *gW, int part0)
 {
     constexpr int NT = TwNT<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
-    const int part = blockIdx.x;
+    const int part = blockIdx.x + part0;
     const bool top = blockIdx.y == 0;
     if (top ? part == 0 : part == p - 1) return; // the whole CTA: no such spike
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
@@ -237,12 +237,12 @@ __global__ void __launch_bounds__(TwNT<KB>::value, 4)
 template <class T, int KB>
 __global__ void __launch_bounds__(NTOf<KB>::value, 4)
     k_tw_merge(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gV, T *gW,
-               unsigned *err)
+               unsigned *err, int part0)
 {
     constexpr int NT = NTOf<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
-    const int part = blockIdx.x;
+    const int part = blockIdx.x + part0;
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
     const size_t tb = (size_t)blk_off[part] * TS;
     const T *gTp = gT + (size_t)blk_off[part] * 3 * TS;
@@ -309,12 +309,12 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
 template <class T, int KB>
 __global__ void __launch_bounds__(TwNT<KB>::value, 4)
     k_tw_bwd(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE, T *gV,
-             T *gW)
+             T *gW, int part0)
 {
     constexpr int NT = TwNT<KB>::value;
     using TL = Tile<T, KB, NT>;
     constexpr size_t TS = (size_t)KB * KB;
-    const int part = blockIdx.x, which = blockIdx.y;
+    const int part = blockIdx.x + part0, which = blockIdx.y;
     const bool isV = which >= 2, top = (which & 1) == 0;
     if (isV ? part == p - 1 : part == 0) return; // the whole CTA: no such spike
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
@@ -368,7 +368,9 @@ __global__ void __launch_bounds__(TwNT<KB>::value, 4)
     }
 }
 
-template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd)
+// Partitions [part0, part1): the forward part (both elimination chains, the
+// spikes' forward sweeps, the middle block) or the back substitution.
+template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd, int part0, int part1)
 {
     if constexpr (!TwistFits<T, KB>::ok) {
         return SPK_EBAND;
@@ -388,27 +390,29 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd)
                 return SPK_ECUDA;
             attr = true;
         }
-        const int p = P->p;
+        const int p = P->p, np = part1 - part0;
+        if (np <= 0) return SPK_OK;
         if (fwd) {
-            k_tw_lu<T, KB><<<dim3(p, 2), NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
-                                                               (T *)P->d_G, (T *)P->d_E, P->d_err);
+            k_tw_lu<T, KB><<<dim3(np, 2), NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+                                                                           (T *)P->d_G, (T *)P->d_E, P->d_err, part0);
             SPK_CHECK_LAUNCH();
             P->launches++;
             if (p > 1) {
-                k_tw_sweep<T, KB><<<dim3(p, 2), NT, C::smem, st>>>(P->d_part_start, P->d_blk_off, p,
-                                                                      (const T *)P->d_L, (const T *)P->d_E,
-                                                                      (const T *)P->d_Bhat, (T *)P->d_V,
-                                                                      (T *)P->d_W);
+                k_tw_sweep<T, KB><<<dim3(np, 2), NT, C::smem, st>>>(P->d_part_start, P->d_blk_off, p,
+                                                                    (const T *)P->d_L, (const T *)P->d_E,
+                                                                    (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W,
+                                                                    part0);
                 SPK_CHECK_LAUNCH();
                 P->launches++;
             }
-            k_tw_merge<T, KB><<<p, NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
-                                                         (T *)P->d_G, (T *)P->d_V, (T *)P->d_W, P->d_err);
+            k_tw_merge<T, KB><<<np, NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
+                                                                    (T *)P->d_G, (T *)P->d_V, (T *)P->d_W, P->d_err,
+                                                                    part0);
             SPK_CHECK_LAUNCH();
             P->launches++;
         } else if (p > 1) {
-            k_tw_bwd<T, KB><<<dim3(p, 4), NT, C::smem, st>>>(P->d_blk_off, p, (const T *)P->d_G,
-                                                                (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W);
+            k_tw_bwd<T, KB><<<dim3(np, 4), NT, C::smem, st>>>(P->d_blk_off, p, (const T *)P->d_G, (const T *)P->d_E,
+                                                              (T *)P->d_V, (T *)P->d_W, part0);
             SPK_CHECK_LAUNCH();
             P->launches++;
         }
@@ -416,12 +420,12 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd)
     }
 }
 
-template <class T> int disp_twist(spk_plan *P, cudaStream_t st, bool fwd)
+template <class T> int disp_twist(spk_plan *P, cudaStream_t st, bool fwd, int part0, int part1)
 {
     switch (P->KB) {
-    case 16: return run_twist<T, 16>(P, st, fwd);
-    case 32: return run_twist<T, 32>(P, st, fwd);
-    case 64: return run_twist<T, 64>(P, st, fwd);
+    case 16: return run_twist<T, 16>(P, st, fwd, part0, part1);
+    case 32: return run_twist<T, 32>(P, st, fwd, part0, part1);
+    case 64: return run_twist<T, 64>(P, st, fwd, part0, part1);
     default: return SPK_EBAND;
     }
 }
@@ -444,10 +448,12 @@ extern "C" int spk_twist_supported(int KB, int is_complex, int mode)
     return mode == SPK_MIXED ? twist_ok<float>(KB) : twist_ok<double>(KB);
 }
 
-extern "C" int spk_twist_factor(spk_plan *P, int forward, void *stream)
+extern "C" int spk_twist_factor(spk_plan *P, int forward, int part0, int part1, void *stream)
 {
     cudaStream_t st = (cudaStream_t)stream;
     const bool f = forward != 0;
-    if (P->is_complex) return P->mode == SPK_MIXED ? disp_twist<cfloat>(P, st, f) : disp_twist<cdouble>(P, st, f);
-    return P->mode == SPK_MIXED ? disp_twist<float>(P, st, f) : disp_twist<double>(P, st, f);
+    if (P->is_complex)
+        return P->mode == SPK_MIXED ? disp_twist<cfloat>(P, st, f, part0, part1)
+                                    : disp_twist<cdouble>(P, st, f, part0, part1);
+    return P->mode == SPK_MIXED ? disp_twist<float>(P, st, f, part0, part1) : disp_twist<double>(P, st, f, part0, part1);
 }

@@ -359,6 +359,44 @@ def test_reused_plan_validates_each_call():
         ctx.close()
 
 
+def test_host_arrays_copy_overlaps_factorization():
+    # a reference-API call with host arrays and the previous call's shape sends
+    # the matrix in partition ranges while each range's factorization runs
+    ctx = hs.Context()
+    try:
+        n = 220000
+        rp, ci, a, xt, b = hs.gen_banded(n, 32, 32, 1.5, seed=31, nrhs=2)
+        assert len(ci) >= 8 << 20
+        x1 = hs.solve(rp, ci, a, b, ctx=ctx)      # plans
+        x2 = hs.solve(rp, ci, a, b, ctx=ctx)      # copies overlap the factorization
+        assert ctx.info().twisted == 1
+        assert relerr(x2, x1) <= 1e-13
+        assert oracle.residual(rp, ci, a, x2, b).max() <= RES_TOL
+        assert relerr(x2, xt) <= 1e-10
+        # a new band class with the same shape: the call re-plans after the copy
+        ci60 = ci.copy()
+        ci60[rp[1] - 1] = 60
+        x = hs.solve(rp, ci60, a, b, ctx=ctx)
+        assert ctx.info().block == 64
+        assert oracle.residual(rp, ci60, a, x, b).max() <= RES_TOL
+        hs.solve(rp, ci60, a, b, ctx=ctx)
+        # invalid CSR with the reused shape
+        bad = ci60.copy()
+        bad[1000], bad[1001] = bad[1001], bad[1000]
+        with pytest.raises(hs.SpikeError) as e:
+            hs.solve(rp, bad, a, b, ctx=ctx)
+        assert e.value.name == "csr"
+        badp = rp.copy()
+        badp[n // 2] = len(ci) + 7
+        with pytest.raises(hs.SpikeError) as e:
+            hs.solve(badp, ci60, a, b, ctx=ctx)
+        assert e.value.name == "csr"
+        x = hs.solve(rp, ci60, a, b, ctx=ctx)
+        assert oracle.residual(rp, ci60, a, x, b).max() <= RES_TOL
+    finally:
+        ctx.close()
+
+
 def test_bandwidth_above_tile_is_rejected():
     rp, ci, a, xt, b = hs.gen_banded(2000, 130, 130, 1.5, seed=18)
     x = np.zeros_like(b, order="F")
