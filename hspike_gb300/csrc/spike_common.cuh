@@ -227,6 +227,7 @@ template <class T, int KB, int NT> struct Tile {
 
     int tx, ty;
     int wr0, wr1; // rows [wr0, wr1) of the tile are owned by this thread's warp
+    int wc0, wc1; // and columns [wc0, wc1)
     bool act;
     __device__ __forceinline__ Tile(int tid)
     {
@@ -238,11 +239,15 @@ template <class T, int KB, int NT> struct Tile {
             ty = (warp / WPR) * WY + (lane / WX);
             wr0 = (warp / WPR) * WY * TR;
             wr1 = wr0 + WY * TR;
+            wc0 = (warp % WPR) * WX * TC;
+            wc1 = wc0 + WX * TC;
         } else {
             tx = tid % TX;
             ty = tid / TX;
             wr0 = ((tid & ~31) / TX) * TR;          // first row of the warp
             wr1 = ((tid | 31) / TX) * TR + TR;      // one past its last row
+            wc0 = 0;
+            wc1 = KB;
         }
         if (wr1 > KB) wr1 = KB;
     }
@@ -338,14 +343,15 @@ template <class T, int KB, int NT> struct Tile {
         }
     }
     // acc (+|-)= A * B with A given transposed (At, column-major): vector fetches.
-    // TRI = 1: A is upper triangular, TRI = 2: lower triangular -- the k range
-    // where the warp's rows of A are zero is skipped (warp-uniform bounds, so
-    // only exact zeros are left out and the result is unchanged).
+    // TRI = 1: A is upper triangular, 2: A lower triangular, 3: B lower
+    // triangular, 4: B upper triangular -- the k range where the warp's rows
+    // of A (columns of B) are zero is skipped (warp-uniform bounds, so only
+    // exact zeros are left out and the result is unchanged).
     template <bool SUB, int TRI = 0> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
     {
         if (!act) return;
-        const int k0 = TRI == 1 ? wr0 : 0;
-        const int k1 = TRI == 2 ? wr1 : KB;
+        const int k0 = TRI == 1 ? wr0 : TRI == 3 ? wc0 : 0;
+        const int k1 = TRI == 2 ? wr1 : TRI == 4 ? wc1 : KB;
 #pragma unroll 4
         for (int k = k0; k < k1; k++) {
             T a[TR], b[TC];
@@ -367,6 +373,9 @@ template <class T, int KB, int NT> struct Tile {
     // A lower triangular (acc += A B) / upper triangular (acc -= A B)
     __device__ __forceinline__ void mma_tl(Reg &acc, const T *At, const T *B) const { mm_tA<false, 2>(acc, At, B); }
     __device__ __forceinline__ void mms_tu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 1>(acc, At, B); }
+    // acc -= A B with B lower / upper triangular
+    __device__ __forceinline__ void mms_t_bl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 3>(acc, At, B); }
+    __device__ __forceinline__ void mms_t_bu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 4>(acc, At, B); }
 
     // In-place Gauss-Jordan inverse of the register tile, no pivoting (the
     // diagonal blocks of a diagonally dominant A stay diagonally dominant

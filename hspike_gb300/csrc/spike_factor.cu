@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
             __syncthreads();
             // S_J = D_J - L_J E_{J-1};  z_J = -L_J z_{J-1}
             t.rload(acc, sD);
-            t.mms_t(acc, sF, sEp);
+            t.mms_t_bl(acc, sF, sEp); // E_{J-1} = A(J-1, J) is lower triangular
             if (doW) {
                 t.rzero(accZ);
                 t.mms_t(accZ, sF, sZ);
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
             for (int i = 0; i < TL::TR; i++)
 #pragma unroll
                 for (int j = 0; j < TL::TC; j++) acc[i][j] = dreg[i][j];
-            t.mms_t(acc, sF, sE);
+            t.mms_t_bl(acc, sF, sE); // A(J-1, J) is lower triangular
             __syncthreads(); // sF, sE and sG are free from here on
             cp_async_tile<T, KB, NT>(sE, gTp + (size_t)J * 3 * TS + 2 * TS); // E_J
             if (J + 1 < N) cp_async_tile<T, KB, NT>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
                 t.gstore_t(gL + tb + J * TS, acc);
                 __syncthreads();
                 rcopy<TL>(acc, dreg);
-                t.mms_t(acc, sF, sE); // S_J = D_J - L_J A(J-1,J)
+                t.mms_t_bl(acc, sF, sE); // S_J = D_J - L_J A(J-1,J); A(J-1,J) is lower triangular
                 __syncthreads();
                 cp_async_tile<T, KB, NT>(sE, gTp + (size_t)J * 3 * TS + 2 * TS);
                 if (J + 1 < M) cp_async_tile<T, KB, NT>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
                 t.gstore_t((J == M ? gE : gL) + tb + J * TS, acc);
                 __syncthreads();
                 rcopy<TL>(acc, dreg);
-                t.mms_t(acc, sY, sX); // T_J = D_J - U_J A(J+1,J)
+                t.mms_t_bu(acc, sY, sX); // T_J = D_J - U_J A(J+1,J); A(J+1,J) is upper triangular
                 if (J == M) {
                     t.gstore(gG + tb + J * TS, acc); // T'_M for k_tw_merge
                     break;
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
     t.gstore_t(gL + tb + M * TS, acc);
     __syncthreads();
     t.gload(acc, gG + tb + M * TS); // T'_M
-    t.mms_t(acc, sC, sB);           // S_M = T'_M - L_M A(M-1,M)
+    t.mms_t_bl(acc, sC, sB);        // S_M = T'_M - L_M A(M-1,M) (lower triangular)
     const bool ok = t.inverse(acc, buf);
     t.rstore_t(sA, acc); // G_M as a left operand
     t.gstore_t(gG + tb + M * TS, acc);
