@@ -692,6 +692,152 @@ __global__ void __launch_bounds__(QuadApply<T, KB>::NT)
 }
 
 // interface unknowns u (FP64 / complex128) -> factor precision
+// Two-sided partitions, KB <= 4 (the factors' layout of spike_twist.cu):
+// chains per (partition, column) and half.  k_qtw_apply_fwd runs the top
+// half's z_J = r_J - L_J z_{J-1} (J < M) and the bottom half's
+// w_J = r_J - U_J w_{J+1} (J >= M) into y; k_qtw_apply_mid forms
+// y_M = G_M (w_M - L_M z_{M-1}); k_qtw_apply_bwd runs y_J = G_J (z_J -
+// A(J,J+1) y_{J+1}) upwards and y_J = H_J (w_J - A(J,J-1) y_{J-1}) downwards.
+template <class T, int KB>
+__global__ void __launch_bounds__(QuadApply<T, KB>::NT)
+    k_qtw_apply_fwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                    const T *__restrict__ gL, const T *__restrict__ gE,
+                    const typename HighOf<T>::type *__restrict__ r, int n, int nrhs, long long NP, T *gy)
+{
+    using H = typename HighOf<T>::type;
+    using C = QuadApply<T, KB>;
+    constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int CT = TS * (int)sizeof(T) / 16;
+    extern __shared__ __align__(16) char smc[];
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int lr = threadIdx.x % KB;
+    const int pc = ch >> 1;
+    const bool bottom = ch & 1;
+    const int part = pc / nrhs, h = pc - part * nrhs;
+    if (part >= p) return; // whole segments; no CTA barriers below
+    const unsigned m = seg_mask<KB>();
+    char *slot = smc + (threadIdx.x / KB) * C::SLOT;
+    const int s = part_start[part], mrows = part_start[part + 1] - s;
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *yh = gy + (size_t)h * NP + (size_t)blk_off[part] * KB;
+    const H *rh = r + (size_t)h * n + s;
+    const int cnt = bottom ? N - M : M;
+    auto blk = [&](int i) { return bottom ? N - 1 - i : i; };
+    auto issue = [&](int i) {
+        if (i < cnt) {
+            const int J = blk(i);
+            char *st = slot + (i % D) * C::STAGE;
+            if (i > 0) { // the coupling tile: L_J above M, U_J below (U_M in gE)
+                const T *cpl = (bottom && J == M ? gE : gL) + tb + (size_t)J * TS;
+                for (int q = lr; q < CT; q += KB) cp_async16(st + 16 * q, (const char *)cpl + 16 * q);
+            }
+            if (J * KB + lr < mrows) cp_async_elem<(int)sizeof(H)>(st + C::VEC + lr * sizeof(H), rh + J * KB + lr);
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int i = 0; i < D - 1; i++) issue(i);
+    T z = sc_zero<T>();
+    for (int i = 0; i < cnt; i++) {
+        const int J = blk(i);
+        issue(i + D - 1);
+        cp_async_wait_n<D - 1>();
+        __syncwarp(m);
+        const char *st = slot + (i % D) * C::STAGE;
+        T v = J * KB + lr < mrows ? sc_cvt<T, H>(*(const H *)(st + C::VEC + lr * sizeof(H))) : sc_zero<T>();
+        if (i > 0) {
+            const T *L = (const T *)st; // column-major
+#pragma unroll
+            for (int c = 0; c < KB; c++) v = msub(v, L[c * KB + lr], seg_shfl<KB>(m, z, c));
+        }
+        __syncwarp(m); // the ring entry may be refilled from here on
+        z = v;
+        yh[(size_t)J * KB + lr] = z;
+    }
+    cp_async_wait_all();
+}
+
+template <class T, int KB>
+__global__ void k_qtw_apply_mid(const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
+                                const T *__restrict__ gG, int nrhs, long long NP, T *gy)
+{
+    constexpr int TS = KB * KB;
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int lr = threadIdx.x % KB;
+    const int part = ch / nrhs, h = ch - part * nrhs;
+    if (part >= p) return; // whole segments
+    const unsigned m = seg_mask<KB>();
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *yh = gy + (size_t)h * NP + (size_t)blk_off[part] * KB;
+    const T zp = yh[(size_t)(M - 1) * KB + lr];
+    T v = yh[(size_t)M * KB + lr]; // w_M
+#pragma unroll
+    for (int c = 0; c < KB; c++) v = msub(v, gL[tb + (size_t)M * TS + c * KB + lr], seg_shfl<KB>(m, zp, c));
+    T y = sc_zero<T>();
+#pragma unroll
+    for (int c = 0; c < KB; c++) y = madd(y, gG[tb + (size_t)M * TS + c * KB + lr], seg_shfl<KB>(m, v, c));
+    yh[(size_t)M * KB + lr] = y;
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(QuadApply<T, KB>::NT)
+    k_qtw_apply_bwd(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE,
+                    int nrhs, long long NP, T *gy)
+{
+    using C = QuadApply<T, KB>;
+    constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int CT = TS * (int)sizeof(T) / 16;
+    extern __shared__ __align__(16) char smc[];
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int lr = threadIdx.x % KB;
+    const int pc = ch >> 1;
+    const bool bottom = ch & 1;
+    const int part = pc / nrhs, h = pc - part * nrhs;
+    if (part >= p) return; // whole segments; no CTA barriers below
+    const unsigned m = seg_mask<KB>();
+    char *slot = smc + (threadIdx.x / KB) * C::SLOT;
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *yh = gy + (size_t)h * NP + (size_t)blk_off[part] * KB;
+    const int cnt = bottom ? N - 1 - M : M;
+    auto blk = [&](int i) { return bottom ? M + 1 + i : M - 1 - i; };
+    auto issue = [&](int i) {
+        if (i < cnt) {
+            const int J = blk(i);
+            char *st = slot + (i % D) * C::STAGE;
+            for (int q = lr; q < CT; q += KB) {
+                cp_async16(st + 16 * q, (const char *)(gG + tb + (size_t)J * TS) + 16 * q);
+                cp_async16(st + TS * sizeof(T) + 16 * q, (const char *)(gE + tb + (size_t)J * TS) + 16 * q);
+            }
+            cp_async_elem<(int)sizeof(T)>(st + C::VEC + lr * sizeof(T), yh + (size_t)J * KB + lr); // own z / w
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int i = 0; i < D - 1; i++) issue(i);
+    T y = yh[(size_t)M * KB + lr]; // y_M
+    for (int i = 0; i < cnt; i++) {
+        const int J = blk(i);
+        issue(i + D - 1);
+        cp_async_wait_n<D - 1>();
+        __syncwarp(m);
+        const char *st = slot + (i % D) * C::STAGE;
+        const T *G = (const T *)st, *E = (const T *)(st + TS * sizeof(T));
+        T t = *(const T *)(st + C::VEC + lr * sizeof(T));
+#pragma unroll
+        for (int c = 0; c < KB; c++) t = msub(t, E[c * KB + lr], seg_shfl<KB>(m, y, c));
+        T acc = sc_zero<T>();
+#pragma unroll
+        for (int c = 0; c < KB; c++) acc = madd(acc, G[c * KB + lr], seg_shfl<KB>(m, t, c));
+        __syncwarp(m);
+        y = acc;
+        yh[(size_t)J * KB + lr] = y;
+    }
+    cp_async_wait_all();
+}
+
 template <class T>
 __global__ void k_u_narrow(const typename HighOf<T>::type *__restrict__ u, T *ut, long long count)
 {
@@ -785,9 +931,42 @@ template <class T, int KB> int run_apply_1(spk_plan *P, const void *r, int nrhs,
     return SPK_OK;
 }
 
+template <class T, int KB> int run_qtw_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
+{
+    using CA = QuadApply<T, KB>;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_qtw_apply_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)CA::SMEM) != cudaSuccess ||
+            cudaFuncSetAttribute(k_qtw_apply_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)CA::SMEM) != cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
+    const long long chains = 2LL * P->p * nrhs;
+    const int cpc = chains_per_cta(chains, CA::CPC);
+    k_qtw_apply_fwd<T, KB><<<(int)((chains + cpc - 1) / cpc), cpc * KB, (size_t)cpc * CA::SLOT, st>>>(
+        P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_E,
+        (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP, (T *)P->d_y);
+    SPK_CHECK_LAUNCH();
+    const long long mch = (long long)P->p * nrhs;
+    k_qtw_apply_mid<T, KB><<<(int)((mch + 31) / 32), 32 * KB, 0, st>>>(P->d_blk_off, P->p, (const T *)P->d_L,
+                                                                       (const T *)P->d_G, nrhs, P->NP, (T *)P->d_y);
+    SPK_CHECK_LAUNCH();
+    k_qtw_apply_bwd<T, KB><<<(int)((chains + cpc - 1) / cpc), cpc * KB, (size_t)cpc * CA::SLOT, st>>>(
+        P->d_blk_off, P->p, (const T *)P->d_G, (const T *)P->d_E, nrhs, P->NP, (T *)P->d_y);
+    SPK_CHECK_LAUNCH();
+    P->launches += 3;
+    return SPK_OK;
+}
+
 template <class T, int KB> int run_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
-    const int rc = P->twist ? run_tw_apply<T, KB>(P, r, nrhs, st) : run_apply_1<T, KB>(P, r, nrhs, st);
+    int rc;
+    if constexpr (KB <= 4)
+        rc = P->twist ? run_qtw_apply<T, KB>(P, r, nrhs, st) : run_apply_1<T, KB>(P, r, nrhs, st);
+    else
+        rc = P->twist ? run_tw_apply<T, KB>(P, r, nrhs, st) : run_apply_1<T, KB>(P, r, nrhs, st);
     if (rc != SPK_OK) return rc;
     if (P->n_iface > 0) {
         k_ytips<T, KB><<<P->n_iface, 128, 0, st>>>(P->d_part_start, P->d_blk_off, (const T *)P->d_y, P->NP, nrhs,

@@ -365,11 +365,12 @@ int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex,
     P->total_blocks = P->blk_off[p];
     P->NP = (long long)P->total_blocks * KB;
     /* two-sided partition solves pay off on long partitions (eight blocks or
-     * more each, so that V's and W's right-hand sides sit in opposite halves) */
+     * more each, so that V's and W's right-hand sides sit in opposite halves);
+     * on KB lanes per chain only while the chains are too few to fill the GPU */
     int min_blocks = 1 << 30;
     for (int i = 0; i < p; i++)
         if (P->blk_off[i + 1] - P->blk_off[i] < min_blocks) min_blocks = P->blk_off[i + 1] - P->blk_off[i];
-    P->twist_cap = spk_twist_supported(KB, is_complex, mode) && min_blocks >= 8;
+    P->twist_cap = spk_twist_supported(KB, is_complex, mode) && min_blocks >= 8 && (KB > 4 || p <= 2048);
     P->twist = P->twist_cap;
 
     /* cyclic-reduction levels of the reduced system */
@@ -776,6 +777,7 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     const int chunk = nrhs < RHS_CHUNK ? nrhs : RHS_CHUNK;
     if (!Q || Q->n != n || Q->nnz != nnz || Q->is_complex != cplx || Q->mode != c->mode || !Q->twist_cap || !c->twist ||
         Q->p != choose_partitions(n, Q->KB, c->partitions) || chunk > Q->nrhs_max || Q->p < PIPE_RANGES ||
+        Q->KB < 16 || Q->KB > 64 ||
         nnz < (8LL << 20) || c->timing)
         return SPK_EARG;
     /* the ranges' entry bounds come from the caller's row pointers */

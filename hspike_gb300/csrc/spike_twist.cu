@@ -368,6 +368,278 @@ __global__ void __launch_bounds__(TwNT<KB>::value, 4)
     }
 }
 
+// ------------------------------------------------------------ small bands
+// KB <= 4: the same two-sided recurrences on KB lanes per chain (lane r owns
+// row r of every tile; the other rows arrive by shuffles), with each chain's
+// next blocks streaming into its own shared-memory ring, as k_quad_fwd /
+// k_quad_bwd.  Here the W forward sweep rides along the top elimination
+// chain and V's forward sweep along the bottom one.
+template <class T, int KB> struct QTw {
+    static constexpr int TS = KB * KB;
+    static constexpr int DEPTH = 4;
+    static constexpr int STAGE = 3 * TS;                             // three tiles per block
+    static constexpr int SLOT = DEPTH * STAGE * (int)sizeof(T) + 16; // per chain
+    static constexpr int CPC = chain_threads(SLOT);                  // chains per CTA
+    static constexpr int NT = CPC * KB;
+    static constexpr size_t SMEM = (size_t)CPC * SLOT;
+};
+
+// chains 2*part (top) and 2*part + 1 (bottom)
+template <class T, int KB>
+__global__ void __launch_bounds__(QTw<T, KB>::NT)
+    k_qtw_lu(const T *__restrict__ gT, const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+             const T *__restrict__ gBhat, T *gL, T *gG, T *gE, T *gV, T *gW, unsigned *err)
+{
+    using C = QTw<T, KB>;
+    constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int CH = C::STAGE * (int)sizeof(T) / 16;
+    extern __shared__ __align__(16) char smc[];
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int r = threadIdx.x % KB;
+    const int part = ch >> 1;
+    const bool bottom = ch & 1;
+    if (part >= p) return; // whole segments leave together; no CTA barriers below
+    const unsigned m = seg_mask<KB>();
+    T *slot = (T *)(smc + (threadIdx.x / KB) * C::SLOT);
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * C::STAGE;
+    const int cnt = bottom ? N - M : M;
+    auto issue = [&](int i) {
+        if (i < cnt) {
+            const int J = bottom ? N - 1 - i : i;
+            for (int q = r; q < CH; q += KB)
+                cp_async16((char *)(slot + (i % D) * C::STAGE) + 16 * q,
+                           (const char *)(gTp + (size_t)J * C::STAGE) + 16 * q);
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int i = 0; i < D - 1; i++) issue(i);
+    bool ok = true;
+    if (!bottom) {
+        // L_J = A(J,J-1) G_{J-1}, S_J = D_J - L_J A(J-1,J), G_J = S_J^{-1}; z_J = -L_J z_{J-1}
+        const bool doW = part > 0;
+        T g[KB], ep[KB], zp[KB];
+#pragma unroll
+        for (int c = 0; c < KB; c++) {
+            g[c] = ep[c] = sc_zero<T>();
+            zp[c] = doW ? gW[tb + r * KB + c] : sc_zero<T>(); // z_0 = C^
+        }
+        for (int J = 0; J < cnt; J++) {
+            issue(J + D - 1);
+            cp_async_wait_n<D - 1>();
+            __syncwarp(m);
+            const T *sc = slot + (J % D) * C::STAGE;
+            T sr[KB];
+#pragma unroll
+            for (int c = 0; c < KB; c++) sr[c] = sc[r * KB + c]; // D_J
+            if (J > 0) {
+                T f[KB], l[KB];
+#pragma unroll
+                for (int c = 0; c < KB; c++) f[c] = sc[TS + c * KB + r]; // row r of A(J,J-1) (column-major)
+                row_mul<T, KB>(m, l, f, g);
+#pragma unroll
+                for (int c = 0; c < KB; c++) gL[tb + (size_t)J * TS + c * KB + r] = l[c];
+                row_msub<T, KB>(m, sr, l, ep);
+                if (doW) {
+                    T z[KB];
+#pragma unroll
+                    for (int c = 0; c < KB; c++) z[c] = sc_zero<T>();
+                    row_msub<T, KB>(m, z, l, zp);
+#pragma unroll
+                    for (int c = 0; c < KB; c++) {
+                        gW[tb + (size_t)J * TS + r * KB + c] = z[c];
+                        zp[c] = z[c];
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < KB; c++) ep[c] = sc[2 * TS + r * KB + c]; // row r of A(J,J+1) (row-major)
+            __syncwarp(m); // the ring entry may be refilled from here on
+            ok = row_inv<T, KB>(m, sr, r) && ok;
+#pragma unroll
+            for (int c = 0; c < KB; c++) {
+                gG[tb + (size_t)J * TS + c * KB + r] = sr[c];
+                g[c] = sr[c];
+            }
+        }
+    } else {
+        // U_J = A(J,J+1) H_{J+1}, T_J = D_J - U_J A(J+1,J), H_J = T_J^{-1}; w_J = r_J - U_J w_{J+1}
+        // with V's right-hand side r = [0; B^] in blocks J0 (rows o..KB-1) and
+        // J0+1 (rows 0..o-1); every partition has >= 8 blocks, so J0 > M
+        const bool doV = part < p - 1;
+        const int mrows = part_start[part + 1] - part_start[part];
+        const int J0 = (mrows - KB) / KB, o = mrows - KB - J0 * KB;
+        const T *B = gBhat + (size_t)part * TS;
+        T h[KB], xn[KB], wp[KB];
+#pragma unroll
+        for (int c = 0; c < KB; c++) h[c] = xn[c] = wp[c] = sc_zero<T>();
+        for (int i = 0; i < cnt; i++) {
+            const int J = N - 1 - i;
+            issue(i + D - 1);
+            cp_async_wait_n<D - 1>();
+            __syncwarp(m);
+            const T *sc = slot + (i % D) * C::STAGE;
+            T sr[KB], rv[KB];
+#pragma unroll
+            for (int c = 0; c < KB; c++) {
+                sr[c] = sc[r * KB + c]; // D_J
+                rv[c] = (J == J0 && r >= o) ? B[(r - o) * KB + c]
+                                            : (o > 0 && J == J0 + 1 && r < o) ? B[(KB - o + r) * KB + c] : sc_zero<T>();
+            }
+            if (i > 0) {
+                T y[KB], u[KB];
+#pragma unroll
+                for (int c = 0; c < KB; c++) y[c] = sc[2 * TS + c * KB + r]; // row r of A(J,J+1) (column-major)
+                row_mul<T, KB>(m, u, y, h);
+                T *gU = (J == M ? gE : gL) + tb + (size_t)J * TS;
+#pragma unroll
+                for (int c = 0; c < KB; c++) gU[c * KB + r] = u[c];
+                row_msub<T, KB>(m, sr, u, xn);
+                if (doV) row_msub<T, KB>(m, rv, u, wp);
+            }
+            if (doV) {
+#pragma unroll
+                for (int c = 0; c < KB; c++) {
+                    gV[tb + (size_t)J * TS + r * KB + c] = rv[c];
+                    wp[c] = rv[c];
+                }
+            }
+            if (J == M) { // T'_M for the middle block, row-major
+#pragma unroll
+                for (int c = 0; c < KB; c++) gG[tb + (size_t)J * TS + r * KB + c] = sr[c];
+                break;
+            }
+#pragma unroll
+            for (int c = 0; c < KB; c++) xn[c] = sc[TS + r * KB + c]; // row r of A(J,J-1) (row-major)
+            __syncwarp(m);
+            ok = row_inv<T, KB>(m, sr, r) && ok;
+#pragma unroll
+            for (int c = 0; c < KB; c++) {
+                gG[tb + (size_t)J * TS + c * KB + r] = sr[c];
+                h[c] = sr[c];
+            }
+        }
+    }
+    cp_async_wait_all();
+    if (!ok && r == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+
+// the middle block of every partition (KB lanes each): L_M, G_M, and X_M of W and V
+template <class T, int KB>
+__global__ void k_qtw_merge(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gV,
+                            T *gW, unsigned *err)
+{
+    constexpr int TS = KB * KB;
+    const int part = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int r = threadIdx.x % KB;
+    if (part >= p) return; // whole segments
+    const unsigned m = seg_mask<KB>();
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * 3 * TS;
+    T f[KB], g[KB], l[KB], sr[KB], ep[KB], zp[KB], w[KB];
+#pragma unroll
+    for (int c = 0; c < KB; c++) {
+        f[c] = gTp[(size_t)M * 3 * TS + TS + c * KB + r];           // row r of A(M,M-1) (column-major)
+        g[c] = gG[tb + (size_t)(M - 1) * TS + c * KB + r];           // row r of G_{M-1}
+        sr[c] = gG[tb + (size_t)M * TS + r * KB + c];                // row r of T'_M (row-major)
+        ep[c] = gTp[(size_t)(M - 1) * 3 * TS + 2 * TS + r * KB + c]; // row r of A(M-1,M) (row-major)
+        zp[c] = part > 0 ? gW[tb + (size_t)(M - 1) * TS + r * KB + c] : sc_zero<T>();
+        w[c] = part < p - 1 ? gV[tb + (size_t)M * TS + r * KB + c] : sc_zero<T>();
+    }
+    row_mul<T, KB>(m, l, f, g); // L_M
+    row_msub<T, KB>(m, sr, l, ep);
+    const bool ok = row_inv<T, KB>(m, sr, r); // G_M
+    __syncwarp(m); // every lane has read its rows of T'_M and w_M before they are overwritten
+#pragma unroll
+    for (int c = 0; c < KB; c++) {
+        gL[tb + (size_t)M * TS + c * KB + r] = l[c];
+        gG[tb + (size_t)M * TS + c * KB + r] = sr[c];
+    }
+    if (part > 0) { // W: z_M = -L_M z_{M-1}, X_M = G_M z_M
+        T z[KB], x[KB];
+#pragma unroll
+        for (int c = 0; c < KB; c++) z[c] = sc_zero<T>();
+        row_msub<T, KB>(m, z, l, zp);
+        row_mul<T, KB>(m, x, sr, z);
+#pragma unroll
+        for (int c = 0; c < KB; c++) gW[tb + (size_t)M * TS + c * KB + r] = x[c];
+    }
+    if (part < p - 1) { // V: X_M = G_M w_M
+        T x[KB];
+        row_mul<T, KB>(m, x, sr, w);
+#pragma unroll
+        for (int c = 0; c < KB; c++) gV[tb + (size_t)M * TS + c * KB + r] = x[c];
+    }
+    if (!ok && r == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+
+// back substitution from X_M outwards; chain 4*part + {0: W top, 1: W bottom,
+// 2: V top, 3: V bottom}; the ring holds G or H, the coupling tile and Z
+template <class T, int KB>
+__global__ void __launch_bounds__(QTw<T, KB>::NT)
+    k_qtw_bwd(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE, T *gV,
+              T *gW)
+{
+    using C = QTw<T, KB>;
+    constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int CT = TS * (int)sizeof(T) / 16;
+    extern __shared__ __align__(16) char smc[];
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int r = threadIdx.x % KB;
+    const int part = ch >> 2, which = ch & 3;
+    const bool isV = which >= 2, top = (which & 1) == 0;
+    if (part >= p || (isV ? part == p - 1 : part == 0)) return; // whole segments
+    const unsigned m = seg_mask<KB>();
+    T *slot = (T *)(smc + (threadIdx.x / KB) * C::SLOT);
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *gX = isV ? gV : gW;
+    const bool hasZ = isV ? !top : top;
+    const int cnt = top ? M : N - 1 - M;
+    auto blk = [&](int i) { return top ? M - 1 - i : M + 1 + i; };
+    auto issue = [&](int i) {
+        if (i < cnt) {
+            const int J = blk(i);
+            char *st = (char *)(slot + (i % D) * C::STAGE);
+            for (int q = r; q < CT; q += KB) {
+                cp_async16(st + 16 * q, (const char *)(gG + tb + (size_t)J * TS) + 16 * q);
+                cp_async16(st + TS * sizeof(T) + 16 * q, (const char *)(gE + tb + (size_t)J * TS) + 16 * q);
+                if (hasZ)
+                    cp_async16(st + 2 * TS * sizeof(T) + 16 * q, (const char *)(gX + tb + (size_t)J * TS) + 16 * q);
+            }
+        }
+        cp_async_commit();
+    };
+#pragma unroll
+    for (int i = 0; i < D - 1; i++) issue(i);
+    T x[KB]; // row r of the previous X (X_M first, column-major in memory)
+#pragma unroll
+    for (int c = 0; c < KB; c++) x[c] = gX[tb + (size_t)M * TS + c * KB + r];
+    for (int i = 0; i < cnt; i++) {
+        const int J = blk(i);
+        issue(i + D - 1);
+        cp_async_wait_n<D - 1>();
+        __syncwarp(m);
+        const T *sc = slot + (i % D) * C::STAGE;
+        T t[KB], e[KB], g[KB];
+#pragma unroll
+        for (int c = 0; c < KB; c++) {
+            t[c] = hasZ ? sc[2 * TS + r * KB + c] : sc_zero<T>();
+            e[c] = sc[TS + c * KB + r]; // row r of the coupling tile (column-major)
+            g[c] = sc[c * KB + r];      // row r of G_J or H_J (column-major)
+        }
+        __syncwarp(m); // the ring entry may be refilled from here on
+        row_msub<T, KB>(m, t, e, x);
+        row_mul<T, KB>(m, x, g, t);
+#pragma unroll
+        for (int c = 0; c < KB; c++) gX[tb + (size_t)J * TS + c * KB + r] = x[c];
+    }
+    cp_async_wait_all();
+}
+
 // Partitions [part0, part1): the forward part (both elimination chains, the
 // spikes' forward sweeps, the middle block) or the back substitution.
 template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd, int part0, int part1)
@@ -420,9 +692,46 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
     }
 }
 
+template <class T, int KB> int run_qtwist(spk_plan *P, cudaStream_t st, bool fwd, int part0, int part1)
+{
+    using C = QTw<T, KB>;
+    if (part0 != 0 || part1 != P->p) return SPK_EARG; // whole plans only
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_qtw_lu<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_qtw_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM) !=
+                cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
+    const int p = P->p;
+    if (fwd) {
+        const int cpc = chains_per_cta(2LL * p, C::CPC);
+        k_qtw_lu<T, KB><<<(2 * p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * C::SLOT, st>>>(
+            (const T *)P->d_T, P->d_part_start, P->d_blk_off, p, (const T *)P->d_Bhat, (T *)P->d_L, (T *)P->d_G,
+            (T *)P->d_E, (T *)P->d_V, (T *)P->d_W, P->d_err);
+        SPK_CHECK_LAUNCH();
+        const int mpc = 32; // chains per CTA of the middle-block kernel
+        k_qtw_merge<T, KB><<<(p + mpc - 1) / mpc, mpc * KB, 0, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
+                                                                     (T *)P->d_G, (T *)P->d_V, (T *)P->d_W, P->d_err);
+        SPK_CHECK_LAUNCH();
+        P->launches += 2;
+    } else if (p > 1) {
+        const int cpc = chains_per_cta(4LL * p, C::CPC);
+        k_qtw_bwd<T, KB><<<(4 * p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * C::SLOT, st>>>(
+            P->d_blk_off, p, (const T *)P->d_G, (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W);
+        SPK_CHECK_LAUNCH();
+        P->launches++;
+    }
+    return SPK_OK;
+}
+
 template <class T> int disp_twist(spk_plan *P, cudaStream_t st, bool fwd, int part0, int part1)
 {
     switch (P->KB) {
+    case 2: return run_qtwist<T, 2>(P, st, fwd, part0, part1);
+    case 4: return run_qtwist<T, 4>(P, st, fwd, part0, part1);
     case 16: return run_twist<T, 16>(P, st, fwd, part0, part1);
     case 32: return run_twist<T, 32>(P, st, fwd, part0, part1);
     case 64: return run_twist<T, 64>(P, st, fwd, part0, part1);
@@ -433,6 +742,8 @@ template <class T> int disp_twist(spk_plan *P, cudaStream_t st, bool fwd, int pa
 template <class T> bool twist_ok(int KB)
 {
     switch (KB) {
+    case 2:
+    case 4: return true; // KB lanes per chain: no shared-memory tiles to fit
     case 16: return TwistFits<T, 16>::ok;
     case 32: return TwistFits<T, 32>::ok;
     case 64: return TwistFits<T, 64>::ok;

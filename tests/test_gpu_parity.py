@@ -124,6 +124,8 @@ CASES_TWIST = [
     (40000, 32, 32, 1.5, 10, 2),
     (30000, 16, 9, 1.5, 12, 17),        # ku != kl, two right-hand-side chunks
     (60000, 20, 20, 1.2, 1, 1),         # one partition
+    (20000, 1, 1, 2.0, 16, 1),          # 2-row tiles on lanes
+    (30001, 3, 2, 1.2, 8, 4),           # 4-row tiles on lanes, ku != kl
 ]
 
 
@@ -146,12 +148,19 @@ def test_two_sided_partitions_in_plain_fp64():
     rp, ci, a, xt, b = hs.gen_banded(50000, 24, 24, 1.5, seed=77, nrhs=2)
     x, info = check(rp, ci, a, b, 8, "fp64", x_true=xt)
     assert info.twisted == 1 and info.block == 32
+    rp, ci, a, xt, b = hs.gen_banded(50000, 3, 3, 1.5, seed=78, nrhs=3)
+    x, info = check(rp, ci, a, b, 12, "fp64", x_true=xt)
+    assert info.twisted == 1 and info.block == 4
 
 
 def test_two_sided_factor_handle_and_complex():
     rp, ci, a, xt, b = hs.gen_banded(40000, 12, 12, 1.5, seed=78, complex_=True, nrhs=2)
     x, info = check(rp, ci, a, b, 8, "mixed", x_true=xt)
     assert info.twisted == 1
+    for mode in ("mixed", "fp64"):  # complex heptadiagonal on 4-row tiles, both halves on lanes
+        rp, ci, a, xt, b = hs.gen_banded(60000, 3, 3, 1.2, seed=79, complex_=True, nrhs=4)
+        x, info = check(rp, ci, a, b, 16, mode, x_true=xt)
+        assert info.twisted == 1 and info.block == 4
     rp, ci, a, xt, b = hs.gen_banded(80000, 64, 64, 1.5, seed=79, nrhs=1)
     hs.set_option(hs.SPIKE_OPT_PARTITIONS, 16)
     try:
