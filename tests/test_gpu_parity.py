@@ -402,6 +402,14 @@ def test_host_arrays_copy_overlaps_factorization():
         assert e.value.name == "csr"
         x = hs.solve(rp, ci60, a, b, ctx=ctx)
         assert oracle.residual(rp, ci60, a, x, b).max() <= RES_TOL
+        # complex data through the same path (zspike_core_host semantics)
+        rp, ci, a, xt, b = hs.gen_banded(220000, 20, 20, 1.5, seed=32, complex_=True, nrhs=1)
+        assert len(ci) >= 8 << 20
+        for _ in range(2):
+            x = hs.solve(rp, ci, a, b, ctx=ctx)
+            assert ctx.info().twisted == 1
+            assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
+            assert relerr(x, xt) <= 1e-10
     finally:
         ctx.close()
 
