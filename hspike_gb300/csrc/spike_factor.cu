@@ -46,8 +46,9 @@ template <class T, int KB> struct FactorSmem {
 // row-major, zeroed by the caller): C^ coupling (J == 0, columns s-KB..s-1);
 // gBhat (global, row-major): B^ coupling (columns e..e+KB-1).
 // One warp per row: the row's entries are contiguous, so the loads are
-// coalesced and every entry's row is known without a search; four 32-entry
-// chunks of a row are in flight per iteration.
+// coalesced and every entry's row is known without a search; up to five
+// 32-entry chunks of a row (a whole row of a 64-row tile's band) are in
+// flight per iteration.
 template <class T, class H, int KB, int LD>
 __device__ __forceinline__ void place_entry(int lr, int lrow, int c, H a, int s, int m, int J, T *F, T *D, T *En,
                                             T *gZ, T *gBhat, unsigned *err)
@@ -99,6 +100,8 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
     for (int lr = nr + threadIdx.x; lr < KB; lr += NT) D[lr * LD + lr] = sc_one<T>(); // identity padding
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // pieces per iteration: a whole row of the band (2 KB + 1 entries) in one go
+    constexpr int PPR = (2 * KB + 1 + 31) / 32 < 1 ? 1 : (2 * KB + 1 + 31) / 32 > 5 ? 5 : (2 * KB + 1 + 31) / 32;
     int ku = 0, kl = 0;
     for (int lr = warp; lr < nr; lr += NW) {
         const int t0 = srp[lr], t1 = srp[lr + 1];
@@ -108,19 +111,19 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
         }
         const int grow = s + lrow0 + lr; // the row's index in the system
         int carry = -1;                  // last column of the previous iteration
-        for (int base = t0; base < t1; base += 128) { // warp-uniform: the shuffles see every lane
+        for (int base = t0; base < t1; base += 32 * PPR) { // warp-uniform: the shuffles see every lane
             const int t = base + lane;
-            int c[4];
-            H a[4];
+            int c[PPR];
+            H a[PPR];
 #pragma unroll
-            for (int u = 0; u < 4; u++) // four 32-entry pieces of the row in flight at once
+            for (int u = 0; u < PPR; u++) // the row's 32-entry pieces in flight at once
                 if (t + 32 * u < t1) {
                     c[u] = __ldg(colind + t + 32 * u);
                     a[u] = aij[t + 32 * u];
                 }
             if constexpr (VAL) {
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
+                for (int u = 0; u < PPR; u++) {
                     const int up = __shfl_up_sync(0xffffffffu, c[u], 1);
                     const int wrap = __shfl_sync(0xffffffffu, u ? c[u > 0 ? u - 1 : 0] : carry, 31);
                     const int pred = lane ? up : (u ? wrap : carry);
@@ -131,10 +134,10 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
                         kl = max(kl, grow - c[u]);
                     }
                 }
-                carry = __shfl_sync(0xffffffffu, c[3], 31); // used only when the next iteration's entries exist
+                carry = __shfl_sync(0xffffffffu, c[PPR - 1], 31); // used only when the next iteration's entries exist
             }
 #pragma unroll
-            for (int u = 0; u < 4; u++)
+            for (int u = 0; u < PPR; u++)
                 if (t + 32 * u < t1)
                     place_entry<T, H, KB, LD>(lr, lrow0 + lr, c[u], a[u], s, m, J, F, D, En, gZ, gBhat, err);
         }
