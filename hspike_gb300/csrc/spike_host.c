@@ -144,6 +144,7 @@ static void ctx_free(spike_context_t c)
     if (c->copy_stream) spk_stream_destroy(c->copy_stream);
     for (int i = 0; i < 4; i++)
         if (c->range_streams[i]) spk_stream_destroy(c->range_streams[i]);
+    if (c->aux_stream) spk_stream_destroy(c->aux_stream);
     if (t_default == c) t_default = NULL;
     free(c);
 }
@@ -531,29 +532,55 @@ static int check_device_error(spk_plan *P, void *stream, unsigned *e)
     return SPK_OK;
 }
 
+/* The reduced factorization needs only the spikes' tips and the first
+ * right-hand-side sweep y = A_i^{-1} b only the block factors: with an aux
+ * stream (and no phase timing) the two run side by side, b0 being the first
+ * chunk of nr0 columns.  Below OVERLAP_MIN_ROWS both are a few microseconds
+ * and the fork and join would cost more than they save. */
+#define OVERLAP_MIN_ROWS (1 << 18)
+static int reduced_and_first_sweep(spk_plan *P, void *stream, void *aux, const void *b0, int nr0)
+{
+    P->first_applied = 0;
+    if (aux && b0 && nr0 > 0 && !P->timing && P->n >= OVERLAP_MIN_ROWS) {
+        TRY(spk_stream_fork(stream, aux));
+        TRY(spk_reduced_factor(P, aux));
+        TRY(spk_apply(P, b0, nr0, stream));
+        TRY(spk_stream_fork(aux, stream));
+        P->first_applied = 1;
+        return SPK_OK;
+    }
+    spk_phase_begin(P, SPK_PH_RED_FACTOR, stream);
+    TRY(spk_reduced_factor(P, stream));
+    spk_phase_end(P, stream);
+    return SPK_OK;
+}
+
 /* e (optional): the device error word and, with P->validate, ku and kl */
-static int factor_phase_e(spk_plan *P, const int *rp, const int *ci, const void *aij, void *stream, unsigned *e)
+static int factor_phase_e(spk_plan *P, const int *rp, const int *ci, const void *aij, void *stream, unsigned *e,
+                          void *aux, const void *b0, int nr0)
 {
     unsigned w[4];
     TRY(spk_memset(P->d_err, 0, sizeof(unsigned) * 4, stream));
     TRY(spk_factor(P, rp, ci, aij, stream));
-    spk_phase_begin(P, SPK_PH_RED_FACTOR, stream);
-    TRY(spk_reduced_factor(P, stream));
-    spk_phase_end(P, stream);
+    TRY(reduced_and_first_sweep(P, stream, aux, b0, nr0));
     return check_device_error(P, stream, e ? e : w);
 }
 
 static int factor_phase(spk_plan *P, const int *rp, const int *ci, const void *aij, void *stream)
 {
-    return factor_phase_e(P, rp, ci, aij, stream, NULL);
+    return factor_phase_e(P, rp, ci, aij, stream, NULL, NULL, NULL, 0);
 }
 
 /* one SPIKE application: x (+)= A_spike^{-1} r */
 static int spike_apply_once(spk_plan *P, void *x, const void *r, int nrhs, int red, int accumulate, void *stream)
 {
-    spk_phase_begin(P, SPK_PH_APPLY, stream);
-    TRY(spk_apply(P, r, nrhs, stream));
-    spk_phase_end(P, stream);
+    if (P->first_applied) {
+        P->first_applied = 0; /* y = A_i^{-1} r ran beside the reduced factorization */
+    } else {
+        spk_phase_begin(P, SPK_PH_APPLY, stream);
+        TRY(spk_apply(P, r, nrhs, stream));
+        spk_phase_end(P, stream);
+    }
     spk_phase_begin(P, SPK_PH_RED_SOLVE, stream);
     TRY(spk_reduced_solve(P, nrhs, red, stream));
     spk_phase_end(P, stream);
@@ -665,7 +692,9 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
         Q->timing = c->timing;
         Q->validate = 1;
         TRY(ensure(&c->d_r, &c->c_r, hs0 * (size_t)n * chunk0, spk_ctx_astream(c)));
-        const int frc = factor_phase_e(Q, rp, ci, aij, c->stream, e);
+        if (!c->aux_stream && n >= OVERLAP_MIN_ROWS) TRY(spk_stream_create(&c->aux_stream));
+        const int frc = factor_phase_e(Q, rp, ci, aij, c->stream, e, c->aux_stream, b,
+                                       nrhs < Q->nrhs_max ? nrhs : Q->nrhs_max);
         Q->validate = 0;
         const int ku = (int)e[1], kl = (int)e[2], kmax = ku > kl ? ku : kl;
         const int same = !(e[0] & (SPK_DEV_ERR_CSR | SPK_DEV_ERR_BAND)) && spk_choose_block(kmax < 1 ? 1 : kmax) == Q->KB;
@@ -674,11 +703,13 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
             Q->kl = kl;
             int rc = frc;
             if (rc == SPK_OK) rc = solve_all(Q, rp, ci, aij, x, b, c->d_r, nrhs, o, c->stream);
+            Q->first_applied = 0;
             if (Q->timing && (rc == SPK_OK || rc == SPK_ECONV) && spk_phase_collect(Q) != SPK_OK) rc = SPK_ECUDA;
             *launches = Q->launches;
             fill_info(c, Q, o, Q->launches);
             return rc;
         }
+        Q->first_applied = 0;
         if (frc != SPK_OK && frc != SPK_ECSR && frc != SPK_EPIVOT) return frc;
         /* otherwise: the full path below */
     }
@@ -709,8 +740,11 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
     P->timing = c->timing;
     const size_t hs = (is_complex ? 2 : 1) * 8;
     TRY(ensure(&c->d_r, &c->c_r, hs * (size_t)n * chunk, spk_ctx_astream(c)));
-    int rc = factor_phase(P, rp, ci, aij, c->stream);
+    if (!c->aux_stream && n >= OVERLAP_MIN_ROWS) TRY(spk_stream_create(&c->aux_stream));
+    int rc = factor_phase_e(P, rp, ci, aij, c->stream, NULL, c->aux_stream, b,
+                            nrhs < P->nrhs_max ? nrhs : P->nrhs_max);
     if (rc == SPK_OK) rc = solve_all(P, rp, ci, aij, x, b, c->d_r, nrhs, o, c->stream);
+    P->first_applied = 0;
     if (P->timing && (rc == SPK_OK || rc == SPK_ECONV) && spk_phase_collect(P) != SPK_OK) rc = SPK_ECUDA;
     *launches = P->launches;
     fill_info(c, P, o, P->launches);
@@ -820,7 +854,9 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     for (int i = 0; i < 4 && rc == SPK_OK; i++) rc = spk_stream_fork(c->range_streams[i], c->stream);
     if (rc == SPK_OK) rc = spk_stream_fork(cs, c->stream);
     if (rc == SPK_OK) rc = spk_factor_tips(Q, c->stream);
-    if (rc == SPK_OK) rc = spk_reduced_factor(Q, c->stream);
+    if (rc == SPK_OK && !c->aux_stream) rc = spk_stream_create(&c->aux_stream);
+    if (rc == SPK_OK)
+        rc = reduced_and_first_sweep(Q, c->stream, c->aux_stream, c->d_b, nrhs < Q->nrhs_max ? nrhs : Q->nrhs_max);
     Q->validate = 0;
     unsigned e[4] = {0, 0, 0, 0};
     if (rc == SPK_OK) {
@@ -829,6 +865,7 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
         const int same =
             !(e[0] & (SPK_DEV_ERR_CSR | SPK_DEV_ERR_BAND)) && spk_choose_block(kmax < 1 ? 1 : kmax) == Q->KB;
         if (!same) {
+            Q->first_applied = 0;
             /* the whole matrix is on the device now: the general path re-plans */
             long long l2 = 0;
             rc = run_device(c, n, nnz, nrhs, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, c->d_x,
@@ -843,6 +880,7 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     if (rc == SPK_OK)
         rc = solve_all(Q, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, c->d_x, c->d_b, c->d_r, nrhs, o,
                        c->stream);
+    Q->first_applied = 0;
     *launches = Q->launches;
     fill_info(c, Q, o, Q->launches);
     return rc;

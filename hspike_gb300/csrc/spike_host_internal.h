@@ -25,6 +25,7 @@ struct spike_context_s {
     void *own_stream, *stream;
     void *copy_stream;     /* host -> device copies that overlap the factorization (created on demand) */
     void *range_streams[4]; /* the factorization of those copies' partition ranges (created on demand) */
+    void *aux_stream;       /* the reduced factorization, beside the first sweep (created on demand) */
     /* options */
     int refs; /* the creator's reference + one per factor handle or batch using the context */
     int mode, partitions, max_refine, red_refine, timing, twist;

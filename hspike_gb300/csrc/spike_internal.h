@@ -94,6 +94,9 @@ typedef struct spk_plan {
     /* k_band_tiles also validates the CSR and measures the bandwidth into
      * d_err[1..2] (set when the separate analysis pass was skipped) */
     int validate;
+    /* the first right-hand-side chunk's y = A_i^{-1} b already ran (next to
+     * the reduced factorization, on another stream) */
+    int first_applied;
     /* device copies of the schedule */
     int *d_part_start, *d_blk_off;
     int *d_blk_part; /* total_blocks: partition of each block */

@@ -414,6 +414,40 @@ def test_host_arrays_copy_overlaps_factorization():
         ctx.close()
 
 
+@pytest.mark.parametrize("n,k,nrhs,complex_,mode,twist",
+                         [(300_000, 8, 1, False, "mixed", 1), (300_000, 24, 40, False, "mixed", 1),
+                          (300_000, 24, 3, False, "mixed", 0), (280_000, 3, 2, True, "mixed", 1),
+                          (280_000, 16, 2, False, "fp64", 1), (262_144, 100, 1, False, "mixed", 1)],
+                         ids=lambda v: str(v))
+def test_reduced_factorization_beside_first_sweep(n, k, nrhs, complex_, mode, twist):
+    # from 2^18 rows the reduced factorization runs on a second stream beside
+    # the first right-hand-side sweep; with phase timing the two run one after
+    # the other: the same kernels on the same data, so x is bit-identical
+    # (from 8M entries the reused plan's call also sends the matrix in ranges,
+    # whose factorization sums in another order: there 1e-13)
+    rp, ci, a, xt, b = hs.gen_banded(n, k, k, 1.5, seed=900 + k, complex_=complex_, nrhs=nrhs)
+    ctx = hs.Context()
+    try:
+        ctx.set_option(hs.SPIKE_OPT_TWIST, twist)
+        xs = []
+        for timing in (0, 0, 1):  # plan; reused plan; serialised phases
+            ctx.set_option(hs.SPIKE_OPT_PHASE_TIMING, timing)
+            xs.append(hs.solve(rp, ci, a, b, precision=MODES[mode], ctx=ctx))
+            assert ctx.info().relres_max <= RES_TOL
+        if not twist or k > 64:
+            assert ctx.info().twisted == 0
+        assert np.array_equal(xs[0], xs[2])
+        if len(ci) < 8 << 20:
+            assert np.array_equal(xs[1], xs[2])
+        else:
+            assert relerr(xs[1], xs[2]) <= 1e-13
+        assert xs[0].shape == xt.shape == (n, nrhs)
+        assert oracle.residual(rp, ci, a, xs[0], b).max() <= RES_TOL
+        assert relerr(xs[0], xt) <= 1e-10
+    finally:
+        ctx.close()
+
+
 def test_bandwidth_above_tile_is_rejected():
     rp, ci, a, xt, b = hs.gen_banded(2000, 130, 130, 1.5, seed=18)
     x = np.zeros_like(b, order="F")
