@@ -21,20 +21,6 @@ namespace {
 constexpr int RC = 32;      // right-hand-side columns per CTA
 constexpr int RCS = RC + 1; // row stride of the shared [KB][RC] vectors (odd: column-wise writes spread over banks)
 
-template <class T> __device__ __forceinline__ T shfl_xor_any(T v, int off)
-{
-    if constexpr (sizeof(T) == 4) {
-        return __shfl_xor_sync(0xffffffffu, v, off);
-    } else {
-        T other;
-        const unsigned *src = (const unsigned *)&v;
-        unsigned *dst = (unsigned *)&other;
-#pragma unroll
-        for (int w = 0; w < (int)(sizeof(T) / 4); w++) dst[w] = __shfl_xor_sync(0xffffffffu, src[w], off);
-        return other;
-    }
-}
-
 // out[r][h] = sign * sum_k M[r][k] v[k][h] (+ base[r][h]), r < KB, h < nr.
 // Mt: shared tile holding M transposed (the factor tiles are column-major in
 // global memory); v, base, out: shared [KB][RC] vectors with row stride RCS.

@@ -854,6 +854,52 @@ template <> __device__ __forceinline__ cfloat cvt_fast<cfloat, cdouble>(cdouble 
     return {f64_to_f32(v.re), f64_to_f32(v.im)};
 }
 
+// ------------------------------------------------------------ warp sums
+// __shfl_xor_sync for any scalar (complex types move as 32-bit words)
+template <class T> __device__ __forceinline__ T shfl_xor_any(T v, int off)
+{
+    if constexpr (sizeof(T) == 4) {
+        return __shfl_xor_sync(0xffffffffu, v, off);
+    } else {
+        T other;
+        const unsigned *src = (const unsigned *)&v;
+        unsigned *dst = (unsigned *)&other;
+#pragma unroll
+        for (int w = 0; w < (int)(sizeof(T) / 4); w++) dst[w] = __shfl_xor_sync(0xffffffffu, src[w], off);
+        return other;
+    }
+}
+
+// Sums V per-lane values over the 32 lanes at once (V a power of two, <= 32):
+// each exchange step halves the values a lane holds, so the whole reduction
+// takes V - 1 + (5 - log2 V) shuffles instead of 5 V.  Afterwards v[0] of
+// lane l holds the total of value index l >> (5 - log2 V).
+template <int N, int OFF, class T, int V> __device__ __forceinline__ void warp_tsum_step(T (&v)[V], int lane)
+{
+    if constexpr (OFF >= 1) {
+        if constexpr (N > 1) {
+            constexpr int H = N / 2;
+            const bool up = (lane & OFF) != 0;
+#pragma unroll
+            for (int j = 0; j < H; j++) {
+                const T send = up ? v[j] : v[j + H];
+                const T keep = up ? v[j + H] : v[j];
+                v[j] = keep + shfl_xor_any(send, OFF);
+            }
+            warp_tsum_step<H, OFF / 2>(v, lane);
+        } else {
+            v[0] = v[0] + shfl_xor_any(v[0], OFF);
+            warp_tsum_step<1, OFF / 2>(v, lane);
+        }
+    }
+}
+template <class T, int V> __device__ __forceinline__ T warp_tsum(T (&v)[V], int lane)
+{
+    static_assert(V >= 1 && V <= 32 && (V & (V - 1)) == 0, "V: a power of two up to 32");
+    warp_tsum_step<V, 16>(v, lane);
+    return v[0];
+}
+
 // 16-byte-aligned carve-up of dynamic shared memory
 __device__ __forceinline__ char *smem_align(char *p)
 {

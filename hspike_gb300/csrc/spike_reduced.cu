@@ -350,6 +350,255 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// ---------------------------------------------------------------- solve, one latency per level (KB 32, 64)
+// The kernels above fetch their tiles one after another, each behind a
+// __syncthreads, so a level costs several memory latencies.  Here a CTA asks
+// for every tile it needs at once (cp.async), then each warp forms whole rows
+// of the matrix-vector products: lanes run along k (conflict-free shared
+// reads) and warp_tsum reduces a group of rows x right-hand sides together.
+// Level 0 reads the FP64 right-hand side of R directly and accumulates the
+// FP64 solution itself (no separate narrowing and accumulation launches).
+constexpr int QNT = 256;       // threads per CTA (8 warps)
+constexpr int QWARPS = QNT / 32;
+
+template <class T, int KB, int NRC> struct QSolve {
+    static constexpr size_t TS = (size_t)KB * KB;
+    static constexpr int R = 2 * KB;             // rows of a level block
+    static constexpr int RPW = R / QWARPS;       // rows per warp
+    static constexpr int G = RPW * NRC <= 32 ? RPW : 32 / NRC; // rows per reduction group
+    static constexpr int V = G * NRC;            // values per warp_tsum
+    // six tiles and four 2KB-vectors per column
+    static constexpr size_t bytes = 6 * TS * sizeof(T) + 4 * (size_t)R * NRC * sizeof(T) + 64;
+    static_assert(KB % 32 == 0 && RPW % G == 0 && (V & (V - 1)) == 0 && V <= 32, "QSolve shape");
+};
+
+// element (row q, column h) of level block a: input g (FP64 at level 0)
+template <class T, class H>
+__device__ __forceinline__ T q_in(const void *g, bool l0, long long ld, long long a, int q, int h, int KB)
+{
+    const long long o = h * ld + a * 2 * KB + q;
+    return l0 ? cvt_fast<T, H>(((const H *)g)[o]) : ((const T *)g)[o];
+}
+
+template <class T> __device__ __forceinline__ void q_tiles(T *s, const T *g, int ntiles, int KB)
+{
+    const int chunks = ntiles * KB * KB * (int)sizeof(T) / 16;
+    for (int c = threadIdx.x; c < chunks; c += QNT) cp_async16((char *)s + 16 * c, (const char *)g + 16 * c);
+}
+
+// rows [r0, r0 + RPW) of out[q][h] = sum_k A(q, k) x[h][k], k < NK, for the
+// rows of one warp; A(q, k) = At[q - qa][k] for k < KB and Bt[q - qa][k - KB]
+// beyond (two row-major KB x KB tiles side by side).  emit(q, h, sum) is
+// called once per (row, column) by one lane.
+template <class T, int KB, int NRC, int NK, class Emit>
+__device__ __forceinline__ void q_rows(const T *At, const T *Bt, int qa, const T *x, int r0, int nr, Emit emit)
+{
+    using Q = QSolve<T, KB, NRC>;
+    constexpr int E = NK / 32;
+    const int lane = threadIdx.x & 31;
+    T xv[NRC][E];
+#pragma unroll
+    for (int h = 0; h < NRC; h++)
+#pragma unroll
+        for (int e = 0; e < E; e++) xv[h][e] = h < nr ? x[h * 2 * KB + lane + 32 * e] : sc_zero<T>();
+#pragma unroll 1
+    for (int g0 = 0; g0 < Q::RPW; g0 += Q::G) {
+        T v[Q::V];
+#pragma unroll
+        for (int g = 0; g < Q::G; g++) {
+            const int rr = r0 + g0 + g - qa;
+            T m[E];
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                const int k = lane + 32 * e;
+                m[e] = k < KB ? At[rr * KB + k] : Bt[rr * KB + k - KB];
+            }
+#pragma unroll
+            for (int h = 0; h < NRC; h++) {
+                T acc = sc_zero<T>();
+#pragma unroll
+                for (int e = 0; e < E; e++) acc = madd(acc, m[e], xv[h][e]);
+                v[g * NRC + h] = acc;
+            }
+        }
+        const T sum = warp_tsum(v, lane);
+        constexpr int SH = 5 - (Q::V == 1 ? 0 : Q::V == 2 ? 1 : Q::V == 4 ? 2 : Q::V == 8 ? 3 : Q::V == 16 ? 4 : 5);
+        if ((lane & ((1 << SH) - 1)) == 0) {
+            const int idx = lane >> SH, g = idx / NRC, h = idx - g * NRC;
+            if (h < nr) emit(r0 + g0 + g, h, sum);
+        }
+    }
+}
+
+// Forward reduction, one CTA per even block i of level l:
+//   g'_i = g_i - [X_i (M00 x0 + M01 x1)_{i-1} ; Y_i (M10 x0 + M11 x1)_{i+1}]
+// g at level 0 is FP64 (gld = n_iface * 2KB); level l+1 goes to gn.
+template <class T, int KB, int NRC>
+__global__ void __launch_bounds__(QNT)
+    k_crq_fwd(const T *__restrict__ Xl, const T *__restrict__ Yl, const T *__restrict__ Ml, int cnt, const void *gin,
+              int l0, long long gld, long long off_l, T *gn, long long stride, long long off_n, int nrhs)
+{
+    using H = typename HighOf<T>::type;
+    using Q = QSolve<T, KB, NRC>;
+    constexpr size_t TS = Q::TS;
+    const int i = 2 * blockIdx.x;
+    const int h0 = blockIdx.y * NRC, nr = min(NRC, nrhs - h0);
+    extern __shared__ char smraw[];
+    T *sM = (T *)smem_align(smraw); // [half][M_half0 | M_half1]: 4 tiles
+    T *sC = sM + 4 * TS;            // X_i, Y_i
+    T *sx = sC + 2 * TS;            // [half][h][2KB]: the neighbours' blocks
+    T *sw = sx + 2 * NRC * 2 * KB;  // [half][h][2KB] (first KB used): w
+    const bool has[2] = {i - 1 >= 0, i + 1 < cnt};
+    if (has[0]) {
+        q_tiles(sM, Ml + (size_t)((i - 2) / 2) * 4 * TS, 2, KB); // M00, M01 of odd block i-1
+        q_tiles(sC, Xl + (size_t)i * TS, 1, KB);
+    }
+    if (has[1]) {
+        q_tiles(sM + 2 * TS, Ml + (size_t)(i / 2) * 4 * TS + 2 * TS, 2, KB); // M10, M11 of odd block i+1
+        q_tiles(sC + TS, Yl + (size_t)i * TS, 1, KB);
+    }
+    cp_async_commit();
+    for (int q = threadIdx.x; q < 2 * NRC * 2 * KB; q += QNT) {
+        const int half = q / (NRC * 2 * KB), rem = q - half * NRC * 2 * KB, h = rem / (2 * KB), k = rem - h * 2 * KB;
+        sx[q] = has[half] && h < nr ? q_in<T, H>(gin, l0, gld, off_l + i + (half ? 1 : -1), k, h0 + h, KB)
+                                    : sc_zero<T>();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, r0 = warp * Q::RPW, half = r0 / KB;
+    // w rows: half h of the neighbour's M times its block
+    if (has[half])
+        q_rows<T, KB, NRC, 2 * KB>(sM + half * 2 * TS, sM + half * 2 * TS + TS, half * KB, sx + half * NRC * 2 * KB, r0,
+                                   nr, [&](int q, int h, T v) { sw[(half * NRC + h) * 2 * KB + q - half * KB] = v; });
+    __syncthreads();
+    T *gout = gn + (off_n + blockIdx.x) * 2 * KB;
+    if (has[half]) {
+        q_rows<T, KB, NRC, KB>(sC + half * TS, sC + half * TS, half * KB, sw + half * NRC * 2 * KB, r0, nr,
+                               [&](int q, int h, T v) {
+                                   gout[(h0 + h) * stride + q] = q_in<T, H>(gin, l0, gld, off_l + i, q, h0 + h, KB) - v;
+                               });
+    } else {
+        for (int q = r0 + (threadIdx.x & 31); q < r0 + Q::RPW; q += 32)
+            for (int h = 0; h < nr; h++) gout[(h0 + h) * stride + q] = q_in<T, H>(gin, l0, gld, off_l + i, q, h0 + h, KB);
+    }
+}
+
+// Back substitution at level l (top = the single top block): odd j (and the
+// top block) solve u_j = M_j (g_j - [X_j u0_{j-1} ; Y_j u1_{j+1}]) with the
+// even neighbours' values from level l+1 (un); even j copy theirs from there.
+// Level 0 writes the FP64 solution U (ld gld): U = d on the first refinement
+// pass, U += d after.
+template <class T, int KB, int NRC>
+__global__ void __launch_bounds__(QNT)
+    k_crq_bwd(const T *__restrict__ Xl, const T *__restrict__ Yl, const T *__restrict__ Ml, int cnt, const void *gin,
+              int l0, long long gld, long long off_l, const T *un, long long off_n, T *u, long long stride, void *U,
+              int first, int nrhs, int top)
+{
+    using H = typename HighOf<T>::type;
+    using Q = QSolve<T, KB, NRC>;
+    constexpr size_t TS = Q::TS;
+    const int j = blockIdx.x;
+    const int h0 = blockIdx.y * NRC, nr = min(NRC, nrhs - h0);
+    auto put = [&](int q, int h, T v) {
+        if (l0) {
+            H *o = (H *)U + (h0 + h) * gld + (long long)j * 2 * KB + q;
+            const H d = cvt_fast<H, T>(v);
+            *o = first ? d : *o + d;
+        } else {
+            u[(h0 + h) * stride + (off_l + j) * 2 * KB + q] = v;
+        }
+    };
+    if (!top && (j & 1) == 0) {
+        for (int q = threadIdx.x; q < 2 * KB * nr; q += QNT) {
+            const int h = q / (2 * KB), rr = q - h * 2 * KB;
+            put(rr, h, un[(h0 + h) * stride + (off_n + j / 2) * 2 * KB + rr]);
+        }
+        return;
+    }
+    extern __shared__ char smraw[];
+    T *sM = (T *)smem_align(smraw); // M00 M01 M10 M11
+    T *sC = sM + 4 * TS;            // X_j, Y_j
+    T *sv = sC + 2 * TS;            // [half][h][2KB] (first KB used): neighbour values
+    T *ss = sv + 2 * NRC * 2 * KB;  // [h][2KB]: g_j minus the couplings
+    const bool has[2] = {!top && j - 1 >= 0, !top && j + 1 < cnt};
+    q_tiles(sM, Ml + (size_t)(top ? 0 : (j - 1) / 2) * 4 * TS, 4, KB);
+    if (has[0]) q_tiles(sC, Xl + (size_t)j * TS, 1, KB);
+    if (has[1]) q_tiles(sC + TS, Yl + (size_t)j * TS, 1, KB);
+    cp_async_commit();
+    for (int q = threadIdx.x; q < NRC * 2 * KB; q += QNT) {
+        const int h = q / (2 * KB), k = q - h * 2 * KB;
+        ss[q] = h < nr ? q_in<T, H>(gin, l0, gld, off_l + j, k, h0 + h, KB) : sc_zero<T>();
+        const int half = k / KB, kk = k - half * KB; // the even neighbours sit in the level above
+        sv[(half * NRC + h) * 2 * KB + kk] =
+            has[half] && h < nr ? un[(h0 + h) * stride + (off_n + (j + (half ? 1 : -1)) / 2) * 2 * KB + half * KB + kk]
+                                : sc_zero<T>();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, r0 = warp * Q::RPW, half = r0 / KB;
+    if (has[half])
+        q_rows<T, KB, NRC, KB>(sC + half * TS, sC + half * TS, half * KB, sv + half * NRC * 2 * KB, r0, nr,
+                               [&](int q, int h, T v) { ss[h * 2 * KB + q] = ss[h * 2 * KB + q] - v; });
+    __syncthreads();
+    q_rows<T, KB, NRC, 2 * KB>(sM + half * 2 * TS, sM + half * 2 * TS + TS, half * KB, ss, r0, nr,
+                               [&](int q, int h, T v) { put(q, h, v); });
+}
+
+template <class T, int KB, int NRC> int run_red_solve_q(spk_plan *P, int nrhs, int iters, cudaStream_t st)
+{
+    using H = typename HighOf<T>::type;
+    using Q = QSolve<T, KB, NRC>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const long long NR = (long long)P->n_iface * 2 * KB;
+    const long long stride = P->crg_stride;
+    T *cg = (T *)P->d_crg;
+    T *cu = cg + stride * P->nrhs_max;
+    const T *cX = (const T *)P->d_crX, *cY = (const T *)P->d_crY, *cM = (const T *)P->d_crM;
+    const int L = P->cr_levels;
+    const int hy = (nrhs + NRC - 1) / NRC;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_crq_fwd<T, KB, NRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q::bytes) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_crq_bwd<T, KB, NRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q::bytes) !=
+                cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
+    for (int it = 0; it < iters; it++) {
+        const H *res = it == 0 ? (const H *)P->d_g : (const H *)P->d_rr;
+        for (int l = 0; l < L; l++) {
+            const int cnt = P->cr_count[l];
+            k_crq_fwd<T, KB, NRC><<<dim3((cnt + 1) / 2, hy), QNT, Q::bytes, st>>>(
+                cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS, cM + (size_t)P->cr_moff[l] * 4 * TS, cnt,
+                l == 0 ? (const void *)res : (const void *)cg, l == 0, l == 0 ? NR : stride, P->cr_off[l], cg, stride,
+                P->cr_off[l + 1], nrhs);
+            P->launches++;
+        }
+        // the top block: level L (level 0 itself when R has one block)
+        k_crq_bwd<T, KB, NRC><<<dim3(1, hy), QNT, Q::bytes, st>>>(
+            nullptr, nullptr, cM + (size_t)P->cr_moff[L] * 4 * TS, 1, L == 0 ? (const void *)res : (const void *)cg,
+            L == 0, L == 0 ? NR : stride, P->cr_off[L], nullptr, 0, cu, stride, P->d_u, it == 0, nrhs, 1);
+        P->launches++;
+        for (int l = L - 1; l >= 0; l--) {
+            const int cnt = P->cr_count[l];
+            k_crq_bwd<T, KB, NRC><<<dim3(cnt, hy), QNT, Q::bytes, st>>>(
+                cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS, cM + (size_t)P->cr_moff[l] * 4 * TS, cnt,
+                l == 0 ? (const void *)res : (const void *)cg, l == 0, l == 0 ? NR : stride, P->cr_off[l], cu,
+                P->cr_off[l + 1], cu, stride, P->d_u, it == 0, nrhs, 0);
+            P->launches++;
+        }
+        if (it + 1 < iters) {
+            k_red_resid<H, KB><<<P->n_iface, 128, 0, st>>>((const H *)P->d_RP, (const H *)P->d_RQ, (const H *)P->d_RX,
+                                                           (const H *)P->d_RY, (const H *)P->d_g, (const H *)P->d_u,
+                                                           (H *)P->d_rr, P->n_iface, nrhs);
+            P->launches++;
+        }
+        SPK_CHECK_LAUNCH();
+    }
+    return SPK_OK;
+}
+
 template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
 {
     using S = RedSmem<T, KB>;
@@ -398,6 +647,10 @@ template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
 
 template <class T, int KB> int run_red_solve(spk_plan *P, int nrhs, int iters, cudaStream_t st)
 {
+    if constexpr (KB == 32 || (KB == 64 && sizeof(T) <= 8)) {
+        if (nrhs == 1) return run_red_solve_q<T, KB, 1>(P, nrhs, iters, st);
+        return run_red_solve_q<T, KB, 4>(P, nrhs, iters, st);
+    }
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
     const long long NR = (long long)P->n_iface * 2 * KB;
