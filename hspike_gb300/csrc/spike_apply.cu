@@ -88,6 +88,37 @@ __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, 
         return;
       }
     }
+    // One column: a thread takes 4 rows (one 16-byte load per k) over an
+    // interleaved slice of k, and the SL slices of a row group are summed by
+    // one grouped transpose sum.
+    if constexpr (KB >= 16) {
+        constexpr int RG = KB / 4, SL = NT / RG, KS = KB / SL;
+        static_assert(SL >= 4 && SL <= 32 && KS * SL == KB, "one-column slices");
+        if (nr == 1) {
+            const int lane = threadIdx.x & 31, slice = threadIdx.x & (SL - 1), r0 = (threadIdx.x / SL) * 4;
+            T acc[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) acc[i] = sc_zero<T>();
+#pragma unroll
+            for (int kk = 0; kk < KS; kk++) {
+                const int k = kk * SL + slice;
+                T m[4];
+                vld<T, 4>(m, Mt + k * LD + r0);
+                const T x = v[k * S];
+#pragma unroll
+                for (int i = 0; i < 4; i++) acc[i] = madd(acc[i], m[i], x);
+            }
+            const T sum = warp_tsum<T, 4, SL>(acc, lane);
+            constexpr int SH = (SL == 4 ? 2 : SL == 8 ? 3 : SL == 16 ? 4 : 5) - 2;
+            if ((slice & ((1 << SH) - 1)) == 0) {
+                const int r = r0 + (slice >> SH);
+                T val = negate ? -sum : sum;
+                if (HAS_BASE) val = base[r * S] + val;
+                out[r * S] = val;
+            }
+            return;
+        }
+    }
     const int O = KB * nr;
     int spl = 1;
     while (spl < 32 && spl * 2 * O <= NT && spl * 2 <= KB) spl *= 2;

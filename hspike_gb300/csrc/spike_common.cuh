@@ -870,10 +870,11 @@ template <class T> __device__ __forceinline__ T shfl_xor_any(T v, int off)
     }
 }
 
-// Sums V per-lane values over the 32 lanes at once (V a power of two, <= 32):
-// each exchange step halves the values a lane holds, so the whole reduction
-// takes V - 1 + (5 - log2 V) shuffles instead of 5 V.  Afterwards v[0] of
-// lane l holds the total of value index l >> (5 - log2 V).
+// Sums V per-lane values over each group of W consecutive lanes at once (V,
+// W powers of two, V <= W <= 32): each exchange step halves the values a lane
+// holds, so the whole reduction takes V - 1 + log2 W - log2 V shuffles instead
+// of V log2 W.  Afterwards v[0] of lane l holds its group's total of value
+// index (l mod W) >> (log2 W - log2 V).
 template <int N, int OFF, class T, int V> __device__ __forceinline__ void warp_tsum_step(T (&v)[V], int lane)
 {
     if constexpr (OFF >= 1) {
@@ -893,10 +894,11 @@ template <int N, int OFF, class T, int V> __device__ __forceinline__ void warp_t
         }
     }
 }
-template <class T, int V> __device__ __forceinline__ T warp_tsum(T (&v)[V], int lane)
+template <class T, int V, int W = 32> __device__ __forceinline__ T warp_tsum(T (&v)[V], int lane)
 {
-    static_assert(V >= 1 && V <= 32 && (V & (V - 1)) == 0, "V: a power of two up to 32");
-    warp_tsum_step<V, 16>(v, lane);
+    static_assert(V >= 1 && V <= W && W <= 32 && (V & (V - 1)) == 0 && (W & (W - 1)) == 0,
+                  "V <= W <= 32, powers of two");
+    warp_tsum_step<V, W / 2>(v, lane);
     return v[0];
 }
 
