@@ -85,11 +85,13 @@ __device__ __forceinline__ void place_entry(int lr, int lrow, int c, H a, int s,
 // was reused), so this pass also validates the CSR -- row pointers in range
 // and non-decreasing, columns in [0, n) and increasing within a row -- and
 // measures the exact bandwidth: err[1] = ku, err[2] = kl.  A row with bad
-// pointers is flagged and not read.
-template <class T, class H, int KB, int LD, bool VAL>
+// pointers is flagged and not read.  impl_kl >= 0: colind is not read; the
+// host verified that every row is the full band, so entry t of row r is
+// column max(0, r - impl_kl) + (t - rowptr[r]).
+template <class T, class H, int KB, int LD, bool VAL, bool IMPL = false>
 __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
                               const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *gZ,
-                              T *gBhat, unsigned *err, int *srp, int n, long long nnz)
+                              T *gBhat, unsigned *err, int *srp, int n, long long nnz, int impl_kl)
 {
     constexpr int NT = NTOf<KB>::value;
     constexpr int NW = NT / 32;
@@ -110,6 +112,7 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
             continue;
         }
         const int grow = s + lrow0 + lr; // the row's index in the system
+        const int cfirst = IMPL ? max(0, grow - impl_kl) - t0 : 0; // implied columns: cfirst + t
         int carry = -1;                  // last column of the previous iteration
         for (int base = t0; base < t1; base += 32 * PPR) { // warp-uniform: the shuffles see every lane
             const int t = base + lane;
@@ -118,7 +121,7 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
 #pragma unroll
             for (int u = 0; u < PPR; u++) // the row's 32-entry pieces in flight at once
                 if (t + 32 * u < t1) {
-                    c[u] = __ldg(colind + t + 32 * u);
+                    c[u] = IMPL ? cfirst + t + 32 * u : __ldg(colind + t + 32 * u);
                     a[u] = aij[t + 32 * u];
                 }
             if constexpr (VAL) {
@@ -200,7 +203,7 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
                  const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
                  const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
                  unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys, int twist,
-                 int validate, int n, long long nnz, int gb0, int nb_total)
+                 int validate, int n, long long nnz, int gb0, int nb_total, int impl_kl)
 {
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
@@ -234,12 +237,15 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     __syncthreads();
     if (validate) {
         scatter_block<T, H, KB, LD1, true>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
-                                           err, srp, n, nnz);
+                                           err, srp, n, nnz, impl_kl);
         if (threadIdx.x == 0 && ((gb == 0 && rowptr[0] != 0) || (gb == nb_total - 1 && (long long)rowptr[n] != nnz)))
             atomicOr(err, SPK_DEV_ERR_CSR);
+    } else if (impl_kl >= 0) {
+        scatter_block<T, H, KB, LD1, false, true>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz,
+                                                  gBhat + (size_t)part * TS, err, srp, n, nnz, impl_kl);
     } else {
         scatter_block<T, H, KB, LD1, false>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
-                                            err, srp, n, nnz);
+                                            err, srp, n, nnz, impl_kl);
     }
     __syncthreads();
     T *g = gT + (size_t)gb * 3 * TS;
@@ -883,7 +889,8 @@ template <class T, int KB> int run_factor_range(spk_plan *P, const int *rowptr, 
     k_band_tiles<T, KB><<<b1 - b0, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off,
                                                       P->d_blk_part, (T *)P->d_T, (T *)P->d_E, (T *)P->d_W,
                                                       (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist,
-                                                      P->validate && !P->d_sys, P->n, P->nnz, b0, P->total_blocks);
+                                                      P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz, b0,
+                                                      P->total_blocks, P->impl_cols ? P->impl_kl : -1);
     SPK_CHECK_LAUNCH();
     P->launches++;
     int rc = spk_twist_factor(P, 1, part0, part1, st);
@@ -933,8 +940,9 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     k_band_tiles<T, KB><<<P->total_blocks, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start,
                                                               P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
                                                               (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys,
-                                                              P->d_part_sys, P->twist, P->validate && !P->d_sys,
-                                                              P->n, P->nnz, 0, P->total_blocks);
+                                                              P->d_part_sys, P->twist,
+                                                              P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz,
+                                                              0, P->total_blocks, P->impl_cols ? P->impl_kl : -1);
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
     if (P->twist) { // two-sided chains (spike_twist.cu)

@@ -17,7 +17,10 @@
  * current CUDA device, and a missing or failing device is an error.
  */
 #include <math.h>
+#include <pthread.h>
+#include <sched.h>
 #include <stdarg.h>
+#include <stdatomic.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -117,6 +120,7 @@ Error_t spike_context_create(spike_context_t *out)
     c->max_refine = 3;
     c->red_refine = 0;
     c->twist = 1;
+    c->host_threads = 8;
     c->tol = 1e-12;
     if (spk_malloc((void **)&c->d_scratch, 4 * sizeof(int)) != SPK_OK) {
         spk_stream_destroy(c->own_stream);
@@ -145,6 +149,8 @@ static void ctx_free(spike_context_t c)
     for (int i = 0; i < 4; i++)
         if (c->range_streams[i]) spk_stream_destroy(c->range_streams[i]);
     if (c->aux_stream) spk_stream_destroy(c->aux_stream);
+    for (int i = 0; i < 9; i++)
+        if (c->range_events[i]) spk_event_destroy(c->range_events[i]);
     if (t_default == c) t_default = NULL;
     free(c);
 }
@@ -211,6 +217,10 @@ Error_t spike_set_option(spike_context_t c, int opt, double v)
     case SPIKE_OPT_TWIST:
         c->twist = v != 0;
         break;
+    case SPIKE_OPT_HOST_THREADS:
+        if (v < 0 || v > 64) return spk_fail(SPIKE_ERR_ARGUMENT, "host threads must be in [0, 64]");
+        c->host_threads = (int)v;
+        break;
     case SPIKE_OPT_STREAM_ALLOC:
         if ((v != 0) != (c->stream_alloc != 0)) {
             /* workspace changes allocator: release it (it is rebuilt on demand) */
@@ -246,6 +256,7 @@ Error_t spike_get_option(spike_context_t c, int opt, double *v)
     case SPIKE_OPT_REDUCED_REFINE: *v = c->red_refine; break;
     case SPIKE_OPT_PHASE_TIMING: *v = c->timing; break;
     case SPIKE_OPT_TWIST: *v = c->twist; break;
+    case SPIKE_OPT_HOST_THREADS: *v = c->host_threads; break;
     case SPIKE_OPT_STREAM_ALLOC: *v = c->stream_alloc; break;
     default: return spk_fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
     }
@@ -658,6 +669,7 @@ static void fill_info(spike_context_t c, const spk_plan *P, const refine_opts *o
     c->info.kernel_launches = launches;
     c->info.device_bytes = P->bytes;
     c->info.twisted = P->twist;
+    c->info.columns_implied = P->impl_cols;
 }
 
 static Error_t finish(int rc, const char *where, const refine_opts *o)
@@ -797,13 +809,92 @@ Error_t spike_zsolve(spike_context_t ctx, integer_t n, integer_t nnz, integer_t 
     return solve_on(ctx, SPK_Z, "spike_zsolve", n, nnz, nrhs, colind, rowptr, aij, x, b);
 }
 
+/* ---- the full-band check of a host CSR, on worker threads ----
+ * A call with host arrays sends the matrix over the host link, the larger
+ * part of its time.  When every row r holds exactly the columns
+ * max(0, r - kl) .. min(n - 1, r + ku) -- the full band of the plan's ku, kl,
+ * as the reference's own banded systems are stored -- the column indices
+ * follow from the row pointers, so only the values need to travel: worker
+ * threads check the rows range by range while the values' copies run, and
+ * each range's kernels start once its rows have passed.  The first range
+ * that fails sends the column indices after all and finishes on the general
+ * path (the band tiles then validate it on the device). */
+#define PIPE_RANGES 8
+#define SCAN_MAX_THREADS 64
+
+typedef struct {
+    const int *rowptr, *colind;
+    int n, ku, kl, nthreads;
+    long long nnz;
+    int row_lo[PIPE_RANGES + 1];
+    atomic_int done[PIPE_RANGES]; /* workers finished with range g */
+    atomic_int bad[PIPE_RANGES];  /* a row of range g is not the full band */
+    atomic_int stop;              /* no further rows need checking */
+} band_scan;
+
+typedef struct {
+    band_scan *S;
+    int id;
+} band_scan_arg;
+
+/* 16-byte generic vectors (GCC's vector extension, no target intrinsics):
+ * the check streams host memory, and scalar code would bind it to the core */
+typedef int spk_v4i __attribute__((vector_size(16)));
+
+static int rows_full_band(const band_scan *S, int r0, int r1)
+{
+    const int n = S->n, ku = S->ku, kl = S->kl;
+    const spk_v4i step = {8, 8, 8, 8};
+    for (int r = r0; r < r1; r++) {
+        const int c0 = r - kl < 0 ? 0 : r - kl, c1 = r + ku > n - 1 ? n - 1 : r + ku, len = c1 - c0 + 1;
+        const long long t0 = S->rowptr[r], t1 = S->rowptr[r + 1];
+        if (t0 < 0 || t1 > S->nnz || t1 - t0 != (long long)len) return 0;
+        const int *ci = S->colind + t0;
+        spk_v4i ia = {c0, c0 + 1, c0 + 2, c0 + 3}, ib = ia + 4, da = {0, 0, 0, 0}, db = da;
+        int t = 0;
+        for (; t + 8 <= len; t += 8) {
+            spk_v4i va, vb;
+            memcpy(&va, ci + t, sizeof va);
+            memcpy(&vb, ci + t + 4, sizeof vb);
+            da |= va ^ ia;
+            db |= vb ^ ib;
+            ia += step;
+            ib += step;
+        }
+        da |= db;
+        int diff = da[0] | da[1] | da[2] | da[3];
+        for (; t < len; t++) diff |= ci[t] ^ (c0 + t);
+        if (diff) return 0;
+    }
+    return 1;
+}
+
+static void *band_scan_worker(void *p)
+{
+    const band_scan_arg *a = (const band_scan_arg *)p;
+    band_scan *S = a->S;
+    for (int g = 0; g < PIPE_RANGES; g++) {
+        if (!atomic_load(&S->stop)) {
+            const long long lo = S->row_lo[g], len = S->row_lo[g + 1] - lo;
+            const int r0 = (int)(lo + len * a->id / S->nthreads), r1 = (int)(lo + len * (a->id + 1) / S->nthreads);
+            if (!rows_full_band(S, r0, r1)) {
+                atomic_store(&S->bad[g], 1); /* before stop: a range skipped after it counts as unchecked */
+                atomic_store(&S->stop, 1);
+            }
+        }
+        atomic_fetch_add(&S->done[g], 1);
+    }
+    return NULL;
+}
+
 /* Host arrays, plan reused (same shape as the previous call on the context)
  * and two-sided: the matrix goes to the device in partition ranges on a copy
  * stream, and each range's band tiles and chains start as soon as its rows
  * have arrived, so the factorization hides behind the copy (host -> device
- * copies are the larger part of such a call).  Returns SPK_EARG when the
- * path does not apply; the caller then copies everything and solves. */
-#define PIPE_RANGES 8
+ * copies are the larger part of such a call).  With host threads the column
+ * indices stay on the host when the rows are the full band (above).  Returns
+ * SPK_EARG when the path does not apply; the caller then copies everything
+ * and solves. */
 static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, const int *colind, const int *rowptr,
                           const void *aij, const void *b, int cplx, refine_opts *o, long long *launches)
 {
@@ -826,7 +917,10 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     if (!c->copy_stream) TRY(spk_stream_create(&c->copy_stream));
     for (int i = 0; i < 4; i++)
         if (!c->range_streams[i]) TRY(spk_stream_create(&c->range_streams[i]));
+    for (int i = 0; i <= PIPE_RANGES; i++)
+        if (!c->range_events[i]) TRY(spk_event_create(&c->range_events[i]));
     void *cs = c->copy_stream;
+    void **ev = c->range_events; /* ev[r]: range r's entries are on the device; ev[PIPE_RANGES]: all columns */
     TRY(spk_stream_fork(c->stream, cs)); /* after whatever the caller queued on the context's stream */
     TRY(spk_memcpy_h2d(c->d_rowptr, rowptr, sizeof(int) * ((size_t)n + 1), cs));
     TRY(spk_memcpy_h2d(c->d_b, b, hs * (size_t)n * nrhs, cs));
@@ -835,22 +929,94 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     Q->launches = 0;
     Q->timing = 0;
     Q->validate = 1;
+    Q->impl_cols = 0;
+    Q->impl_kl = Q->kl;
     int rc = spk_memset(Q->d_err, 0, sizeof(unsigned) * 4, c->stream);
     if (rc == SPK_OK) rc = spk_stream_fork(c->stream, cs); /* the cleared error word before any range */
+
+    /* the band check's workers (none: copy the columns with the values) */
+    band_scan S;
+    pthread_t th[SCAN_MAX_THREADS];
+    band_scan_arg args[SCAN_MAX_THREADS];
+    int workers = 0;
+    int implied = 0; /* ranges so far have implied columns */
+    if (rc == SPK_OK && c->host_threads > 0 && rowptr[0] == 0) {
+        const int want = c->host_threads < SCAN_MAX_THREADS ? c->host_threads : SCAN_MAX_THREADS;
+        S.rowptr = rowptr;
+        S.colind = colind;
+        S.n = n;
+        S.ku = Q->ku;
+        S.kl = Q->kl;
+        S.nnz = nnz;
+        S.nthreads = want;
+        for (int r = 0; r <= PIPE_RANGES; r++) S.row_lo[r] = Q->part_start[(int)((long long)Q->p * r / PIPE_RANGES)];
+        for (int g = 0; g < PIPE_RANGES; g++) {
+            atomic_init(&S.done[g], 0);
+            atomic_init(&S.bad[g], 0);
+        }
+        atomic_init(&S.stop, 0);
+        for (int i = 0; i < want; i++) {
+            args[i].S = &S;
+            args[i].id = i;
+            if (pthread_create(&th[i], NULL, band_scan_worker, &args[i]) != 0) break;
+            workers++;
+        }
+        if (workers < want) { /* the rows are split among `want`: without all of them, copy the columns */
+            atomic_store(&S.stop, 1);
+            for (int i = 0; i < workers; i++) pthread_join(th[i], NULL);
+            workers = 0;
+        }
+        implied = workers > 0;
+    }
+    int columns_sent = 0; /* every column index is (or will be, on cs) on the device */
+    if (implied) { /* the values first, all of them: their copies are what the check hides behind */
+        for (int r = 0; r < PIPE_RANGES && rc == SPK_OK; r++) {
+            const size_t e0 = (size_t)tb[r], ne = (size_t)(tb[r + 1] - tb[r]);
+            if (ne) rc = spk_memcpy_h2d((char *)c->d_aij + hs * e0, (const char *)aij + hs * e0, hs * ne, cs);
+            if (rc == SPK_OK) rc = spk_event_record(ev[r], cs);
+        }
+    }
+    const int all_tried = implied;
+    int all_implied = implied;
+    int late = 0; /* the column indices follow every value (a range failed the check) */
+    int n_implied = 0; /* ranges factored with implied columns */
     /* ranges are factored on a few streams at once: one range's chains use a
      * fraction of the GPU */
     for (int r = 0; r < PIPE_RANGES && rc == SPK_OK; r++) {
         const int p0 = (int)((long long)Q->p * r / PIPE_RANGES), p1 = (int)((long long)Q->p * (r + 1) / PIPE_RANGES);
         const size_t e0 = (size_t)tb[r], ne = (size_t)(tb[r + 1] - tb[r]);
         void *rs = c->range_streams[r % 4];
-        if (ne) {
-            rc = spk_memcpy_h2d((int *)c->d_colind + e0, colind + e0, sizeof(int) * ne, cs);
-            if (rc == SPK_OK) rc = spk_memcpy_h2d((char *)c->d_aij + hs * e0, (const char *)aij + hs * e0, hs * ne, cs);
+        if (implied) {
+            while (atomic_load(&S.done[r]) < workers) sched_yield();
+            if (atomic_load(&S.bad[r])) { /* from this range on: the columns go over as well */
+                implied = 0;
+                all_implied = 0;
+                late = 1;
+                rc = spk_memcpy_h2d(c->d_colind, colind, sizeof(int) * (size_t)nnz, cs);
+                if (rc == SPK_OK) rc = spk_event_record(ev[PIPE_RANGES], cs);
+                columns_sent = 1;
+            }
+        } else if (!all_tried) { /* no check: each range's columns and values together */
+            if (ne) {
+                rc = spk_memcpy_h2d((int *)c->d_colind + e0, colind + e0, sizeof(int) * ne, cs);
+                if (rc == SPK_OK)
+                    rc = spk_memcpy_h2d((char *)c->d_aij + hs * e0, (const char *)aij + hs * e0, hs * ne, cs);
+            }
+            if (rc == SPK_OK) rc = spk_event_record(ev[r], cs);
+            if (r == PIPE_RANGES - 1) columns_sent = 1;
         }
-        if (rc == SPK_OK) rc = spk_stream_fork(cs, rs);
-        if (rc == SPK_OK)
+        if (rc == SPK_OK) rc = spk_stream_wait_event(rs, late ? ev[PIPE_RANGES] : ev[r]);
+        if (rc == SPK_OK) {
+            Q->impl_cols = implied;
+            n_implied += implied;
             rc = spk_factor_range(Q, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, p0, p1, rs);
+        }
     }
+    if (workers) {
+        atomic_store(&S.stop, 1);
+        for (int i = 0; i < workers; i++) pthread_join(th[i], NULL);
+    }
+    Q->impl_cols = all_implied; /* the residual reads columns unless every range had them implied */
     for (int i = 0; i < 4 && rc == SPK_OK; i++) rc = spk_stream_fork(c->range_streams[i], c->stream);
     if (rc == SPK_OK) rc = spk_stream_fork(cs, c->stream);
     if (rc == SPK_OK) rc = spk_factor_tips(Q, c->stream);
@@ -861,15 +1027,24 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     unsigned e[4] = {0, 0, 0, 0};
     if (rc == SPK_OK) {
         const int frc = check_device_error(Q, c->stream, e);
-        const int ku = (int)e[1], kl = (int)e[2], kmax = ku > kl ? ku : kl;
+        /* ranges with implied columns are the plan's band exactly; the others measured theirs */
+        int ku = (int)e[1], kl = (int)e[2];
+        if (n_implied) {
+            if (Q->ku > ku) ku = Q->ku;
+            if (Q->kl > kl) kl = Q->kl;
+        }
+        const int kmax = ku > kl ? ku : kl;
         const int same =
             !(e[0] & (SPK_DEV_ERR_CSR | SPK_DEV_ERR_BAND)) && spk_choose_block(kmax < 1 ? 1 : kmax) == Q->KB;
         if (!same) {
             Q->first_applied = 0;
-            /* the whole matrix is on the device now: the general path re-plans */
+            Q->impl_cols = 0;
+            /* the general path re-plans with the whole matrix on the device */
+            if (!columns_sent) rc = spk_memcpy_h2d(c->d_colind, colind, sizeof(int) * (size_t)nnz, c->stream);
             long long l2 = 0;
-            rc = run_device(c, n, nnz, nrhs, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij, c->d_x,
-                            c->d_b, cplx, o, &l2);
+            if (rc == SPK_OK)
+                rc = run_device(c, n, nnz, nrhs, (const int *)c->d_rowptr, (const int *)c->d_colind, c->d_aij,
+                                c->d_x, c->d_b, cplx, o, &l2);
             *launches = Q->launches + l2;
             return rc;
         }
@@ -883,6 +1058,7 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     Q->first_applied = 0;
     *launches = Q->launches;
     fill_info(c, Q, o, Q->launches);
+    Q->impl_cols = 0;
     return rc;
 }
 

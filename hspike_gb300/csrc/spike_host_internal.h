@@ -26,9 +26,11 @@ struct spike_context_s {
     void *copy_stream;     /* host -> device copies that overlap the factorization (created on demand) */
     void *range_streams[4]; /* the factorization of those copies' partition ranges (created on demand) */
     void *aux_stream;       /* the reduced factorization, beside the first sweep (created on demand) */
+    void *range_events[9];  /* one per partition range's copy, one for the column indices (on demand) */
     /* options */
     int refs; /* the creator's reference + one per factor handle or batch using the context */
     int mode, partitions, max_refine, red_refine, timing, twist;
+    int host_threads; /* SPIKE_OPT_HOST_THREADS */
     int stream_alloc; /* workspace allocated stream-ordered on `stream` */
     double tol;
     /* cached plan for the reference-API and device-pointer calls */

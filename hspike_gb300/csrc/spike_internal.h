@@ -94,6 +94,11 @@ typedef struct spk_plan {
     /* k_band_tiles also validates the CSR and measures the bandwidth into
      * d_err[1..2] (set when the separate analysis pass was skipped) */
     int validate;
+    /* impl_cols: the device holds no column indices for this call -- the host
+     * verified that every row r is the full band, columns max(0, r - impl_kl)
+     * .. min(n - 1, r + ku) -- so the band tiles and the residual derive the
+     * column of entry t of row r as max(0, r - impl_kl) + (t - rowptr[r]) */
+    int impl_cols, impl_kl;
     /* the first right-hand-side chunk's y = A_i^{-1} b already ran (next to
      * the reduced factorization, on another stream) */
     int first_applied;
@@ -208,6 +213,11 @@ int spk_graph_launch(void *graph_exec, void *stream);
 void spk_graph_destroy(void *graph_exec);
 /* make `child` wait for the work issued so far on `parent` */
 int spk_stream_fork(void *parent, void *child);
+/* events without timing: record on a stream, make another stream wait */
+int spk_event_create(void **event);
+void spk_event_destroy(void *event);
+int spk_event_record(void *event, void *stream);
+int spk_stream_wait_event(void *stream, void *event);
 /* timing with an event pair on one stream (ms between begin and end) */
 int spk_timer_begin(void **timer, void *stream);
 int spk_timer_end(void *timer, void *stream, double *ms);

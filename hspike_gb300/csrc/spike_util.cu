@@ -270,11 +270,11 @@ extern "C" int spk_narrow(const void *src, void *dst, long long count, int is_co
 // into norms[].
 constexpr int RES_MAXH = 32;
 
-template <class H, int G, int NH>
+template <class H, int G, int NH, bool IMPL>
 __global__ void __launch_bounds__(256)
     k_residual(int n, const int *__restrict__ rowptr, const int *__restrict__ colind, const H *__restrict__ aij,
                const H *__restrict__ x, const H *__restrict__ b, H *r, int h0, int nr, int want_b, double *norms,
-               int nrhs_total)
+               int nrhs_total, int impl_kl)
 {
     __shared__ double sr[RES_MAXH], sb[RES_MAXH];
     for (int q = threadIdx.x; q < RES_MAXH; q += blockDim.x) sr[q] = sb[q] = 0.0;
@@ -298,12 +298,14 @@ __global__ void __launch_bounds__(256)
             const long long row = base + lane / G;
             const bool valid = row < n;
             const int t0 = valid ? rowptr[row] : 0, t1 = valid ? rowptr[row + 1] : 0;
+            // IMPL: the row is the full band (checked on the host), colind is not read
+            const int cfirst = IMPL ? max(0, (int)row - impl_kl) - t0 : 0;
             H acc[NH];
 #pragma unroll
             for (int j = 0; j < NH; j++) acc[j] = sc_zero<H>();
             for (int t = t0 + sub; t < t1; t += G) {
                 const H av = aij[t];
-                const int c = colind[t];
+                const int c = IMPL ? cfirst + t : colind[t];
 #pragma unroll
                 for (int j = 0; j < NH; j++)
                     if (hb + j < nr) acc[j] = madd(acc[j], av, xj[j][c]);
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-template <class H, int G>
+template <class H, int G, bool IMPL>
 static int launch_residual(const spk_plan *P, const int *rp, const int *ci, const void *a, const void *x, const void *b,
                            void *r, int nrhs, int want_b, double *norms, cudaStream_t st)
 {
@@ -366,14 +368,17 @@ static int launch_residual(const spk_plan *P, const int *rp, const int *ci, cons
     for (int h0 = 0; h0 < nrhs; h0 += RES_MAXH) {
         const int nr = nrhs - h0 < RES_MAXH ? nrhs - h0 : RES_MAXH;
         if (nr >= 4)
-            k_residual<H, G, 4><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
-                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs);
+            k_residual<H, G, 4, IMPL><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
+                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs,
+                                                                 P->impl_cols ? P->impl_kl : -1);
         else if (nr >= 2)
-            k_residual<H, G, 2><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
-                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs);
+            k_residual<H, G, 2, IMPL><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
+                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs,
+                                                                 P->impl_cols ? P->impl_kl : -1);
         else
-            k_residual<H, G, 1><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
-                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs);
+            k_residual<H, G, 1, IMPL><<<(unsigned)blocks, 256, 0, st>>>(P->n, rp, ci, (const H *)a, (const H *)x,
+                                                                 (const H *)b, (H *)r, h0, nr, want_b, norms, nrhs,
+                                                                 P->impl_cols ? P->impl_kl : -1);
         if (cudaGetLastError() != cudaSuccess) return SPK_ECUDA;
         ((spk_plan *)P)->launches++;
     }
@@ -387,9 +392,14 @@ static int residual_g(const spk_plan *P, const int *rp, const int *ci, const voi
     // few lanes per row: every shuffle step of the row reduction is an FP64
     // add per lane, and GB300's FP64 pipe is the residual's bottleneck
     const double per_row = P->n > 0 ? (double)P->nnz / P->n : 1.0;
-    if (per_row >= 64) return launch_residual<H, 4>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    if (per_row >= 12) return launch_residual<H, 2>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    return launch_residual<H, 1>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (P->impl_cols) {
+        if (per_row >= 64) return launch_residual<H, 4, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+        if (per_row >= 12) return launch_residual<H, 2, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+        return launch_residual<H, 1, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    }
+    if (per_row >= 64) return launch_residual<H, 4, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (per_row >= 12) return launch_residual<H, 2, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    return launch_residual<H, 1, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
 }
 
 extern "C" int spk_residual(const spk_plan *P, const int *d_rowptr, const int *d_colind, const void *d_aij,
@@ -583,6 +593,25 @@ extern "C" int spk_graph_launch(void *graph_exec, void *stream)
 extern "C" void spk_graph_destroy(void *graph_exec)
 {
     if (graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)graph_exec);
+}
+extern "C" int spk_event_create(void **event)
+{
+    cudaEvent_t e;
+    const int r = ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    *event = r == SPK_OK ? (void *)e : nullptr;
+    return r;
+}
+extern "C" void spk_event_destroy(void *event)
+{
+    if (event) cudaEventDestroy((cudaEvent_t)event);
+}
+extern "C" int spk_event_record(void *event, void *stream)
+{
+    return ck(cudaEventRecord((cudaEvent_t)event, (cudaStream_t)stream));
+}
+extern "C" int spk_stream_wait_event(void *stream, void *event)
+{
+    return ck(cudaStreamWaitEvent((cudaStream_t)stream, (cudaEvent_t)event, 0));
 }
 extern "C" int spk_stream_fork(void *parent, void *child)
 {

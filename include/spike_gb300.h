@@ -43,6 +43,10 @@ typedef struct spike_factor_s *spike_factor_t;
 #define SPIKE_OPT_TWIST 7          /* 1 = eliminate each partition from both ends at once where the kernels
                                       allow it (tiles 16..64 fitting four CTAs per SM, >= 8 blocks per
                                       partition); 0 = top-down only (default 1) */
+#define SPIKE_OPT_HOST_THREADS 8   /* host threads that, in a call with host arrays whose plan is reused,
+                                      check that the CSR is the full band while its values travel, so
+                                      the column indices stay on the host (default 8; 0 = always copy
+                                      them) */
 
 #define SPIKE_PRECISION_MIXED 0 /* FP32 / complex64 factors, FP64 residual + update + reduced solve */
 #define SPIKE_PRECISION_FP64 1  /* FP64 / complex128 everywhere */
@@ -81,6 +85,7 @@ typedef struct {
     long long kernel_launches; /* kernels launched by the last call */
     size_t device_bytes;      /* device memory held by the context's plan */
     int twisted;              /* 1 if the partitions were eliminated from both ends (SPIKE_OPT_TWIST) */
+    int columns_implied;      /* 1 if the column indices stayed on the host (full band, SPIKE_OPT_HOST_THREADS) */
 } spike_info_t;
 Error_t spike_get_info(spike_context_t ctx, spike_info_t *info);
 

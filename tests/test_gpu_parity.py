@@ -448,6 +448,62 @@ def test_reduced_factorization_beside_first_sweep(n, k, nrhs, complex_, mode, tw
         ctx.close()
 
 
+def test_host_arrays_full_band_columns_stay_on_host():
+    # a reused plan's call with host arrays checks on host threads that the CSR
+    # is the full band while the values travel; the column indices then never
+    # cross the host link, and the results equal those of the copied columns
+    ctx = hs.Context()
+    try:
+        n, k = 220000, 30
+        rp, ci, a, xt, b = hs.gen_banded(n, k, k, 1.5, seed=33, nrhs=2)
+        assert len(ci) >= 8 << 20
+        hs.solve(rp, ci, a, b, ctx=ctx)                       # plans
+        x_imp = hs.solve(rp, ci, a, b, ctx=ctx)
+        assert ctx.info().columns_implied == 1 and ctx.info().twisted == 1
+        assert (ctx.info().ku, ctx.info().kl) == (k, k)
+        ctx.set_option(hs.SPIKE_OPT_HOST_THREADS, 0)
+        x_cols = hs.solve(rp, ci, a, b, ctx=ctx)
+        assert ctx.info().columns_implied == 0
+        ctx.set_option(hs.SPIKE_OPT_HOST_THREADS, 8)
+        assert np.array_equal(x_imp, x_cols)
+        assert oracle.residual(rp, ci, a, x_imp, b).max() <= RES_TOL
+        assert relerr(x_imp, xt) <= 1e-10
+        # one row past the middle reaches one column further left: the ranges
+        # before it keep implied columns, the rest are sent and validated
+        r = int(n * 0.7)
+        ci2 = ci.copy()
+        ci2[rp[r]] = r - k - 1
+        x2 = hs.solve(rp, ci2, a, b, ctx=ctx)
+        assert ctx.info().columns_implied == 0
+        assert (ctx.info().ku, ctx.info().kl) == (k, k + 1)
+        assert oracle.residual(rp, ci2, a, x2, b).max() <= RES_TOL
+        # the band of the new plan (kl = k + 1) is not the full band either
+        x2b = hs.solve(rp, ci2, a, b, ctx=ctx)
+        assert ctx.info().columns_implied == 0 and np.array_equal(x2, x2b)
+        # back to the full band (kl = k, within the plan's tile class)
+        x3 = hs.solve(rp, ci, a, b, ctx=ctx)
+        assert oracle.residual(rp, ci, a, x3, b).max() <= RES_TOL
+        x3 = hs.solve(rp, ci, a, b, ctx=ctx)
+        assert ctx.info().columns_implied == 1 and np.array_equal(x3, x_imp)
+        # an unsorted row in the middle is still caught (on the device, after the check fails)
+        bad = ci.copy()
+        q = rp[int(n * 0.4)] + 5
+        bad[q], bad[q + 1] = bad[q + 1], bad[q]
+        with pytest.raises(hs.SpikeError) as e:
+            hs.solve(rp, bad, a, b, ctx=ctx)
+        assert e.value.name == "csr"
+        # complex data
+        rp, ci, a, xt, b = hs.gen_banded(200000, 24, 24, 1.5, seed=34, complex_=True, nrhs=1)
+        assert len(ci) >= 8 << 20
+        for _ in range(2):
+            x = hs.solve(rp, ci, a, b, ctx=ctx)
+        assert ctx.info().columns_implied == 1
+        assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
+        assert relerr(x, xt) <= 1e-10
+    finally:
+        ctx.close()
+
+
 def test_bandwidth_above_tile_is_rejected():
     rp, ci, a, xt, b = hs.gen_banded(2000, 130, 130, 1.5, seed=18)
     x = np.zeros_like(b, order="F")
