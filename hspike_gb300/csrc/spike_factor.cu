@@ -36,7 +36,11 @@ template <class T, int KB> struct FactorSmem {
     static constexpr bool BIG = KB >= 128;
     static constexpr size_t tile = sizeof(T) * TL::ELEMS;
     static constexpr size_t fwd = (BIG ? 3 : 6) * tile + sizeof(T) * TL::INV_BUF + 64;
-    static constexpr size_t band = 3 * sizeof(T) * KB * (KB + 1) + sizeof(int) * (KB + 1) + 64;
+    // k_band_tiles: small tiles pack BG row blocks into one CTA (one warp or
+    // warp pair each), so the grid is not a million one-warp CTAs
+    static constexpr int BG = KB <= 16 ? 256 / NTOf<KB>::value : 1;
+    static constexpr size_t band_one = (3 * sizeof(T) * KB * (KB + 1) + sizeof(int) * (KB + 1) + 15) / 16 * 16;
+    static constexpr size_t band = BG * band_one + 64;
     static constexpr size_t bwd = (BIG ? 3 : 6) * tile + 64; // (also k_wsweep_big: three tiles)
 };
 
@@ -91,20 +95,69 @@ __device__ __forceinline__ void place_entry(int lr, int lrow, int c, H a, int s,
 template <class T, class H, int KB, int LD, bool VAL, bool IMPL = false>
 __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, const int *__restrict__ colind,
                               const H *__restrict__ aij, int s, int e, int J, T *F, T *D, T *En, T *gZ,
-                              T *gBhat, unsigned *err, int *srp, int n, long long nnz, int impl_kl)
+                              T *gBhat, unsigned *err, int *srp, int n, long long nnz, int impl_kl, int tid,
+                              bool live)
 {
     constexpr int NT = NTOf<KB>::value;
     constexpr int NW = NT / 32;
     const int m = e - s;
     const int lrow0 = J * KB;
     const int nr = min(KB, m - lrow0); // real rows in the block, >= 1
-    for (int q = threadIdx.x; q <= nr; q += NT) srp[q] = rowptr[s + lrow0 + q];
-    for (int lr = nr + threadIdx.x; lr < KB; lr += NT) D[lr * LD + lr] = sc_one<T>(); // identity padding
+    if (live) {
+        for (int q = tid; q <= nr; q += NT) srp[q] = rowptr[s + lrow0 + q];
+        for (int lr = nr + tid; lr < KB; lr += NT) D[lr * LD + lr] = sc_one<T>(); // identity padding
+    }
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (!live) return; // (a CTA's spare block slot: every barrier above is shared)
+    const int warp = tid >> 5, lane = tid & 31;
     // pieces per iteration: a whole row of the band (2 KB + 1 entries) in one go
     constexpr int PPR = (2 * KB + 1 + 31) / 32 < 1 ? 1 : (2 * KB + 1 + 31) / 32 > 5 ? 5 : (2 * KB + 1 + 31) / 32;
     int ku = 0, kl = 0;
+    if constexpr (KB <= 16) {
+        // Short rows (2 KB + 1 <= 33 entries): the block's entries are one
+        // contiguous run, so the threads take it flat -- every entry of every
+        // row in flight at once -- and find each entry's row among the block's
+        // row pointers in shared memory.
+        const int T0 = srp[0], T1 = srp[nr];
+        bool rows_ok = T0 >= 0 && (long long)T1 <= nnz && T1 >= T0;
+        if constexpr (VAL) {
+            for (int q = tid; q < nr; q += NT)
+                if (srp[q] < 0 || (long long)srp[q + 1] > nnz || srp[q + 1] < srp[q]) atomicOr(err, SPK_DEV_ERR_CSR);
+            if (!rows_ok && tid == 0) atomicOr(err, SPK_DEV_ERR_CSR);
+        }
+        constexpr int U = 4; // entries per thread in flight
+        for (int base = rows_ok ? T0 : T1; base < T1; base += NT * U) {
+            int c[U], lrs[U];
+            H a[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int t = base + tid + u * NT;
+                lrs[u] = 0;
+                if (t < T1) {
+                    int lr = 0;
+#pragma unroll
+                    for (int q = 1; q < KB; q++) lr += (q < nr && srp[q] <= t);
+                    lrs[u] = lr;
+                    c[u] = IMPL ? max(0, s + lrow0 + lr - impl_kl) + (t - srp[lr]) : __ldg(colind + t);
+                    a[u] = aij[t];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int t = base + tid + u * NT;
+                if (t < T1) {
+                    const int lr = lrs[u], grow = s + lrow0 + lr;
+                    if constexpr (VAL) {
+                        if (c[u] < 0 || c[u] >= n || (t > srp[lr] && __ldg(colind + t - 1) >= c[u]))
+                            atomicOr(err, SPK_DEV_ERR_CSR);
+                        ku = max(ku, c[u] - grow);
+                        kl = max(kl, grow - c[u]);
+                    }
+                    place_entry<T, H, KB, LD>(lr, lrow0 + lr, c[u], a[u], s, m, J, F, D, En, gZ, gBhat, err);
+                }
+            }
+        }
+    } else
     for (int lr = warp; lr < nr; lr += NW) {
         const int t0 = srp[lr], t1 = srp[lr + 1];
         if (VAL && (t0 < 0 || (long long)t1 > nnz || t1 < t0)) {
@@ -150,9 +203,13 @@ __device__ __forceinline__ void scatter_block(const int *__restrict__ rowptr, co
             ku = max(ku, __shfl_xor_sync(0xffffffffu, ku, o));
             kl = max(kl, __shfl_xor_sync(0xffffffffu, kl, o));
         }
+        // every warp of every block reaches here: read first and update only
+        // with a larger value, so the two words see a handful of atomics
+        // instead of millions serialised at one L2 slice (a stale read only
+        // costs an atomic that was not needed)
         if (lane == 0) {
-            atomicMax(err + 1, (unsigned)ku);
-            atomicMax(err + 2, (unsigned)kl);
+            if ((unsigned)ku > *(volatile const unsigned *)(err + 1)) atomicMax(err + 1, (unsigned)ku);
+            if ((unsigned)kl > *(volatile const unsigned *)(err + 2)) atomicMax(err + 2, (unsigned)kl);
         }
     }
 }
@@ -198,22 +255,27 @@ __device__ __forceinline__ void store_tile_cm(T *g, const T *s)
 // bottom-up chain instead (spike_twist.cu): A(J,J-1) row-major in gT and
 // column-major in gE for J > M, A(J,J+1) column-major in gT for J >= M.
 template <class T, int KB>
-__global__ void __launch_bounds__(NTOf<KB>::value)
+__global__ void __launch_bounds__(NTOf<KB>::value * FactorSmem<T, KB>::BG)
     k_band_tiles(const int *__restrict__ rowptr, const int *__restrict__ colind,
                  const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
                  const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
                  unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys, int twist,
-                 int validate, int n, long long nnz, int gb0, int nb_total, int impl_kl)
+                 int validate, int n, long long nnz, int gb0, int gb_end, int nb_total, int impl_kl)
 {
     using H = typename HighOf<T>::type;
+    using FS = FactorSmem<T, KB>;
+    constexpr int NT = NTOf<KB>::value;
     constexpr size_t TS = (size_t)KB * KB;
-    const int gb = blockIdx.x + gb0; // this launch covers blocks [gb0, gb0 + gridDim.x)
-    const int part = blk_part[gb];
-    const int J = gb - blk_off[part];
-    const int M = twist ? (blk_off[part + 1] - blk_off[part]) / 2 : 1 << 30; // middle block
-    int s = part_start[part], e = part_start[part + 1];
-    const bool zt = J == 0 && part > 0;
-    if (sys) { // batch group: the partition's own system, in its local rows
+    // this launch covers blocks [gb0, gb_end), FS::BG per CTA (NT threads each)
+    const int grp = threadIdx.x / NT, tid = threadIdx.x - grp * NT;
+    const int gb = (int)blockIdx.x * FS::BG + grp + gb0;
+    const bool live = gb < gb_end;
+    const int part = live ? blk_part[gb] : 0;
+    const int J = live ? gb - blk_off[part] : 0;
+    const int M = twist && live ? (blk_off[part + 1] - blk_off[part]) / 2 : 1 << 30; // middle block
+    int s = live ? part_start[part] : 0, e = live ? part_start[part + 1] : 0;
+    const bool zt = live && J == 0 && part > 0;
+    if (sys && live) { // batch group: the partition's own system, in its local rows
         const spk_sysref &S = sys[part_sys[part]];
         rowptr = S.rowptr;
         colind = S.colind;
@@ -226,40 +288,43 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     constexpr int LD1 = KB + 1;
     constexpr int EL1 = KB * LD1;
     extern __shared__ char smraw[];
-    T *sD = (T *)smem_align(smraw), *sF = sD + EL1, *sE = sF + EL1;
+    T *sD = (T *)(smem_align(smraw) + grp * FS::band_one), *sF = sD + EL1, *sE = sF + EL1;
     int *srp = (int *)(sE + EL1);
     T *gz = zt ? gZ + (size_t)blk_off[part] * TS : nullptr;
-    zero_tile<T, KB, LD1>(sD);
-    zero_tile<T, KB, LD1>(sF);
-    zero_tile<T, KB, LD1>(sE);
+    for (int q = tid; q < 3 * EL1; q += NT) sD[q] = sc_zero<T>(); // sD, sF, sE are consecutive
     if (zt)
-        for (int q = threadIdx.x; q < KB * KB; q += NTOf<KB>::value) gz[q] = sc_zero<T>();
+        for (int q = tid; q < KB * KB; q += NT) gz[q] = sc_zero<T>();
     __syncthreads();
     if (validate) {
         scatter_block<T, H, KB, LD1, true>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
-                                           err, srp, n, nnz, impl_kl);
-        if (threadIdx.x == 0 && ((gb == 0 && rowptr[0] != 0) || (gb == nb_total - 1 && (long long)rowptr[n] != nnz)))
+                                           err, srp, n, nnz, impl_kl, tid, live);
+        if (live && tid == 0 && ((gb == 0 && rowptr[0] != 0) || (gb == nb_total - 1 && (long long)rowptr[n] != nnz)))
             atomicOr(err, SPK_DEV_ERR_CSR);
     } else if (impl_kl >= 0) {
         scatter_block<T, H, KB, LD1, false, true>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz,
-                                                  gBhat + (size_t)part * TS, err, srp, n, nnz, impl_kl);
+                                                  gBhat + (size_t)part * TS, err, srp, n, nnz, impl_kl, tid, live);
     } else {
         scatter_block<T, H, KB, LD1, false>(rowptr, colind, aij, s, e, J, sF, sD, sE, gz, gBhat + (size_t)part * TS,
-                                            err, srp, n, nnz, impl_kl);
+                                            err, srp, n, nnz, impl_kl, tid, live);
     }
     __syncthreads();
+    if (!live) return;
+    // shared tile (row stride LD1) -> global tile, row-major or column-major
+    auto put = [&](T *g, const T *sm, bool cm) {
+        for (int q = tid; q < KB * KB; q += NT) {
+            const int a = q / KB, b = q - a * KB;
+            g[q] = cm ? sm[b * LD1 + a] : sm[a * LD1 + b];
+        }
+    };
     T *g = gT + (size_t)gb * 3 * TS;
-    store_tile<T, KB, LD1>(g, sD);
-    if (J <= M)
-        store_tile<T, KB, LD1>(g + TS, sF); // the shared image of F^T: A(J,J-1) column-major
-    else
-        store_tile_cm<T, KB, LD1>(g + TS, sF); // A(J,J-1) row-major
+    put(g, sD, false);
+    put(g + TS, sF, J > M); // J <= M: the shared image of F^T, A(J,J-1) column-major; beyond: row-major
     if (J < M) {
-        store_tile<T, KB, LD1>(g + 2 * TS, sE);
-        store_tile_cm<T, KB, LD1>(gE + (size_t)gb * TS, sE);
+        put(g + 2 * TS, sE, false);
+        put(gE + (size_t)gb * TS, sE, true);
     } else {
-        store_tile_cm<T, KB, LD1>(g + 2 * TS, sE); // A(J,J+1) column-major
-        if (J > M) store_tile<T, KB, LD1>(gE + (size_t)gb * TS, sF); // A(J,J-1) column-major
+        put(g + 2 * TS, sE, true); // A(J,J+1) column-major
+        if (J > M) put(gE + (size_t)gb * TS, sF, false); // A(J,J-1) column-major
     }
 }
 
@@ -886,11 +951,11 @@ template <class T, int KB> int run_factor_range(spk_plan *P, const int *rowptr, 
     const int b0 = P->blk_off[part0], b1 = P->blk_off[part1];
     if (cudaMemsetAsync((T *)P->d_Bhat + (size_t)part0 * TS, 0, sizeof(T) * TS * (part1 - part0), st) != cudaSuccess)
         return SPK_ECUDA;
-    k_band_tiles<T, KB><<<b1 - b0, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off,
-                                                      P->d_blk_part, (T *)P->d_T, (T *)P->d_E, (T *)P->d_W,
-                                                      (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist,
-                                                      P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz, b0,
-                                                      P->total_blocks, P->impl_cols ? P->impl_kl : -1);
+    k_band_tiles<T, KB><<<(b1 - b0 + S::BG - 1) / S::BG, NT * S::BG, S::band, st>>>(
+        rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
+        (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist,
+        P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz, b0, b1, P->total_blocks,
+        P->impl_cols ? P->impl_kl : -1);
     SPK_CHECK_LAUNCH();
     P->launches++;
     int rc = spk_twist_factor(P, 1, part0, part1, st);
@@ -937,12 +1002,11 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     const size_t TS = (size_t)KB * KB;
     if (cudaMemsetAsync(P->d_Bhat, 0, sizeof(T) * TS * P->p, st) != cudaSuccess) return SPK_ECUDA;
     spk_phase_begin(P, SPK_PH_BAND_TILES, st);
-    k_band_tiles<T, KB><<<P->total_blocks, NT, S::band, st>>>(rowptr, colind, (const H *)aij, P->d_part_start,
-                                                              P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
-                                                              (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys,
-                                                              P->d_part_sys, P->twist,
-                                                              P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz,
-                                                              0, P->total_blocks, P->impl_cols ? P->impl_kl : -1);
+    k_band_tiles<T, KB><<<(P->total_blocks + S::BG - 1) / S::BG, NT * S::BG, S::band, st>>>(
+        rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
+        (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist,
+        P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz, 0, P->total_blocks, P->total_blocks,
+        P->impl_cols ? P->impl_kl : -1);
     SPK_CHECK_LAUNCH();
     spk_phase_end(P, st);
     if (P->twist) { // two-sided chains (spike_twist.cu)

@@ -209,9 +209,9 @@ __global__ void k_analyze(int n, long long nnz, const int *__restrict__ rowptr, 
         kl = max(kl, __shfl_xor_sync(0xffffffffu, kl, o));
         flags |= __shfl_xor_sync(0xffffffffu, flags, o);
     }
-    if (lane == 0) {
-        atomicMax(&out[0], ku);
-        atomicMax(&out[1], kl);
+    if (lane == 0) { // (read first: most warps have nothing larger to add)
+        if (ku > *(volatile const int *)&out[0]) atomicMax(&out[0], ku);
+        if (kl > *(volatile const int *)&out[1]) atomicMax(&out[1], kl);
         if (flags) atomicOr((unsigned *)&out[2], flags);
     }
 }
