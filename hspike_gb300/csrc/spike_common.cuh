@@ -751,7 +751,7 @@ template <class T, int KB> __device__ __forceinline__ bool row_inv(unsigned m, T
     for (int j = 0; j < KB; j++) {
         const T piv = seg_shfl<KB>(m, s[j], j);
         if (!sc_finite_nonzero(piv)) ok = false;
-        const T ip = sc_recip(piv);
+        const T ip = sc_rcp_fast(piv);
         if (r == j) {
 #pragma unroll
             for (int c = 0; c < KB; c++)

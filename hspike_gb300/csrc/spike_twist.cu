@@ -384,7 +384,9 @@ template <class T, int KB> struct QTw {
     static constexpr size_t SMEM = (size_t)CPC * SLOT;
 };
 
-// chains 2*part (top) and 2*part + 1 (bottom)
+// The first half of the grid runs the top chains, the second half the
+// bottom chains, so a warp never holds both: their loops differ, and a warp
+// with both would step through one and then the other.
 template <class T, int KB>
 __global__ void __launch_bounds__(QTw<T, KB>::NT)
     k_qtw_lu(const T *__restrict__ gT, const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
@@ -394,10 +396,10 @@ __global__ void __launch_bounds__(QTw<T, KB>::NT)
     constexpr int TS = C::TS, D = C::DEPTH;
     constexpr int CH = C::STAGE * (int)sizeof(T) / 16;
     extern __shared__ __align__(16) char smc[];
-    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
+    const int half_grid = (int)gridDim.x / 2; // CTAs per direction
+    const bool bottom = (int)blockIdx.x >= half_grid;
+    const int part = ((int)blockIdx.x - (bottom ? half_grid : 0)) * ((int)blockDim.x / KB) + (int)threadIdx.x / KB;
     const int r = threadIdx.x % KB;
-    const int part = ch >> 1;
-    const bool bottom = ch & 1;
     if (part >= p) return; // whole segments leave together; no CTA barriers below
     const unsigned m = seg_mask<KB>();
     T *slot = (T *)(smc + (threadIdx.x / KB) * C::SLOT);
@@ -708,7 +710,7 @@ template <class T, int KB> int run_qtwist(spk_plan *P, cudaStream_t st, bool fwd
     const int p = P->p;
     if (fwd) {
         const int cpc = chains_per_cta(2LL * p, C::CPC);
-        k_qtw_lu<T, KB><<<(2 * p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * C::SLOT, st>>>(
+        k_qtw_lu<T, KB><<<2 * ((p + cpc - 1) / cpc), cpc * KB, (size_t)cpc * C::SLOT, st>>>(
             (const T *)P->d_T, P->d_part_start, P->d_blk_off, p, (const T *)P->d_Bhat, (T *)P->d_L, (T *)P->d_G,
             (T *)P->d_E, (T *)P->d_V, (T *)P->d_W, P->d_err);
         SPK_CHECK_LAUNCH();
