@@ -772,6 +772,48 @@ template <class T, int KB> __device__ __forceinline__ bool row_inv(unsigned m, T
     return ok;
 }
 
+// ------------------------------------------------------------ tiles on lanes, one element each
+// A chain of a tiny band (KB <= 4) that is mostly products and inverses runs
+// on KB*KB consecutive lanes: lane e of the segment holds element (e / KB,
+// e % KB) of every KB x KB tile, so a tile product is KB pairs of shuffles and
+// one multiply-add per lane (a lane holding a whole row needs KB times that).
+// out(r, c) = sum_k A(r, k) B(k, c)
+template <class T, int KB> __device__ __forceinline__ T el_mul(unsigned m, T a, T b, int r, int c)
+{
+    constexpr int EL = KB * KB;
+    T acc = sc_zero<T>();
+#pragma unroll
+    for (int k = 0; k < KB; k++) acc = madd(acc, seg_shfl<EL>(m, a, r * KB + k), seg_shfl<EL>(m, b, k * KB + c));
+    return acc;
+}
+// out(r, c) - sum_k A(r, k) B(k, c)
+template <class T, int KB> __device__ __forceinline__ T el_msub(unsigned m, T out, T a, T b, int r, int c)
+{
+    constexpr int EL = KB * KB;
+#pragma unroll
+    for (int k = 0; k < KB; k++) out = msub(out, seg_shfl<EL>(m, a, r * KB + k), seg_shfl<EL>(m, b, k * KB + c));
+    return out;
+}
+// In-place Gauss-Jordan inverse without pivoting, the same steps as row_inv
+// on elements: S[j][c] *= 1/p, S[j][j] = 1/p; S[r][c] -= S[r][j] S[j][c],
+// S[r][j] = -S[r][j]/p.  false on a zero or non-finite pivot (in every lane).
+template <class T, int KB> __device__ __forceinline__ bool el_inv(unsigned m, T &s, int r, int c)
+{
+    constexpr int EL = KB * KB;
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < KB; j++) {
+        const T piv = seg_shfl<EL>(m, s, j * KB + j);
+        if (!sc_finite_nonzero(piv)) ok = false;
+        const T ip = sc_rcp_fast(piv);
+        if (r == j) s = c == j ? ip : s * ip;
+        const T rowj = seg_shfl<EL>(m, s, j * KB + c); // S[j][c], scaled
+        const T colj = seg_shfl<EL>(m, s, r * KB + j); // S[r][j] (unchanged so far for r != j)
+        if (r != j) s = c == j ? -(colj * ip) : msub(s, colj, rowj);
+    }
+    return ok;
+}
+
 // Chains per CTA at launch: spread the chains over every SM (two CTAs each
 // where there are enough), at most cpc_max per CTA.
 static inline int chains_per_cta(long long chains, int cpc_max)

@@ -376,33 +376,35 @@ __global__ void __launch_bounds__(TwNT<KB>::value, 4)
 // chain and V's forward sweep along the bottom one.
 template <class T, int KB> struct QTw {
     static constexpr int TS = KB * KB;
+    static constexpr int EL = KB * KB;                               // lanes per chain: one tile element each
     static constexpr int DEPTH = 4;
     static constexpr int STAGE = 3 * TS;                             // three tiles per block
     static constexpr int SLOT = DEPTH * STAGE * (int)sizeof(T) + 16; // per chain
-    static constexpr int CPC = chain_threads(SLOT);                  // chains per CTA
-    static constexpr int NT = CPC * KB;
+    static constexpr int CPC = 256 / EL;                             // chains per CTA, at most
+    static constexpr int NT = CPC * EL;
     static constexpr size_t SMEM = (size_t)CPC * SLOT;
 };
 
 // The first half of the grid runs the top chains, the second half the
 // bottom chains, so a warp never holds both: their loops differ, and a warp
-// with both would step through one and then the other.
+// with both would step through one and then the other.  A chain takes KB*KB
+// lanes, lane (r, c) holding element (r, c) of each tile (el_mul, el_inv).
 template <class T, int KB>
 __global__ void __launch_bounds__(QTw<T, KB>::NT)
     k_qtw_lu(const T *__restrict__ gT, const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
              const T *__restrict__ gBhat, T *gL, T *gG, T *gE, T *gV, T *gW, unsigned *err)
 {
     using C = QTw<T, KB>;
-    constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int TS = C::TS, D = C::DEPTH, EL = C::EL;
     constexpr int CH = C::STAGE * (int)sizeof(T) / 16;
     extern __shared__ __align__(16) char smc[];
     const int half_grid = (int)gridDim.x / 2; // CTAs per direction
     const bool bottom = (int)blockIdx.x >= half_grid;
-    const int part = ((int)blockIdx.x - (bottom ? half_grid : 0)) * ((int)blockDim.x / KB) + (int)threadIdx.x / KB;
-    const int r = threadIdx.x % KB;
+    const int part = ((int)blockIdx.x - (bottom ? half_grid : 0)) * ((int)blockDim.x / EL) + (int)threadIdx.x / EL;
+    const int e = threadIdx.x % EL, r = e / KB, c = e % KB;
     if (part >= p) return; // whole segments leave together; no CTA barriers below
-    const unsigned m = seg_mask<KB>();
-    T *slot = (T *)(smc + (threadIdx.x / KB) * C::SLOT);
+    const unsigned m = seg_mask<EL>();
+    T *slot = (T *)(smc + (threadIdx.x / EL) * C::SLOT);
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
     const size_t tb = (size_t)blk_off[part] * TS;
     const T *gTp = gT + (size_t)blk_off[part] * C::STAGE;
@@ -410,7 +412,7 @@ __global__ void __launch_bounds__(QTw<T, KB>::NT)
     auto issue = [&](int i) {
         if (i < cnt) {
             const int J = bottom ? N - 1 - i : i;
-            for (int q = r; q < CH; q += KB)
+            for (int q = e; q < CH; q += EL)
                 cp_async16((char *)(slot + (i % D) * C::STAGE) + 16 * q,
                            (const char *)(gTp + (size_t)J * C::STAGE) + 16 * q);
         }
@@ -419,52 +421,32 @@ __global__ void __launch_bounds__(QTw<T, KB>::NT)
 #pragma unroll
     for (int i = 0; i < D - 1; i++) issue(i);
     bool ok = true;
+    const int rm = r * KB + c, cm = c * KB + r; // element (r, c) of a row-major / column-major tile
     if (!bottom) {
         // L_J = A(J,J-1) G_{J-1}, S_J = D_J - L_J A(J-1,J), G_J = S_J^{-1}; z_J = -L_J z_{J-1}
         const bool doW = part > 0;
-        T g[KB], ep[KB], zp[KB];
-#pragma unroll
-        for (int c = 0; c < KB; c++) {
-            g[c] = ep[c] = sc_zero<T>();
-            zp[c] = doW ? gW[tb + r * KB + c] : sc_zero<T>(); // z_0 = C^
-        }
+        T g = sc_zero<T>(), ep = sc_zero<T>();
+        T zp = doW ? gW[tb + rm] : sc_zero<T>(); // z_0 = C^
         for (int J = 0; J < cnt; J++) {
             issue(J + D - 1);
             cp_async_wait_n<D - 1>();
             __syncwarp(m);
             const T *sc = slot + (J % D) * C::STAGE;
-            T sr[KB];
-#pragma unroll
-            for (int c = 0; c < KB; c++) sr[c] = sc[r * KB + c]; // D_J
+            T sv = sc[rm]; // D_J
             if (J > 0) {
-                T f[KB], l[KB];
-#pragma unroll
-                for (int c = 0; c < KB; c++) f[c] = sc[TS + c * KB + r]; // row r of A(J,J-1) (column-major)
-                row_mul<T, KB>(m, l, f, g);
-#pragma unroll
-                for (int c = 0; c < KB; c++) gL[tb + (size_t)J * TS + c * KB + r] = l[c];
-                row_msub<T, KB>(m, sr, l, ep);
+                const T l = el_mul<T, KB>(m, sc[TS + cm], g, r, c); // A(J,J-1) is column-major
+                gL[tb + (size_t)J * TS + cm] = l;
+                sv = el_msub<T, KB>(m, sv, l, ep, r, c);
                 if (doW) {
-                    T z[KB];
-#pragma unroll
-                    for (int c = 0; c < KB; c++) z[c] = sc_zero<T>();
-                    row_msub<T, KB>(m, z, l, zp);
-#pragma unroll
-                    for (int c = 0; c < KB; c++) {
-                        gW[tb + (size_t)J * TS + r * KB + c] = z[c];
-                        zp[c] = z[c];
-                    }
+                    zp = el_msub<T, KB>(m, sc_zero<T>(), l, zp, r, c);
+                    gW[tb + (size_t)J * TS + rm] = zp;
                 }
             }
-#pragma unroll
-            for (int c = 0; c < KB; c++) ep[c] = sc[2 * TS + r * KB + c]; // row r of A(J,J+1) (row-major)
-            __syncwarp(m); // the ring entry may be refilled from here on
-            ok = row_inv<T, KB>(m, sr, r) && ok;
-#pragma unroll
-            for (int c = 0; c < KB; c++) {
-                gG[tb + (size_t)J * TS + c * KB + r] = sr[c];
-                g[c] = sr[c];
-            }
+            ep = sc[2 * TS + rm]; // A(J,J+1), row-major
+            __syncwarp(m);        // the ring entry may be refilled from here on
+            ok = el_inv<T, KB>(m, sv, r, c) && ok;
+            gG[tb + (size_t)J * TS + cm] = sv;
+            g = sv;
         }
     } else {
         // U_J = A(J,J+1) H_{J+1}, T_J = D_J - U_J A(J+1,J), H_J = T_J^{-1}; w_J = r_J - U_J w_{J+1}
@@ -474,58 +456,39 @@ __global__ void __launch_bounds__(QTw<T, KB>::NT)
         const int mrows = part_start[part + 1] - part_start[part];
         const int J0 = (mrows - KB) / KB, o = mrows - KB - J0 * KB;
         const T *B = gBhat + (size_t)part * TS;
-        T h[KB], xn[KB], wp[KB];
-#pragma unroll
-        for (int c = 0; c < KB; c++) h[c] = xn[c] = wp[c] = sc_zero<T>();
+        T h = sc_zero<T>(), xn = sc_zero<T>(), wp = sc_zero<T>();
         for (int i = 0; i < cnt; i++) {
             const int J = N - 1 - i;
             issue(i + D - 1);
             cp_async_wait_n<D - 1>();
             __syncwarp(m);
             const T *sc = slot + (i % D) * C::STAGE;
-            T sr[KB], rv[KB];
-#pragma unroll
-            for (int c = 0; c < KB; c++) {
-                sr[c] = sc[r * KB + c]; // D_J
-                rv[c] = (J == J0 && r >= o) ? B[(r - o) * KB + c]
-                                            : (o > 0 && J == J0 + 1 && r < o) ? B[(KB - o + r) * KB + c] : sc_zero<T>();
-            }
+            T sv = sc[rm]; // D_J
+            T rv = (J == J0 && r >= o) ? B[(r - o) * KB + c]
+                                       : (o > 0 && J == J0 + 1 && r < o) ? B[(KB - o + r) * KB + c] : sc_zero<T>();
             if (i > 0) {
-                T y[KB], u[KB];
-#pragma unroll
-                for (int c = 0; c < KB; c++) y[c] = sc[2 * TS + c * KB + r]; // row r of A(J,J+1) (column-major)
-                row_mul<T, KB>(m, u, y, h);
-                T *gU = (J == M ? gE : gL) + tb + (size_t)J * TS;
-#pragma unroll
-                for (int c = 0; c < KB; c++) gU[c * KB + r] = u[c];
-                row_msub<T, KB>(m, sr, u, xn);
-                if (doV) row_msub<T, KB>(m, rv, u, wp);
+                const T u = el_mul<T, KB>(m, sc[2 * TS + cm], h, r, c); // A(J,J+1) is column-major here
+                ((J == M ? gE : gL) + tb + (size_t)J * TS)[cm] = u;
+                sv = el_msub<T, KB>(m, sv, u, xn, r, c);
+                if (doV) rv = el_msub<T, KB>(m, rv, u, wp, r, c);
             }
             if (doV) {
-#pragma unroll
-                for (int c = 0; c < KB; c++) {
-                    gV[tb + (size_t)J * TS + r * KB + c] = rv[c];
-                    wp[c] = rv[c];
-                }
+                gV[tb + (size_t)J * TS + rm] = rv;
+                wp = rv;
             }
             if (J == M) { // T'_M for the middle block, row-major
-#pragma unroll
-                for (int c = 0; c < KB; c++) gG[tb + (size_t)J * TS + r * KB + c] = sr[c];
+                gG[tb + (size_t)J * TS + rm] = sv;
                 break;
             }
-#pragma unroll
-            for (int c = 0; c < KB; c++) xn[c] = sc[TS + r * KB + c]; // row r of A(J,J-1) (row-major)
+            xn = sc[TS + rm]; // A(J,J-1), row-major
             __syncwarp(m);
-            ok = row_inv<T, KB>(m, sr, r) && ok;
-#pragma unroll
-            for (int c = 0; c < KB; c++) {
-                gG[tb + (size_t)J * TS + c * KB + r] = sr[c];
-                h[c] = sr[c];
-            }
+            ok = el_inv<T, KB>(m, sv, r, c) && ok;
+            gG[tb + (size_t)J * TS + cm] = sv;
+            h = sv;
         }
     }
     cp_async_wait_all();
-    if (!ok && r == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+    if (!ok && e == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
 }
 
 // the middle block of every partition (KB lanes each): L_M, G_M, and X_M of W and V
@@ -586,27 +549,28 @@ __global__ void __launch_bounds__(QTw<T, KB>::NT)
               T *gW)
 {
     using C = QTw<T, KB>;
-    constexpr int TS = C::TS, D = C::DEPTH;
+    constexpr int TS = C::TS, D = C::DEPTH, EL = C::EL;
     constexpr int CT = TS * (int)sizeof(T) / 16;
     extern __shared__ __align__(16) char smc[];
-    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
-    const int r = threadIdx.x % KB;
+    const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / EL;
+    const int e = threadIdx.x % EL, r = e / KB, c = e % KB;
     const int part = ch >> 2, which = ch & 3;
     const bool isV = which >= 2, top = (which & 1) == 0;
     if (part >= p || (isV ? part == p - 1 : part == 0)) return; // whole segments
-    const unsigned m = seg_mask<KB>();
-    T *slot = (T *)(smc + (threadIdx.x / KB) * C::SLOT);
+    const unsigned m = seg_mask<EL>();
+    T *slot = (T *)(smc + (threadIdx.x / EL) * C::SLOT);
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
     const size_t tb = (size_t)blk_off[part] * TS;
     T *gX = isV ? gV : gW;
     const bool hasZ = isV ? !top : top;
     const int cnt = top ? M : N - 1 - M;
+    const int rm = r * KB + c, cm = c * KB + r;
     auto blk = [&](int i) { return top ? M - 1 - i : M + 1 + i; };
     auto issue = [&](int i) {
         if (i < cnt) {
             const int J = blk(i);
             char *st = (char *)(slot + (i % D) * C::STAGE);
-            for (int q = r; q < CT; q += KB) {
+            for (int q = e; q < CT; q += EL) {
                 cp_async16(st + 16 * q, (const char *)(gG + tb + (size_t)J * TS) + 16 * q);
                 cp_async16(st + TS * sizeof(T) + 16 * q, (const char *)(gE + tb + (size_t)J * TS) + 16 * q);
                 if (hasZ)
@@ -617,27 +581,19 @@ __global__ void __launch_bounds__(QTw<T, KB>::NT)
     };
 #pragma unroll
     for (int i = 0; i < D - 1; i++) issue(i);
-    T x[KB]; // row r of the previous X (X_M first, column-major in memory)
-#pragma unroll
-    for (int c = 0; c < KB; c++) x[c] = gX[tb + (size_t)M * TS + c * KB + r];
+    T x = gX[tb + (size_t)M * TS + cm]; // X_M (column-major)
     for (int i = 0; i < cnt; i++) {
         const int J = blk(i);
         issue(i + D - 1);
         cp_async_wait_n<D - 1>();
         __syncwarp(m);
         const T *sc = slot + (i % D) * C::STAGE;
-        T t[KB], e[KB], g[KB];
-#pragma unroll
-        for (int c = 0; c < KB; c++) {
-            t[c] = hasZ ? sc[2 * TS + r * KB + c] : sc_zero<T>();
-            e[c] = sc[TS + c * KB + r]; // row r of the coupling tile (column-major)
-            g[c] = sc[c * KB + r];      // row r of G_J or H_J (column-major)
-        }
+        T t = hasZ ? sc[2 * TS + rm] : sc_zero<T>(); // Z_J (row-major)
+        const T ev = sc[TS + cm], gv = sc[cm];     // the coupling tile and G_J or H_J (column-major)
         __syncwarp(m); // the ring entry may be refilled from here on
-        row_msub<T, KB>(m, t, e, x);
-        row_mul<T, KB>(m, x, g, t);
-#pragma unroll
-        for (int c = 0; c < KB; c++) gX[tb + (size_t)J * TS + c * KB + r] = x[c];
+        t = el_msub<T, KB>(m, t, ev, x, r, c);
+        x = el_mul<T, KB>(m, gv, t, r, c);
+        gX[tb + (size_t)J * TS + cm] = x;
     }
     cp_async_wait_all();
 }
@@ -710,7 +666,7 @@ template <class T, int KB> int run_qtwist(spk_plan *P, cudaStream_t st, bool fwd
     const int p = P->p;
     if (fwd) {
         const int cpc = chains_per_cta(2LL * p, C::CPC);
-        k_qtw_lu<T, KB><<<2 * ((p + cpc - 1) / cpc), cpc * KB, (size_t)cpc * C::SLOT, st>>>(
+        k_qtw_lu<T, KB><<<2 * ((p + cpc - 1) / cpc), cpc * C::EL, (size_t)cpc * C::SLOT, st>>>(
             (const T *)P->d_T, P->d_part_start, P->d_blk_off, p, (const T *)P->d_Bhat, (T *)P->d_L, (T *)P->d_G,
             (T *)P->d_E, (T *)P->d_V, (T *)P->d_W, P->d_err);
         SPK_CHECK_LAUNCH();
@@ -721,7 +677,7 @@ template <class T, int KB> int run_qtwist(spk_plan *P, cudaStream_t st, bool fwd
         P->launches += 2;
     } else if (p > 1) {
         const int cpc = chains_per_cta(4LL * p, C::CPC);
-        k_qtw_bwd<T, KB><<<(4 * p + cpc - 1) / cpc, cpc * KB, (size_t)cpc * C::SLOT, st>>>(
+        k_qtw_bwd<T, KB><<<(4 * p + cpc - 1) / cpc, cpc * C::EL, (size_t)cpc * C::SLOT, st>>>(
             P->d_blk_off, p, (const T *)P->d_G, (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W);
         SPK_CHECK_LAUNCH();
         P->launches++;
