@@ -715,15 +715,31 @@ __global__ void __launch_bounds__(QuadApply<T, KB>::NT)
 // w_J = r_J - U_J w_{J+1} (J >= M) into y; k_qtw_apply_mid forms
 // y_M = G_M (w_M - L_M z_{M-1}); k_qtw_apply_bwd runs y_J = G_J (z_J -
 // A(J,J+1) y_{J+1}) upwards and y_J = H_J (w_J - A(J,J-1) y_{J-1}) downwards.
+// The lane sweeps' ring: a stage carries S consecutive steps' tiles and
+// vector elements, so a chain waits and synchronises once per S steps.
+template <class T, int KB> struct QTwApply {
+    using H = typename HighOf<T>::type;
+    static constexpr int TS = KB * KB;
+    static constexpr int S = 4;                                  // steps per stage
+    static constexpr int DEPTH = 3;                              // stages in flight
+    static constexpr int VEC = 2 * TS * (int)sizeof(T);          // byte offset of a step's vector elements
+    static constexpr int STEP = (VEC + KB * (int)sizeof(H) + 15) / 16 * 16;
+    static constexpr int STAGE = S * STEP;
+    static constexpr int SLOT = DEPTH * STAGE + 16;
+    static constexpr int CPC = chain_threads(SLOT);
+    static constexpr int NT = CPC * KB;
+    static constexpr size_t SMEM = (size_t)CPC * SLOT;
+};
+
 template <class T, int KB>
-__global__ void __launch_bounds__(QuadApply<T, KB>::NT)
+__global__ void __launch_bounds__(QTwApply<T, KB>::NT)
     k_qtw_apply_fwd(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
                     const T *__restrict__ gL, const T *__restrict__ gE,
                     const typename HighOf<T>::type *__restrict__ r, int n, int nrhs, long long NP, T *gy)
 {
     using H = typename HighOf<T>::type;
-    using C = QuadApply<T, KB>;
-    constexpr int TS = C::TS, D = C::DEPTH;
+    using C = QTwApply<T, KB>;
+    constexpr int TS = C::TS, D = C::DEPTH, S = C::S;
     constexpr int CT = TS * (int)sizeof(T) / 16;
     extern __shared__ __align__(16) char smc[];
     const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
@@ -741,36 +757,48 @@ __global__ void __launch_bounds__(QuadApply<T, KB>::NT)
     const H *rh = r + (size_t)h * n + s;
     const int cnt = bottom ? N - M : M;
     auto blk = [&](int i) { return bottom ? N - 1 - i : i; };
-    auto issue = [&](int i) {
-        if (i < cnt) {
-            const int J = blk(i);
-            char *st = slot + (i % D) * C::STAGE;
-            if (i > 0) { // the coupling tile: L_J above M, U_J below (U_M in gE)
-                const T *cpl = (bottom && J == M ? gE : gL) + tb + (size_t)J * TS;
-                for (int q = lr; q < CT; q += KB) cp_async16(st + 16 * q, (const char *)cpl + 16 * q);
+    auto issue = [&](int g) { // stage g: steps g*S .. g*S+S-1
+#pragma unroll
+        for (int q = 0; q < S; q++) {
+            const int i = g * S + q;
+            if (i < cnt) {
+                const int J = blk(i);
+                char *st = slot + (g % D) * C::STAGE + q * C::STEP;
+                if (i > 0) { // the coupling tile: L_J above M, U_J below (U_M in gE)
+                    const T *cpl = (bottom && J == M ? gE : gL) + tb + (size_t)J * TS;
+                    for (int k = lr; k < CT; k += KB) cp_async16(st + 16 * k, (const char *)cpl + 16 * k);
+                }
+                if (J * KB + lr < mrows)
+                    cp_async_elem<(int)sizeof(H)>(st + C::VEC + lr * sizeof(H), rh + J * KB + lr);
             }
-            if (J * KB + lr < mrows) cp_async_elem<(int)sizeof(H)>(st + C::VEC + lr * sizeof(H), rh + J * KB + lr);
         }
         cp_async_commit();
     };
+    const int ng = (cnt + S - 1) / S;
 #pragma unroll
-    for (int i = 0; i < D - 1; i++) issue(i);
+    for (int g = 0; g < D - 1; g++) issue(g);
     T z = sc_zero<T>();
-    for (int i = 0; i < cnt; i++) {
-        const int J = blk(i);
-        issue(i + D - 1);
+    for (int g = 0; g < ng; g++) {
+        issue(g + D - 1);
         cp_async_wait_n<D - 1>();
         __syncwarp(m);
-        const char *st = slot + (i % D) * C::STAGE;
-        T v = J * KB + lr < mrows ? sc_cvt<T, H>(*(const H *)(st + C::VEC + lr * sizeof(H))) : sc_zero<T>();
-        if (i > 0) {
-            const T *L = (const T *)st; // column-major
 #pragma unroll
-            for (int c = 0; c < KB; c++) v = msub(v, L[c * KB + lr], seg_shfl<KB>(m, z, c));
+        for (int q = 0; q < S; q++) {
+            const int i = g * S + q;
+            if (i < cnt) {
+                const int J = blk(i);
+                const char *st = slot + (g % D) * C::STAGE + q * C::STEP;
+                T v = J * KB + lr < mrows ? sc_cvt<T, H>(*(const H *)(st + C::VEC + lr * sizeof(H))) : sc_zero<T>();
+                if (i > 0) {
+                    const T *L = (const T *)st; // column-major
+#pragma unroll
+                    for (int c = 0; c < KB; c++) v = msub(v, L[c * KB + lr], seg_shfl<KB>(m, z, c));
+                }
+                z = v;
+                yh[(size_t)J * KB + lr] = z;
+            }
         }
-        __syncwarp(m); // the ring entry may be refilled from here on
-        z = v;
-        yh[(size_t)J * KB + lr] = z;
+        __syncwarp(m); // the stage may be refilled from here on
     }
     cp_async_wait_all();
 }
@@ -799,12 +827,12 @@ __global__ void k_qtw_apply_mid(const int *__restrict__ blk_off, int p, const T 
 }
 
 template <class T, int KB>
-__global__ void __launch_bounds__(QuadApply<T, KB>::NT)
+__global__ void __launch_bounds__(QTwApply<T, KB>::NT)
     k_qtw_apply_bwd(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE,
                     int nrhs, long long NP, T *gy)
 {
-    using C = QuadApply<T, KB>;
-    constexpr int TS = C::TS, D = C::DEPTH;
+    using C = QTwApply<T, KB>;
+    constexpr int TS = C::TS, D = C::DEPTH, S = C::S;
     constexpr int CT = TS * (int)sizeof(T) / 16;
     extern __shared__ __align__(16) char smc[];
     const int ch = (blockIdx.x * blockDim.x + threadIdx.x) / KB;
@@ -820,37 +848,48 @@ __global__ void __launch_bounds__(QuadApply<T, KB>::NT)
     T *yh = gy + (size_t)h * NP + (size_t)blk_off[part] * KB;
     const int cnt = bottom ? N - 1 - M : M;
     auto blk = [&](int i) { return bottom ? M + 1 + i : M - 1 - i; };
-    auto issue = [&](int i) {
-        if (i < cnt) {
-            const int J = blk(i);
-            char *st = slot + (i % D) * C::STAGE;
-            for (int q = lr; q < CT; q += KB) {
-                cp_async16(st + 16 * q, (const char *)(gG + tb + (size_t)J * TS) + 16 * q);
-                cp_async16(st + TS * sizeof(T) + 16 * q, (const char *)(gE + tb + (size_t)J * TS) + 16 * q);
+    auto issue = [&](int g) {
+#pragma unroll
+        for (int q = 0; q < S; q++) {
+            const int i = g * S + q;
+            if (i < cnt) {
+                const int J = blk(i);
+                char *st = slot + (g % D) * C::STAGE + q * C::STEP;
+                for (int k = lr; k < CT; k += KB) {
+                    cp_async16(st + 16 * k, (const char *)(gG + tb + (size_t)J * TS) + 16 * k);
+                    cp_async16(st + TS * sizeof(T) + 16 * k, (const char *)(gE + tb + (size_t)J * TS) + 16 * k);
+                }
+                // the forward sweep's own z_J / w_J: y_J is written only when the chain gets there
+                cp_async_elem<(int)sizeof(T)>(st + C::VEC + lr * sizeof(T), yh + (size_t)J * KB + lr);
             }
-            cp_async_elem<(int)sizeof(T)>(st + C::VEC + lr * sizeof(T), yh + (size_t)J * KB + lr); // own z / w
         }
         cp_async_commit();
     };
+    const int ng = (cnt + S - 1) / S;
 #pragma unroll
-    for (int i = 0; i < D - 1; i++) issue(i);
+    for (int g = 0; g < D - 1; g++) issue(g);
     T y = yh[(size_t)M * KB + lr]; // y_M
-    for (int i = 0; i < cnt; i++) {
-        const int J = blk(i);
-        issue(i + D - 1);
+    for (int g = 0; g < ng; g++) {
+        issue(g + D - 1);
         cp_async_wait_n<D - 1>();
         __syncwarp(m);
-        const char *st = slot + (i % D) * C::STAGE;
-        const T *G = (const T *)st, *E = (const T *)(st + TS * sizeof(T));
-        T t = *(const T *)(st + C::VEC + lr * sizeof(T));
 #pragma unroll
-        for (int c = 0; c < KB; c++) t = msub(t, E[c * KB + lr], seg_shfl<KB>(m, y, c));
-        T acc = sc_zero<T>();
+        for (int q = 0; q < S; q++) {
+            const int i = g * S + q;
+            if (i < cnt) {
+                const char *st = slot + (g % D) * C::STAGE + q * C::STEP;
+                const T *G = (const T *)st, *E = (const T *)(st + TS * sizeof(T));
+                T t = *(const T *)(st + C::VEC + lr * sizeof(T));
 #pragma unroll
-        for (int c = 0; c < KB; c++) acc = madd(acc, G[c * KB + lr], seg_shfl<KB>(m, t, c));
+                for (int c = 0; c < KB; c++) t = msub(t, E[c * KB + lr], seg_shfl<KB>(m, y, c));
+                T acc = sc_zero<T>();
+#pragma unroll
+                for (int c = 0; c < KB; c++) acc = madd(acc, G[c * KB + lr], seg_shfl<KB>(m, t, c));
+                y = acc;
+                yh[(size_t)blk(i) * KB + lr] = y;
+            }
+        }
         __syncwarp(m);
-        y = acc;
-        yh[(size_t)J * KB + lr] = y;
     }
     cp_async_wait_all();
 }
@@ -950,7 +989,7 @@ template <class T, int KB> int run_apply_1(spk_plan *P, const void *r, int nrhs,
 
 template <class T, int KB> int run_qtw_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
-    using CA = QuadApply<T, KB>;
+    using CA = QTwApply<T, KB>;
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_qtw_apply_fwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
