@@ -544,6 +544,213 @@ __global__ void __launch_bounds__(QNT)
                                [&](int q, int h, T v) { put(q, h, v); });
 }
 
+// Small tiles (KB <= 16): the same one-latency levels, with PPC block pairs
+// (or blocks) per 128-thread CTA and one thread per (row, column) output
+// summing over k itself -- a level block's products are too small for a warp
+// per row.
+template <class T, int KB, int NRC> struct SSolve {
+    static constexpr int TS = KB * KB;
+    static constexpr int R = 2 * KB;
+    static constexpr int UNIT = R * NRC;                     // threads per block pair
+    static constexpr int PPC = 128 / UNIT > 0 ? 128 / UNIT : 1; // pairs per CTA
+    static constexpr int NT = PPC * UNIT;
+    static constexpr size_t PAIR = ((6 * TS + 4 * R * NRC) * sizeof(T) + 15) / 16 * 16; // smem per pair
+    static constexpr size_t bytes = PPC * PAIR + 64;
+    static_assert(UNIT <= 128, "SSolve shape");
+};
+
+template <class T, int KB, int NRC>
+__global__ void __launch_bounds__(SSolve<T, KB, NRC>::NT)
+    k_crs_fwd(const T *__restrict__ Xl, const T *__restrict__ Yl, const T *__restrict__ Ml, int cnt, const void *gin,
+              int l0, long long gld, long long off_l, T *gn, long long stride, long long off_n, int nrhs)
+{
+    using H = typename HighOf<T>::type;
+    using Q = SSolve<T, KB, NRC>;
+    constexpr int TS = Q::TS, R = Q::R;
+    const int slot = threadIdx.x / Q::UNIT, lt = threadIdx.x - slot * Q::UNIT;
+    const int a = blockIdx.x * Q::PPC + slot; // the new block a <- even block i = 2a
+    const int i = 2 * a;
+    const bool live = i < cnt;
+    const int h0 = blockIdx.y * NRC, nr = min(NRC, nrhs - h0);
+    extern __shared__ char smraw[];
+    T *sM = (T *)(smem_align(smraw) + slot * Q::PAIR); // [half][M_half0 | M_half1]
+    T *sC = sM + 4 * TS;                                // X_i, Y_i
+    T *sx = sC + 2 * TS;                                // [half][h][2KB]
+    T *sw = sx + 2 * NRC * R;                           // [half][h][2KB] (first KB used)
+    const bool has0 = live && i - 1 >= 0, has1 = live && i + 1 < cnt;
+    // every tile of the CTA's pairs at once (each pair's UNIT threads copy its own)
+    auto tiles = [&](T *dst, const T *src, int ntiles) {
+        const int chunks = ntiles * TS * (int)sizeof(T) / 16;
+        for (int c = lt; c < chunks; c += Q::UNIT) cp_async16((char *)dst + 16 * c, (const char *)src + 16 * c);
+    };
+    if (has0) {
+        tiles(sM, Ml + (size_t)((i - 2) / 2) * 4 * TS, 2);
+        tiles(sC, Xl + (size_t)i * TS, 1);
+    }
+    if (has1) {
+        tiles(sM + 2 * TS, Ml + (size_t)(i / 2) * 4 * TS + 2 * TS, 2);
+        tiles(sC + TS, Yl + (size_t)i * TS, 1);
+    }
+    cp_async_commit();
+    for (int q = lt; q < 2 * NRC * R; q += Q::UNIT) {
+        const int half = q / (NRC * R), rem = q - half * NRC * R, h = rem / R, k = rem - h * R;
+        const bool has = half ? has1 : has0;
+        sx[q] = has && h < nr ? q_in<T, H>(gin, l0, gld, off_l + i + (half ? 1 : -1), k, h0 + h, KB) : sc_zero<T>();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const int q = lt / NRC, h = lt - q * NRC, half = q / KB, rr = q - half * KB;
+    const bool has = half ? has1 : has0;
+    if (has && h < nr) { // w = [M_h0 M_h1] x_nb, row rr of this half
+        const T *M0 = sM + half * 2 * TS, *x = sx + (half * NRC + h) * R;
+        T acc = sc_zero<T>();
+#pragma unroll
+        for (int k = 0; k < KB; k++) acc = madd(acc, M0[rr * KB + k], x[k]);
+#pragma unroll
+        for (int k = 0; k < KB; k++) acc = madd(acc, M0[TS + rr * KB + k], x[KB + k]);
+        sw[(half * NRC + h) * R + rr] = acc;
+    }
+    __syncthreads();
+    if (live && h < nr) {
+        T v = q_in<T, H>(gin, l0, gld, off_l + i, q, h0 + h, KB);
+        if (has) {
+            const T *Ct = sC + half * TS, *w = sw + (half * NRC + h) * R;
+#pragma unroll
+            for (int k = 0; k < KB; k++) v = msub(v, Ct[rr * KB + k], w[k]);
+        }
+        gn[(h0 + h) * stride + (off_n + a) * 2 * KB + q] = v;
+    }
+}
+
+template <class T, int KB, int NRC>
+__global__ void __launch_bounds__(SSolve<T, KB, NRC>::NT)
+    k_crs_bwd(const T *__restrict__ Xl, const T *__restrict__ Yl, const T *__restrict__ Ml, int cnt, const void *gin,
+              int l0, long long gld, long long off_l, const T *un, long long off_n, T *u, long long stride, void *U,
+              int first, int nrhs, int top)
+{
+    using H = typename HighOf<T>::type;
+    using Q = SSolve<T, KB, NRC>;
+    constexpr int TS = Q::TS, R = Q::R;
+    const int slot = threadIdx.x / Q::UNIT, lt = threadIdx.x - slot * Q::UNIT;
+    const int j = blockIdx.x * Q::PPC + slot;
+    const bool live = j < cnt;
+    const int h0 = blockIdx.y * NRC, nr = min(NRC, nrhs - h0);
+    const int q = lt / NRC, h = lt - q * NRC, half = q / KB, rr = q - half * KB;
+    auto put = [&](T v) {
+        if (l0) {
+            H *o = (H *)U + (h0 + h) * gld + (long long)j * 2 * KB + q;
+            const H d = cvt_fast<H, T>(v);
+            *o = first ? d : *o + d;
+        } else {
+            u[(h0 + h) * stride + (off_l + j) * 2 * KB + q] = v;
+        }
+    };
+    const bool odd = live && (top || (j & 1));
+    extern __shared__ char smraw[];
+    T *sM = (T *)(smem_align(smraw) + slot * Q::PAIR); // M00 M01 M10 M11
+    T *sC = sM + 4 * TS;                                // X_j, Y_j
+    T *sv = sC + 2 * TS;                                // [half][h][2KB] (first KB used): neighbour values
+    T *ss = sv + 2 * NRC * R;                           // [h][2KB]: g_j minus the couplings
+    const bool has0 = odd && !top && j - 1 >= 0, has1 = odd && !top && j + 1 < cnt;
+    auto tiles = [&](T *dst, const T *src, int ntiles) {
+        const int chunks = ntiles * TS * (int)sizeof(T) / 16;
+        for (int c = lt; c < chunks; c += Q::UNIT) cp_async16((char *)dst + 16 * c, (const char *)src + 16 * c);
+    };
+    if (odd) tiles(sM, Ml + (size_t)(top ? 0 : (j - 1) / 2) * 4 * TS, 4);
+    if (has0) tiles(sC, Xl + (size_t)j * TS, 1);
+    if (has1) tiles(sC + TS, Yl + (size_t)j * TS, 1);
+    cp_async_commit();
+    if (odd)
+        for (int t = lt; t < NRC * R; t += Q::UNIT) {
+            const int hh = t / R, k = t - hh * R, hf = k / KB, kk = k - hf * KB;
+            const bool hs = hf ? has1 : has0;
+            ss[t] = hh < nr ? q_in<T, H>(gin, l0, gld, off_l + j, k, h0 + hh, KB) : sc_zero<T>();
+            sv[(hf * NRC + hh) * R + kk] =
+                hs && hh < nr ? un[(h0 + hh) * stride + (off_n + (j + (hf ? 1 : -1)) / 2) * 2 * KB + hf * KB + kk]
+                              : sc_zero<T>();
+        }
+    cp_async_wait_all();
+    __syncthreads();
+    if (live && !odd && h < nr) put(un[(h0 + h) * stride + (off_n + j / 2) * 2 * KB + q]); // even block: from above
+    // (every thread, of even blocks and spare slots too, passes the barriers below)
+    const bool hs = half ? has1 : has0;
+    T sv_q = sc_zero<T>();
+    if (odd && h < nr) {
+        sv_q = ss[h * R + q];
+        if (hs) {
+            const T *Ct = sC + half * TS, *v = sv + (half * NRC + h) * R;
+#pragma unroll
+            for (int k = 0; k < KB; k++) sv_q = msub(sv_q, Ct[rr * KB + k], v[k]);
+        }
+    }
+    __syncthreads();
+    if (odd && h < nr) ss[h * R + q] = sv_q;
+    __syncthreads();
+    if (odd && h < nr) {
+        const T *Mq = sM + half * 2 * TS, *x = ss + h * R; // [M_half0 M_half1] row rr
+        T acc = sc_zero<T>();
+#pragma unroll
+        for (int k = 0; k < KB; k++) acc = madd(acc, Mq[rr * KB + k], x[k]);
+#pragma unroll
+        for (int k = 0; k < KB; k++) acc = madd(acc, Mq[TS + rr * KB + k], x[KB + k]);
+        put(acc);
+    }
+}
+
+template <class T, int KB, int NRC> int run_red_solve_s(spk_plan *P, int nrhs, int iters, cudaStream_t st)
+{
+    using H = typename HighOf<T>::type;
+    using Q = SSolve<T, KB, NRC>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const long long NR = (long long)P->n_iface * 2 * KB;
+    const long long stride = P->crg_stride;
+    T *cg = (T *)P->d_crg;
+    T *cu = cg + stride * P->nrhs_max;
+    const T *cX = (const T *)P->d_crX, *cY = (const T *)P->d_crY, *cM = (const T *)P->d_crM;
+    const int L = P->cr_levels;
+    const int hy = (nrhs + NRC - 1) / NRC;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_crs_fwd<T, KB, NRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q::bytes) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_crs_bwd<T, KB, NRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q::bytes) !=
+                cudaSuccess)
+            return SPK_ECUDA;
+        attr = true;
+    }
+    for (int it = 0; it < iters; it++) {
+        const H *res = it == 0 ? (const H *)P->d_g : (const H *)P->d_rr;
+        for (int l = 0; l < L; l++) {
+            const int cnt = P->cr_count[l], pairs = (cnt + 1) / 2;
+            k_crs_fwd<T, KB, NRC><<<dim3((pairs + Q::PPC - 1) / Q::PPC, hy), Q::NT, Q::bytes, st>>>(
+                cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS, cM + (size_t)P->cr_moff[l] * 4 * TS, cnt,
+                l == 0 ? (const void *)res : (const void *)cg, l == 0, l == 0 ? NR : stride, P->cr_off[l], cg, stride,
+                P->cr_off[l + 1], nrhs);
+            P->launches++;
+        }
+        k_crs_bwd<T, KB, NRC><<<dim3(1, hy), Q::NT, Q::bytes, st>>>(
+            nullptr, nullptr, cM + (size_t)P->cr_moff[L] * 4 * TS, 1, L == 0 ? (const void *)res : (const void *)cg,
+            L == 0, L == 0 ? NR : stride, P->cr_off[L], nullptr, 0, cu, stride, P->d_u, it == 0, nrhs, 1);
+        P->launches++;
+        for (int l = L - 1; l >= 0; l--) {
+            const int cnt = P->cr_count[l];
+            k_crs_bwd<T, KB, NRC><<<dim3((cnt + Q::PPC - 1) / Q::PPC, hy), Q::NT, Q::bytes, st>>>(
+                cX + (size_t)P->cr_off[l] * TS, cY + (size_t)P->cr_off[l] * TS, cM + (size_t)P->cr_moff[l] * 4 * TS, cnt,
+                l == 0 ? (const void *)res : (const void *)cg, l == 0, l == 0 ? NR : stride, P->cr_off[l], cu,
+                P->cr_off[l + 1], cu, stride, P->d_u, it == 0, nrhs, 0);
+            P->launches++;
+        }
+        if (it + 1 < iters) {
+            k_red_resid<H, KB><<<P->n_iface, 128, 0, st>>>((const H *)P->d_RP, (const H *)P->d_RQ, (const H *)P->d_RX,
+                                                           (const H *)P->d_RY, (const H *)P->d_g, (const H *)P->d_u,
+                                                           (H *)P->d_rr, P->n_iface, nrhs);
+            P->launches++;
+        }
+        SPK_CHECK_LAUNCH();
+    }
+    return SPK_OK;
+}
+
 template <class T, int KB, int NRC> int run_red_solve_q(spk_plan *P, int nrhs, int iters, cudaStream_t st)
 {
     using H = typename HighOf<T>::type;
@@ -650,6 +857,10 @@ template <class T, int KB> int run_red_solve(spk_plan *P, int nrhs, int iters, c
     if constexpr (KB == 32 || (KB == 64 && sizeof(T) <= 8)) {
         if (nrhs == 1) return run_red_solve_q<T, KB, 1>(P, nrhs, iters, st);
         return run_red_solve_q<T, KB, 4>(P, nrhs, iters, st);
+    }
+    if constexpr (KB <= 16 && KB * (int)sizeof(T) >= 16) { // a tile row of 16 bytes or more: cp.async-sized tiles
+        if (nrhs == 1) return run_red_solve_s<T, KB, 1>(P, nrhs, iters, st);
+        return run_red_solve_s<T, KB, 4>(P, nrhs, iters, st);
     }
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
