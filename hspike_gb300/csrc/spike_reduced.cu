@@ -132,28 +132,37 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     const bool left = i - 1 >= 0, right = i + 1 < cnt;
     const T *Ml_left = left ? Ml + (size_t)((i - 2) / 2) * 4 * TS : nullptr;  // odd block i-1
     const T *Ml_right = right ? Ml + (size_t)(i / 2) * 4 * TS : nullptr;      // odd block i+1
-    // P'
-    __syncthreads();
-    ld<T, KB>(sA, Pl + (size_t)i * TS);
-    __syncthreads();
-    t.rload(acc, sA);
-    if (left) chain3<T, KB>(t, acc, Xl + (size_t)i * TS, Ml_left + 1 * TS, Yl + (size_t)(i - 1) * TS, sA, sB, sC, true);
-    t.gstore(Pn + (size_t)a_out * TS, acc);
-    // Q'
-    __syncthreads();
-    ld<T, KB>(sA, Ql + (size_t)i * TS);
-    __syncthreads();
-    t.rload(acc, sA);
-    if (right) chain3<T, KB>(t, acc, Yl + (size_t)i * TS, Ml_right + 2 * TS, Xl + (size_t)(i + 1) * TS, sA, sB, sC, true);
-    t.gstore(Qn + (size_t)a_out * TS, acc);
-    // X'
-    t.rzero(acc);
-    if (left) chain3<T, KB>(t, acc, Xl + (size_t)i * TS, Ml_left + 0 * TS, Xl + (size_t)(i - 1) * TS, sA, sB, sC, true);
-    t.gstore(Xn + (size_t)a_out * TS, acc);
-    // Y'
-    t.rzero(acc);
-    if (right) chain3<T, KB>(t, acc, Yl + (size_t)i * TS, Ml_right + 3 * TS, Yl + (size_t)(i + 1) * TS, sA, sB, sC, true);
-    t.gstore(Yn + (size_t)a_out * TS, acc);
+    // the four results are independent: one CTA each (blockIdx.y), so a level
+    // of few blocks still spreads over the SMs
+    switch (blockIdx.y) {
+    case 0: // P'
+        ld<T, KB>(sA, Pl + (size_t)i * TS);
+        __syncthreads();
+        t.rload(acc, sA);
+        if (left)
+            chain3<T, KB>(t, acc, Xl + (size_t)i * TS, Ml_left + 1 * TS, Yl + (size_t)(i - 1) * TS, sA, sB, sC, true);
+        t.gstore(Pn + (size_t)a_out * TS, acc);
+        break;
+    case 1: // Q'
+        ld<T, KB>(sA, Ql + (size_t)i * TS);
+        __syncthreads();
+        t.rload(acc, sA);
+        if (right)
+            chain3<T, KB>(t, acc, Yl + (size_t)i * TS, Ml_right + 2 * TS, Xl + (size_t)(i + 1) * TS, sA, sB, sC, true);
+        t.gstore(Qn + (size_t)a_out * TS, acc);
+        break;
+    case 2: // X'
+        t.rzero(acc);
+        if (left)
+            chain3<T, KB>(t, acc, Xl + (size_t)i * TS, Ml_left + 0 * TS, Xl + (size_t)(i - 1) * TS, sA, sB, sC, true);
+        t.gstore(Xn + (size_t)a_out * TS, acc);
+        break;
+    default: // Y'
+        t.rzero(acc);
+        if (right)
+            chain3<T, KB>(t, acc, Yl + (size_t)i * TS, Ml_right + 3 * TS, Yl + (size_t)(i + 1) * TS, sA, sB, sC, true);
+        t.gstore(Yn + (size_t)a_out * TS, acc);
+    }
 }
 
 // ---------------------------------------------------------------- solve
@@ -367,8 +376,11 @@ template <class T, int KB, int NRC> struct QSolve {
     static constexpr int RPW = R / QWARPS;       // rows per warp
     static constexpr int G = RPW * NRC <= 32 ? RPW : 32 / NRC; // rows per reduction group
     static constexpr int V = G * NRC;            // values per warp_tsum
-    // six tiles and four 2KB-vectors per column
-    static constexpr size_t bytes = 6 * TS * sizeof(T) + 4 * (size_t)R * NRC * sizeof(T) + 64;
+    // 128-row tiles (64 KB each) are read from global memory where they lie,
+    // coalesced along k; smaller ones are staged in shared memory
+    static constexpr bool GT = KB >= 128;
+    // six tiles (staged) and four 2KB-vectors per column
+    static constexpr size_t bytes = (GT ? 0 : 6 * TS * sizeof(T)) + 4 * (size_t)R * NRC * sizeof(T) + 64;
     static_assert(KB % 32 == 0 && RPW % G == 0 && (V & (V - 1)) == 0 && V <= 32, "QSolve shape");
 };
 
@@ -444,18 +456,23 @@ __global__ void __launch_bounds__(QNT)
     const int i = 2 * blockIdx.x;
     const int h0 = blockIdx.y * NRC, nr = min(NRC, nrhs - h0);
     extern __shared__ char smraw[];
-    T *sM = (T *)smem_align(smraw); // [half][M_half0 | M_half1]: 4 tiles
-    T *sC = sM + 4 * TS;            // X_i, Y_i
-    T *sx = sC + 2 * TS;            // [half][h][2KB]: the neighbours' blocks
-    T *sw = sx + 2 * NRC * 2 * KB;  // [half][h][2KB] (first KB used): w
+    T *sM = (T *)smem_align(smraw);               // [half][M_half0 | M_half1]: 4 tiles (staged)
+    T *sC = sM + (Q::GT ? 0 : 4 * TS);            // X_i, Y_i (staged)
+    T *sx = sC + (Q::GT ? 0 : 2 * TS);            // [half][h][2KB]: the neighbours' blocks
+    T *sw = sx + 2 * NRC * 2 * KB;                // [half][h][2KB] (first KB used): w
     const bool has[2] = {i - 1 >= 0, i + 1 < cnt};
-    if (has[0]) {
-        q_tiles(sM, Ml + (size_t)((i - 2) / 2) * 4 * TS, 2, KB); // M00, M01 of odd block i-1
-        q_tiles(sC, Xl + (size_t)i * TS, 1, KB);
-    }
-    if (has[1]) {
-        q_tiles(sM + 2 * TS, Ml + (size_t)(i / 2) * 4 * TS + 2 * TS, 2, KB); // M10, M11 of odd block i+1
-        q_tiles(sC + TS, Yl + (size_t)i * TS, 1, KB);
+    const T *gM[2] = {has[0] ? Ml + (size_t)((i - 2) / 2) * 4 * TS : nullptr,       // M00, M01 of odd block i-1
+                      has[1] ? Ml + (size_t)(i / 2) * 4 * TS + 2 * TS : nullptr};  // M10, M11 of odd block i+1
+    const T *gC[2] = {Xl + (size_t)i * TS, Yl + (size_t)i * TS};
+    if constexpr (!Q::GT) {
+        if (has[0]) {
+            q_tiles(sM, gM[0], 2, KB);
+            q_tiles(sC, gC[0], 1, KB);
+        }
+        if (has[1]) {
+            q_tiles(sM + 2 * TS, gM[1], 2, KB);
+            q_tiles(sC + TS, gC[1], 1, KB);
+        }
     }
     cp_async_commit();
     for (int q = threadIdx.x; q < 2 * NRC * 2 * KB; q += QNT) {
@@ -467,13 +484,14 @@ __global__ void __launch_bounds__(QNT)
     __syncthreads();
     const int warp = threadIdx.x >> 5, r0 = warp * Q::RPW, half = r0 / KB;
     // w rows: half h of the neighbour's M times its block
+    const T *tM = Q::GT ? gM[half] : sM + half * 2 * TS, *tC = Q::GT ? gC[half] : sC + half * TS;
     if (has[half])
-        q_rows<T, KB, NRC, 2 * KB>(sM + half * 2 * TS, sM + half * 2 * TS + TS, half * KB, sx + half * NRC * 2 * KB, r0,
+        q_rows<T, KB, NRC, 2 * KB>(tM, tM + TS, half * KB, sx + half * NRC * 2 * KB, r0,
                                    nr, [&](int q, int h, T v) { sw[(half * NRC + h) * 2 * KB + q - half * KB] = v; });
     __syncthreads();
     T *gout = gn + (off_n + blockIdx.x) * 2 * KB;
     if (has[half]) {
-        q_rows<T, KB, NRC, KB>(sC + half * TS, sC + half * TS, half * KB, sw + half * NRC * 2 * KB, r0, nr,
+        q_rows<T, KB, NRC, KB>(tC, tC, half * KB, sw + half * NRC * 2 * KB, r0, nr,
                                [&](int q, int h, T v) {
                                    gout[(h0 + h) * stride + q] = q_in<T, H>(gin, l0, gld, off_l + i, q, h0 + h, KB) - v;
                                });
@@ -516,14 +534,18 @@ __global__ void __launch_bounds__(QNT)
         return;
     }
     extern __shared__ char smraw[];
-    T *sM = (T *)smem_align(smraw); // M00 M01 M10 M11
-    T *sC = sM + 4 * TS;            // X_j, Y_j
-    T *sv = sC + 2 * TS;            // [half][h][2KB] (first KB used): neighbour values
-    T *ss = sv + 2 * NRC * 2 * KB;  // [h][2KB]: g_j minus the couplings
+    T *sM = (T *)smem_align(smraw);    // M00 M01 M10 M11 (staged)
+    T *sC = sM + (Q::GT ? 0 : 4 * TS); // X_j, Y_j (staged)
+    T *sv = sC + (Q::GT ? 0 : 2 * TS); // [half][h][2KB] (first KB used): neighbour values
+    T *ss = sv + 2 * NRC * 2 * KB;     // [h][2KB]: g_j minus the couplings
     const bool has[2] = {!top && j - 1 >= 0, !top && j + 1 < cnt};
-    q_tiles(sM, Ml + (size_t)(top ? 0 : (j - 1) / 2) * 4 * TS, 4, KB);
-    if (has[0]) q_tiles(sC, Xl + (size_t)j * TS, 1, KB);
-    if (has[1]) q_tiles(sC + TS, Yl + (size_t)j * TS, 1, KB);
+    const T *gMj = Ml + (size_t)(top ? 0 : (j - 1) / 2) * 4 * TS;
+    const T *gC[2] = {Xl + (size_t)j * TS, Yl + (size_t)j * TS};
+    if constexpr (!Q::GT) {
+        q_tiles(sM, gMj, 4, KB);
+        if (has[0]) q_tiles(sC, gC[0], 1, KB);
+        if (has[1]) q_tiles(sC + TS, gC[1], 1, KB);
+    }
     cp_async_commit();
     for (int q = threadIdx.x; q < NRC * 2 * KB; q += QNT) {
         const int h = q / (2 * KB), k = q - h * 2 * KB;
@@ -536,12 +558,12 @@ __global__ void __launch_bounds__(QNT)
     cp_async_wait_all();
     __syncthreads();
     const int warp = threadIdx.x >> 5, r0 = warp * Q::RPW, half = r0 / KB;
+    const T *tC = Q::GT ? gC[half] : sC + half * TS, *tM = (Q::GT ? gMj : sM) + half * 2 * TS;
     if (has[half])
-        q_rows<T, KB, NRC, KB>(sC + half * TS, sC + half * TS, half * KB, sv + half * NRC * 2 * KB, r0, nr,
+        q_rows<T, KB, NRC, KB>(tC, tC, half * KB, sv + half * NRC * 2 * KB, r0, nr,
                                [&](int q, int h, T v) { ss[h * 2 * KB + q] = ss[h * 2 * KB + q] - v; });
     __syncthreads();
-    q_rows<T, KB, NRC, 2 * KB>(sM + half * 2 * TS, sM + half * 2 * TS + TS, half * KB, ss, r0, nr,
-                               [&](int q, int h, T v) { put(q, h, v); });
+    q_rows<T, KB, NRC, 2 * KB>(tM, tM + TS, half * KB, ss, r0, nr, [&](int q, int h, T v) { put(q, h, v); });
 }
 
 // Small tiles (KB <= 16): the same one-latency levels, with PPC block pairs
@@ -836,7 +858,7 @@ template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
             k_cr_odd<T, KB><<<nodd, NT, S::bytes, st>>>(cP + o, cQ + o, 1, 2, Ml, P->d_err);
             SPK_CHECK_LAUNCH();
         }
-        k_cr_even<T, KB><<<neven, NT, S::bytes, st>>>(cP + o, cQ + o, cX + o, cY + o, Ml, cnt, cP + on, cQ + on, cX + on,
+        k_cr_even<T, KB><<<dim3(neven, 4), NT, S::bytes, st>>>(cP + o, cQ + o, cX + o, cY + o, Ml, cnt, cP + on, cQ + on, cX + on,
                                                       cY + on);
         SPK_CHECK_LAUNCH();
         P->launches += 2;
@@ -854,7 +876,7 @@ template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
 
 template <class T, int KB> int run_red_solve(spk_plan *P, int nrhs, int iters, cudaStream_t st)
 {
-    if constexpr (KB == 32 || (KB == 64 && sizeof(T) <= 8)) {
+    if constexpr (KB == 32 || (KB == 64 && sizeof(T) <= 8) || (KB == 128 && sizeof(T) == 4)) {
         if (nrhs == 1) return run_red_solve_q<T, KB, 1>(P, nrhs, iters, st);
         return run_red_solve_q<T, KB, 4>(P, nrhs, iters, st);
     }
