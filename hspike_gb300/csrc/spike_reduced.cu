@@ -165,6 +165,176 @@ __global__ void __launch_bounds__(NTOf<KB>::value)
     }
 }
 
+// ---------------------------------------------------------------- tensor-core products
+// The reduced system's 2KB x 2KB block products for KB >= 64 (FP32 factors)
+// run on the tensor cores: warp-level mma.sync m16n8k8 with TF32 operands,
+// each FP32 operand split into a TF32 high part and a TF32 remainder, and
+// the three significant partial products (lo*hi, hi*lo, hi*hi) accumulated
+// in FP32, which keeps FP32 accuracy.  Warp w of the CTA (KB*KB/512 warps:
+// the Tile kernels' own thread count) owns the 32 x 16 output block at rows
+// 32 (w / (KB/16)), columns 16 (w % (KB/16)); operands are shared tiles in
+// the Tile layout (row-major, row stride KB + 4).
+__device__ __forceinline__ void tf32_split(float x, uint32_t &hi, uint32_t &lo)
+{
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(x - __uint_as_float(h)));
+    hi = h;
+    lo = l;
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
+{
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+using TcAcc = float[2][2][4];
+__device__ __forceinline__ void tc_zero(TcAcc &acc)
+{
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[i][j][e] = 0.f;
+}
+// acc += A B (A, B: KB x KB shared tiles, row-major, row stride KB + 4)
+template <int KB> __device__ __forceinline__ void tc_mm(TcAcc &acc, const float *A, const float *B)
+{
+    constexpr int LD = TileLD<float, KB>::value;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int r0 = (warp / (KB / 16)) * 32, c0 = (warp % (KB / 16)) * 16;
+#pragma unroll 2
+    for (int k0 = 0; k0 < KB; k0 += 8) {
+        uint32_t ah[2][4], al[2][4], bh[2][2], bl[2][2];
+#pragma unroll
+        for (int i = 0; i < 2; i++) { // A fragment: (g, t), (g + 8, t), (g, t + 4), (g + 8, t + 4)
+            const float *Ar = A + (r0 + i * 16 + g) * LD + k0 + t;
+            tf32_split(Ar[0], ah[i][0], al[i][0]);
+            tf32_split(Ar[8 * LD], ah[i][1], al[i][1]);
+            tf32_split(Ar[4], ah[i][2], al[i][2]);
+            tf32_split(Ar[8 * LD + 4], ah[i][3], al[i][3]);
+        }
+#pragma unroll
+        for (int j = 0; j < 2; j++) { // B fragment: (t, g), (t + 4, g)
+            const float *Bc = B + (k0 + t) * LD + c0 + j * 8 + g;
+            tf32_split(Bc[0], bh[j][0], bl[j][0]);
+            tf32_split(Bc[4 * LD], bh[j][1], bl[j][1]);
+        }
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                mma_tf32(acc[i][j], al[i], bh[j]);
+                mma_tf32(acc[i][j], ah[i], bl[j]);
+                mma_tf32(acc[i][j], ah[i], bh[j]);
+            }
+    }
+}
+// f(row, col, value) for every accumulator element this thread holds:
+// (g, 2t), (g, 2t + 1), (g + 8, 2t), (g + 8, 2t + 1) of each 16 x 8 block
+template <int KB, class F> __device__ __forceinline__ void tc_each(const TcAcc &acc, F f)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int r0 = (warp / (KB / 16)) * 32, c0 = (warp % (KB / 16)) * 16;
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 2; j++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) f(r0 + i * 16 + g + (e >> 1) * 8, c0 + j * 8 + 2 * t + (e & 1), acc[i][j][e]);
+}
+
+// k_cr_odd with tensor-core products: S = I - Q P, M11 = S^{-1} (the Tile
+// inverse), M10 = -M11 Q, M01 = -P M11, M00 = I - P M10.
+template <int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_cr_odd_tc(const float *__restrict__ Pl, const float *__restrict__ Ql, int first, int stride, float *M,
+                unsigned *err)
+{
+    constexpr int NT = NTOf<KB>::value, LD = TileLD<float, KB>::value;
+    using TL = Tile<float, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    static_assert(NT == KB * KB / 16, "one warp per 32 x 16 output block");
+    const int j = first + blockIdx.x * stride;
+    float *Mj = M + (size_t)blockIdx.x * 4 * TS;
+    extern __shared__ char smraw[];
+    float *sP = (float *)smem_align(smraw), *sQ = sP + TL::ELEMS, *sH = sQ + TL::ELEMS;
+    float *buf = sH + TL::ELEMS;
+    TL t(threadIdx.x);
+    typename TL::Reg a;
+    TcAcc acc;
+    ld<float, KB>(sP, Pl + (size_t)j * TS);
+    ld<float, KB>(sQ, Ql + (size_t)j * TS);
+    __syncthreads();
+    tc_zero(acc);
+    tc_mm<KB>(acc, sQ, sP);
+    tc_each<KB>(acc, [&](int r, int c, float v) { sH[r * LD + c] = (r == c ? 1.f : 0.f) - v; }); // S
+    __syncthreads();
+    t.rload(a, sH);
+    const bool ok = t.inverse(a, buf);
+    if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+    __syncthreads();
+    t.rstore(sH, a); // M11
+    t.gstore(Mj + 3 * TS, a);
+    __syncthreads();
+    tc_zero(acc);
+    tc_mm<KB>(acc, sH, sQ);
+    tc_each<KB>(acc, [&](int r, int c, float v) { Mj[2 * TS + r * KB + c] = -v; }); // M10
+    __syncthreads(); // every read of Q is done
+    tc_each<KB>(acc, [&](int r, int c, float v) { sQ[r * LD + c] = -v; });
+    tc_zero(acc);
+    tc_mm<KB>(acc, sP, sH);
+    tc_each<KB>(acc, [&](int r, int c, float v) { Mj[TS + r * KB + c] = -v; }); // M01
+    __syncthreads();
+    tc_zero(acc);
+    tc_mm<KB>(acc, sP, sQ);
+    tc_each<KB>(acc, [&](int r, int c, float v) { Mj[r * KB + c] = (r == c ? 1.f : 0.f) - v; }); // M00
+}
+
+// k_cr_even with tensor-core products: blockIdx.y picks the result
+//   0: P' = P_i - X_i (M01 Y)_{i-1}   1: Q' = Q_i - Y_i (M10 X)_{i+1}
+//   2: X' = -X_i (M00 X)_{i-1}        3: Y' = -Y_i (M11 Y)_{i+1}
+template <int KB>
+__global__ void __launch_bounds__(NTOf<KB>::value)
+    k_cr_even_tc(const float *__restrict__ Pl, const float *__restrict__ Ql, const float *__restrict__ Xl,
+                 const float *__restrict__ Yl, const float *__restrict__ Ml, int cnt, float *Pn, float *Qn,
+                 float *Xn, float *Yn)
+{
+    constexpr int NT = NTOf<KB>::value, LD = TileLD<float, KB>::value;
+    using TL = Tile<float, KB, NT>;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int i = 2 * blockIdx.x, a_out = blockIdx.x, which = blockIdx.y;
+    const bool left = i - 1 >= 0, right = i + 1 < cnt;
+    const bool has = (which == 0 || which == 2) ? left : right;
+    const float *base = which == 0 ? Pl + (size_t)i * TS : which == 1 ? Ql + (size_t)i * TS : nullptr;
+    float *out = (which == 0 ? Pn : which == 1 ? Qn : which == 2 ? Xn : Yn) + (size_t)a_out * TS;
+    if (!has) { // no neighbour on this side: P' = P_i, Q' = Q_i, X' = Y' = 0
+        for (int q = threadIdx.x; q < KB * KB; q += NT) out[q] = base ? base[q] : 0.f;
+        return;
+    }
+    const float *Mnb = Ml + (size_t)(left && (which == 0 || which == 2) ? (i - 2) / 2 : i / 2) * 4 * TS;
+    const float *Lt = (which == 0 || which == 2 ? Xl : Yl) + (size_t)i * TS;
+    const float *Mq = Mnb + (size_t)(which == 0 ? 1 : which == 1 ? 2 : which == 2 ? 0 : 3) * TS;
+    const float *Rt = (which == 0 || which == 3 ? Yl : Xl) + (size_t)(which == 0 || which == 2 ? i - 1 : i + 1) * TS;
+    extern __shared__ char smraw[];
+    float *sA = (float *)smem_align(smraw), *sB = sA + TL::ELEMS, *sC = sB + TL::ELEMS;
+    ld<float, KB>(sA, Mq);
+    ld<float, KB>(sB, Rt);
+    __syncthreads();
+    TcAcc acc;
+    tc_zero(acc);
+    tc_mm<KB>(acc, sA, sB);
+    tc_each<KB>(acc, [&](int r, int c, float v) { sC[r * LD + c] = v; });
+    __syncthreads();
+    ld<float, KB>(sA, Lt);
+    __syncthreads();
+    tc_zero(acc);
+    tc_mm<KB>(acc, sA, sC);
+    tc_each<KB>(acc, [&](int r, int c, float v) { out[r * KB + c] = (base ? base[r * KB + c] : 0.f) - v; });
+}
+
 // ---------------------------------------------------------------- solve
 // vectors: level block a holds 2KB rows; element (row q, column h) of block a
 // at level offset off lives at g[h * stride + (off + a) * 2KB + q].
@@ -833,13 +1003,28 @@ template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
     using S = RedSmem<T, KB>;
     constexpr int NT = NTOf<KB>::value;
     constexpr size_t TS = (size_t)KB * KB;
+    // FP32 factors with 64- or 128-row tiles: the block products on the tensor cores
+    constexpr bool TC = std::is_same<T, float>::value && (KB == 64 || KB == 128);
     static bool attr = false;
     if (!attr) {
         if (cudaFuncSetAttribute(k_cr_odd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes) != cudaSuccess ||
             cudaFuncSetAttribute(k_cr_even<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes) != cudaSuccess)
             return SPK_ECUDA;
+        if constexpr (TC) {
+            if (cudaFuncSetAttribute(k_cr_odd_tc<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_cr_even_tc<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::bytes) !=
+                    cudaSuccess)
+                return SPK_ECUDA;
+        }
         attr = true;
     }
+    auto odd = [&](const T *Pp, const T *Qp, int first, int stride, int count, T *Mo) {
+        if constexpr (TC)
+            k_cr_odd_tc<KB><<<count, NT, S::bytes, st>>>(Pp, Qp, first, stride, Mo, P->d_err);
+        else
+            k_cr_odd<T, KB><<<count, NT, S::bytes, st>>>(Pp, Qp, first, stride, Mo, P->d_err);
+    };
     using H = typename HighOf<T>::type;
     const long long c0 = (long long)P->n_iface * TS;
     k_red_cvt<T><<<256, 256, 0, st>>>((const H *)P->d_RP, (T *)P->d_crP, c0);
@@ -855,11 +1040,15 @@ template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
         T *Ml = cM + (size_t)P->cr_moff[l] * 4 * TS;
         const int nodd = cnt / 2, neven = (cnt + 1) / 2;
         if (nodd > 0) {
-            k_cr_odd<T, KB><<<nodd, NT, S::bytes, st>>>(cP + o, cQ + o, 1, 2, Ml, P->d_err);
+            odd(cP + o, cQ + o, 1, 2, nodd, Ml);
             SPK_CHECK_LAUNCH();
         }
-        k_cr_even<T, KB><<<dim3(neven, 4), NT, S::bytes, st>>>(cP + o, cQ + o, cX + o, cY + o, Ml, cnt, cP + on, cQ + on, cX + on,
-                                                      cY + on);
+        if constexpr (TC)
+            k_cr_even_tc<KB><<<dim3(neven, 4), NT, S::bytes, st>>>(cP + o, cQ + o, cX + o, cY + o, Ml, cnt, cP + on,
+                                                                   cQ + on, cX + on, cY + on);
+        else
+            k_cr_even<T, KB><<<dim3(neven, 4), NT, S::bytes, st>>>(cP + o, cQ + o, cX + o, cY + o, Ml, cnt, cP + on,
+                                                                   cQ + on, cX + on, cY + on);
         SPK_CHECK_LAUNCH();
         P->launches += 2;
     }
@@ -867,7 +1056,7 @@ template <class T, int KB> int run_red_factor(spk_plan *P, cudaStream_t st)
     {
         const int L = P->cr_levels;
         const size_t o = (size_t)P->cr_off[L] * TS;
-        k_cr_odd<T, KB><<<1, NT, S::bytes, st>>>(cP + o, cQ + o, 0, 1, cM + (size_t)P->cr_moff[L] * 4 * TS, P->d_err);
+        odd(cP + o, cQ + o, 0, 1, 1, cM + (size_t)P->cr_moff[L] * 4 * TS);
         SPK_CHECK_LAUNCH();
         P->launches++;
     }
