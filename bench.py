@@ -385,6 +385,8 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true", help="omit the host-buffer end-to-end leg")
     ap.add_argument("--n", type=int, default=N, help="rows (smaller cases for profiler captures)")
     ap.add_argument("--partitions", type=int, default=P)
+    ap.add_argument("--k", type=int, default=K_BAND,
+                    help="half-bandwidth kl = ku (profiler captures of other tile sizes; the roofline figures assume 64)")
     ap.add_argument("--batch", type=int, default=4096, help="systems in the batched leg (0 = skip it)")
     ap.add_argument("--batch-only", action="store_true", help="run only the batched leg (profiler captures)")
     ap.add_argument("--no-autotune", action="store_true", help="batched leg: schedules by rule")
@@ -393,6 +395,8 @@ def main():
     ap.add_argument("--complex-only", action="store_true", help="run only the complex leg")
     ap.add_argument("--skip-complex", action="store_true", help="omit the complex leg")
     args = ap.parse_args()
+    if args.k != K_BAND:
+        globals()["K_BAND"] = args.k
     if args.impl == "reference":
         return reference_arm(args)
 
