@@ -306,7 +306,7 @@ def complex_leg(torch, dev, hs, steps, warmup, n=4_000_000, k=3, nrhs=4, p=512, 
 
 
 # --------------------------------------------------------------------- serving leg
-def serving_leg(hs, count, rate=20_000.0, slots=8, k_max=128):
+def serving_leg(hs, count, rate=20_000.0, slots=16, k_max=128):
     """The serving stream: Poisson arrivals at `rate`/s, per request n
     log-normal (median 20,000, sigma 1, clipped to [500, 2,000,000]), k uniform
     in {1..k_max}, nrhs uniform in {1..32}, dominance 1.05, 30 % reusing an
