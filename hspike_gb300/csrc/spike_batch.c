@@ -182,9 +182,9 @@ static int group_build_plan(struct spike_batch_s *B, bgroup *G, int KB, int rpp)
     for (int j = 0; j < G->nsys; j++) {
         const int n = B->sys[G->members[j]].n;
         const int pj = spike_batch_partitions(n, KB, rpp);
-        const int nreg = n / pj; /* the reference's rule: remainder in the last partition */
+        const int nreg = n / pj, rem = n % pj; /* the remainder spread one row each over the first partitions */
         for (int i = 0; i < pj; i++, q++) {
-            ps[q] = (int)(G->h_sys[j].row0 + (long long)i * nreg);
+            ps[q] = (int)(G->h_sys[j].row0 + (long long)i * nreg + (i < rem ? i : rem));
             psys[q] = j;
         }
     }

@@ -475,9 +475,13 @@ static int plan_create(int n, long long nnz, int ku, int kl, int is_complex, int
     const int p = choose_partitions(n, KB, partitions);
     int *ps = (int *)malloc(sizeof(int) * (p + 1));
     if (!ps) return SPK_EMEM;
-    /* spike_solve_analysis: regular partitions, remainder in the last one */
-    const int nreg = n / p;
-    for (int i = 0; i < p; i++) ps[i] = i * nreg;
+    /* A partition count the caller asked for gets the reference's layout
+     * (spike_solve_analysis: n/p rows each, the remainder in the last one);
+     * a count chosen here spreads the remainder one row each over the first
+     * partitions, since a long last partition's chain would set the time
+     * (with many small partitions the remainder can be a hundred blocks). */
+    const int nreg = n / p, rem = partitions > 0 ? 0 : n % p;
+    for (int i = 0; i < p; i++) ps[i] = i * nreg + (i < rem ? i : rem);
     ps[p] = n;
     const int rc = spk_plan_build(n, nnz, ku, kl, KB, is_complex, mode, p, ps, nrhs_max, stream, stream_alloc, out);
     free(ps);
@@ -491,7 +495,13 @@ size_t spk_solve_footprint(int n, long long nnz, int k, int nrhs, int is_complex
     if (!KB || n <= 0) return 0;
     const int p = choose_partitions(n, KB, partitions);
     const int nreg = n / p;
-    long long blocks = (long long)(p - 1) * ((nreg + KB - 1) / KB) + ((n - (long long)(p - 1) * nreg) + KB - 1) / KB;
+    long long blocks;
+    if (partitions > 0) /* the reference's layout (plan_create) */
+        blocks = (long long)(p - 1) * ((nreg + KB - 1) / KB) + ((n - (long long)(p - 1) * nreg) + KB - 1) / KB;
+    else { /* balanced: n % p partitions of nreg + 1 rows */
+        const int rem = n % p;
+        blocks = (long long)rem * ((nreg + 1 + KB - 1) / KB) + (long long)(p - rem) * ((nreg + KB - 1) / KB);
+    }
     const long long nif = p > 1 ? p - 1 : 1;
     long long tiles = 0, mtiles = 0;
     for (long long c = nif, l = 0;; l++) {
@@ -1402,8 +1412,8 @@ Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, 
     int part_start[NOALLOC_MAX_PARTS + 1], blk_off[NOALLOC_MAX_PARTS + 1];
     int cr_count[32];
     long long cr_off[33], cr_moff[33];
-    const int nreg = n / p;
-    for (int i = 0; i < p; i++) part_start[i] = i * nreg;
+    const int nreg = n / p, rem = n % p; /* balanced, as plan_create for an automatic count */
+    for (int i = 0; i < p; i++) part_start[i] = i * nreg + (i < rem ? i : rem);
     part_start[p] = n;
     blk_off[0] = 0;
     for (int i = 0; i < p; i++) blk_off[i + 1] = blk_off[i] + (part_start[i + 1] - part_start[i] + KB - 1) / KB;
