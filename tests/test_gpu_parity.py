@@ -209,7 +209,7 @@ def test_single_partition_and_auto_partitions():
     assert relerr(x, xt) <= 1e-10
 
 
-def test_baseline_c1_config():
+def test_pentadiagonal_100k_on_four_partitions():
     """Plain FP64 SPIKE, 4 partitions, pentadiagonal n = 100,000, 1 RHS, dominance 2.0."""
     rp, ci, a, xt, b = hs.gen_banded(100_000, 2, 2, 2.0, seed=1)
     check(rp, ci, a, b, 4, "fp64", x_true=xt)
