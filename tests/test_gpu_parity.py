@@ -492,7 +492,7 @@ def test_host_arrays_full_band_columns_stay_on_host():
         with pytest.raises(hs.SpikeError) as e:
             hs.solve(rp, bad, a, b, ctx=ctx)
         assert e.value.name == "csr"
-        # complex data
+        # complex data, then a band break in it (a row reaching one column further)
         rp, ci, a, xt, b = hs.gen_banded(200000, 24, 24, 1.5, seed=34, complex_=True, nrhs=1)
         assert len(ci) >= 8 << 20
         for _ in range(2):
@@ -500,6 +500,19 @@ def test_host_arrays_full_band_columns_stay_on_host():
         assert ctx.info().columns_implied == 1
         assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
         assert relerr(x, xt) <= 1e-10
+        r = 150000
+        ci3 = ci.copy()
+        ci3[rp[r + 1] - 1] = r + 25  # last column r + 24 -> r + 25: still sorted, not the full band
+        x = hs.solve(rp, ci3, a, b, ctx=ctx)
+        assert ctx.info().columns_implied == 0 and ctx.info().ku == 25
+        assert oracle.residual(rp, ci3, a, x, b).max() <= RES_TOL
+        # plain FP64 through the same path
+        rp, ci, a, xt, b = hs.gen_banded(200000, 24, 24, 1.5, seed=35, nrhs=2)
+        for _ in range(2):
+            x = hs.solve(rp, ci, a, b, precision=hs.SPIKE_PRECISION_FP64, ctx=ctx)
+        assert ctx.info().columns_implied == 1
+        assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
+        assert relerr(x, xt) <= 1e-12
     finally:
         ctx.close()
 
