@@ -168,7 +168,8 @@ def reference_arm(args):
 # --------------------------------------------------------------------- peaks
 def sgemm_tflops(torch, dev):
     """FP32 CUDA-core peak as measured here: cuBLAS SGEMM 8192^3 with TF32 off,
-    best of 5 (the FP32 analogue of the measured bf16 figure)."""
+    best of 5 (the FP32 analogue of the measured bf16 GEMM peak in
+    MEASURED_PEAKS.json)."""
     prev = torch.backends.cuda.matmul.allow_tf32
     torch.backends.cuda.matmul.allow_tf32 = False
     a = torch.randn(8192, 8192, device=dev)
@@ -494,7 +495,7 @@ def main():
     sweeps = info.refine_sweeps
     out = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-           "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
+           "scaling": "weak", "vs_baseline": None,
            "dtype": "f32 factors / f64 residual+update+reduced", "data": "synthetic (seeded generator)",
            "config": {"workload": WORKLOAD if (n, p) == (N, P) else WORKLOAD.replace(f"n={N:,}", f"n={n:,}").replace(
                           f"partitions={P}", f"partitions={p}"), "l2": "inputs (3.1 GB CSR) larger than the 129 MB L2; no flush",

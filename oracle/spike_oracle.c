@@ -1,7 +1,7 @@
 /*
  * spike_oracle.c -- CPU restatement of the reference SPIKE solve.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU path is
  * compared against; the product library never links, loads or calls it.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
  * it.

@@ -1,7 +1,7 @@
 """bench.py's reference arm, run on a small case of the same band without a GPU.
 
 The reference arm times the CPU restatement of the reference path (oracle/)
-and prints the line the driver reads: impl "reference", the metric, a value,
+and prints one JSON line: impl "reference", the metric, a value,
 cpu_baseline and e2e.  Run here at n = 20,000 so it takes seconds.
 """
 import json
