@@ -384,7 +384,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
     ap.add_argument("--skip-extras", action="store_true", help="mixed-precision device timing only")
     ap.add_argument("--skip-e2e", action="store_true", help="omit the host-buffer end-to-end leg")
-    ap.add_argument("--n", type=int, default=N, help="rows (smaller cases for profiler captures)")
+    ap.add_argument("--n", "--rows", dest="n", type=int, default=N,
+                    help="rows (smaller cases for profiler captures; --rows under torch.distributed.run)")
     ap.add_argument("--partitions", type=int, default=P)
     ap.add_argument("--k", type=int, default=K_BAND,
                     help="half-bandwidth kl = ku (profiler captures of other tile sizes; the roofline figures assume 64)")
