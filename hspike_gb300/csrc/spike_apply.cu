@@ -158,15 +158,10 @@ __device__ void tile_mv(T *out, const T *Mt, const T *v, const T *base, int nr, 
     }
 }
 
-template <class T, int KB> __device__ void load_tile_s(T *s, const T *g)
-{
-    copy_tile_g2s<T, KB, NTOf<KB>::value>(s, g);
-}
-
+// Right-hand-side rows of block J (FP64 -> factor precision) into registers.
 // Vector elements q < KB * nr of block J: column h = q / KB, row lr = q % KB,
 // so consecutive threads touch consecutive rows of one column (coalesced
 // global accesses) and only the live columns are fetched.
-// right-hand-side rows of block J (FP64 -> factor precision) into registers
 template <class T, class H, int KB, int VPT>
 __device__ __forceinline__ void fetch_r(T (&nxt)[VPT], const H *__restrict__ r, int n, int s, int m, int h0, int nr,
                                         int J)

@@ -261,13 +261,6 @@ template <class T, int KB, int NT> struct Tile {
 #pragma unroll
             for (int j = 0; j < TC; j++) a[i][j] = sc_zero<T>();
     }
-    __device__ __forceinline__ void ridentity(Reg &a) const
-    {
-#pragma unroll
-        for (int i = 0; i < TR; i++)
-#pragma unroll
-            for (int j = 0; j < TC; j++) a[i][j] = (row(i) == col(j)) ? sc_one<T>() : sc_zero<T>();
-    }
     // register tile <- shared tile (threads without a sub-tile hold zeros)
     __device__ __forceinline__ void rload(Reg &a, const T *s) const
     {
@@ -661,8 +654,6 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-// all but the most recently committed group complete
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 // all but the N most recently committed groups complete
 template <int N> __device__ __forceinline__ void cp_async_wait_n()
 {
@@ -689,12 +680,6 @@ template <int E> __device__ __forceinline__ void cp_async_elem(void *smem, const
     else
         cp_async4(smem, gmem);
 }
-// `chunks` 16-byte pieces from global to shared, issued by this thread alone
-__device__ __forceinline__ void cp_async_chunks(void *s, const void *g, int chunks)
-{
-    for (int q = 0; q < chunks; q++) cp_async16((char *)s + 16 * q, (const char *)g + 16 * q);
-}
-
 // ------------------------------------------------------------ tile rows across lanes
 // A chain of a small band (KB <= 4) runs on KB consecutive lanes of a warp:
 // lane r owns row r of every KB x KB tile, and rows of another lane arrive by
