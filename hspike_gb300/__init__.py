@@ -52,6 +52,7 @@ EXPORTS = [
     "spike_batch_partitions", "spike_server_create", "spike_server_submit", "spike_server_wait",
     "spike_server_drain", "spike_server_stats", "spike_server_clock", "spike_server_destroy",
     "spike_rcm_permutation", "spike_permute_csr", "spike_permute_vector", "spike_dsolve_reordered",
+    "spike_csr_full_band",
     "matrix_ComputeBandwidth", "matrix_LoadCSR", "matrix_SaveCSR", "matrix_ExportBinary",
     "matrix_CreateFromComponents", "matrix_Deallocate", "directSolver_CreateHandler", "directSolver_Configure",
     "directSolver_Factorize", "directSolver_SolveForRHS", "directSolver_ShowStatistics", "directSolver_Finalize",
@@ -197,6 +198,7 @@ def load(path: str | None = None):
     L.spike_permute_csr.argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp]
     L.spike_permute_vector.argtypes = [i, i, i, vp, vp]
     L.spike_dsolve_reordered.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, vp]
+    L.spike_csr_full_band.argtypes = [i, i, i, i, vp, vp, C.POINTER(C.c_int)]
     mp, hp = C.POINTER(Matrix), C.POINTER(DirectSolverHandler)
     L.matrix_ComputeBandwidth.argtypes = [i, vp, vp, vp, ip, ip]
     L.matrix_LoadCSR.argtypes = [C.c_char_p]
@@ -567,6 +569,18 @@ def solve_reordered(rowptr, colind, aij, b, ctx: Context | None = None):
 def batch_partitions(n: int, block: int, rows_per_partition: int) -> int:
     """The batch partition rule (host only, no device needed)."""
     return int(load().spike_batch_partitions(n, block, rows_per_partition))
+
+
+def csr_full_band(rowptr, colind, ku: int, kl: int) -> bool:
+    """True when every row r holds exactly the columns max(0, r - kl) ..
+    min(n - 1, r + ku) in order: the layout whose column indices a solve with
+    host arrays leaves on the host (host only, no device needed)."""
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    colind = np.ascontiguousarray(colind, np.int32)
+    full = C.c_int(-1)
+    _check(load().spike_csr_full_band(len(rowptr) - 1, len(colind), ku, kl, _ptr(colind), _ptr(rowptr),
+                                      C.byref(full)))
+    return bool(full.value)
 
 
 # ------------------------------------------------ reference matrix helpers + plugin

@@ -879,6 +879,22 @@ static int rows_full_band(const band_scan *S, int r0, int r1)
     return 1;
 }
 
+Error_t spike_csr_full_band(integer_t n, integer_t nnz, integer_t ku, integer_t kl, const integer_t *colind,
+                            const integer_t *rowptr, int *full)
+{
+    if (n < 0 || nnz < 0 || ku < 0 || kl < 0 || !full || (n > 0 && !rowptr) || (nnz > 0 && !colind))
+        return spk_fail(SPIKE_ERR_ARGUMENT, "spike_csr_full_band: bad argument");
+    band_scan S;
+    S.rowptr = rowptr;
+    S.colind = colind;
+    S.n = n;
+    S.ku = ku;
+    S.kl = kl;
+    S.nnz = nnz;
+    *full = n == 0 ? nnz == 0 : rowptr[0] == 0 && rowptr[n] == nnz && rows_full_band(&S, 0, n);
+    return spk_succeed();
+}
+
 static void *band_scan_worker(void *p)
 {
     const band_scan_arg *a = (const band_scan_arg *)p;

@@ -290,6 +290,15 @@ Error_t spike_dsolve_reordered(spike_context_t ctx, integer_t n, integer_t nnz, 
                                const integer_t *colind, const integer_t *rowptr, const double *aij, double *x,
                                const double *b, integer_t *perm_out);
 
+/* ---- host check of the full-band layout ----
+ * *full = 1 when row r of the CSR holds exactly the columns
+ * max(0, r - kl) .. min(n - 1, r + ku) in increasing order, for every row
+ * (rowptr[0] = 0, rowptr[n] = nnz) -- the layout for which a solve with host
+ * arrays leaves the column indices on the host (spike_info_t.columns_implied)
+ * -- else 0.  Reads only rowptr[0..n] and the colind entries they delimit. */
+Error_t spike_csr_full_band(integer_t n, integer_t nnz, integer_t ku, integer_t kl, const integer_t *colind,
+                            const integer_t *rowptr, int *full);
+
 #ifdef __cplusplus
 }
 #endif
