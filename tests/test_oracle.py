@@ -125,3 +125,25 @@ def test_superlu_restatement_agrees():
     x2 = spike_superlu(rp, ci, a, b, p=5)
     np.testing.assert_allclose(x1, x2, rtol=1e-11, atol=1e-13)
     np.testing.assert_allclose(x1, xt, rtol=1e-10, atol=1e-12)
+
+
+def test_oracle_on_ragged_random_systems():
+    """Random shapes the fixtures do not cover: n not a multiple of p, one-sided
+    bands (ku = 0 or kl = 0), ku != kl, p up to n / (2 max(ku, kl)), several
+    right-hand sides, real and complex; against a dense solve."""
+    import hspike_gb300 as hs
+
+    rng = np.random.default_rng(5)
+    for case in range(120):
+        n = int(rng.integers(10, 400))
+        ku, kl = int(rng.integers(0, 7)), int(rng.integers(0, 7))
+        k = max(ku, kl, 1)
+        p = int(rng.integers(1, min(max(1, n // (2 * k)), 16) + 1))
+        nrhs = int(rng.integers(1, 4))
+        rp, ci, a, xt, b = hs.gen_banded(n, ku, kl, 1.2, case, nrhs=nrhs, complex_=case % 3 == 0)
+        A = np.zeros((n, n), a.dtype)
+        for r in range(n):
+            A[r, ci[rp[r]:rp[r + 1]]] = a[rp[r]:rp[r + 1]]
+        x = oracle.spike(rp, ci, a, b, p=p).reshape(n, -1)
+        xd = np.linalg.solve(A, b.reshape(n, -1))
+        assert np.abs(x - xd).max() <= 1e-10 * np.abs(xd).max(), (case, n, ku, kl, p)
