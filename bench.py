@@ -130,6 +130,32 @@ def cpu_baseline(system=None, p=P):
             "seconds": dt}
 
 
+def cpu_one_core(n=N, p=P, parts=32):
+    """The oracle on one host core: `parts` partitions of the workload's shape
+    (n // p rows each, the same band, dominance and seed) solved as one system,
+    the time scaled by p / parts to the whole workload (the partitions are
+    independent and the reduced system grows linearly with their count)."""
+    import hspike_gb300 as hs
+    from oracle import oracle
+
+    parts = max(1, min(parts, p))
+    rows = (n // p) * parts
+    rp, ci, a, xt, b = hs.gen_banded(rows, K_BAND, K_BAND, DOM, SEED, nrhs=NRHS)
+    oracle.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        x = oracle.spike(rp, ci, a, b, p=parts)
+        dt = time.perf_counter() - t0
+    finally:
+        oracle.set_threads(0)
+    rel = float(oracle.residual(rp, ci, a, x, b).max())
+    est = dt * p / parts
+    return {"value": 1.0 / est, "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": (f"{parts} of the {p} partitions ({rows:,} rows, same band) solved by oracle/spike_oracle.c "
+                       f"on one thread: {dt:.2f} s, relres {rel:.1e}; x {p / parts:g} for the whole workload = "
+                       f"{est:.1f} s per solve")}
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -649,6 +675,7 @@ def main():
 
     if not args.skip_cpu and rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline((rp, ci, a, b), p)
+        out["cpu_baseline"]["one_core"] = cpu_one_core(n, p)
 
     ctx.close()
     if dist:

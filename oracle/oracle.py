@@ -37,6 +37,8 @@ def _lib():
         L.oracle_schedule.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, ip, ip]
         L.oracle_reduced_nnz.argtypes = [C.c_int, C.c_int, C.c_int]
         L.oracle_reduced_nnz.restype = i64
+        L.oracle_set_threads.argtypes = [C.c_int]
+        L.oracle_set_threads.restype = C.c_int
         for pfx in ("d", "z"):
             f = getattr(L, pfx + "oracle_spike")
             f.argtypes = [C.c_int, C.c_int, C.c_int, ip, ip, dp, dp, dp, C.c_int, ip, ip, dp, dp, dp]
@@ -86,6 +88,12 @@ def schedule(n, p, ku, kl):
     if _lib().oracle_schedule(n, p, ku, kl, _ip(nb), _ip(rb)):
         raise ValueError("bad schedule")
     return nb, rb
+
+
+def set_threads(threads: int) -> int:
+    """Threads for the oracle's partition loops (0: the OpenMP default);
+    returns the previous limit."""
+    return int(_lib().oracle_set_threads(threads))
 
 
 def spike(rowptr, colind, aij, b, p=4, return_reduced=False):

@@ -32,6 +32,9 @@
  * parallel with OpenMP when it is enabled (the reference loops serially).
  */
 #include <complex.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -132,6 +135,22 @@ int oracle_reduced_pattern(int P, int ku, int kl, int *rowptr, int *colind)
     }
     (void)nrows;
     return 0;
+}
+
+/* Threads for the partition loops of later calls (0: the OpenMP default);
+ * returns the previous limit.  Used to time the oracle on one core. */
+int oracle_set_threads(int threads)
+{
+#ifdef _OPENMP
+    const int prev = omp_get_max_threads();
+    static int dflt = 0;
+    if (!dflt) dflt = prev;
+    omp_set_num_threads(threads > 0 ? threads : dflt);
+    return prev;
+#else
+    (void)threads;
+    return 1;
+#endif
 }
 #endif /* !ORACLE_COMPLEX */
 
