@@ -44,3 +44,15 @@ def test_reference_arm_under_two_ranks_prints_once():
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+
+
+def test_one_core_sample_runs_on_one_thread_and_restores_the_default():
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import oracle
+
+    before = oracle.set_threads(0)
+    line = bench.cpu_one_core(20000, 8, 2)
+    assert line["cores"] == 1 and line["kind"] == "port" and line["value"] > 0
+    assert "2 of the 8 partitions" in line["sample"]
+    assert oracle.set_threads(0) == before
