@@ -675,7 +675,10 @@ def main():
 
     if not args.skip_cpu and rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline((rp, ci, a, b), p)
-        out["cpu_baseline"]["one_core"] = cpu_one_core(n, p)
+        try:  # a supplementary figure: its failure must not cost the line
+            out["cpu_baseline"]["one_core"] = cpu_one_core(n, p)
+        except Exception as e:  # noqa: BLE001
+            out["cpu_baseline"]["one_core"] = {"error": f"{type(e).__name__}: {e}"}
 
     ctx.close()
     if dist:
