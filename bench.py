@@ -62,24 +62,45 @@ def alg_flops(n, k, nrhs, applies, residuals):
 
 # --------------------------------------------------------------------- clocks
 class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples over a timed region:
+    start() launches the sampler and returns once its first sample is in (the
+    tool is live), begin() marks the region's start, stop() summarises the
+    samples taken after the mark."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, interval_ms=50, cmd="nvidia-smi"):
         self.index = index
+        self.interval_ms = interval_ms
+        self.cmd = cmd
         self.rows = []
+        self.mark = 0
         self.proc = None
 
-    def start(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except Exception:
-            self.proc = None
+    def start(self, wait_s=3.0):
+        # the requested interval first, the tool's customary 200 ms if that one yields nothing
+        for interval in dict.fromkeys((self.interval_ms, 200)):
+            try:
+                self.proc = subprocess.Popen(
+                    [self.cmd, "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                     "-lms", str(interval)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                self.thread = threading.Thread(target=self._read, daemon=True)
+                self.thread.start()
+            except Exception:
+                self.proc = None
+                return
+            t0 = time.monotonic()
+            while not self.rows and self.proc.poll() is None and time.monotonic() - t0 < wait_s:
+                time.sleep(0.005)
+            if self.rows or self.proc.poll() is None:
+                self.interval_ms = interval
+                break
+            self.thread.join(timeout=2)
+        self.begin()
+
+    def begin(self):
+        self.mark = len(self.rows)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -96,13 +117,15 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.thread.join(timeout=2)
-        rows = self.rows
+        region = self.rows[self.mark:]
+        # a region shorter than the interval may hold no sample: the one just before it stands in
+        rows = region or self.rows[-1:]
         sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
         mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "samples": len(rows), "reasons": reasons}
+                "samples": len(region), "interval_ms": self.interval_ms, "reasons": reasons}
 
 
 # --------------------------------------------------------------------- CPU baseline
@@ -404,7 +427,7 @@ def serving_leg(hs, count, rate=20_000.0, slots=16, k_max=128):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline leg")
@@ -496,6 +519,8 @@ def main():
         if clocks:
             clocks.start()
         barrier()
+        if clocks:
+            clocks.begin()
         ev[0].record(stream)
         for s in range(steps):
             solve(ctx_, d_x_, d_b_, nrhs)

@@ -56,3 +56,62 @@ def test_one_core_sample_runs_on_one_thread_and_restores_the_default():
     assert line["cores"] == 1 and line["kind"] == "port" and line["value"] > 0
     assert "2 of the 8 partitions" in line["sample"]
     assert oracle.set_threads(0) == before
+
+
+def test_clock_sampler_counts_only_the_timed_region(tmp_path):
+    """The sampler against a stand-in for nvidia-smi that prints a row every
+    20 ms: start() returns once rows flow, and stop() summarises the rows
+    after begin() (clock median, max clock, throttle reasons seen)."""
+    sys.path.insert(0, ROOT)
+    import time
+
+    import bench
+
+    fake = tmp_path / "fake-smi"
+    fake.write_text(f"#!{sys.executable}\n"
+                    "import time\n"
+                    "i = 0\n"
+                    "while True:\n"
+                    "    cap = 'Active' if i >= 8 else 'Not Active'\n"
+                    "    print(f'{1800 + 100 * (i % 3)}, 2070, 900.5, 0x0, Not Active, Not Active, Not Active, {cap}',"
+                    " flush=True)\n"
+                    "    i += 1\n"
+                    "    time.sleep(0.02)\n")
+    fake.chmod(0o755)
+    s = bench.ClockSampler(0, interval_ms=20, cmd=str(fake))
+    s.start()
+    assert s.rows and s.mark == len(s.rows)
+    s.begin()
+    time.sleep(0.4)
+    out = s.stop()
+    assert out["samples"] >= 5 and out["interval_ms"] == 20
+    assert out["sm_max_mhz"] == 2070.0 and 1800.0 <= out["sm_mhz"] <= 2000.0
+    assert out["reasons"] == ["sw_power_cap"]
+    missing = bench.ClockSampler(0, cmd=str(tmp_path / "absent"))
+    missing.start()
+    assert missing.stop()["reasons"] == ["nvidia-smi unavailable"]
+
+
+def test_clock_sampler_falls_back_to_200_ms(tmp_path):
+    """A tool that refuses the short interval (exits without output) is
+    started again at 200 ms."""
+    sys.path.insert(0, ROOT)
+    import time
+
+    import bench
+
+    fake = tmp_path / "picky-smi"
+    fake.write_text(f"#!{sys.executable}\n"
+                    "import sys, time\n"
+                    "if sys.argv[sys.argv.index('-lms') + 1] != '200':\n"
+                    "    sys.exit(2)\n"
+                    "while True:\n"
+                    "    print('2070, 2070, 800.0, 0x0, Not Active, Not Active, Not Active, Not Active', flush=True)\n"
+                    "    time.sleep(0.2)\n")
+    fake.chmod(0o755)
+    s = bench.ClockSampler(0, interval_ms=50, cmd=str(fake))
+    s.start()
+    s.begin()
+    time.sleep(0.5)
+    out = s.stop()
+    assert out["interval_ms"] == 200 and out["samples"] >= 1 and out["sm_mhz"] == 2070.0 and out["reasons"] == []
