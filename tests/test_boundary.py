@@ -8,6 +8,7 @@
 * without a device the solve fails loudly (no CPU fallback).
 """
 import ctypes as C
+import glob
 import os
 import re
 import subprocess
@@ -88,3 +89,17 @@ def test_no_device_fails_loudly():
     code, msg = hs.last_error()
     assert hs.ERR_NAMES[code] == "no_device", msg
     assert not x.any()  # nothing computed on the host
+
+
+@pytest.mark.parametrize("lang", ["c99", "c++17"])
+def test_public_headers_compile_alone(tmp_path, lang):
+    """Every header under include/ compiles on its own and together, warning
+    free, as C99 (the reference's dialect) and as C++17."""
+    heads = sorted(os.path.basename(h) for h in glob.glob(os.path.join(ROOT, "include", "*.h")))
+    for group in [[h] for h in heads] + [heads]:
+        ext, cc = (".c", "gcc") if lang == "c99" else (".cpp", "g++")
+        src = tmp_path / ("t" + ext)
+        src.write_text("".join(f'#include "{h}"\n' for h in group) + "int main(void) { return 0; }\n")
+        r = subprocess.run([cc, f"-std={lang}", "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+                            "-I", os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, (group, r.stderr)
