@@ -856,7 +856,8 @@ static int rows_full_band(const band_scan *S, int r0, int r1)
     const int n = S->n, ku = S->ku, kl = S->kl;
     const spk_v4i step = {8, 8, 8, 8};
     for (int r = r0; r < r1; r++) {
-        const int c0 = r - kl < 0 ? 0 : r - kl, c1 = r + ku > n - 1 ? n - 1 : r + ku, len = c1 - c0 + 1;
+        const long long lo = (long long)r - kl, hi = (long long)r + ku; /* any ku, kl: no int overflow */
+        const int c0 = lo < 0 ? 0 : (int)lo, c1 = hi > n - 1 ? n - 1 : (int)hi, len = c1 - c0 + 1;
         const long long t0 = S->rowptr[r], t1 = S->rowptr[r + 1];
         if (t0 < 0 || t1 > S->nnz || t1 - t0 != (long long)len) return 0;
         const int *ci = S->colind + t0;

@@ -78,6 +78,10 @@ def test_empty_and_diagonal_and_bad_arguments():
     assert hs.csr_full_band(np.zeros(1, np.int32), np.zeros(0, np.int32), 0, 0)
     assert hs.csr_full_band(np.arange(4, dtype=np.int32), np.arange(3, dtype=np.int32), 0, 0)
     assert not hs.csr_full_band(np.arange(4, dtype=np.int32), np.array([0, 2, 1], np.int32), 0, 0)
+    # bandwidths past the matrix edge mean the edge (no overflow in r + ku)
+    rp, ci, _, _, _ = hs.gen_banded(6, 5, 5, 1.5, 3)
+    assert hs.csr_full_band(rp, ci, 2**31 - 1, 2**31 - 1)
+    assert hs.csr_full_band(rp, ci, 5, 100)
     with pytest.raises(hs.SpikeError) as e:
         hs.csr_full_band(np.arange(4, dtype=np.int32), np.arange(3, dtype=np.int32), -1, 0)
     assert e.value.name == "argument"
