@@ -31,6 +31,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "solves/s & HBM GB/s at resid≤1e-12, mixed vs plain FP64 on 1 GPU; p50/p99 ms"
 N, K_BAND, P, NRHS, DOM, SEED = 2_000_000, 64, 256, 1, 1.5, 2
+# the CPU arm's caps: one step is a full CPU solve of the workload
+REF_MAX_STEPS, REF_MAX_WARMUP = 20, 3
 WORKLOAD = (f"large-band real SPIKE: n={N:,} kl=ku={K_BAND} partitions={P} nrhs={NRHS} float64 CSR, "
             f"dominance {DOM}, off-diagonals U[-1,1], seed {SEED}")
 
@@ -129,11 +131,13 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------- CPU baseline
-def cpu_baseline(system=None, p=P):
+def cpu_baseline(system=None, p=P, keep_x=False):
     """Time the CPU oracle -- the restated reference path (oracle/spike_oracle.c:
     banded partial-pivoting LU per partition, reduced system on R's band,
     implicit retrieval), OpenMP over partitions on every host core -- on the
-    whole workload (one solve, a few seconds of wall time)."""
+    whole workload (one solve, a few seconds of wall time).  keep_x: the
+    oracle's solution rides along under "x" (the GPU results are compared
+    with it)."""
     import hspike_gb300 as hs
     from oracle import oracle
 
@@ -146,11 +150,25 @@ def cpu_baseline(system=None, p=P):
     x = oracle.spike(rp, ci, a, b, p=p)
     dt = time.perf_counter() - t0
     rel = float(oracle.residual(rp, ci, a, x, b).max())
-    return {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": (f"one full solve of the workload by oracle/spike_oracle.c (restated reference SPIKE, "
-                       f"banded partial-pivoting LU inner solver, {p} partitions) with {cores} OpenMP threads: "
-                       f"{dt:.2f} s, relres {rel:.1e}"),
-            "seconds": dt}
+    out = {"value": 1.0 / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+           "sample": (f"one full solve of the workload by oracle/spike_oracle.c (restated reference SPIKE, "
+                      f"banded partial-pivoting LU inner solver, {p} partitions) with {cores} OpenMP threads: "
+                      f"{dt:.2f} s, relres {rel:.1e}"),
+           "seconds": dt}
+    if keep_x:
+        out["x"] = x
+    return out
+
+
+def measured_peaks():
+    """MEASURED_PEAKS.json (the machine's measured copy bandwidth and GEMM rates), or {}."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
+
+
+def relerr(x, ref):
+    x, ref = np.asarray(x), np.asarray(ref)
+    return float(np.linalg.norm(x - ref) / max(np.linalg.norm(ref), 1e-300))
 
 
 def cpu_one_core(n=N, p=P, parts=32):
@@ -193,17 +211,21 @@ def reference_arm(args):
     n, p = args.n, args.partitions
     rp, ci, a, xt, b = hs.gen_banded(n, K_BAND, K_BAND, DOM, SEED, nrhs=NRHS)
     runs = []
-    # each step is one full CPU solve (~2-3 s on 16 cores); cap the count so
-    # the whole reference run stays within a few minutes
-    steps = max(1, min(args.steps, 10))
-    for _ in range(min(args.warmup, 1)):
+    # each step is one full CPU solve (~2 s on 16 cores); the counts are capped
+    # so that the whole reference run stays within a few minutes, and the line
+    # reports the counts that actually ran
+    steps = max(1, min(args.steps, REF_MAX_STEPS))
+    warmup = max(0, min(args.warmup, REF_MAX_WARMUP))
+    for _ in range(warmup):
         cpu_baseline((rp, ci, a, b), p)
     for _ in range(steps):
         runs.append(cpu_baseline((rp, ci, a, b), p))
     vals = [r["value"] for r in runs]
     v = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+            "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+            "steps_requested": args.steps, "warmup_requested": args.warmup,
+            "timed_s": sum(r["seconds"] for r in runs),
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD if (n, p) == (N, P) else WORKLOAD.replace(f"n={N:,}", f"n={n:,}").replace(
                           f"partitions={P}", f"partitions={p}"), "note": "reference C code cannot be built here (MKL / SuperLU_MT "
@@ -247,6 +269,7 @@ def batched_leg(torch, dev, hs, count, steps, warmup, autotune=True):
     FP64, each with its autotuned schedule.  Device-resident inputs; each step
     is spike_batch_run (graph launch + convergence check)."""
     from hspike_gb300 import workloads as W
+    from oracle import oracle
 
     t0 = time.perf_counter()
     draws = W.batch_draws(count, seed=4)
@@ -284,18 +307,25 @@ def batched_leg(torch, dev, hs, count, steps, warmup, autotune=True):
         ms = ev[0].elapsed_time(ev[k]) / k
         inf = bt.info()
         rr = bt.relres()
-        # error against x_true on a sample of systems
-        errs = []
+        # error against x_true, and against the oracle (the restated reference
+        # path at its own default of 4 partitions), on a sample of systems
+        errs, oerrs = [], []
         for i in range(0, count, max(1, count // 64)):
             n, kk, nrhs, _ = draws[i]
             o = int(hb.v_off[i])
             x = t["x"][o:o + n * nrhs].cpu().numpy()
             xt = hb.x_true[o:o + n * nrhs]
-            errs.append(float(np.linalg.norm(x - xt) / np.linalg.norm(xt)))
+            errs.append(relerr(x, xt))
+            if name == "mixed":
+                rp_i, ci_i, a_i, _, b_i = hb.system(i)
+                xo = oracle.spike(rp_i, ci_i, a_i, b_i, p=4)
+                oerrs.append(relerr(x.reshape((n, nrhs), order="F"), xo))
         out[name] = {"value": count / (ms / 1000.0), "unit": "systems/s", "ms_per_step": ms,
                      "batches_per_s": 1000.0 / ms, "hbm_gbs": B / (ms / 1000.0) / 1e9,
                      "p50_ms": statistics.median(per), "p99_ms": float(np.percentile(per, 99)),
                      "relres_max": float(rr.max()), "err_vs_xtrue_max_sampled": max(errs),
+                     **({"err_vs_oracle_max_sampled": max(oerrs), "oracle_sampled_systems": len(oerrs)}
+                        if oerrs else {}),
                      "groups": inf.groups, "graph_kernel_launches": inf.graph_kernel_launches,
                      "graph_sweeps": inf.graph_sweeps, "extra_sweeps": inf.extra_sweeps,
                      "create_s": create_s, "tune_device_ms": inf.tune_ms,
@@ -317,14 +347,22 @@ def complex_leg(torch, dev, hs, steps, warmup, n=4_000_000, k=3, nrhs=4, p=512, 
     complex128, re/im off-diagonals U[-1,1], diagonal 1.2 x the row's |sum| x
     e^{i theta}, nrhs = 4, 512 partitions; complex64 factors + complex128
     refinement against plain complex128.  Device-resident inputs."""
+    from oracle import oracle
+
     rp, ci, a, xt, b = hs.gen_banded(n, k, k, dom, seed, complex_=True, nrhs=nrhs)
     nnz = len(ci)
     d_rp, d_ci, d_a = (torch.from_numpy(v).to(dev) for v in (rp, ci, a))
     d_b = torch.from_numpy(np.ascontiguousarray(b.T)).to(dev)
     stream = torch.cuda.current_stream(dev)
     B = 20 * nnz + 4 * (n + 1) + 32 * n * nrhs
+    hbm_peak = measured_peaks().get("hbm_gbs", 6800.0)
+    # the oracle's complex128 solve of the same system, same partitions
+    t0 = time.perf_counter()
+    xo = oracle.spike(rp, ci, a, b, p=p)
+    oracle_s = time.perf_counter() - t0
     out = {"workload": f"complex heptadiagonal: n={n:,} kl=ku={k} complex128, nrhs={nrhs}, {p} partitions, "
-                       f"dominance {dom} x |row sum| x e^(i theta), seed {seed}", "algorithmic_bytes": B}
+                       f"dominance {dom} x |row sum| x e^(i theta), seed {seed}", "algorithmic_bytes": B,
+           "hbm_peak_gbs": hbm_peak, "oracle_s": oracle_s}
     for name, prec in (("mixed", hs.SPIKE_PRECISION_MIXED), ("fp64", hs.SPIKE_PRECISION_FP64)):
         ctx = hs.Context()
         ctx.set_stream(stream.cuda_stream)
@@ -346,9 +384,9 @@ def complex_leg(torch, dev, hs, steps, warmup, n=4_000_000, k=3, nrhs=4, p=512, 
         x = d_x.cpu().numpy().T
         inf = ctx.info()
         out[name] = {"value": 1000.0 / ms, "unit": "solves/s", "ms_per_step": ms, "hbm_gbs": B / (ms / 1000) / 1e9,
-                     "hbm_frac": B / (ms / 1000) / 1e9 / 6662.6, "relres_max": inf.relres_max,
+                     "hbm_frac": B / (ms / 1000) / 1e9 / hbm_peak, "relres_max": inf.relres_max,
                      "refine_sweeps": inf.refine_sweeps, "block": inf.block,
-                     "err_vs_xtrue": float(np.linalg.norm(x - xt) / np.linalg.norm(xt))}
+                     "err_vs_xtrue": relerr(x, xt), "err_vs_oracle": relerr(x, xo)}
         ctx.close()
         del d_x
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
@@ -560,6 +598,14 @@ def main():
         dist.barrier()
         return 0
 
+    # the CPU oracle's solve of the same system with the same partitions: the
+    # CPU baseline's timing, and the reference every GPU result is held to
+    xo = cpu = None
+    if not args.skip_cpu and world == 1:
+        cpu = cpu_baseline((rp, ci, a, b), p, keep_x=True)
+        xo = cpu.pop("x")
+        out["err_vs_oracle"] = relerr(x, xo)
+
     if args.serve > 0 and not args.skip_extras:
         # first of the extra legs: its latencies depend on host threads and
         # device memory that the heavier legs below would leave in use
@@ -580,8 +626,7 @@ def main():
         for k in fams:
             fams[k]["share"] = ph[k][0] / tot
         dom = max(fams, key=lambda k: ph[k][0])
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        peaks = measured_peaks()
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         p32 = sgemm_tflops(torch, dev)
         KB = info.block
@@ -648,8 +693,12 @@ def main():
         d_x64 = torch.zeros_like(d_b)
         t64, per64, _, _ = timed(ctx64, 3, d_x64, d_b, NRHS, 1)
         i64 = ctx64.info()
+        x64 = d_x64.cpu().numpy().T
         out["fp64"] = {"value": 3 / (t64 / 1000.0), "unit": "solves/s", "ms_per_step": t64 / 3,
-                       "relres_max": i64.relres_max, "mixed_over_fp64": value / (3 / (t64 / 1000.0))}
+                       "relres_max": i64.relres_max, "mixed_over_fp64": value / (3 / (t64 / 1000.0)),
+                       "err_vs_xtrue": relerr(x64, xt)}
+        if xo is not None:
+            out["fp64"]["err_vs_oracle"] = relerr(x64, xo)
         ctx64.close()
         del d_x64
 
@@ -662,8 +711,11 @@ def main():
         x16 = d_x16.cpu().numpy().T
         out["nrhs16"] = {"value": 3 / (t16 / 1000.0), "unit": "solves/s", "ms_per_step": t16 / 3,
                          "hbm_gbs": alg_bytes(n, K_BAND, 16) / (t16 / 3000.0) / 1e9,
-                         "relres_max": ctx.info().relres_max,
-                         "err_vs_xtrue": float(np.linalg.norm(x16 - gen16[3]) / np.linalg.norm(gen16[3]))}
+                         "relres_max": ctx.info().relres_max, "err_vs_xtrue": relerr(x16, gen16[3])}
+        if not args.skip_cpu:
+            from oracle import oracle
+
+            out["nrhs16"]["err_vs_oracle"] = relerr(x16, oracle.spike(rp, ci, a, gen16[4], p=p))
         del d_b16, d_x16, gen16
 
     if args.batch > 0 and not args.skip_extras:
@@ -696,10 +748,12 @@ def main():
                       "d2h_bytes_per_step": int(xh.nbytes), "api": "dspike_core_host (pinned host buffers)",
                       "columns_implied": implied,
                       "host_threads": int(hs.get_option(hs.SPIKE_OPT_HOST_THREADS)),
-                      "err_vs_xtrue": float(np.linalg.norm(xh - xt) / np.linalg.norm(xt))}
+                      "err_vs_xtrue": relerr(xh, xt)}
+        if xo is not None:
+            out["e2e"]["err_vs_oracle"] = relerr(xh, xo)
 
-    if not args.skip_cpu and rank == 0 and world == 1:
-        out["cpu_baseline"] = cpu_baseline((rp, ci, a, b), p)
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
         try:  # a supplementary figure: its failure must not cost the line
             out["cpu_baseline"]["one_core"] = cpu_one_core(n, p)
         except Exception as e:  # noqa: BLE001

@@ -152,8 +152,8 @@ void spk_phase_destroy(spk_plan *P);
 
 /* ---- fixed workspace of the no-allocation solve (spike_noalloc.cu) ---- */
 #define SPK_NOALLOC_SCRATCH_BYTES (32u << 20) /* 32 MiB per device */
-/* device address of the fixed workspace on the current device (first call
- * per device resolves it with cudaGetSymbolAddress) */
+/* device address of the fixed workspace on the current device, resolved with
+ * cudaGetSymbolAddress on every call */
 int spk_noalloc_scratch(void **ptr, size_t *bytes);
 
 /* ---- device / memory (spike_util.cu) ---- */

@@ -117,22 +117,23 @@ Error_t spike_zsolve_device(spike_context_t ctx, integer_t n, integer_t nnz, int
                             complex16 *d_x, const complex16 *d_b);
 
 /* ---- solve without device allocation ----
- * No counterpart in the reference.  For callers that must not allocate device
- * memory while they solve: code running under CUDA stream capture (cudaMalloc
- * cannot be captured), latency-critical loops that cannot absorb the device
- * synchronisation of cudaMalloc/cudaFree, and programs whose pool allocator
- * owns the device heap.  Same meaning as spike_dsolve_device (device arrays,
- * mixed precision, FP64 refinement to 1e-12, automatic partitions), but every
- * temporary lives in one fixed workspace of SPIKE_NOALLOC_WORKSPACE_BYTES that
- * the library reserves on each device that loads it, for the life of the
- * process; no context is used and nothing is allocated, on the device or the
- * host.  Work runs on `cuda_stream` (NULL = the legacy default stream), and the
- * call returns after synchronising it.
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they solve: programs whose own pool allocator has taken the
+ * device heap (a library's cudaMalloc would fail or fragment it), latency-
+ * critical loops that cannot absorb the device-wide synchronisation of
+ * cudaFree, and plugin hosts that do not let a library allocate on their
+ * behalf.  Same meaning as spike_dsolve_device (device arrays, mixed precision,
+ * FP64 refinement to 1e-12, automatic partitions), but every temporary lives in
+ * one fixed workspace of SPIKE_NOALLOC_WORKSPACE_BYTES that the library keeps
+ * on each device that loads it, for the life of the process; no context is
+ * used and nothing is allocated, on the device or the host.  Work runs on
+ * `cuda_stream` (NULL = the legacy default stream); the call synchronises that
+ * stream (after the bandwidth analysis and after each residual) and returns
+ * when the solve is done.
  *   - A system whose workspace exceeds the fixed size (roughly n * max(ku,kl)
  *     past a few million, e.g. n = 100,000 with ku = kl = 8) is rejected with
- *     SPIKE_ERR_MEMORY before any work is queued.
- *   - The first call on a device resolves the workspace's device address; make
- *     that first call before any stream capture begins.
+ *     SPIKE_ERR_MEMORY once the bandwidth analysis -- the only work queued
+ *     before the check -- has fixed its tile size.
  *   - All calls on a device share the workspace and it keeps the previous
  *     call's contents (the solve clears what it needs cleared).  Calls whose
  *     GPU work overlaps -- from two host threads, or on two streams -- race on

@@ -1,8 +1,8 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
-Run once in a container where the reference tree is mounted:
+Run once in a container where the reference tree is mounted, giving its path:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout>
 
 It copies the reference's small binary CSR fixtures (Tests/*) byte for byte
 and transcribes the known answers its readme files record into
@@ -86,4 +86,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

@@ -24,6 +24,23 @@ def test_reference_arm_prints_its_line():
     assert "n=20,000" in line["config"]["workload"] and "partitions=8" in line["config"]["workload"]
 
 
+def test_reference_arm_reports_the_counts_it_ran():
+    """The line's steps and warmup are the solves actually timed and run
+    before them (requests above the caps are cut, and the line says so), and
+    steps x ms_per_step stays within the timed seconds it reports."""
+    import bench
+
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--n", "20000", "--partitions",
+           "8", "--steps", str(bench.REF_MAX_STEPS + 5), "--warmup", str(bench.REF_MAX_WARMUP + 2)]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["steps"] == bench.REF_MAX_STEPS and line["warmup"] == bench.REF_MAX_WARMUP
+    assert line["steps_requested"] == bench.REF_MAX_STEPS + 5
+    # the median step is at most the mean: K median steps fit in the timed total
+    assert line["steps"] * line["ms_per_step"] / 1000.0 <= line["timed_s"] * 1.5
+
+
 def _free_port():
     import socket
     with socket.socket() as s:

@@ -1,15 +1,18 @@
 """The solve that allocates nothing (spike_dsolve_device_noalloc), through the C ABI.
 
-Callers that cannot allocate device memory while they solve -- code under CUDA
-stream capture, latency-critical loops that cannot absorb the device-wide
-synchronisation of cudaMalloc/cudaFree, programs whose own pool owns the device
-heap -- get a solve whose temporaries all live in one fixed, per-device
-workspace that the library reserves when it loads.
+Some callers cannot allocate device memory while they solve: programs whose
+own pool allocator has taken the device heap, latency-critical loops that
+cannot absorb the device-wide synchronisation of cudaFree, plugin hosts that
+do not let a library allocate on their behalf.  They get a solve whose
+temporaries all live in one fixed, per-device workspace that the library keeps
+for the life of the process.  Each case here calls it twice in a row (two
+right-hand sides, so the second call runs on the first call's leftovers in the
+shared workspace) and compares it with the allocating entry point
+spike_dsolve_device, within the tolerance of the other GPU parity tests.
 
 This file is collected last on purpose: if it fails, a run that stops at the
 first failure has already run every other test.  It passes alone in a fresh
-process and after the other tests (the workspace is resolved on first use and
-the solve clears what it needs).
+process and after the other tests.
 """
 import ctypes as C
 
@@ -36,14 +39,20 @@ def _relerr(x, ref):
     return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
 
 
-def test_noalloc_matches_allocating_solve_twice_in_a_row():
+# (n, k, nrhs): 8-row tiles; 32- and 64-row tiles (two-sided-capable bands,
+# 64 partitions at most) that still fit the workspace; more right-hand sides
+# than one internal pass takes (64), so several passes share the workspace.
+CASES = [(20_000, 8, 2), (16_000, 24, 2), (4_000, 64, 3), (5_000, 8, 70)]
+
+
+@pytest.mark.parametrize("n,k,nrhs", CASES)
+def test_noalloc_matches_allocating_solve_twice_in_a_row(n, k, nrhs):
     torch = pytest.importorskip("torch")
     from oracle import oracle
 
     L = _lib()
     dev = torch.device("cuda:0")
-    n, k, nrhs = 20_000, 8, 2
-    rp, ci, a, xt, b = hs.gen_banded(n, k, k, 1.5, seed=4242, nrhs=nrhs)
+    rp, ci, a, xt, b = hs.gen_banded(n, k, k, 1.5, seed=4242 + k, nrhs=nrhs)
     t_rp, t_ci, t_a = (torch.from_numpy(v).to(dev) for v in (rp, ci, a))
     stream = torch.cuda.current_stream(dev)
 
