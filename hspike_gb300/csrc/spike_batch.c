@@ -275,6 +275,7 @@ static int read_worst(bgroup *G, double *worst, unsigned *err)
 
 static int dev_error(unsigned e)
 {
+    if (e & SPK_DEV_ERR_TIMEOUT) return SPK_ETIMEOUT;
     if (e & SPK_DEV_ERR_PIVOT) return SPK_EPIVOT;
     if (e & (SPK_DEV_ERR_BAND | SPK_DEV_ERR_CSR)) return SPK_ECSR;
     return SPK_OK;

@@ -614,6 +614,327 @@ template <class T, int KB> struct TwistFits {
     static constexpr bool ok = KB >= 16 && KB <= 64 && TL::INV_BUF <= TL::ELEMS && 4 * (smem + 1024) <= 228 * 1024;
 };
 
+// c ? a : b on two register values, in a form the compiler cannot turn into
+// a select of addresses (which would move a register array to local memory)
+__device__ __forceinline__ float reg_sel(bool c, float a, float b)
+{
+    float r;
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.s32 p, %3, 0;\n\tselp.f32 %0, %1, %2, p;\n\t}"
+        : "=f"(r)
+        : "f"(a), "f"(b), "r"((int)c));
+    return r;
+}
+
+// ------------------------------------------------------------ 8 x 8 sub-tiles
+// A 64 x 64 FP32 tile on 64 threads, each owning an 8 x 8 register sub-tile.
+// Per k step of a product a thread reads 8 elements of each operand (four
+// 16-byte shared loads, sixteen wavefronts per warp) for 64 FMAs: a warp's
+// shared-memory wavefronts then match what the FMA pipe retires (an SM
+// retires four warp FMAs per wavefront), where a 4 x 4 sub-tile issues two
+// wavefronts per four FMAs and caps the FMA pipe at half.
+//
+// Thread (tx, ty), tx, ty in 0..7: rows ty*8 .. ty*8+7 (contiguous) and the
+// columns of two 4-wide chunks, tx*4 .. tx*4+3 and 32 + tx*4 .. 32 + tx*4+3,
+// so the eight lanes of a quarter-warp (one ty, tx = 0..7) read 128
+// contiguous bytes of a right operand row (no bank conflict) and broadcast
+// one 32-byte piece of the transposed left operand.  A warp holds four
+// sub-tile rows (32 rows of the tile) and all 64 columns.
+template <class T, int KB> struct Tile88 {
+    static_assert(KB == 64, "8 x 8 sub-tiles on 64 threads: 64-row tiles");
+    static constexpr int TX = 8, TY = 8, TC = 8, TR = 8;
+    static constexpr int HALF = KB / 2; // column offset of the second chunk
+    static constexpr int LD = TileLD<T, KB>::value;
+    static constexpr int ELEMS = KB * LD;
+    static constexpr int ACTIVE = 64;
+    static constexpr int NT = 64;
+    static constexpr int INV_HALF = 12 * KB + 16;
+    static constexpr int INV_BUF = 2 * INV_HALF + KB;
+
+    using Reg = T[TR][TC];
+
+    int tx, ty;
+    int wr0, wr1, wc0, wc1;
+    bool act;
+    __device__ __forceinline__ Tile88(int tid)
+    {
+        const int warp = tid >> 5, lane = tid & 31;
+        act = tid < ACTIVE;
+        tx = lane & 7;
+        ty = warp * 4 + (lane >> 3);
+        wr0 = warp * 32;
+        wr1 = wr0 + 32;
+        wc0 = 0;
+        wc1 = KB;
+    }
+    __device__ __forceinline__ int row(int i) const { return ty * TR + i; }
+    __device__ __forceinline__ int col(int j) const { return (j >> 2) * HALF + tx * 4 + (j & 3); }
+
+    // the eight entries of sub-tile row i <-> two 4-wide chunks of a row at p (p = row start)
+    __device__ __forceinline__ void ld_row(T (&d)[TC], const T *p) const
+    {
+        T a[4], b[4];
+        vld<T, 4>(a, p + tx * 4);
+        vld<T, 4>(b, p + HALF + tx * 4);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            d[j] = a[j];
+            d[4 + j] = b[j];
+        }
+    }
+    __device__ __forceinline__ void st_row(T *p, const T (&d)[TC]) const
+    {
+        T a[4], b[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            a[j] = d[j];
+            b[j] = d[4 + j];
+        }
+        vst<T, 4>(p + tx * 4, a);
+        vst<T, 4>(p + HALF + tx * 4, b);
+    }
+
+    __device__ __forceinline__ void rzero(Reg &a) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++)
+#pragma unroll
+            for (int j = 0; j < TC; j++) a[i][j] = sc_zero<T>();
+    }
+    __device__ __forceinline__ void rload(Reg &a, const T *s) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++) ld_row(a[i], s + row(i) * LD);
+    }
+    __device__ __forceinline__ void rstore(T *s, const Reg &a) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++) st_row(s + row(i) * LD, a[i]);
+    }
+    // shared tile, transposed (element (r, c) at c*LD + r)
+    __device__ __forceinline__ void rstore_t(T *s, const Reg &a) const
+    {
+#pragma unroll
+        for (int j = 0; j < TC; j++) {
+            T c[TR];
+#pragma unroll
+            for (int i = 0; i < TR; i++) c[i] = a[i][j];
+            vst<T, TR>(s + col(j) * LD + row(0), c);
+        }
+    }
+    __device__ __forceinline__ void gload(Reg &a, const T *g) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++) ld_row(a[i], g + row(i) * KB);
+    }
+    __device__ __forceinline__ void gstore(T *g, const Reg &a) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++) st_row(g + row(i) * KB, a[i]);
+    }
+    __device__ __forceinline__ void gstore_t(T *g, const Reg &a) const
+    {
+#pragma unroll
+        for (int j = 0; j < TC; j++) {
+            T c[TR];
+#pragma unroll
+            for (int i = 0; i < TR; i++) c[i] = a[i][j];
+            vst<T, TR>(g + col(j) * KB + row(0), c);
+        }
+    }
+    // acc (+|-)= A B, A given transposed (At, column-major).  TRI as Tile::mm_tA:
+    // 1 / 2 = A upper / lower triangular (a warp skips the k where its rows of
+    // A are zero); 3 / 4 = B lower / upper triangular (a warp holds every
+    // column, so nothing is skipped).
+    template <bool SUB, int TRI = 0> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
+    {
+        const int k0 = TRI == 1 ? wr0 : 0;
+        const int k1 = TRI == 2 ? wr1 : KB;
+#pragma unroll 2
+        for (int k = k0; k < k1; k++) {
+            T a[TR], b[TC];
+            vld<T, TR>(a, At + k * LD + row(0));
+            ld_row(b, B + k * LD);
+#pragma unroll
+            for (int i = 0; i < TR; i++)
+#pragma unroll
+                for (int j = 0; j < TC; j++) acc[i][j] = SUB ? msub(acc[i][j], a[i], b[j]) : madd(acc[i][j], a[i], b[j]);
+        }
+    }
+    __device__ __forceinline__ void mma_t(Reg &acc, const T *At, const T *B) const { mm_tA<false>(acc, At, B); }
+    __device__ __forceinline__ void mms_t(Reg &acc, const T *At, const T *B) const { mm_tA<true>(acc, At, B); }
+    __device__ __forceinline__ void mma_tu(Reg &acc, const T *At, const T *B) const { mm_tA<false, 1>(acc, At, B); }
+    __device__ __forceinline__ void mms_tl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 2>(acc, At, B); }
+    __device__ __forceinline__ void mma_tl(Reg &acc, const T *At, const T *B) const { mm_tA<false, 2>(acc, At, B); }
+    __device__ __forceinline__ void mms_tu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 1>(acc, At, B); }
+    __device__ __forceinline__ void mms_t_bl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 3>(acc, At, B); }
+    __device__ __forceinline__ void mms_t_bu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 4>(acc, At, B); }
+
+    // In-place Gauss-Jordan inverse without pivoting, blocked by 4 x 4 pivot
+    // blocks: the update of Tile::inverse_b4 (S <- S - U'V', U' = pivot
+    // columns - I on the pivot rows, V' = P^{-1} (pivot rows + I on the pivot
+    // columns)) on this layout.  Pivot block q covers rows and columns
+    // 4q .. 4q+3: its rows are register rows 4 (q & 1) .. +3 of sub-tile row
+    // q / 2, its columns register columns 4 (q / 8) .. +3 of sub-tile column
+    // q & 7.  Rows are scaled to a unit diagonal first and the inverse's
+    // columns back after.  buf: INV_BUF elements of shared memory (16-byte
+    // aligned).  All threads must call; false in every thread on a zero or
+    // non-finite pivot.  The register offsets of each step are template
+    // arguments, so the sub-tile never leaves the registers.
+    __device__ __forceinline__ bool inverse(Reg &s, T *buf) const
+    {
+        bool ok = true;
+        T *dg = buf + 2 * INV_HALF; // the diagonal, KB entries
+        // diagonal entry (c, c), c = h*32 + tx*4 + j, sits in sub-tile row
+        // 4h + tx/2, register row 4 (tx & 1) + j, register column 4h + j
+        const bool odd = (tx & 1) != 0;
+#pragma unroll
+        for (int h = 0; h < 2; h++)
+            if (ty == 4 * h + (tx >> 1)) {
+                T d[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) d[j] = reg_sel(odd, s[4 + j][4 * h + j], s[j][4 * h + j]);
+                vst<T, 4>(dg + h * HALF + tx * 4, d);
+            }
+        __syncthreads();
+        {
+            T dr[TR];
+            vld<T, TR>(dr, dg + row(0));
+#pragma unroll
+            for (int i = 0; i < TR; i++) {
+                if (!sc_finite_nonzero(dr[i])) ok = false;
+                const T rr = sc_rcp_fast(dr[i]);
+#pragma unroll
+                for (int jj = 0; jj < TC; jj++) s[i][jj] = s[i][jj] * rr;
+            }
+        }
+        // q = 2 q2 + HQ; pivot columns in register columns 4..7 from q = 8 on
+        for (int q2 = 0; q2 < KB / 16; q2++) {
+            inv_step<false, 0>(s, buf, q2, ok);
+            inv_step<false, 1>(s, buf, q2, ok);
+        }
+        for (int q2 = KB / 16; q2 < KB / 8; q2++) {
+            inv_step<true, 0>(s, buf, q2, ok);
+            inv_step<true, 1>(s, buf, q2, ok);
+        }
+        // columns of the inverse back by the diagonal: S^{-1} = (D^{-1} S)^{-1} D^{-1}
+        {
+            T dc[TC];
+            ld_row(dc, dg);
+#pragma unroll
+            for (int jj = 0; jj < TC; jj++) {
+                const T rc = sc_rcp_fast(dc[jj]);
+#pragma unroll
+                for (int i = 0; i < TR; i++) s[i][jj] = s[i][jj] * rc;
+            }
+        }
+        __syncthreads();
+        return __syncthreads_and(ok ? 1 : 0) != 0;
+    }
+
+    // one 4 x 4 pivot block of inverse(): q = 2 q2 + HQ, its rows register
+    // rows 4 HQ .. 4 HQ + 3 of sub-tile row q2, its columns register columns
+    // (HI ? 4 : 0) .. +3 of sub-tile column q & 7.  The eight owners of the
+    // pivot rows are one quarter-warp: each takes the pivot block P from its
+    // owner by shuffles, inverts it (the same steps in all eight, no barrier)
+    // and forms its own columns of V' = P^{-1} (pivot rows + I); the owners of
+    // the pivot columns publish U'.  One barrier, then every thread applies
+    // S <- S - U' V' to its sub-tile.
+    template <bool HI, int HQ> __device__ __forceinline__ void inv_step(Reg &s, T *buf, int q2, bool &ok) const
+    {
+        constexpr int CO = HI ? 4 : 0, RO = 4 * HQ;
+        const int q = 2 * q2 + HQ;
+        T *cbuf = buf + HQ * INV_HALF; // [KB][4] pivot columns U'
+        T *vbuf = cbuf + 4 * KB;       // [4][KB] V'
+        const bool rown = ty == q2, cown = tx == (q & 7);
+        if (rown) {
+            const int lane = threadIdx.x & 31;
+            const unsigned qmask = 0xffu << (lane & 24);
+            const int src = (lane & 24) + (q & 7); // the pivot block's owner in this quarter-warp
+            T pinv[4][4];
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) pinv[a][b] = __shfl_sync(qmask, s[RO + a][CO + b], src);
+#pragma unroll
+            for (int k = 0; k < 4; k++) { // unblocked Gauss-Jordan in registers
+                const T piv = pinv[k][k];
+                if (!sc_finite_nonzero(piv)) ok = false;
+                const T pr = sc_rcp_fast(piv);
+#pragma unroll
+                for (int b = 0; b < 4; b++)
+                    if (b != k) pinv[k][b] = pinv[k][b] * pr;
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+                    if (a != k) {
+                        const T f = pinv[a][k];
+#pragma unroll
+                        for (int b = 0; b < 4; b++)
+                            if (b != k) pinv[a][b] = msub(pinv[a][b], f, pinv[k][b]);
+                        pinv[a][k] = -(f * pr);
+                    }
+                pinv[k][k] = pr;
+            }
+#pragma unroll
+            for (int tt = 0; tt < 4; tt++) {
+                T vrow[TC];
+#pragma unroll
+                for (int jj = 0; jj < TC; jj++) {
+                    T acc = sc_zero<T>();
+#pragma unroll
+                    for (int a = 0; a < 4; a++) {
+                        const T bb = (cown && jj == CO + a) ? s[RO + a][jj] + sc_one<T>() : s[RO + a][jj];
+                        acc = madd(acc, pinv[tt][a], bb);
+                    }
+                    vrow[jj] = acc;
+                }
+                st_row(vbuf + tt * KB, vrow);
+            }
+        }
+        if (cown) {
+#pragma unroll
+            for (int i = 0; i < TR; i++) {
+                T u[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++) u[t] = (rown && i == RO + t) ? s[i][CO + t] - sc_one<T>() : s[i][CO + t];
+                vst<T, 4>(cbuf + row(i) * 4, u);
+            }
+        }
+        __syncthreads();
+        T u[TR][4], v[4][TC];
+#pragma unroll
+        for (int i = 0; i < TR; i++) vld<T, 4>(u[i], cbuf + row(i) * 4);
+#pragma unroll
+        for (int t = 0; t < 4; t++) ld_row(v[t], vbuf + t * KB);
+#pragma unroll
+        for (int i = 0; i < TR; i++)
+#pragma unroll
+            for (int jj = 0; jj < TC; jj++) {
+                T acc = s[i][jj];
+#pragma unroll
+                for (int t = 0; t < 4; t++) acc = msub(acc, u[i][t], v[t][jj]);
+                s[i][jj] = acc;
+            }
+    }
+};
+
+// Thread counts and tile geometry of the two-sided kernels: FP32 64-row
+// tiles run on 64 threads with 8 x 8 sub-tiles (Tile88), everything else on
+// the Tile layouts above (NTOf threads for the kernels with a tile inverse,
+// TwNT for the product-only ones).
+template <class T, int KB> struct TwCfg {
+    static constexpr bool T88 = sizeof(T) == 4 && KB == 64 && TileLD<T, KB>::value == KB + 4;
+    static constexpr int NT_LU = T88 ? 64 : NTOf<KB>::value;
+    static constexpr int NT_PROD = T88 ? 64 : TwNT<KB>::value;
+};
+template <class T, int KB, bool T88 = TwCfg<T, KB>::T88> struct TwTiles {
+    using LU = Tile<T, KB, TwCfg<T, KB>::NT_LU>;
+    using PROD = Tile<T, KB, TwCfg<T, KB>::NT_PROD>;
+};
+template <class T, int KB> struct TwTiles<T, KB, true> {
+    using LU = Tile88<T, KB>;
+    using PROD = Tile88<T, KB>;
+};
+
 // Dense global tile (KB*KB elements, 16-byte aligned) -> shared tile with row
 // stride TileLD (the element order is kept: a column-major global tile lands
 // as a transposed shared tile).  Every thread issues all of its 16-byte loads
@@ -680,6 +1001,102 @@ template <int E> __device__ __forceinline__ void cp_async_elem(void *smem, const
     else
         cp_async4(smem, gmem);
 }
+// ------------------------------------------------------------ bulk copies (TMA) with mbarriers
+// A tile lands in shared memory by one bulk copy per row
+// (cp.async.bulk global -> shared, issued by one warp), each completing its
+// bytes on the tile's mbarrier; the threads that read the tile wait on the
+// barrier's phase.  Rows are KB * sizeof(T) >= 64 bytes and the shared rows
+// keep their 16-byte padding (TileLD), so both ends stay 16-byte aligned and
+// the padded layout (no bank conflicts) is unchanged.  The copies read this
+// GPU's own memory into the issuing CTA's shared memory only (no cluster, no
+// multicast).
+#define SPK_MBAR_SPIN_LIMIT (1 << 22)
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// make the initialised barriers visible to the copy engine's proxy
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// order this thread's earlier generic-proxy shared accesses before later bulk copies into them
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+    unsigned done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+// Wait for the phase of `bar` with parity `parity` to complete; gives up after
+// SPK_MBAR_SPIN_LIMIT polls (each poll may suspend the thread for a short,
+// hardware-chosen time) and returns false, so a copy that never lands ends in
+// an error status instead of a hang.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+{
+    for (int i = 0; i < SPK_MBAR_SPIN_LIMIT; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// Dense global tile (KB x KB, row-major or column-major as stored) -> shared
+// tile with row stride TileLD, by KB bulk copies on `bar`.  Called by all 32
+// lanes of one warp, after a barrier that ends every read of `s`.
+template <class T, int KB> __device__ __forceinline__ void bulk_tile(T *s, const T *g, uint64_t *bar)
+{
+    constexpr int LD = TileLD<T, KB>::value;
+    constexpr unsigned ROW = KB * sizeof(T);
+    static_assert(ROW % 16 == 0 && (LD * sizeof(T)) % 16 == 0, "bulk copies move 16-byte multiples");
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, ROW * KB);
+    }
+    __syncwarp();
+    for (int r = lane; r < KB; r += 32) bulk_g2s(s + r * LD, g + (size_t)r * KB, ROW, bar);
+}
+// One shared tile's barrier as every thread of the CTA tracks it: the parity
+// of its next phase and whether a copy is in flight.  All threads call
+// issue() (warp 0 issues the copies) and wait(), on uniform conditions.
+struct TileBar {
+    uint64_t *bar;
+    unsigned phase;
+    bool inflight;
+    template <class T, int KB> __device__ __forceinline__ void issue(T *s, const T *g)
+    {
+        if (threadIdx.x < 32) bulk_tile<T, KB>(s, g, bar);
+        inflight = true;
+    }
+    // wait for the tile in flight; false on a timeout
+    __device__ __forceinline__ bool wait()
+    {
+        const bool ok = mbar_wait(bar, phase);
+        phase ^= 1u;
+        inflight = false;
+        return ok;
+    }
+    // before leaving the kernel: let a copy still in flight land (bounded)
+    __device__ __forceinline__ void drain()
+    {
+        if (inflight) wait();
+    }
+};
+
 // ------------------------------------------------------------ tile rows across lanes
 // A chain of a small band (KB <= 4) runs on KB consecutive lanes of a warp:
 // lane r owns row r of every KB x KB tile, and rows of another lane arrive by

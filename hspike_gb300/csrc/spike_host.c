@@ -54,6 +54,8 @@ Error_t spk_fail_code(int code, const char *where)
     case SPK_EBAND: return spk_fail(SPIKE_ERR_BANDWIDTH, "%s: bandwidth not supported in this precision", where);
     case SPK_EPIVOT: return spk_fail(SPIKE_ERR_PIVOT, "%s: zero or non-finite pivot", where);
     case SPK_ECSR: return spk_fail(SPIKE_ERR_CSR, "%s: invalid CSR (row pointers, column range or ordering)", where);
+    case SPK_ETIMEOUT:
+        return spk_fail(SPIKE_ERR_CUDA, "%s: a kernel gave up waiting for a bulk copy into shared memory", where);
     default: return spk_fail(code, "%s: error %d", where, code);
     }
 }
@@ -548,6 +550,7 @@ static int check_device_error(spk_plan *P, void *stream, unsigned *e)
     e[0] = e[1] = e[2] = e[3] = 0;
     TRY(spk_memcpy_d2h(e, P->d_err, sizeof(unsigned) * 4, stream));
     TRY(spk_stream_sync(stream));
+    if (e[0] & SPK_DEV_ERR_TIMEOUT) return SPK_ETIMEOUT;
     if (e[0] & SPK_DEV_ERR_PIVOT) return SPK_EPIVOT;
     if (e[0] & (SPK_DEV_ERR_BAND | SPK_DEV_ERR_CSR)) return SPK_ECSR;
     return SPK_OK;

@@ -40,7 +40,8 @@ enum spk_err {
     SPK_EPIVOT = 6,     /* zero or non-finite pivot in a diagonal block */
     SPK_ECONV = 7,      /* refinement did not reach the tolerance */
     SPK_ENODEV = 8,     /* no CUDA device */
-    SPK_EHANDLE = 9     /* bad or released handle */
+    SPK_EHANDLE = 9,    /* bad or released handle */
+    SPK_ETIMEOUT = 10   /* a kernel gave up waiting for a bulk copy into shared memory */
 };
 
 /* kernel families timed by the phase timer */
@@ -62,6 +63,7 @@ enum spk_phase {
 #define SPK_DEV_ERR_PIVOT 1u
 #define SPK_DEV_ERR_BAND 2u
 #define SPK_DEV_ERR_CSR 4u
+#define SPK_DEV_ERR_TIMEOUT 8u /* a bounded wait on a bulk copy gave up; the kernel returned early */
 
 /* One system of a batch as the kernels see it.  A batch group lays its
  * systems end to end in one row space (system s owns rows [row0, row0 + n));

@@ -61,12 +61,33 @@ template <class TL, class Reg> __device__ __forceinline__ void rcopy(Reg &d, con
         for (int j = 0; j < TL::TC; j++) d[i][j] = s[i][j];
 }
 
+// Shared layout of the two-sided kernels: three tiles, then the mbarriers of
+// the tiles that arrive by bulk copies (TwistFits::smem keeps 64 bytes for the
+// 16-byte alignment and up to four barriers).
+template <class T, class TL> __device__ __forceinline__ uint64_t *tw_bars(char *smraw)
+{
+    return (uint64_t *)((T *)smem_align(smraw) + 3 * TL::ELEMS);
+}
+
+// A timed-out wait (a bulk copy that never landed) ends the kernel in every
+// thread at the barrier that follows it: the error word records it, and the
+// copies still in flight get their own bounded wait before the CTA leaves.
+__device__ __forceinline__ void tw_bail(unsigned *err, TileBar &a, TileBar &b)
+{
+    if (threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_TIMEOUT);
+    a.drain();
+    b.drain();
+}
+
+// The two elimination chains of each partition (blockIdx.y 0: top, 1: bottom).
+// The coupling tiles of the next block arrive by bulk copies while the
+// current block's inverse runs, and the next diagonal block by register loads
+// issued at the same point, so no step waits on memory.
 template <class T, int KB>
-__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+__global__ void __launch_bounds__(TwCfg<T, KB>::NT_LU, 4)
     k_tw_lu(const T *__restrict__ gT, const int *__restrict__ blk_off, T *gL, T *gG, T *gE, unsigned *err, int part0)
 {
-    constexpr int NT = NTOf<KB>::value;
-    using TL = Tile<T, KB, NT>;
+    using TL = typename TwTiles<T, KB>::LU;
     constexpr size_t TS = (size_t)KB * KB;
     const int part = blockIdx.x + part0;
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
@@ -75,36 +96,46 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
 
     extern __shared__ char smraw[];
     T *s0 = (T *)smem_align(smraw), *s1 = s0 + TL::ELEMS, *s2 = s1 + TL::ELEMS;
+    uint64_t *bars = tw_bars<T, TL>(smraw);
     T *buf = s0; // the inverse's scratch: G_{J-1} / H_{J+1} are consumed before it starts
     TL t(threadIdx.x);
     typename TL::Reg acc, dreg;
-    bool ok = true;
+    bool ok = true, tmo = false;
+    if (threadIdx.x == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    TileBar b1{bars, 0u, false}, b2{bars + 1, 0u, false}; // tiles s1, s2
 
     if (blockIdx.y == 0) {
         // top chain, J = 0..M-1 (M >= 4)
         T *sG = s0, *sE = s1, *sF = s2;
-        cp_async_tile<T, KB, NT>(sE, gTp + 2 * TS);  // A(0,1), row-major
-        cp_async_tile<T, KB, NT>(sF, gTp + 4 * TS);  // A(1,0), column-major
-        cp_async_commit();
-        t.gload(acc, gTp); // S_0 = D_0
+        b1.issue<T, KB>(sE, gTp + 2 * TS); // A(0,1), row-major
+        b2.issue<T, KB>(sF, gTp + 4 * TS); // A(1,0), column-major
+        t.gload(acc, gTp);                 // S_0 = D_0
+        t.gload(dreg, gTp + 3 * TS);       // D_1
         for (int J = 0; J < M; J++) {
             if (J > 0) {
-                t.gload(dreg, gTp + (size_t)J * 3 * TS); // D_J, lands during the L product
+                tmo |= !b2.wait();
                 t.rzero(acc);
                 t.mma_tu(acc, sF, sG); // L_J; A(J,J-1) is upper triangular
-                __syncthreads();
+                if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 t.rstore_t(sF, acc);
                 t.gstore_t(gL + tb + J * TS, acc);
-                __syncthreads();
+                tmo |= !b1.wait();
+                if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 rcopy<TL>(acc, dreg);
                 t.mms_t_bl(acc, sF, sE); // S_J = D_J - L_J A(J-1,J); A(J-1,J) is lower triangular
                 __syncthreads();
-                cp_async_tile<T, KB, NT>(sE, gTp + (size_t)J * 3 * TS + 2 * TS);
-                if (J + 1 < M) cp_async_tile<T, KB, NT>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);
-                cp_async_commit();
+                if (J + 1 < M) {
+                    b1.issue<T, KB>(sE, gTp + (size_t)J * 3 * TS + 2 * TS);
+                    b2.issue<T, KB>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);
+                    t.gload(dreg, gTp + (size_t)(J + 1) * 3 * TS); // D_{J+1}, lands during the inverse
+                }
             }
             ok = t.inverse(acc, buf) && ok;
-            cp_async_wait_all();
             t.rstore(sG, acc);
             t.gstore_t(gG + tb + J * TS, acc);
             __syncthreads();
@@ -112,19 +143,20 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
     } else {
         // bottom chain, J = N-1..M+1, then U_M and T'_M
         T *sH = s0, *sY = s1, *sX = s2;
-        cp_async_tile<T, KB, NT>(sY, gTp + (size_t)(N - 2) * 3 * TS + 2 * TS); // A(N-2,N-1), column-major
-        cp_async_tile<T, KB, NT>(sX, gTp + (size_t)(N - 1) * 3 * TS + TS);     // A(N-1,N-2), row-major
-        cp_async_commit();
-        t.gload(acc, gTp + (size_t)(N - 1) * 3 * TS); // T_{N-1} = D_{N-1}
+        b1.issue<T, KB>(sY, gTp + (size_t)(N - 2) * 3 * TS + 2 * TS); // A(N-2,N-1), column-major
+        b2.issue<T, KB>(sX, gTp + (size_t)(N - 1) * 3 * TS + TS);     // A(N-1,N-2), row-major
+        t.gload(acc, gTp + (size_t)(N - 1) * 3 * TS);                   // T_{N-1} = D_{N-1}
+        t.gload(dreg, gTp + (size_t)(N - 2) * 3 * TS);                  // D_{N-2}
         for (int J = N - 1; J >= M; J--) {
             if (J < N - 1) {
-                t.gload(dreg, gTp + (size_t)J * 3 * TS);
+                tmo |= !b1.wait();
                 t.rzero(acc);
                 t.mma_tl(acc, sY, sH); // U_J = A(J,J+1) H_{J+1}; A(J,J+1) is lower triangular
-                __syncthreads();
+                if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 t.rstore_t(sY, acc);
                 t.gstore_t((J == M ? gE : gL) + tb + J * TS, acc);
-                __syncthreads();
+                tmo |= !b2.wait();
+                if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 rcopy<TL>(acc, dreg);
                 t.mms_t_bu(acc, sY, sX); // T_J = D_J - U_J A(J+1,J); A(J+1,J) is upper triangular
                 if (J == M) {
@@ -132,17 +164,18 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
                     break;
                 }
                 __syncthreads();
-                cp_async_tile<T, KB, NT>(sY, gTp + (size_t)(J - 1) * 3 * TS + 2 * TS);
-                cp_async_tile<T, KB, NT>(sX, gTp + (size_t)J * 3 * TS + TS);
-                cp_async_commit();
+                b1.issue<T, KB>(sY, gTp + (size_t)(J - 1) * 3 * TS + 2 * TS);
+                b2.issue<T, KB>(sX, gTp + (size_t)J * 3 * TS + TS);
+                t.gload(dreg, gTp + (size_t)(J - 1) * 3 * TS); // D_{J-1}
             }
             ok = t.inverse(acc, buf) && ok;
-            cp_async_wait_all();
             t.rstore(sH, acc);
             t.gstore_t(gG + tb + J * TS, acc);
             __syncthreads();
         }
     }
+    b1.drain();
+    b2.drain();
     if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
 }
 
@@ -168,13 +201,15 @@ __device__ __forceinline__ void bhat_block(const TL &t, typename TL::Reg &a, con
         }
 }
 
+// The spikes' forward sweeps.  The factor tiles of consecutive blocks
+// alternate between two shared buffers (sA: even J, sB: odd J), each filled by
+// bulk copies one block ahead; the parity of a buffer's phase follows from J.
 template <class T, int KB>
-__global__ void __launch_bounds__(TwNT<KB>::value, 4)
+__global__ void __launch_bounds__(TwCfg<T, KB>::NT_PROD, 4)
     k_tw_sweep(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p, const T *__restrict__ gL,
-               const T *__restrict__ gE, const T *__restrict__ gBhat, T *gV, T *gW, int part0)
+               const T *__restrict__ gE, const T *__restrict__ gBhat, T *gV, T *gW, int part0, unsigned *err)
 {
-    constexpr int NT = TwNT<KB>::value;
-    using TL = Tile<T, KB, NT>;
+    using TL = typename TwTiles<T, KB>::PROD;
     constexpr size_t TS = (size_t)KB * KB;
     const int part = blockIdx.x + part0;
     const bool top = blockIdx.y == 0;
@@ -184,26 +219,41 @@ __global__ void __launch_bounds__(TwNT<KB>::value, 4)
 
     extern __shared__ char smraw[];
     T *sZ = (T *)smem_align(smraw), *sA = sZ + TL::ELEMS, *sB = sA + TL::ELEMS;
+    uint64_t *bars = tw_bars<T, TL>(smraw); // [0] sA, [1] sB, [2] sZ
     TL t(threadIdx.x);
     typename TL::Reg acc;
+    if (threadIdx.x == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init(bars + 2, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    bool tmo = false;
+    // ring buffer of block J and the parity of its wait for block J
+    auto ring = [&](int J) { return (J & 1) ? sB : sA; };
+    auto issue = [&](int J, const T *g) {
+        if (threadIdx.x < 32) bulk_tile<T, KB>(ring(J), g, bars + (J & 1));
+    };
+    auto bail = [&](int Jn, unsigned ph) { // a copy for block Jn may be in flight
+        if (threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_TIMEOUT);
+        if (Jn >= 0) mbar_wait(bars + (Jn & 1), ph);
+    };
 
     if (top) {
         // W: z_0 = C^ (gW tile 0, from k_band_tiles), z_J = -L_J z_{J-1}, J = 1..M-1
-        cp_async_tile<T, KB, NT>(sZ, gW + tb);
-        cp_async_tile<T, KB, NT>(sB, gL + tb + TS);
-        cp_async_commit();
-        cp_async_wait_all();
-        __syncthreads();
+        if (threadIdx.x < 32) bulk_tile<T, KB>(sZ, gW + tb, bars + 2);
+        issue(1, gL + tb + TS);
+        tmo |= !mbar_wait(bars + 2, 0);
         for (int J = 1; J < M; J++) {
-            T *cur = (J & 1) ? sB : sA, *nxt = (J & 1) ? sA : sB;
-            if (J + 1 < M) cp_async_tile<T, KB, NT>(nxt, gL + tb + (size_t)(J + 1) * TS);
-            cp_async_commit();
+            const bool more = J + 1 < M;
+            if (more) issue(J + 1, gL + tb + (size_t)(J + 1) * TS);
+            tmo |= !mbar_wait(bars + (J & 1), ((J - 1) >> 1) & 1);
             t.rzero(acc);
-            t.mms_t(acc, cur, sZ);
-            __syncthreads();
+            t.mms_t(acc, ring(J), sZ);
+            if (__syncthreads_or(tmo)) return bail(more ? J + 1 : -1, (J >> 1) & 1);
             t.rstore(sZ, acc);
             t.gstore(gW + tb + J * TS, acc);
-            cp_async_wait_all();
             __syncthreads();
         }
     } else {
@@ -212,35 +262,33 @@ __global__ void __launch_bounds__(TwNT<KB>::value, 4)
         const int J0 = (m - KB) / KB, o = (m - KB) - J0 * KB; // m >= 8 KB: o >= 0, J0 > M
         const T *bh = gBhat + (size_t)part * TS;
         auto utile = [&](int J) { return (J == M ? gE : gL) + tb + (size_t)J * TS; };
-        cp_async_tile<T, KB, NT>(((N - 2) & 1) ? sB : sA, utile(N - 2));
-        cp_async_commit();
+        auto phase = [&](int J) { return (unsigned)(((N - 2 - J) >> 1) & 1); };
+        issue(N - 2, utile(N - 2));
         bhat_block<T, KB>(t, acc, bh, N - 1, J0, o);
         t.rstore(sZ, acc);
         t.gstore(gV + tb + (size_t)(N - 1) * TS, acc);
-        cp_async_wait_all();
         __syncthreads();
         for (int J = N - 2; J >= M; J--) {
-            T *cur = (J & 1) ? sB : sA, *nxt = (J & 1) ? sA : sB;
-            if (J - 1 >= M) cp_async_tile<T, KB, NT>(nxt, utile(J - 1));
-            cp_async_commit();
+            const bool more = J - 1 >= M;
+            if (more) issue(J - 1, utile(J - 1));
             bhat_block<T, KB>(t, acc, bh, J, J0, o);
-            t.mms_t(acc, cur, sZ);
-            __syncthreads();
+            tmo |= !mbar_wait(bars + (J & 1), phase(J));
+            t.mms_t(acc, ring(J), sZ);
+            if (__syncthreads_or(tmo)) return bail(more ? J - 1 : -1, phase(J - 1));
             t.rstore(sZ, acc);
             t.gstore(gV + tb + J * TS, acc);
-            cp_async_wait_all();
             __syncthreads();
         }
     }
 }
 
 template <class T, int KB>
-__global__ void __launch_bounds__(NTOf<KB>::value, 4)
+__global__ void __launch_bounds__(TwCfg<T, KB>::NT_LU, 4)
     k_tw_merge(const T *__restrict__ gT, const int *__restrict__ blk_off, int p, T *gL, T *gG, T *gV, T *gW,
                unsigned *err, int part0)
 {
-    constexpr int NT = NTOf<KB>::value;
-    using TL = Tile<T, KB, NT>;
+    constexpr int NT = TwCfg<T, KB>::NT_LU;
+    using TL = typename TwTiles<T, KB>::LU;
     constexpr size_t TS = (size_t)KB * KB;
     const int part = blockIdx.x + part0;
     const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
@@ -307,12 +355,12 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
 // Z_J is the forward sweep where the spike has one (W's top half, V's bottom
 // half), else zero.
 template <class T, int KB>
-__global__ void __launch_bounds__(TwNT<KB>::value, 4)
+__global__ void __launch_bounds__(TwCfg<T, KB>::NT_PROD, 4)
     k_tw_bwd(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE, T *gV,
-             T *gW, int part0)
+             T *gW, int part0, unsigned *err)
 {
-    constexpr int NT = TwNT<KB>::value;
-    using TL = Tile<T, KB, NT>;
+    constexpr int NT = TwCfg<T, KB>::NT_PROD;
+    using TL = typename TwTiles<T, KB>::PROD;
     constexpr size_t TS = (size_t)KB * KB;
     const int part = blockIdx.x + part0, which = blockIdx.y;
     const bool isV = which >= 2, top = (which & 1) == 0;
@@ -325,47 +373,53 @@ __global__ void __launch_bounds__(TwNT<KB>::value, 4)
 
     extern __shared__ char smraw[];
     T *sG = (T *)smem_align(smraw), *sE = sG + TL::ELEMS, *sX = sE + TL::ELEMS;
+    uint64_t *bars = tw_bars<T, TL>(smraw);
     TL t(threadIdx.x);
-    typename TL::Reg acc;
+    typename TL::Reg acc, zreg;
+    if (threadIdx.x == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    TileBar bG{bars, 0u, false}, bE{bars + 1, 0u, false};
+    bool tmo = false;
 
     const int J1 = top ? M - 1 : M + 1;
-    cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)J1 * TS);
-    cp_async_tile<T, KB, NT>(sE, gE + tb + (size_t)J1 * TS);
-    cp_async_commit();
+    bG.issue<T, KB>(sG, gG + tb + (size_t)J1 * TS);
+    bE.issue<T, KB>(sE, gE + tb + (size_t)J1 * TS);
+    if (hasZ) t.gload(zreg, gX + tb + (size_t)J1 * TS); // Z_J of the first step
     load_tile_tr<T, KB, NT>(sX, gX + tb + (size_t)M * TS); // X_M, row-major
-    cp_async_wait_all();
     __syncthreads();
     for (int i = 0; i < cnt; i++) {
         const int J = top ? M - 1 - i : M + 1 + i;
         const int Jn = top ? J - 1 : J + 1;
         const bool more = i + 1 < cnt;
         if (hasZ)
-            t.gload(acc, gX + tb + (size_t)J * TS);
+            rcopy<TL>(acc, zreg);
         else
             t.rzero(acc);
+        tmo |= !bE.wait();
         if (top)
             t.mms_tl(acc, sE, sX); // A(J,J+1) lower triangular
         else
             t.mms_tu(acc, sE, sX); // A(J,J-1) upper triangular
-        __syncthreads();
-        if (more) {
-            cp_async_tile<T, KB, NT>(sE, gE + tb + (size_t)Jn * TS);
-            cp_async_commit();
-        }
+        if (__syncthreads_or(tmo)) return tw_bail(err, bG, bE);
+        if (more) bE.issue<T, KB>(sE, gE + tb + (size_t)Jn * TS);
         t.rstore(sX, acc);
-        __syncthreads();
+        if (hasZ && more) t.gload(zreg, gX + tb + (size_t)Jn * TS); // Z of the next step, lands meanwhile
+        tmo |= !bG.wait();
+        if (__syncthreads_or(tmo)) return tw_bail(err, bG, bE);
         t.rzero(acc);
         t.mma_t(acc, sG, sX);
         __syncthreads();
-        if (more) {
-            cp_async_tile<T, KB, NT>(sG, gG + tb + (size_t)Jn * TS);
-            cp_async_commit();
-        }
+        if (more) bG.issue<T, KB>(sG, gG + tb + (size_t)Jn * TS);
         t.rstore(sX, acc);
         t.gstore_t(gX + tb + (size_t)J * TS, acc);
-        cp_async_wait_all();
         __syncthreads();
     }
+    bG.drain();
+    bE.drain();
 }
 
 // ------------------------------------------------------------ small bands
@@ -606,7 +660,7 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
         return SPK_EBAND;
     } else {
         using C = TwistFits<T, KB>;
-        constexpr int NT = TwNT<KB>::value;
+        constexpr int NT = TwCfg<T, KB>::NT_PROD, NT_LU = TwCfg<T, KB>::NT_LU;
         static bool attr = false;
         if (!attr) {
             if (cudaFuncSetAttribute(k_tw_lu<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem) !=
@@ -623,7 +677,7 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
         const int p = P->p, np = part1 - part0;
         if (np <= 0) return SPK_OK;
         if (fwd) {
-            k_tw_lu<T, KB><<<dim3(np, 2), NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+            k_tw_lu<T, KB><<<dim3(np, 2), NT_LU, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
                                                                            (T *)P->d_G, (T *)P->d_E, P->d_err, part0);
             SPK_CHECK_LAUNCH();
             P->launches++;
@@ -631,18 +685,18 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
                 k_tw_sweep<T, KB><<<dim3(np, 2), NT, C::smem, st>>>(P->d_part_start, P->d_blk_off, p,
                                                                     (const T *)P->d_L, (const T *)P->d_E,
                                                                     (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W,
-                                                                    part0);
+                                                                    part0, P->d_err);
                 SPK_CHECK_LAUNCH();
                 P->launches++;
             }
-            k_tw_merge<T, KB><<<np, NTOf<KB>::value, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
+            k_tw_merge<T, KB><<<np, NT_LU, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, p, (T *)P->d_L,
                                                                     (T *)P->d_G, (T *)P->d_V, (T *)P->d_W, P->d_err,
                                                                     part0);
             SPK_CHECK_LAUNCH();
             P->launches++;
         } else if (p > 1) {
             k_tw_bwd<T, KB><<<dim3(np, 4), NT, C::smem, st>>>(P->d_blk_off, p, (const T *)P->d_G, (const T *)P->d_E,
-                                                              (T *)P->d_V, (T *)P->d_W, part0);
+                                                              (T *)P->d_V, (T *)P->d_W, part0, P->d_err);
             SPK_CHECK_LAUNCH();
             P->launches++;
         }

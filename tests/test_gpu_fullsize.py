@@ -63,7 +63,10 @@ def test_large_band_device_arrays(large_band, precision):
     x = _device_solve(torch, ctx, rp, ci, a, b)
     info = ctx.info()
     ctx.close()
-    assert info.partitions == p and info.block == 64 and info.twisted == 1
+    assert info.partitions == p and info.block == 64
+    # FP32 64-row tiles are eliminated from both ends; FP64 ones (three of
+    # them do not fit four CTAs' shared memory) top-down
+    assert info.twisted == (precision == hs.SPIKE_PRECISION_MIXED)
     assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
     assert relerr(x, xo) <= ERR_TOL, relerr(x, xo)
     assert relerr(xo, xt) <= 1e-10  # the oracle itself reaches x_true
