@@ -339,8 +339,11 @@ template <class T, int KB, int NT> struct Tile {
     // TRI = 1: A is upper triangular, 2: A lower triangular, 3: B lower
     // triangular, 4: B upper triangular -- the k range where the warp's rows
     // of A (columns of B) are zero is skipped (warp-uniform bounds, so only
-    // exact zeros are left out and the result is unchanged).
-    template <bool SUB, int TRI = 0> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
+    // exact zeros are left out and the result is unchanged).  LDA / LDB: row
+    // strides of the two shared operands (LD for a padded tile, KB for a dense
+    // one that arrived by a single bulk copy).
+    template <bool SUB, int TRI = 0, int LDA = LD, int LDB = LD>
+    __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
     {
         if (!act) return;
         const int k0 = TRI == 1 ? wr0 : TRI == 3 ? wc0 : 0;
@@ -348,8 +351,8 @@ template <class T, int KB, int NT> struct Tile {
 #pragma unroll 4
         for (int k = k0; k < k1; k++) {
             T a[TR], b[TC];
-            vld<T, TR>(a, At + k * LD + row(0));
-            vld<T, TC>(b, B + k * LD + col(0));
+            vld<T, TR>(a, At + k * LDA + row(0));
+            vld<T, TC>(b, B + k * LDB + col(0));
 #pragma unroll
             for (int i = 0; i < TR; i++)
 #pragma unroll
@@ -358,17 +361,43 @@ template <class T, int KB, int NT> struct Tile {
     }
     __device__ __forceinline__ void mma(Reg &acc, const T *A, const T *B) const { mm_rowA<false>(acc, A, B); }
     __device__ __forceinline__ void mms(Reg &acc, const T *A, const T *B) const { mm_rowA<true>(acc, A, B); }
-    __device__ __forceinline__ void mma_t(Reg &acc, const T *At, const T *B) const { mm_tA<false>(acc, At, B); }
-    __device__ __forceinline__ void mms_t(Reg &acc, const T *At, const T *B) const { mm_tA<true>(acc, At, B); }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mma_t(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<false, 0, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mms_t(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 0, LDA, LDB>(acc, At, B);
+    }
     // A upper triangular (acc += A B) / lower triangular (acc -= A B)
-    __device__ __forceinline__ void mma_tu(Reg &acc, const T *At, const T *B) const { mm_tA<false, 1>(acc, At, B); }
-    __device__ __forceinline__ void mms_tl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 2>(acc, At, B); }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mma_tu(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<false, 1, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mms_tl(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 2, LDA, LDB>(acc, At, B);
+    }
     // A lower triangular (acc += A B) / upper triangular (acc -= A B)
-    __device__ __forceinline__ void mma_tl(Reg &acc, const T *At, const T *B) const { mm_tA<false, 2>(acc, At, B); }
-    __device__ __forceinline__ void mms_tu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 1>(acc, At, B); }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mma_tl(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<false, 2, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mms_tu(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 1, LDA, LDB>(acc, At, B);
+    }
     // acc -= A B with B lower / upper triangular
-    __device__ __forceinline__ void mms_t_bl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 3>(acc, At, B); }
-    __device__ __forceinline__ void mms_t_bu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 4>(acc, At, B); }
+    template <int LDA = LD, int LDB = LD>
+    __device__ __forceinline__ void mms_t_bl(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 3, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD>
+    __device__ __forceinline__ void mms_t_bu(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 4, LDA, LDB>(acc, At, B);
+    }
 
     // In-place Gauss-Jordan inverse of the register tile, no pivoting (the
     // diagonal blocks of a diagonally dominant A stay diagonally dominant
@@ -744,30 +773,58 @@ template <class T, int KB> struct Tile88 {
     // acc (+|-)= A B, A given transposed (At, column-major).  TRI as Tile::mm_tA:
     // 1 / 2 = A upper / lower triangular (a warp skips the k where its rows of
     // A are zero); 3 / 4 = B lower / upper triangular (a warp holds every
-    // column, so nothing is skipped).
-    template <bool SUB, int TRI = 0> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
+    // column, so nothing is skipped).  LDA / LDB: row strides of the operands
+    // (LD padded, KB dense).
+    template <bool SUB, int TRI = 0, int LDA = LD, int LDB = LD>
+    __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
     {
         const int k0 = TRI == 1 ? wr0 : 0;
         const int k1 = TRI == 2 ? wr1 : KB;
 #pragma unroll 2
         for (int k = k0; k < k1; k++) {
             T a[TR], b[TC];
-            vld<T, TR>(a, At + k * LD + row(0));
-            ld_row(b, B + k * LD);
+            vld<T, TR>(a, At + k * LDA + row(0));
+            ld_row(b, B + k * LDB);
 #pragma unroll
             for (int i = 0; i < TR; i++)
 #pragma unroll
                 for (int j = 0; j < TC; j++) acc[i][j] = SUB ? msub(acc[i][j], a[i], b[j]) : madd(acc[i][j], a[i], b[j]);
         }
     }
-    __device__ __forceinline__ void mma_t(Reg &acc, const T *At, const T *B) const { mm_tA<false>(acc, At, B); }
-    __device__ __forceinline__ void mms_t(Reg &acc, const T *At, const T *B) const { mm_tA<true>(acc, At, B); }
-    __device__ __forceinline__ void mma_tu(Reg &acc, const T *At, const T *B) const { mm_tA<false, 1>(acc, At, B); }
-    __device__ __forceinline__ void mms_tl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 2>(acc, At, B); }
-    __device__ __forceinline__ void mma_tl(Reg &acc, const T *At, const T *B) const { mm_tA<false, 2>(acc, At, B); }
-    __device__ __forceinline__ void mms_tu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 1>(acc, At, B); }
-    __device__ __forceinline__ void mms_t_bl(Reg &acc, const T *At, const T *B) const { mm_tA<true, 3>(acc, At, B); }
-    __device__ __forceinline__ void mms_t_bu(Reg &acc, const T *At, const T *B) const { mm_tA<true, 4>(acc, At, B); }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mma_t(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<false, 0, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mms_t(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 0, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mma_tu(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<false, 1, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mms_tl(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 2, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mma_tl(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<false, 2, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD> __device__ __forceinline__ void mms_tu(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 1, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD>
+    __device__ __forceinline__ void mms_t_bl(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 3, LDA, LDB>(acc, At, B);
+    }
+    template <int LDA = LD, int LDB = LD>
+    __device__ __forceinline__ void mms_t_bu(Reg &acc, const T *At, const T *B) const
+    {
+        mm_tA<true, 4, LDA, LDB>(acc, At, B);
+    }
 
     // In-place Gauss-Jordan inverse without pivoting, blocked by 4 x 4 pivot
     // blocks: the update of Tile::inverse_b4 (S <- S - U'V', U' = pivot
@@ -917,14 +974,15 @@ template <class T, int KB> struct Tile88 {
     }
 };
 
-// Thread counts and tile geometry of the two-sided kernels: FP32 64-row
-// tiles run on 64 threads with 8 x 8 sub-tiles (Tile88), everything else on
-// the Tile layouts above (NTOf threads for the kernels with a tile inverse,
-// TwNT for the product-only ones).
+// Thread counts and tile geometry of the two-sided kernels: the elimination
+// chains of FP32 64-row tiles run on 64 threads with 8 x 8 sub-tiles (Tile88),
+// everything else on the Tile layouts above (NTOf threads for the kernels with
+// a tile inverse, TwNT for the product-only ones, whose 8 x 4 sub-tiles on 128
+// threads timed faster than 8 x 8 on 64: more warps hide the loads).
 template <class T, int KB> struct TwCfg {
     static constexpr bool T88 = sizeof(T) == 4 && KB == 64 && TileLD<T, KB>::value == KB + 4;
     static constexpr int NT_LU = T88 ? 64 : NTOf<KB>::value;
-    static constexpr int NT_PROD = T88 ? 64 : TwNT<KB>::value;
+    static constexpr int NT_PROD = TwNT<KB>::value;
 };
 template <class T, int KB, bool T88 = TwCfg<T, KB>::T88> struct TwTiles {
     using LU = Tile<T, KB, TwCfg<T, KB>::NT_LU>;
@@ -932,7 +990,7 @@ template <class T, int KB, bool T88 = TwCfg<T, KB>::T88> struct TwTiles {
 };
 template <class T, int KB> struct TwTiles<T, KB, true> {
     using LU = Tile88<T, KB>;
-    using PROD = Tile88<T, KB>;
+    using PROD = Tile<T, KB, TwCfg<T, KB>::NT_PROD>;
 };
 
 // Dense global tile (KB*KB elements, 16-byte aligned) -> shared tile with row
@@ -1070,9 +1128,27 @@ template <class T, int KB> __device__ __forceinline__ void bulk_tile(T *s, const
     __syncwarp();
     for (int r = lane; r < KB; r += 32) bulk_g2s(s + r * LD, g + (size_t)r * KB, ROW, bar);
 }
+// Dense global tile -> dense shared tile (row stride KB): one bulk copy of
+// KB * KB elements.  For tiles that serve only as operands read in whole
+// 16-byte pieces -- the transposed left operand, whose lanes broadcast, or a
+// right operand read in contiguous runs -- where the padding buys nothing and
+// one copy replaces KB row copies.  Called by all 32 lanes of one warp, after
+// a barrier that ends every read of `s`.
+template <class T, int KB> __device__ __forceinline__ void bulk_tile_dense(T *s, const T *g, uint64_t *bar)
+{
+    constexpr unsigned BYTES = KB * KB * sizeof(T);
+    static_assert(BYTES % 16 == 0, "bulk copies move 16-byte multiples");
+    if ((threadIdx.x & 31) == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, BYTES);
+        bulk_g2s(s, g, BYTES, bar);
+    }
+}
+
 // One shared tile's barrier as every thread of the CTA tracks it: the parity
 // of its next phase and whether a copy is in flight.  All threads call
-// issue() (warp 0 issues the copies) and wait(), on uniform conditions.
+// issue() / issue_dense() (warp 0 issues the copies) and wait(), on uniform
+// conditions.
 struct TileBar {
     uint64_t *bar;
     unsigned phase;
@@ -1080,6 +1156,11 @@ struct TileBar {
     template <class T, int KB> __device__ __forceinline__ void issue(T *s, const T *g)
     {
         if (threadIdx.x < 32) bulk_tile<T, KB>(s, g, bar);
+        inflight = true;
+    }
+    template <class T, int KB> __device__ __forceinline__ void issue_dense(T *s, const T *g)
+    {
+        if (threadIdx.x < 32) bulk_tile_dense<T, KB>(s, g, bar);
         inflight = true;
     }
     // wait for the tile in flight; false on a timeout

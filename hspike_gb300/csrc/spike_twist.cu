@@ -112,26 +112,26 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_LU, 4)
     if (blockIdx.y == 0) {
         // top chain, J = 0..M-1 (M >= 4)
         T *sG = s0, *sE = s1, *sF = s2;
-        b1.issue<T, KB>(sE, gTp + 2 * TS); // A(0,1), row-major
-        b2.issue<T, KB>(sF, gTp + 4 * TS); // A(1,0), column-major
+        b1.issue_dense<T, KB>(sE, gTp + 2 * TS); // A(0,1), row-major (dense: a right operand)
+        b2.issue_dense<T, KB>(sF, gTp + 4 * TS); // A(1,0), column-major (dense: a left operand)
         t.gload(acc, gTp);                 // S_0 = D_0
         t.gload(dreg, gTp + 3 * TS);       // D_1
         for (int J = 0; J < M; J++) {
             if (J > 0) {
                 tmo |= !b2.wait();
                 t.rzero(acc);
-                t.mma_tu(acc, sF, sG); // L_J; A(J,J-1) is upper triangular
+                t.template mma_tu<KB, TL::LD>(acc, sF, sG); // L_J; A(J,J-1) is upper triangular
                 if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 t.rstore_t(sF, acc);
                 t.gstore_t(gL + tb + J * TS, acc);
                 tmo |= !b1.wait();
                 if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 rcopy<TL>(acc, dreg);
-                t.mms_t_bl(acc, sF, sE); // S_J = D_J - L_J A(J-1,J); A(J-1,J) is lower triangular
+                t.template mms_t_bl<TL::LD, KB>(acc, sF, sE); // S_J = D_J - L_J A(J-1,J); A(J-1,J) lower triangular
                 __syncthreads();
                 if (J + 1 < M) {
-                    b1.issue<T, KB>(sE, gTp + (size_t)J * 3 * TS + 2 * TS);
-                    b2.issue<T, KB>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);
+                    b1.issue_dense<T, KB>(sE, gTp + (size_t)J * 3 * TS + 2 * TS);
+                    b2.issue_dense<T, KB>(sF, gTp + (size_t)(J + 1) * 3 * TS + TS);
                     t.gload(dreg, gTp + (size_t)(J + 1) * 3 * TS); // D_{J+1}, lands during the inverse
                 }
             }
@@ -143,29 +143,29 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_LU, 4)
     } else {
         // bottom chain, J = N-1..M+1, then U_M and T'_M
         T *sH = s0, *sY = s1, *sX = s2;
-        b1.issue<T, KB>(sY, gTp + (size_t)(N - 2) * 3 * TS + 2 * TS); // A(N-2,N-1), column-major
-        b2.issue<T, KB>(sX, gTp + (size_t)(N - 1) * 3 * TS + TS);     // A(N-1,N-2), row-major
+        b1.issue_dense<T, KB>(sY, gTp + (size_t)(N - 2) * 3 * TS + 2 * TS); // A(N-2,N-1), column-major
+        b2.issue_dense<T, KB>(sX, gTp + (size_t)(N - 1) * 3 * TS + TS);     // A(N-1,N-2), row-major
         t.gload(acc, gTp + (size_t)(N - 1) * 3 * TS);                   // T_{N-1} = D_{N-1}
         t.gload(dreg, gTp + (size_t)(N - 2) * 3 * TS);                  // D_{N-2}
         for (int J = N - 1; J >= M; J--) {
             if (J < N - 1) {
                 tmo |= !b1.wait();
                 t.rzero(acc);
-                t.mma_tl(acc, sY, sH); // U_J = A(J,J+1) H_{J+1}; A(J,J+1) is lower triangular
+                t.template mma_tl<KB, TL::LD>(acc, sY, sH); // U_J = A(J,J+1) H_{J+1}; A(J,J+1) lower triangular
                 if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 t.rstore_t(sY, acc);
                 t.gstore_t((J == M ? gE : gL) + tb + J * TS, acc);
                 tmo |= !b2.wait();
                 if (__syncthreads_or(tmo)) return tw_bail(err, b1, b2);
                 rcopy<TL>(acc, dreg);
-                t.mms_t_bu(acc, sY, sX); // T_J = D_J - U_J A(J+1,J); A(J+1,J) is upper triangular
+                t.template mms_t_bu<TL::LD, KB>(acc, sY, sX); // T_J = D_J - U_J A(J+1,J); A(J+1,J) upper triangular
                 if (J == M) {
                     t.gstore(gG + tb + J * TS, acc); // T'_M for k_tw_merge
                     break;
                 }
                 __syncthreads();
-                b1.issue<T, KB>(sY, gTp + (size_t)(J - 1) * 3 * TS + 2 * TS);
-                b2.issue<T, KB>(sX, gTp + (size_t)J * 3 * TS + TS);
+                b1.issue_dense<T, KB>(sY, gTp + (size_t)(J - 1) * 3 * TS + 2 * TS);
+                b2.issue_dense<T, KB>(sX, gTp + (size_t)J * 3 * TS + TS);
                 t.gload(dreg, gTp + (size_t)(J - 1) * 3 * TS); // D_{J-1}
             }
             ok = t.inverse(acc, buf) && ok;
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_PROD, 4)
     // ring buffer of block J and the parity of its wait for block J
     auto ring = [&](int J) { return (J & 1) ? sB : sA; };
     auto issue = [&](int J, const T *g) {
-        if (threadIdx.x < 32) bulk_tile<T, KB>(ring(J), g, bars + (J & 1));
+        if (threadIdx.x < 32) bulk_tile_dense<T, KB>(ring(J), g, bars + (J & 1));
     };
     auto bail = [&](int Jn, unsigned ph) { // a copy for block Jn may be in flight
         if (threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_TIMEOUT);
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_PROD, 4)
             if (more) issue(J + 1, gL + tb + (size_t)(J + 1) * TS);
             tmo |= !mbar_wait(bars + (J & 1), ((J - 1) >> 1) & 1);
             t.rzero(acc);
-            t.mms_t(acc, ring(J), sZ);
+            t.template mms_t<KB, TL::LD>(acc, ring(J), sZ);
             if (__syncthreads_or(tmo)) return bail(more ? J + 1 : -1, (J >> 1) & 1);
             t.rstore(sZ, acc);
             t.gstore(gW + tb + J * TS, acc);
@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_PROD, 4)
             if (more) issue(J - 1, utile(J - 1));
             bhat_block<T, KB>(t, acc, bh, J, J0, o);
             tmo |= !mbar_wait(bars + (J & 1), phase(J));
-            t.mms_t(acc, ring(J), sZ);
+            t.template mms_t<KB, TL::LD>(acc, ring(J), sZ);
             if (__syncthreads_or(tmo)) return bail(more ? J - 1 : -1, phase(J - 1));
             t.rstore(sZ, acc);
             t.gstore(gV + tb + J * TS, acc);
@@ -386,8 +386,8 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_PROD, 4)
     bool tmo = false;
 
     const int J1 = top ? M - 1 : M + 1;
-    bG.issue<T, KB>(sG, gG + tb + (size_t)J1 * TS);
-    bE.issue<T, KB>(sE, gE + tb + (size_t)J1 * TS);
+    bG.issue_dense<T, KB>(sG, gG + tb + (size_t)J1 * TS); // left operands: dense
+    bE.issue_dense<T, KB>(sE, gE + tb + (size_t)J1 * TS);
     if (hasZ) t.gload(zreg, gX + tb + (size_t)J1 * TS); // Z_J of the first step
     load_tile_tr<T, KB, NT>(sX, gX + tb + (size_t)M * TS); // X_M, row-major
     __syncthreads();
@@ -401,19 +401,19 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_PROD, 4)
             t.rzero(acc);
         tmo |= !bE.wait();
         if (top)
-            t.mms_tl(acc, sE, sX); // A(J,J+1) lower triangular
+            t.template mms_tl<KB, TL::LD>(acc, sE, sX); // A(J,J+1) lower triangular
         else
-            t.mms_tu(acc, sE, sX); // A(J,J-1) upper triangular
+            t.template mms_tu<KB, TL::LD>(acc, sE, sX); // A(J,J-1) upper triangular
         if (__syncthreads_or(tmo)) return tw_bail(err, bG, bE);
-        if (more) bE.issue<T, KB>(sE, gE + tb + (size_t)Jn * TS);
+        if (more) bE.issue_dense<T, KB>(sE, gE + tb + (size_t)Jn * TS);
         t.rstore(sX, acc);
         if (hasZ && more) t.gload(zreg, gX + tb + (size_t)Jn * TS); // Z of the next step, lands meanwhile
         tmo |= !bG.wait();
         if (__syncthreads_or(tmo)) return tw_bail(err, bG, bE);
         t.rzero(acc);
-        t.mma_t(acc, sG, sX);
+        t.template mma_t<KB, TL::LD>(acc, sG, sX);
         __syncthreads();
-        if (more) bG.issue<T, KB>(sG, gG + tb + (size_t)Jn * TS);
+        if (more) bG.issue_dense<T, KB>(sG, gG + tb + (size_t)Jn * TS);
         t.rstore(sX, acc);
         t.gstore_t(gX + tb + (size_t)J * TS, acc);
         __syncthreads();
