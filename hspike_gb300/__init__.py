@@ -52,7 +52,7 @@ EXPORTS = [
     "spike_batch_partitions", "spike_server_create", "spike_server_submit", "spike_server_wait",
     "spike_server_drain", "spike_server_stats", "spike_server_clock", "spike_server_destroy",
     "spike_rcm_permutation", "spike_permute_csr", "spike_permute_vector", "spike_dsolve_reordered",
-    "spike_csr_full_band",
+    "spike_csr_full_band", "spike_shard_range", "spike_shard_dsolve", "spike_shard_assemble", "spike_shard_split",
     "matrix_ComputeBandwidth", "matrix_LoadCSR", "matrix_SaveCSR", "matrix_ExportBinary",
     "matrix_CreateFromComponents", "matrix_Deallocate", "directSolver_CreateHandler", "directSolver_Configure",
     "directSolver_Factorize", "directSolver_SolveForRHS", "directSolver_ShowStatistics", "directSolver_Finalize",
@@ -199,6 +199,10 @@ def load(path: str | None = None):
     L.spike_permute_vector.argtypes = [i, i, i, vp, vp]
     L.spike_dsolve_reordered.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, vp]
     L.spike_csr_full_band.argtypes = [i, i, i, i, vp, vp, C.POINTER(C.c_int)]
+    L.spike_shard_range.argtypes = [i, i, i, i, ip, ip, ip, ip]
+    L.spike_shard_dsolve.argtypes = [vp, vp, i, i, i, i, i, vp, vp, vp, vp, vp]
+    L.spike_shard_assemble.argtypes = [i, i, i, i, vp, vp]
+    L.spike_shard_split.argtypes = [i, i, i, i, vp, vp]
     mp, hp = C.POINTER(Matrix), C.POINTER(DirectSolverHandler)
     L.matrix_ComputeBandwidth.argtypes = [i, vp, vp, vp, ip, ip]
     L.matrix_LoadCSR.argtypes = [C.c_char_p]

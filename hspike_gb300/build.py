@@ -26,7 +26,7 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["spike_factor.cu", "spike_twist.cu", "spike_apply.cu", "spike_reduced.cu", "spike_util.cu",
               "spike_noalloc.cu"]
-C_SOURCES = ["spike_host.c", "spike_batch.c", "spike_serve.c", "spike_reorder.c", "spike_compat.c"]
+C_SOURCES = ["spike_host.c", "spike_batch.c", "spike_serve.c", "spike_reorder.c", "spike_compat.c", "spike_shard.c"]
 
 
 def nvcc() -> str:

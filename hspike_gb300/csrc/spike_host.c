@@ -346,6 +346,76 @@ static int palloc(spk_plan *P, void **p, size_t bytes)
     return SPK_OK;
 }
 
+/* The reduced system of p partitions alone (the arrays spk_reduced_factor and
+ * spk_reduced_solve use): the interface blocks RP, RQ, RX, RY, the cyclic
+ * reduction levels and the reduced right-hand side / solution.  No partition
+ * is factored with it; the blocks come from elsewhere (the ranks of a sharded
+ * solve). */
+int spk_plan_reduced_build(int p, int KB, int is_complex, int mode, int nrhs_max, spk_plan **out)
+{
+    *out = NULL;
+    if (p < 2 || !KB || nrhs_max < 1) return SPK_EARG;
+    spk_plan *P = (spk_plan *)calloc(1, sizeof *P);
+    if (!P) return SPK_EMEM;
+    P->KB = KB;
+    P->is_complex = is_complex;
+    P->mode = mode;
+    P->nrhs_max = nrhs_max;
+    P->p = p;
+    P->n_iface = p - 1;
+    int levels = 0;
+    for (int c = P->n_iface; c > 1; c = (c + 1) / 2) levels++;
+    P->cr_levels = levels;
+    P->cr_count = (int *)malloc(sizeof(int) * (levels + 1));
+    P->cr_off = (long long *)malloc(sizeof(long long) * (levels + 2));
+    P->cr_moff = (long long *)malloc(sizeof(long long) * (levels + 2));
+    if (!P->cr_count || !P->cr_off || !P->cr_moff) {
+        spk_plan_destroy(P);
+        return SPK_EMEM;
+    }
+    long long tiles = 0, mtiles = 0;
+    int c = P->n_iface;
+    for (int l = 0; l <= levels; l++) {
+        P->cr_count[l] = c;
+        P->cr_off[l] = tiles;
+        P->cr_moff[l] = mtiles;
+        tiles += c;
+        mtiles += (l < levels) ? c / 2 : 1;
+        c = (c + 1) / 2;
+    }
+    P->cr_off[levels + 1] = tiles;
+    P->cr_moff[levels + 1] = mtiles;
+    P->crg_stride = tiles * 2 * KB;
+    const size_t fs = (is_complex ? 2 : 1) * (mode == SPK_MIXED ? 4 : 8);
+    const size_t hs = (is_complex ? 2 : 1) * 8;
+    const size_t TS = (size_t)KB * KB, nif = (size_t)P->n_iface;
+    int rc = SPK_OK;
+#define PA(ptr, bytes)                                                                                          \
+    if (rc == SPK_OK) rc = palloc(P, (void **)&(ptr), (bytes))
+    PA(P->d_RP, hs * TS * nif);
+    PA(P->d_RQ, hs * TS * nif);
+    PA(P->d_RX, hs * TS * nif);
+    PA(P->d_RY, hs * TS * nif);
+    PA(P->d_crP, fs * TS * tiles);
+    PA(P->d_crQ, fs * TS * tiles);
+    PA(P->d_crX, fs * TS * tiles);
+    PA(P->d_crY, fs * TS * tiles);
+    PA(P->d_crM, fs * TS * 4 * (mtiles > 0 ? mtiles : 1));
+    PA(P->d_crg, fs * 2 * (size_t)P->crg_stride * nrhs_max);
+    PA(P->d_g, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_u, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_rr, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_du, hs * nif * 2 * KB * nrhs_max);
+    PA(P->d_err, sizeof(unsigned) * 4);
+#undef PA
+    if (rc != SPK_OK) {
+        spk_plan_destroy(P);
+        return rc;
+    }
+    *out = P;
+    return SPK_OK;
+}
+
 int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex, int mode, int p,
                    const int *part_start, int nrhs_max, void *stream, int stream_alloc, spk_plan **out)
 {

@@ -62,6 +62,9 @@ SPK_INTERNAL int spk_choose_block(int k);
 SPK_INTERNAL int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex, int mode, int p,
                                 const int *part_start, int nrhs_max, void *stream, int stream_alloc,
                                 spk_plan **out);
+/* The reduced system of p partitions (p - 1 interfaces, tile size KB) alone:
+ * the arrays of spk_reduced_factor / spk_reduced_solve, nothing else. */
+SPK_INTERNAL int spk_plan_reduced_build(int p, int KB, int is_complex, int mode, int nrhs_max, spk_plan **out);
 /* device bytes a solve of this shape holds (plan + staging for host arrays),
  * without allocating; partitions as for spike_set_option (0 = automatic) */
 SPK_INTERNAL size_t spk_solve_footprint(int n, long long nnz, int k, int nrhs, int is_complex, int mode,

@@ -291,6 +291,66 @@ Error_t spike_dsolve_reordered(spike_context_t ctx, integer_t n, integer_t nnz, 
                                const integer_t *colind, const integer_t *rowptr, const double *aij, double *x,
                                const double *b, integer_t *perm_out);
 
+/* ---- one system's partitions sharded across ranks (processes, one GPU each) ----
+ * Replaces the reference's distributed SPIKE (MPI/spike_dm.c:21-202: the
+ * master scatters A_i, f_i, B_i, C_i to workers, gathers their tips, solves
+ * the reduced system and scatters the x tips back, MPI/spike_mpi.c:450-674).
+ * Here rank r holds the CSR rows of a contiguous range of the p partitions
+ * (spike_shard_range) and factors them on its own GPU, couplings to the
+ * neighbouring ranks' rows included; the only exchanges are the tips of the
+ * reduced system (gathered to rank 0, which solves it, and its solution
+ * scattered back), one band of x rows with each neighbour before every FP64
+ * residual, and the residual norms.  The transport is the caller's: the
+ * library calls these functions on host buffers, in the same order on every
+ * rank (NCCL, MPI, a torch.distributed group ...).  Each returns 0 on success. */
+typedef struct {
+    int rank, size; /* this rank and the number of ranks */
+    void *user;     /* handed back to every callback */
+    /* rank r's `bytes` bytes into `recv` on rank 0 at offset r * bytes (recv unused on other ranks) */
+    int (*gather)(void *user, const void *send, size_t bytes, void *recv);
+    /* rank 0's `send` bytes [r * bytes, (r + 1) * bytes) into rank r's `recv` (send unused on other ranks) */
+    int (*scatter)(void *user, const void *send, size_t bytes, void *recv);
+    /* element-wise sum of `count` doubles over all ranks, in place, the result on every rank */
+    int (*allreduce_sum)(void *user, double *buf, int count);
+    /* `bytes` bytes each way with both neighbours: to_lo -> rank - 1 (its from_hi), to_hi -> rank + 1 (its
+     * from_lo); a neighbour that does not exist sends and receives nothing */
+    int (*exchange)(void *user, const void *to_lo, const void *to_hi, void *from_lo, void *from_hi, size_t bytes);
+} spike_comm_t;
+
+/* The rows and partitions rank `rank` of `size` holds: partitions
+ * [*part0, *part1) = [p rank / size, p (rank + 1) / size) and their rows
+ * [*row0, *row1), partition i starting at row i floor(n / p) (the reference's
+ * rule, OpenMP/spike_analysis.c:38-76; the last one takes the remainder). */
+Error_t spike_shard_range(integer_t n, integer_t p, integer_t size, integer_t rank, integer_t *part0, integer_t *part1,
+                          integer_t *row0, integer_t *row1);
+/* Collective solve of A x = b over all ranks of `comm`: every rank passes
+ * its rows [row0, row1) of A -- rowptr (rows + 1 entries, starting at 0),
+ * colind (GLOBAL column indices), aij -- and of b (rows x nrhs, column-major,
+ * ld = rows), and receives the same rows of x.  Mixed precision or FP64 and
+ * the tolerance come from the context (the partition count is `p`, every
+ * partition at least two tiles long); nrhs <= 64 per call.  Returns the same
+ * status on every rank (an error on one rank is reported on all). */
+Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *comm, integer_t n, integer_t p, integer_t nrhs,
+                           integer_t rows, integer_t nnz, const integer_t *colind, const integer_t *rowptr,
+                           const double *aij, double *x, const double *b);
+/* The routing of the reduced system's records between ranks (host only, also
+ * used inside spike_shard_dsolve).  A record belongs to one interface
+ * (between partitions i and i + 1) and holds left_len values that partition i
+ * produces (its bottom tips) followed by right_len values that partition
+ * i + 1 produces (its top tips).  Rank r's slot holds ceil(p / size) + 1
+ * records: those of its local interfaces j = 0 .. part1 - part0, interface j
+ * being the global interface part0 - 1 + j (j = 0 and j = part1 - part0 are
+ * the interfaces with the neighbouring ranks, of which this rank knows one
+ * side only).
+ *   assemble: the p - 1 global records from all ranks' slots (rank 0, after
+ *             a gather), each half from the rank that owns its partition;
+ *   split:    every rank's slot from the global records (rank 0, before a
+ *             scatter), whole records, zeros where no global interface exists. */
+Error_t spike_shard_assemble(integer_t p, integer_t size, integer_t left_len, integer_t right_len,
+                             const double *slots, double *global);
+Error_t spike_shard_split(integer_t p, integer_t size, integer_t left_len, integer_t right_len, const double *global,
+                          double *slots);
+
 /* ---- host check of the full-band layout ----
  * *full = 1 when row r of the CSR holds exactly the columns
  * max(0, r - kl) .. min(n - 1, r + ku) in increasing order, for every row

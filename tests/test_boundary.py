@@ -27,7 +27,8 @@ def declared_symbols():
         text = open(os.path.join(ROOT, "include", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         text = "\n".join(line for line in text.splitlines() if not line.lstrip().startswith("#"))
-        names |= set(re.findall(r"\b(\w+)\s*\([^;{]*\)\s*;", text))
+        # function declarations; "(*name)(...)" members of a struct (callbacks) are not symbols
+        names |= set(re.findall(r"\b(\w+)\s*\((?!\s*\*)[^;{]*\)\s*;", text))
         names |= set(re.findall(r"extern\s+const\s+\w+\s+(\w+)\s*;", text))
     return names
 
