@@ -702,6 +702,34 @@ def main():
         ctx64.close()
         del d_x64
 
+        # ---- the reduced system's cyclic reduction in FP64 (SPIKE_OPT_REDUCED_FP64),
+        # FP32 partition factors as in the headline: the reference solves R in FP64
+        ctxr = hs.Context()
+        ctxr.set_stream(stream.cuda_stream)
+        ctxr.set_option(hs.SPIKE_OPT_PARTITIONS, p)
+        ctxr.set_option(hs.SPIKE_OPT_REDUCED_FP64, 1)
+        d_xr = torch.zeros_like(d_b)
+        tr, _, _, _ = timed(ctxr, 5, d_xr, d_b, NRHS, 2)
+        ir = ctxr.info()
+        xr = d_xr.cpu().numpy().T
+        ctxr.set_option(hs.SPIKE_OPT_PHASE_TIMING, 1)
+        ctxr.phase_times(reset=True)
+        for _ in range(3):
+            solve(ctxr, d_xr, d_b, NRHS)
+        torch.cuda.synchronize()
+        phr = ctxr.phase_times(reset=True)
+        out["reduced_fp64"] = {"value": 5 / (tr / 1000.0), "unit": "solves/s", "ms_per_step": tr / 5,
+                               "relres_max": ir.relres_max, "refine_sweeps": ir.refine_sweeps,
+                               "reduced_fp64": ir.reduced_fp64, "err_vs_xtrue": relerr(xr, xt),
+                               "reduced_factor_ms": phr["reduced_factor"][0] / max(1, phr["reduced_factor"][1]),
+                               "reduced_solve_ms": phr["reduced_solve"][0] / max(1, phr["reduced_solve"][1]),
+                               "reduced_factor_ms_fp32": fams.get("reduced_factor", {}).get("ms_per_launch"),
+                               "reduced_solve_ms_fp32": fams.get("reduced_solve", {}).get("ms_per_launch")}
+        if xo is not None:
+            out["reduced_fp64"]["err_vs_oracle"] = relerr(xr, xo)
+        ctxr.close()
+        del d_xr
+
         # ---- nrhs = 16
         gen16 = hs.gen_banded(n, K_BAND, K_BAND, DOM, SEED, nrhs=16)
         d_b16 = torch.from_numpy(gen16[4].T.copy()).to(dev)

@@ -62,6 +62,7 @@ EXPORTS = [
 SPIKE_OPT_STREAM_ALLOC = 6
 SPIKE_OPT_TWIST = 7
 SPIKE_OPT_HOST_THREADS = 8
+SPIKE_OPT_REDUCED_FP64 = 9
 SPIKE_BATCH_AUTOTUNE = 1
 SPIKE_BATCH_NO_GRAPH = 2
 
@@ -76,7 +77,8 @@ class SpikeError(RuntimeError):
 class Info(C.Structure):
     _fields_ = [("relres_max", C.c_double), ("refine_sweeps", C.c_int), ("partitions", C.c_int), ("ku", C.c_int),
                 ("kl", C.c_int), ("block", C.c_int), ("kernel_launches", C.c_longlong),
-                ("device_bytes", C.c_size_t), ("twisted", C.c_int), ("columns_implied", C.c_int)]
+                ("device_bytes", C.c_size_t), ("twisted", C.c_int), ("columns_implied", C.c_int),
+                ("reduced_fp64", C.c_int)]
 
 
 class DSystem(C.Structure):

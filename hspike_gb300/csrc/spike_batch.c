@@ -197,6 +197,7 @@ static int group_build_plan(struct spike_batch_s *B, bgroup *G, int KB, int rpp)
     int rc = spk_plan_build((int)G->rows, G->nnz, ku, kl, KB, 0, B->ctx->mode, (int)p, ps, G->nrhs, G->stream, 0,
                             &G->P);
     if (rc == SPK_OK) G->P->twist = G->P->twist_cap && B->ctx->twist;
+    if (rc == SPK_OK) G->P->red_fp64 = B->ctx->red_fp64 && G->P->KB <= 64;
     if (rc == SPK_OK) rc = spk_malloc((void **)&G->d_part_sys, sizeof(int) * (size_t)p);
     if (rc == SPK_OK) rc = spk_memcpy_h2d(G->d_part_sys, psys, sizeof(int) * (size_t)p, G->stream);
     if (rc == SPK_OK) rc = spk_stream_sync(G->stream);

@@ -219,6 +219,9 @@ Error_t spike_set_option(spike_context_t c, int opt, double v)
     case SPIKE_OPT_TWIST:
         c->twist = v != 0;
         break;
+    case SPIKE_OPT_REDUCED_FP64:
+        c->red_fp64 = v != 0;
+        break;
     case SPIKE_OPT_HOST_THREADS:
         if (v < 0 || v > 64) return spk_fail(SPIKE_ERR_ARGUMENT, "host threads must be in [0, 64]");
         c->host_threads = (int)v;
@@ -258,6 +261,7 @@ Error_t spike_get_option(spike_context_t c, int opt, double *v)
     case SPIKE_OPT_REDUCED_REFINE: *v = c->red_refine; break;
     case SPIKE_OPT_PHASE_TIMING: *v = c->timing; break;
     case SPIKE_OPT_TWIST: *v = c->twist; break;
+    case SPIKE_OPT_REDUCED_FP64: *v = c->red_fp64; break;
     case SPIKE_OPT_HOST_THREADS: *v = c->host_threads; break;
     case SPIKE_OPT_STREAM_ALLOC: *v = c->stream_alloc; break;
     default: return spk_fail(SPIKE_ERR_ARGUMENT, "unknown option %d", opt);
@@ -386,7 +390,6 @@ int spk_plan_reduced_build(int p, int KB, int is_complex, int mode, int nrhs_max
     P->cr_off[levels + 1] = tiles;
     P->cr_moff[levels + 1] = mtiles;
     P->crg_stride = tiles * 2 * KB;
-    const size_t fs = (is_complex ? 2 : 1) * (mode == SPK_MIXED ? 4 : 8);
     const size_t hs = (is_complex ? 2 : 1) * 8;
     const size_t TS = (size_t)KB * KB, nif = (size_t)P->n_iface;
     int rc = SPK_OK;
@@ -396,12 +399,12 @@ int spk_plan_reduced_build(int p, int KB, int is_complex, int mode, int nrhs_max
     PA(P->d_RQ, hs * TS * nif);
     PA(P->d_RX, hs * TS * nif);
     PA(P->d_RY, hs * TS * nif);
-    PA(P->d_crP, fs * TS * tiles);
-    PA(P->d_crQ, fs * TS * tiles);
-    PA(P->d_crX, fs * TS * tiles);
-    PA(P->d_crY, fs * TS * tiles);
-    PA(P->d_crM, fs * TS * 4 * (mtiles > 0 ? mtiles : 1));
-    PA(P->d_crg, fs * 2 * (size_t)P->crg_stride * nrhs_max);
+    PA(P->d_crP, hs * TS * tiles); /* FP64 scalars: the reduced system may run in FP64 (red_fp64) */
+    PA(P->d_crQ, hs * TS * tiles);
+    PA(P->d_crX, hs * TS * tiles);
+    PA(P->d_crY, hs * TS * tiles);
+    PA(P->d_crM, hs * TS * 4 * (mtiles > 0 ? mtiles : 1));
+    PA(P->d_crg, hs * 2 * (size_t)P->crg_stride * nrhs_max);
     PA(P->d_g, hs * nif * 2 * KB * nrhs_max);
     PA(P->d_u, hs * nif * 2 * KB * nrhs_max);
     PA(P->d_rr, hs * nif * 2 * KB * nrhs_max);
@@ -503,12 +506,12 @@ int spk_plan_build(int n, long long nnz, int ku, int kl, int KB, int is_complex,
     PA(P->d_RQ, hs * TS * nif);
     PA(P->d_RX, hs * TS * nif);
     PA(P->d_RY, hs * TS * nif);
-    PA(P->d_crP, fs * TS * tiles);
-    PA(P->d_crQ, fs * TS * tiles);
-    PA(P->d_crX, fs * TS * tiles);
-    PA(P->d_crY, fs * TS * tiles);
-    PA(P->d_crM, fs * TS * 4 * (mtiles > 0 ? mtiles : 1));
-    PA(P->d_crg, fs * 2 * (size_t)P->crg_stride * nrhs_max);
+    PA(P->d_crP, hs * TS * tiles); /* FP64 scalars: the reduced system may run in FP64 (red_fp64) */
+    PA(P->d_crQ, hs * TS * tiles);
+    PA(P->d_crX, hs * TS * tiles);
+    PA(P->d_crY, hs * TS * tiles);
+    PA(P->d_crM, hs * TS * 4 * (mtiles > 0 ? mtiles : 1));
+    PA(P->d_crg, hs * 2 * (size_t)P->crg_stride * nrhs_max);
     PA(P->d_z, fs * (size_t)P->NP * nrhs_max);
     PA(P->d_y, fs * (size_t)P->NP * nrhs_max);
     PA(P->d_g, hs * nif * 2 * KB * nrhs_max);
@@ -593,8 +596,8 @@ size_t spk_solve_footprint(int n, long long nnz, int k, int nrhs, int is_complex
     b += sizeof(int) * (2 * (size_t)(p + 1) + (size_t)blocks);
     b += fs * TS * (size_t)blocks * 8 + fs * TS * p;            /* L G E W V + 3 band tiles, B^ */
     b += hs * TS * (size_t)nif * 4;                               /* RP RQ RX RY */
-    b += fs * TS * (size_t)tiles * 4 + fs * TS * 4 * (size_t)mtiles; /* cyclic reduction */
-    b += fs * 2 * (size_t)tiles * 2 * KB * chunk;                 /* reduced RHS work */
+    b += hs * TS * (size_t)tiles * 4 + hs * TS * 4 * (size_t)mtiles; /* cyclic reduction (FP64 scalars) */
+    b += hs * 2 * (size_t)tiles * 2 * KB * chunk;                 /* reduced RHS work */
     b += fs * 2 * (size_t)blocks * KB * chunk;                    /* z, y */
     b += hs * (size_t)nif * 2 * KB * chunk * 4;                   /* g u rr du */
     b += 16 + sizeof(double) * 2 * chunk;
@@ -695,7 +698,7 @@ typedef struct {
 static int solve_phase(spk_plan *P, const int *rp, const int *ci, const void *aij, void *x, const void *b, void *r,
                        int nrhs, refine_opts *o, void *stream)
 {
-    const int red = o->red_refine > 0 ? o->red_refine : (P->mode == SPK_MIXED ? 2 : 1);
+    const int red = o->red_refine > 0 ? o->red_refine : (P->mode == SPK_MIXED && !P->red_fp64 ? 2 : 1);
     double norms[2 * RHS_CHUNK];
     double bnorm[RHS_CHUNK];
     TRY(spike_apply_once(P, x, b, nrhs, red, 0, stream));
@@ -753,6 +756,7 @@ static void fill_info(spike_context_t c, const spk_plan *P, const refine_opts *o
     c->info.device_bytes = P->bytes;
     c->info.twisted = P->twist;
     c->info.columns_implied = P->impl_cols;
+    c->info.reduced_fp64 = P->red_fp64 || P->mode == SPK_PLAIN;
 }
 
 static Error_t finish(int rc, const char *where, const refine_opts *o)
@@ -783,6 +787,7 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
         Q->p == choose_partitions(n, Q->KB, c->partitions) && chunk0 <= Q->nrhs_max) {
         unsigned e[4];
         Q->twist = Q->twist_cap && c->twist;
+        Q->red_fp64 = c->red_fp64 && Q->KB <= 64;
         Q->launches = 0;
         Q->timing = c->timing;
         Q->validate = 1;
@@ -831,6 +836,7 @@ static int run_device(spike_context_t c, int n, long long nnz, int nrhs, const i
     P->ku = info[0];
     P->kl = info[1];
     P->twist = P->twist_cap && c->twist;
+    P->red_fp64 = c->red_fp64 && P->KB <= 64;
     P->launches = l0;
     P->timing = c->timing;
     const size_t hs = (is_complex ? 2 : 1) * 8;
@@ -1026,6 +1032,7 @@ static int host_pipelined(spike_context_t c, int n, long long nnz, int nrhs, con
     TRY(spk_memcpy_h2d(c->d_b, b, hs * (size_t)n * nrhs, cs));
     TRY(ensure(&c->d_r, &c->c_r, hs * (size_t)n * chunk, spk_ctx_astream(c)));
     Q->twist = 1;
+    Q->red_fp64 = c->red_fp64 && Q->KB <= 64;
     Q->launches = 0;
     Q->timing = 0;
     Q->validate = 1;
@@ -1342,6 +1349,7 @@ static Error_t factor_common(spike_context_t c, int cplx, const char *name, inte
     if (rc == SPK_OK) {
         f->plan->launches = l0;
         f->plan->twist = f->plan->twist_cap && c->twist;
+        f->plan->red_fp64 = c->red_fp64 && f->plan->KB <= 64;
         rc = factor_phase(f->plan, f->d_rowptr, f->d_colind, f->d_aij, c->stream);
     }
     if (rc != SPK_OK) {

@@ -31,6 +31,7 @@ struct spike_context_s {
     int refs; /* the creator's reference + one per factor handle or batch using the context */
     int mode, partitions, max_refine, red_refine, timing, twist;
     int host_threads; /* SPIKE_OPT_HOST_THREADS */
+    int red_fp64;     /* SPIKE_OPT_REDUCED_FP64 */
     int stream_alloc; /* workspace allocated stream-ordered on `stream` */
     double tol;
     /* cached plan for the reference-API and device-pointer calls */

@@ -93,6 +93,11 @@ typedef struct spk_plan {
     /* two-sided partition solves (spike_twist.cu): every partition is
      * eliminated from both ends towards its block M = N_i / 2 */
     int twist, twist_cap; /* in use / possible for this schedule and precision */
+    /* the reduced system's cyclic reduction in FP64 (complex128) even when
+     * the partitions' factors are FP32 (SPIKE_OPT_REDUCED_FP64; tiles up to
+     * 64 rows).  The cyclic-reduction arrays are allocated with 8-byte
+     * (16-byte complex) scalars whatever the mode, so a call may switch. */
+    int red_fp64;
     /* k_band_tiles also validates the CSR and measures the bandwidth into
      * d_err[1..2] (set when the separate analysis pass was skipped) */
     int validate;

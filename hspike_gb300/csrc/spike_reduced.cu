@@ -1150,8 +1150,9 @@ extern "C" int spk_reduced_factor(spk_plan *P, void *stream)
 {
     if (P->n_iface <= 0) return SPK_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    if (P->is_complex) return P->mode == SPK_MIXED ? disp_rf<cfloat>(P, st) : disp_rf<cdouble>(P, st);
-    return P->mode == SPK_MIXED ? disp_rf<float>(P, st) : disp_rf<double>(P, st);
+    const bool low = P->mode == SPK_MIXED && !P->red_fp64; // factor-precision cyclic reduction
+    if (P->is_complex) return low ? disp_rf<cfloat>(P, st) : disp_rf<cdouble>(P, st);
+    return low ? disp_rf<float>(P, st) : disp_rf<double>(P, st);
 }
 
 extern "C" int spk_reduced_solve(spk_plan *P, int nrhs, int refine_iters, void *stream)
@@ -1159,7 +1160,8 @@ extern "C" int spk_reduced_solve(spk_plan *P, int nrhs, int refine_iters, void *
     if (P->n_iface <= 0) return SPK_OK;
     if (refine_iters < 1) refine_iters = 1;
     cudaStream_t st = (cudaStream_t)stream;
+    const bool low = P->mode == SPK_MIXED && !P->red_fp64;
     if (P->is_complex)
-        return P->mode == SPK_MIXED ? disp_rs<cfloat>(P, nrhs, refine_iters, st) : disp_rs<cdouble>(P, nrhs, refine_iters, st);
-    return P->mode == SPK_MIXED ? disp_rs<float>(P, nrhs, refine_iters, st) : disp_rs<double>(P, nrhs, refine_iters, st);
+        return low ? disp_rs<cfloat>(P, nrhs, refine_iters, st) : disp_rs<cdouble>(P, nrhs, refine_iters, st);
+    return low ? disp_rs<float>(P, nrhs, refine_iters, st) : disp_rs<double>(P, nrhs, refine_iters, st);
 }

@@ -493,6 +493,7 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
     }
     if (rc == SPK_OK) {
         S.P->twist = S.P->twist_cap && c->twist;
+        S.P->red_fp64 = c->red_fp64 && KB <= 64;
         rc = spk_memset(S.P->d_err, 0, sizeof(unsigned) * 4, c->stream);
         if (rc == SPK_OK) rc = spk_factor(S.P, S.d_rp, S.d_ci, S.d_a, c->stream);
         if (rc == SPK_OK) rc = device_error(S.P, c->stream);
@@ -504,6 +505,7 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
         int rc0 = SPK_OK;
         if (cm->rank == 0) {
             rc0 = spk_plan_reduced_build(p, KB, 0, c->mode, nrhs, &S.Pg);
+            if (rc0 == SPK_OK) S.Pg->red_fp64 = c->red_fp64 && KB <= 64;
             if (rc0 == SPK_OK) rc0 = spike_shard_assemble(p, size, 2 * TS, 2 * TS, S.h_all, S.h_glob) == SPIKE_SUCCESS
                                          ? SPK_OK : SPK_EARG;
             if (rc0 == SPK_OK) rc0 = unpack_blocks(&S);
@@ -515,7 +517,7 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
     }
 
     /* solve and FP64 refinement */
-    const int red = c && c->red_refine > 0 ? c->red_refine : (c && c->mode == SPK_MIXED ? 2 : 1);
+    const int red = c && c->red_refine > 0 ? c->red_refine : (c && c->mode == SPK_MIXED && !(c->red_fp64 && KB <= 64) ? 2 : 1);
     double relres = 0.0;
     int sweeps = 0;
     if (rc == SPK_OK) rc = shard_apply(&S, S.d_b, 0, red, &peer);
@@ -559,6 +561,7 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
         c->info.block = KB;
         c->info.twisted = S.P ? S.P->twist : 0;
         c->info.columns_implied = 0;
+        c->info.reduced_fp64 = (c->red_fp64 && KB <= 64) || c->mode == SPK_PLAIN;
     }
     shard_free(&S);
     if (rc == SPK_OK) return spk_succeed();

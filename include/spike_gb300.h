@@ -43,6 +43,10 @@ typedef struct spike_factor_s *spike_factor_t;
 #define SPIKE_OPT_TWIST 7          /* 1 = eliminate each partition from both ends at once where the kernels
                                       allow it (tiles 16..64 fitting four CTAs per SM, >= 8 blocks per
                                       partition); 0 = top-down only (default 1) */
+#define SPIKE_OPT_REDUCED_FP64 9   /* 1 = the reduced system's cyclic reduction in FP64 (complex128) also in
+                                      mixed precision, for tiles up to 64 rows (the reference solves R in FP64
+                                      with PARDISO, OpenMP/spike_algebra.c:263-420); 0 = in the factors'
+                                      precision, FP64 refinement sweeps on R making up the rest (default 0) */
 #define SPIKE_OPT_HOST_THREADS 8   /* host threads that, in a call with host arrays whose plan is reused,
                                       check that the CSR is the full band while its values travel, so
                                       the column indices stay on the host (default 8; 0 = always copy
@@ -86,6 +90,7 @@ typedef struct {
     size_t device_bytes;      /* device memory held by the context's plan */
     int twisted;              /* 1 if the partitions were eliminated from both ends (SPIKE_OPT_TWIST) */
     int columns_implied;      /* 1 if the column indices stayed on the host (full band, SPIKE_OPT_HOST_THREADS) */
+    int reduced_fp64;         /* 1 if the reduced system was factored and solved in FP64 (SPIKE_OPT_REDUCED_FP64) */
 } spike_info_t;
 Error_t spike_get_info(spike_context_t ctx, spike_info_t *info);
 

@@ -534,3 +534,33 @@ def test_128_row_tiles_only_in_real_mixed_precision():
     x = np.zeros_like(b, order="F")
     assert hs.zspike_core_host(3000, len(ci), 1, ci, rp, a, x, b) == hs.SPIKE_ERROR
     assert hs.ERR_NAMES[hs.last_error()[0]] == "bandwidth"
+
+
+@pytest.mark.parametrize("n,k,p,nrhs,complex_",
+                         [(60_000, 2, 16, 2, False), (80_000, 8, 40, 1, False), (120_000, 32, 24, 3, False),
+                          (200_000, 64, 48, 1, False), (90_000, 3, 30, 2, True), (60_000, 100, 12, 1, False)],
+                         ids=lambda v: str(v))
+def test_reduced_system_in_fp64(n, k, p, nrhs, complex_):
+    # SPIKE_OPT_REDUCED_FP64: the reduced system's cyclic reduction in FP64
+    # (the reference solves R in FP64 with PARDISO, OpenMP/spike_algebra.c:
+    # 263-420) beside FP32 partition factors; 128-row tiles keep their FP32
+    # reduced system (the option does not apply there)
+    rp, ci, a, xt, b = hs.gen_banded(n, k, k, 1.5, seed=700 + k, complex_=complex_, nrhs=nrhs)
+    xo = oracle.spike(rp, ci, a, b, p=p)
+    ctx = hs.Context()
+    try:
+        ctx.set_option(hs.SPIKE_OPT_REDUCED_FP64, 1)
+        assert ctx.get_option(hs.SPIKE_OPT_REDUCED_FP64) == 1
+        for call in range(2):  # new plan, then the reused plan
+            x = hs.solve(rp, ci, a, b, precision=hs.SPIKE_PRECISION_MIXED, partitions=p, ctx=ctx)
+            info = ctx.info()
+            assert info.reduced_fp64 == (1 if k <= 64 else 0)
+            assert info.relres_max <= RES_TOL
+            assert oracle.residual(rp, ci, a, x, b).max() <= RES_TOL
+            assert relerr(x, xo) <= ERR_TOL
+        ctx.set_option(hs.SPIKE_OPT_REDUCED_FP64, 0)
+        x32 = hs.solve(rp, ci, a, b, precision=hs.SPIKE_PRECISION_MIXED, partitions=p, ctx=ctx)
+        assert ctx.info().reduced_fp64 == 0
+        assert relerr(x32, xo) <= ERR_TOL
+    finally:
+        ctx.close()
