@@ -1068,7 +1068,12 @@ template <int E> __device__ __forceinline__ void cp_async_elem(void *smem, const
 // the padded layout (no bank conflicts) is unchanged.  The copies read this
 // GPU's own memory into the issuing CTA's shared memory only (no cluster, no
 // multicast).
-#define SPK_MBAR_SPIN_LIMIT (1 << 22)
+// A wait on a bulk copy gives up after SPK_MBAR_TIMEOUT_NS of the GPU's global
+// timer (or SPK_MBAR_SPIN_LIMIT polls, whichever comes first); each poll
+// suspends the thread for at most SPK_MBAR_POLL_NS unless the phase completes.
+#define SPK_MBAR_TIMEOUT_NS 1000000000ull /* 1 s */
+#define SPK_MBAR_POLL_NS 20000u           /* 20 us */
+#define SPK_MBAR_SPIN_LIMIT (1 << 24)
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -1092,24 +1097,37 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+// true when the phase with parity `parity` has completed; otherwise the thread
+// may be suspended for up to SPK_MBAR_POLL_NS (woken early when the phase
+// completes) before false comes back
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
 {
     unsigned done;
-    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
                  "selp.u32 %0, 1, 0, p;\n\t}"
                  : "=r"(done)
-                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "r"(smem_u32(bar)), "r"(parity), "r"(SPK_MBAR_POLL_NS)
                  : "memory");
     return done != 0;
 }
-// Wait for the phase of `bar` with parity `parity` to complete; gives up after
-// SPK_MBAR_SPIN_LIMIT polls (each poll may suspend the thread for a short,
-// hardware-chosen time) and returns false, so a copy that never lands ends in
-// an error status instead of a hang.
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait for the phase of `bar` with parity `parity` to complete.  Gives up --
+// returns false -- after SPK_MBAR_TIMEOUT_NS on the global timer (or
+// SPK_MBAR_SPIN_LIMIT polls), so a copy that never lands ends in an error
+// status instead of a hang.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
 {
-    for (int i = 0; i < SPK_MBAR_SPIN_LIMIT; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (int i = 0; i < SPK_MBAR_SPIN_LIMIT; i++) {
         if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > SPK_MBAR_TIMEOUT_NS) break;
+    }
     return false;
 }
 // Dense global tile (KB x KB, row-major or column-major as stored) -> shared
