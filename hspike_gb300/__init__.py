@@ -39,7 +39,7 @@ SPIKE_PRECISION_MIXED = 0
 SPIKE_PRECISION_FP64 = 1
 
 ERR_NAMES = {0: "none", 1: "argument", 2: "csr", 3: "bandwidth", 4: "cuda", 5: "memory", 6: "pivot",
-             7: "convergence", 8: "no_device", 9: "handle"}
+             7: "convergence", 8: "no_device", 9: "handle", 10: "busy"}
 
 EXPORTS = [
     "sspike_core_host", "dspike_core_host", "cspike_core_host", "zspike_core_host", "dspike_core_host_blocking",
@@ -50,7 +50,7 @@ EXPORTS = [
     "spike_get_phase_times", "spike_dsolve_device_noalloc", "spike_dbatch_create", "spike_batch_run",
     "spike_batch_relres", "spike_batch_get_info", "spike_batch_group", "spike_batch_destroy",
     "spike_batch_partitions", "spike_server_create", "spike_server_submit", "spike_server_wait",
-    "spike_server_drain", "spike_server_stats", "spike_server_clock", "spike_server_destroy",
+    "spike_server_drain", "spike_server_stats", "spike_server_poll", "spike_server_clock", "spike_server_destroy",
     "spike_rcm_permutation", "spike_permute_csr", "spike_permute_vector", "spike_dsolve_reordered",
     "spike_csr_full_band", "spike_shard_range", "spike_shard_dsolve", "spike_shard_assemble", "spike_shard_split",
     "matrix_ComputeBandwidth", "matrix_LoadCSR", "matrix_SaveCSR", "matrix_ExportBinary",
@@ -101,7 +101,7 @@ class BatchGroup(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("slots", C.c_int), ("precision", C.c_int), ("tolerance", C.c_double), ("max_refine", C.c_int),
-                ("hbm_budget", C.c_size_t), ("cache_budget", C.c_size_t)]
+                ("hbm_budget", C.c_size_t), ("cache_budget", C.c_size_t), ("max_queue", C.c_int)]
 
 
 class Request(C.Structure):
@@ -142,7 +142,7 @@ class ServerStats(C.Structure):
                 ("resident_factors", C.c_int), ("device_bytes_running", C.c_size_t),
                 ("device_bytes_cached", C.c_size_t), ("latency_p50", C.c_double), ("latency_p99", C.c_double),
                 ("latency_max", C.c_double), ("mean_queue_wait", C.c_double), ("throughput", C.c_double),
-                ("relres_max", C.c_double)]
+                ("relres_max", C.c_double), ("rejected_busy", C.c_longlong)]
 
 
 _LIB = None
@@ -191,6 +191,7 @@ def load(path: str | None = None):
     L.spike_server_create.argtypes = [C.POINTER(ServerConfig), C.POINTER(vp)]
     L.spike_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_longlong)]
     L.spike_server_wait.argtypes = [vp, C.c_longlong, C.POINTER(RequestStatus)]
+    L.spike_server_poll.argtypes = [vp, C.c_longlong, C.POINTER(RequestStatus)]
     L.spike_server_drain.argtypes = [vp]
     L.spike_server_stats.argtypes = [vp, C.POINTER(ServerStats)]
     L.spike_server_clock.argtypes = [vp]
@@ -472,8 +473,8 @@ class Server:
     admission by device footprint, resident factors under keys."""
 
     def __init__(self, slots=4, precision=SPIKE_PRECISION_MIXED, tolerance=1e-12, max_refine=3, hbm_budget=0,
-                 cache_budget=0):
-        cfg = ServerConfig(slots, precision, tolerance, max_refine, hbm_budget, cache_budget)
+                 cache_budget=0, max_queue=0):
+        cfg = ServerConfig(slots, precision, tolerance, max_refine, hbm_budget, cache_budget, max_queue)
         self._h = C.c_void_p()
         self._keep = {}
         _check(load().spike_server_create(C.byref(cfg), C.byref(self._h)))
@@ -500,6 +501,15 @@ class Server:
         self._keep.pop(ticket, None)
         if check:
             _check(rc)
+        return st
+
+    def poll(self, ticket) -> RequestStatus:
+        """The request's status now, without waiting; the arrays of a finished
+        request are no longer held here (the caller keeps x)."""
+        st = RequestStatus()
+        _check(load().spike_server_poll(self._h, ticket, C.byref(st)))
+        if st.done:
+            self._keep.pop(ticket, None)
         return st
 
     def drain(self):

@@ -69,6 +69,7 @@ struct spike_server_s {
     size_t cache_used;
     struct timespec t0;
     long long completed, rejected, failed, hits, misses;
+    long long nqueued, rejected_busy; /* requests waiting for a slot; turned away on a full queue */
     int running, peak_running;
 };
 
@@ -256,6 +257,7 @@ static void *worker_main(void *arg)
         }
         if (!q) break;
         q->state = 1;
+        S->nqueued--;
         q->t_admit = now_s(S);
         S->used += q->footprint;
         if (++S->running > S->peak_running) S->peak_running = S->running;
@@ -358,6 +360,16 @@ Error_t spike_server_submit(spike_server_t S, const spike_request_t *r, long lon
         snprintf(q->msg, sizeof q->msg, q->footprint == 0 ? "bandwidth %d above the largest tile"
                                                           : "footprint above the server's device budget", k);
         S->rejected++;
+    } else if (S->cfg.max_queue > 0 && S->nqueued >= S->cfg.max_queue) {
+        /* load shedding: a full queue turns the request away at once */
+        q->state = 2;
+        q->t_admit = q->t_done = now_s(S);
+        q->err = SPIKE_ERR_BUSY;
+        snprintf(q->msg, sizeof q->msg, "admission queue full (%d waiting)", S->cfg.max_queue);
+        S->rejected++;
+        S->rejected_busy++;
+    } else {
+        S->nqueued++;
     }
     *ticket = q->ticket;
     pthread_cond_broadcast(&S->cv);
@@ -393,6 +405,19 @@ Error_t spike_server_wait(spike_server_t S, long long ticket, spike_request_stat
     snprintf(msg, sizeof msg, "%s", q->msg);
     pthread_mutex_unlock(&S->mu);
     if (st->error_code) return spk_fail(st->error_code, "request %lld: %s", ticket, msg);
+    return spk_succeed();
+}
+
+Error_t spike_server_poll(spike_server_t S, long long ticket, spike_request_status_t *st)
+{
+    if (!S || !st || ticket < 0) return spk_fail(SPIKE_ERR_ARGUMENT, "spike_server_poll: bad argument");
+    pthread_mutex_lock(&S->mu);
+    if (ticket >= S->nreq) {
+        pthread_mutex_unlock(&S->mu);
+        return spk_fail(SPIKE_ERR_ARGUMENT, "spike_server_poll: unknown ticket");
+    }
+    fill_status(S->reqs[ticket], st);
+    pthread_mutex_unlock(&S->mu);
     return spk_succeed();
 }
 
@@ -436,6 +461,7 @@ Error_t spike_server_stats(spike_server_t S, spike_server_stats_t *st)
     st->submitted = S->nreq;
     st->completed = S->completed;
     st->rejected = S->rejected;
+    st->rejected_busy = S->rejected_busy;
     st->failed = S->failed;
     st->factor_hits = S->hits;
     st->factor_misses = S->misses;

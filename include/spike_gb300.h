@@ -66,6 +66,7 @@ typedef struct spike_factor_s *spike_factor_t;
 #define SPIKE_ERR_CONVERGENCE 7 /* refinement stopped above the tolerance (x holds the last iterate) */
 #define SPIKE_ERR_NO_DEVICE 8
 #define SPIKE_ERR_HANDLE 9
+#define SPIKE_ERR_BUSY 10       /* a server's admission queue was full (spike_server_config_t.max_queue) */
 
 int spike_last_error_code(void);          /* of the calling thread's last call */
 const char *spike_last_error(void);       /* human-readable, thread-local */
@@ -237,6 +238,8 @@ typedef struct {
     int max_refine;      /* refinement sweeps (0 = 3) */
     size_t hbm_budget;   /* device bytes for running requests (0 = 60 % of free memory) */
     size_t cache_budget; /* device bytes for resident factors (0 = 20 % of free memory) */
+    int max_queue;       /* requests waiting for a slot beyond which a new request is completed at once with
+                            SPIKE_ERR_BUSY (load shedding; 0 = an unbounded queue) */
 } spike_server_config_t;
 typedef struct {
     integer_t n, nnz, nrhs;
@@ -263,6 +266,7 @@ typedef struct {
     double latency_p50, latency_p99, latency_max; /* seconds, arrival to completion */
     double mean_queue_wait, throughput;           /* seconds; completed per second */
     double relres_max;
+    long long rejected_busy; /* of `rejected`: turned away because the queue was full */
 } spike_server_stats_t;
 Error_t spike_server_create(const spike_server_config_t *cfg, spike_server_t *server);
 /* Queue a request; a request larger than the whole budget (or with a band
@@ -270,6 +274,8 @@ Error_t spike_server_create(const spike_server_config_t *cfg, spike_server_t *se
 Error_t spike_server_submit(spike_server_t server, const spike_request_t *req, long long *ticket);
 /* Block until the request is done; returns its error, if any. */
 Error_t spike_server_wait(spike_server_t server, long long ticket, spike_request_status_t *status);
+/* The request's status now, without waiting (status->done = 0 while it is queued or running). */
+Error_t spike_server_poll(spike_server_t server, long long ticket, spike_request_status_t *status);
 Error_t spike_server_drain(spike_server_t server);
 Error_t spike_server_stats(spike_server_t server, spike_server_stats_t *stats);
 double spike_server_clock(spike_server_t server); /* seconds since creation */

@@ -108,3 +108,27 @@ def test_band_above_the_largest_tile_is_rejected():
     assert st.done and hs.ERR_NAMES[st.error_code] == "bandwidth"
     assert srv.stats().rejected == 1
     srv.close()
+
+
+def test_a_full_queue_turns_requests_away_at_once():
+    # load shedding: with max_queue waiting requests, the next one is completed
+    # at once with SPIKE_ERR_BUSY; requests already queued still finish, and
+    # poll() reports status without waiting
+    srv = hs.Server(slots=1, max_queue=2)
+    try:
+        rp, ci, a, xt, b = hs.gen_banded(300_000, 64, 64, 1.5, seed=77, nrhs=4)
+        tickets = [srv.submit(rp, ci, a, b, bandwidth=64) for _ in range(12)]  # no pattern scan: quick submits
+        sts = [srv.poll(t) for t, _ in tickets]
+        busy = [s for s in sts if s.done and hs.ERR_NAMES[s.error_code] == "busy"]
+        assert len(busy) >= 12 - 1 - 2 - 2  # one running, two queued, slack for requests done meanwhile
+        srv.drain()
+        st = srv.stats()
+        assert st.rejected_busy == len([1 for t, _ in tickets if hs.ERR_NAMES[srv.poll(t).error_code] == "busy"])
+        assert st.completed + st.rejected_busy == 12 and st.completed >= 1
+        for t, x in tickets:
+            s = srv.poll(t)
+            assert s.done
+            if s.error_code == 0:
+                assert s.relres <= RES_TOL and np.linalg.norm(x - xt) / np.linalg.norm(xt) <= 1e-10
+    finally:
+        srv.close()
