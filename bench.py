@@ -496,8 +496,17 @@ def shard_arm(args, torch, hs, world, rank, local):
     n, p = args.n, args.partitions
     rp, ci, a, xt, b = hs.gen_banded(n, K_BAND, K_BAND, DOM, SEED, nrhs=NRHS)
     part0, part1, row0, row1 = shard.shard_range(n, p, world, rank)
-    lrp, lci, la = shard.rows_of(rp, ci, a, row0, row1)
-    lb = np.asfortranarray(b[row0:row1])
+    tdt = {np.int32: torch.int32, np.float64: torch.float64}
+
+    def pinned_copy(arr):
+        """the rank's slice in pinned host memory (what a caller that streams
+        matrices to the GPU holds), column order kept"""
+        out = torch.empty(arr.size, dtype=tdt[arr.dtype.type], pin_memory=True).numpy()
+        out[:] = arr.reshape(-1, order="F")
+        return out.reshape(arr.shape, order="F")
+
+    lrp, lci, la = (pinned_copy(v) for v in shard.rows_of(rp, ci, a, row0, row1))
+    lb = pinned_copy(np.asfortranarray(b[row0:row1]))
     del rp, ci, a
     ctx = hs.Context()
     ctx.set_option(hs.SPIKE_OPT_PRECISION, hs.SPIKE_PRECISION_MIXED)

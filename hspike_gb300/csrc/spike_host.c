@@ -136,6 +136,7 @@ Error_t spike_context_create(spike_context_t *out)
 static void ctx_free(spike_context_t c)
 {
     void *as = spk_ctx_astream(c);
+    spk_shard_release(c);
     spk_plan_destroy(c->plan);
     spk_free(c->d_scratch);
     spk_free_on(c->d_rowptr, as);

@@ -41,6 +41,7 @@ struct spike_context_s {
     void *d_rowptr, *d_colind, *d_aij, *d_b, *d_x, *d_r, *d_stage;
     size_t c_rowptr, c_colind, c_aij, c_b, c_x, c_r, c_stage;
     spike_info_t info;
+    void *shard; /* the sharded solve's plans and buffers, kept for a next call of the same shape */
 };
 
 /* thread-local error detail (spike_last_error_code / spike_last_error) */
@@ -77,5 +78,7 @@ SPK_INTERNAL Error_t spk_host_solve_ctx(spike_context_t c, int dtype, const char
 /* stream for workspace allocations of this context (NULL: synchronous) */
 static inline void *spk_ctx_astream(spike_context_t c) { return c->stream_alloc ? c->stream : NULL; }
 SPK_INTERNAL void spk_plan_destroy(spk_plan *P);
+/* frees the context's sharded-solve state (spike_shard.c) */
+SPK_INTERNAL void spk_shard_release(spike_context_t c);
 
 #endif /* SPIKE_GB300_HOST_INTERNAL_H */

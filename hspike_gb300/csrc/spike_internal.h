@@ -182,6 +182,11 @@ int spk_stream_sync(void *stream);
 int spk_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
 int spk_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
 int spk_memcpy_d2d(void *dst, const void *src, size_t bytes, void *stream);
+/* height rows of width bytes, dpitch / spitch apart, host or device either side */
+int spk_memcpy_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height, void *stream);
+/* page-locked host memory */
+int spk_host_alloc(void **p, size_t bytes);
+void spk_host_free(void *p);
 int spk_memset(void *dst, int v, size_t bytes, void *stream);
 const char *spk_cuda_error_string(void);
 
@@ -191,6 +196,13 @@ const char *spk_cuda_error_string(void);
  * Synchronizes the stream. */
 int spk_analyze(int n, long long nnz, const int *d_rowptr, const int *d_colind, int *d_scratch, int *out,
                 void *stream, long long *launches);
+/* sharded solve: bandwidth of rows [row0, row0 + m) held with global columns
+ * into d_out (4 device ints: [0] = ku, [1] = kl, [2] = 1 on a bad row pointer
+ * or column), queued on the stream; and the rank's local CSR, in place, with
+ * h identity rows either side (k_shard_local) */
+int spk_rows_band(int m, long long nnz, int row0, int n, const int *d_rowptr, const int *d_colind, int *d_out,
+                  void *stream);
+int spk_shard_local(int m, long long nnz, int h, int row0, int *d_rowptr, int *d_colind, double *d_aij, void *stream);
 /* widen caller values to FP64 / complex128 (S -> D, C -> Z) and narrow back */
 int spk_widen(const void *src, void *dst, long long count, int is_complex, void *stream, long long *launches);
 int spk_narrow(const void *src, void *dst, long long count, int is_complex, void *stream, long long *launches);

@@ -111,41 +111,159 @@ Error_t spike_shard_split(integer_t p, integer_t size, integer_t left_len, integ
 /* ------------------------------------------------------------------ */
 /* the collective solve                                                */
 /* ------------------------------------------------------------------ */
+
+/* The largest halo: 8 tiles of the largest block (128 rows).  The rank's rows
+ * sit this many rows (entries) into the local buffers whatever the block size
+ * turns out to be, so their copies start before the bandwidth is known; the
+ * local CSR begins SHARD_HALO_MAX - h rows (entries) in, h = 8 KB. */
+#define SHARD_HALO_MAX (8 * 128)
+
+/* What a sharded solve holds on its rank, kept on the context for the next
+ * call of the same shape: the plans and device buffers are most of a call's
+ * setup otherwise. */
 typedef struct {
-    const spike_comm_t *cm;
-    spike_context_t c;
-    int n, p, nrhs, rows, part0, part1, row0, KB, h, nloc_if, nrec;
+    /* the rank's rows: keys of the buffers */
+    int n, p, nrhs, rows, size, rank, part0, part1, row0;
     long long nnz;
-    /* local system */
-    int n_loc;
+    int *d_rp_buf, *d_ci_buf; /* rows + 1 + 2 SHARD_HALO_MAX / nnz + 2 SHARD_HALO_MAX */
+    double *d_a_buf;          /* nnz + 2 SHARD_HALO_MAX */
+    /* the block size and precision: keys of the plans */
+    int KB, mode, h, nloc_if, nrec, n_loc;
     long long nnz_loc;
     spk_plan *P;  /* the local system's plan */
     spk_plan *Pg; /* rank 0: the global reduced system */
-    int *d_rp, *d_ci;
-    double *d_a, *d_b, *d_x, *d_r;
+    double *d_b, *d_x, *d_r;
     /* host staging */
     double *h_loc;   /* this rank's slot */
     double *h_all;   /* rank 0: every rank's slot */
     double *h_glob;  /* rank 0: the global records */
     double *h_dev;   /* device-layout staging (interface blocks or reduced right-hand side) */
     double *h_halo;  /* 4 KB x nrhs: to lo, to hi, from lo, from hi */
+    /* this call */
+    const spike_comm_t *cm;
+    spike_context_t c;
+    int *d_rp, *d_ci; /* the local CSR, inside the buffers above */
+    double *d_a;
 } shard_t;
 
-static void shard_free(shard_t *S)
+static void shard_free_plans(shard_t *S)
 {
     spk_plan_destroy(S->P);
     spk_plan_destroy(S->Pg);
-    spk_free(S->d_rp);
-    spk_free(S->d_ci);
-    spk_free(S->d_a);
     spk_free(S->d_b);
     spk_free(S->d_x);
     spk_free(S->d_r);
-    free(S->h_loc);
-    free(S->h_all);
-    free(S->h_glob);
-    free(S->h_dev);
-    free(S->h_halo);
+    spk_host_free(S->h_loc);
+    spk_host_free(S->h_all);
+    spk_host_free(S->h_glob);
+    spk_host_free(S->h_dev);
+    spk_host_free(S->h_halo);
+    S->P = S->Pg = NULL;
+    S->d_b = S->d_x = S->d_r = NULL;
+    S->h_loc = S->h_all = S->h_glob = S->h_dev = S->h_halo = NULL;
+    S->KB = 0;
+}
+
+void spk_shard_release(spike_context_t c)
+{
+    shard_t *S = c ? (shard_t *)c->shard : NULL;
+    if (!S) return;
+    spk_stream_sync(c->stream);
+    if (c->copy_stream) spk_stream_sync(c->copy_stream);
+    shard_free_plans(S);
+    spk_free(S->d_rp_buf);
+    spk_free(S->d_ci_buf);
+    spk_free(S->d_a_buf);
+    free(S);
+    c->shard = NULL;
+}
+
+/* the context's shard state for this shape, its buffers allocated */
+static int shard_buffers(spike_context_t c, const spike_comm_t *cm, int n, int p, int nrhs, int rows, long long nnz,
+                         int part0, int part1, int row0, shard_t **out)
+{
+    shard_t *S = (shard_t *)c->shard;
+    if (S && (S->n != n || S->p != p || S->nrhs != nrhs || S->rows != rows || S->nnz != nnz || S->size != cm->size ||
+              S->rank != cm->rank || S->row0 != row0)) {
+        spk_shard_release(c);
+        S = NULL;
+    }
+    if (!S) {
+        S = (shard_t *)calloc(1, sizeof *S);
+        if (!S) return SPK_EMEM;
+        c->shard = S;
+        S->n = n;
+        S->p = p;
+        S->nrhs = nrhs;
+        S->rows = rows;
+        S->nnz = nnz;
+        S->size = cm->size;
+        S->rank = cm->rank;
+        S->part0 = part0;
+        S->part1 = part1;
+        S->row0 = row0;
+        const size_t H = SHARD_HALO_MAX;
+        TRY(spk_malloc((void **)&S->d_rp_buf, sizeof(int) * ((size_t)rows + 1 + 2 * H)));
+        TRY(spk_malloc((void **)&S->d_ci_buf, sizeof(int) * ((size_t)nnz + 2 * H)));
+        TRY(spk_malloc((void **)&S->d_a_buf, sizeof(double) * ((size_t)nnz + 2 * H)));
+    }
+    *out = S;
+    return SPK_OK;
+}
+
+/* the local plan (halo partition, the rank's partitions, halo partition),
+ * rank 0's global reduced plan and the staging, for tile size KB */
+static int shard_plans(shard_t *S, int KB)
+{
+    spike_context_t c = S->c;
+    if (S->P && S->KB == KB && S->mode == c->mode) return SPK_OK;
+    shard_free_plans(S);
+    const int h = 8 * KB, m = S->rows, nl = m + 2 * h, nr = S->nrhs, p = S->p;
+    S->h = h;
+    S->n_loc = nl;
+    S->nnz_loc = S->nnz + 2LL * h;
+    S->nloc_if = S->part1 - S->part0 + 1;
+    S->nrec = slot_records(p, S->size);
+    if (S->nnz_loc > 0x7fffffffLL) return SPK_EARG;
+    const int np = S->part1 - S->part0, pl = np + 2;
+    int *ps = (int *)malloc(sizeof(int) * ((size_t)pl + 1));
+    if (!ps) return SPK_EMEM;
+    ps[0] = 0;
+    for (int j = 0; j <= np; j++) ps[1 + j] = h + (int)(part_row(S->n, p, S->part0 + j) - S->row0);
+    ps[pl] = nl;
+    int rc = spk_plan_build(nl, S->nnz_loc, KB, KB, KB, 0, c->mode, pl, ps, nr, c->stream, 0, &S->P);
+    free(ps);
+    TRY(rc);
+    const size_t vb = sizeof(double) * (size_t)nl * nr;
+    TRY(spk_malloc((void **)&S->d_b, vb));
+    TRY(spk_malloc((void **)&S->d_x, vb));
+    TRY(spk_malloc((void **)&S->d_r, vb));
+    const size_t TS = (size_t)KB * KB, rec_blk = 4 * TS, rec_red = (size_t)2 * KB * nr;
+    const size_t rec_max = rec_blk > rec_red ? rec_blk : rec_red;
+    /* host staging, page-locked: the records travel between the device and
+     * the exchanges through it */
+    TRY(spk_host_alloc((void **)&S->h_loc, sizeof(double) * rec_max * S->nrec));
+    TRY(spk_host_alloc((void **)&S->h_dev, sizeof(double) * rec_max * (size_t)(p > S->nrec ? p : S->nrec)));
+    TRY(spk_host_alloc((void **)&S->h_halo, sizeof(double) * 4 * (size_t)KB * nr));
+    if (S->rank == 0) {
+        TRY(spk_host_alloc((void **)&S->h_all, sizeof(double) * rec_max * S->nrec * (size_t)S->size));
+        TRY(spk_host_alloc((void **)&S->h_glob, sizeof(double) * rec_max * (size_t)p));
+        TRY(spk_plan_reduced_build(p, KB, 0, c->mode, nr, &S->Pg));
+    }
+    S->KB = KB;
+    S->mode = c->mode;
+    return SPK_OK;
+}
+
+static int device_error(spk_plan *P, void *stream)
+{
+    unsigned e[4] = {0, 0, 0, 0};
+    TRY(spk_memcpy_d2h(e, P->d_err, sizeof e, stream));
+    TRY(spk_stream_sync(stream));
+    if (e[0] & SPK_DEV_ERR_TIMEOUT) return SPK_ETIMEOUT;
+    if (e[0] & SPK_DEV_ERR_PIVOT) return SPK_EPIVOT;
+    if (e[0] & (SPK_DEV_ERR_BAND | SPK_DEV_ERR_CSR)) return SPK_ECSR;
+    return SPK_OK;
 }
 
 /* Every rank's status summed over the ranks: SPK_OK when all succeeded, else
@@ -167,100 +285,39 @@ static int agree(shard_t *S, int rc, int *peer_failed)
     return out;
 }
 
-static int device_error(spk_plan *P, void *stream)
+/* This rank's rows renumbered with h identity rows on either side, in place
+ * in the buffers that received them (the values are already there or on the
+ * way, behind an event on the context's stream), and the local right-hand
+ * side with zero halo rows. */
+static int shard_local(shard_t *S, const double *b)
 {
-    unsigned e[4] = {0, 0, 0, 0};
-    TRY(spk_memcpy_d2h(e, P->d_err, sizeof e, stream));
-    TRY(spk_stream_sync(stream));
-    if (e[0] & SPK_DEV_ERR_TIMEOUT) return SPK_ETIMEOUT;
-    if (e[0] & SPK_DEV_ERR_PIVOT) return SPK_EPIVOT;
-    if (e[0] & (SPK_DEV_ERR_BAND | SPK_DEV_ERR_CSR)) return SPK_ECSR;
-    return SPK_OK;
-}
-
-/* This rank's rows renumbered with h identity rows on either side, on the
- * device, with the local schedule: halo partition, the rank's partitions,
- * halo partition. */
-static int shard_local(shard_t *S, const int *colind, const int *rowptr, const double *aij, const double *b)
-{
-    const int h = S->h, m = S->rows, nl = m + 2 * h;
-    S->n_loc = nl;
-    S->nnz_loc = S->nnz + 2LL * h;
-    int *rp = (int *)malloc(sizeof(int) * ((size_t)nl + 1));
-    int *ci = (int *)malloc(sizeof(int) * (size_t)S->nnz_loc);
-    double *a = (double *)malloc(sizeof(double) * (size_t)S->nnz_loc);
-    double *bl = (double *)calloc((size_t)nl * S->nrhs, sizeof(double));
-    const int np = S->part1 - S->part0, pl = np + 2;
-    int *ps = (int *)malloc(sizeof(int) * ((size_t)pl + 1));
-    int rc = (rp && ci && a && bl && ps) ? SPK_OK : SPK_EMEM;
-    if (rc == SPK_OK) {
-        long long t = 0;
-        for (int i = 0; i < h; i++, t++) {
-            rp[i] = (int)t;
-            ci[t] = i;
-            a[t] = 1.0;
-        }
-        for (int r = 0; r < m && rc == SPK_OK; r++) {
-            rp[h + r] = (int)t;
-            for (long long q = rowptr[r]; q < rowptr[r + 1]; q++, t++) {
-                const long long cl = (long long)colind[q] - S->row0 + h;
-                if (cl < 0 || cl >= nl) { /* farther than the halo reaches: not a band of <= KB */
-                    rc = SPK_ECSR;
-                    break;
-                }
-                ci[t] = (int)cl;
-                a[t] = aij[q];
-            }
-        }
-        for (int i = 0; rc == SPK_OK && i < h; i++, t++) {
-            rp[h + m + i] = (int)t;
-            ci[t] = h + m + i;
-            a[t] = 1.0;
-        }
-        rp[nl] = (int)t;
-        for (int k = 0; k < S->nrhs; k++) memcpy(bl + (size_t)k * nl + h, b + (size_t)k * m, sizeof(double) * m);
-        ps[0] = 0;
-        for (int j = 0; j <= np; j++) ps[1 + j] = h + (int)(part_row(S->n, S->p, S->part0 + j) - S->row0);
-        ps[pl] = nl;
-    }
-    if (rc == SPK_OK)
-        rc = spk_plan_build(nl, S->nnz_loc, S->KB, S->KB, S->KB, 0, S->c->mode, pl, ps, S->nrhs, S->c->stream, 0, &S->P);
-    const size_t vb = sizeof(double) * (size_t)nl * S->nrhs;
-    if (rc == SPK_OK) rc = spk_malloc((void **)&S->d_rp, sizeof(int) * ((size_t)nl + 1));
-    if (rc == SPK_OK) rc = spk_malloc((void **)&S->d_ci, sizeof(int) * (size_t)S->nnz_loc);
-    if (rc == SPK_OK) rc = spk_malloc((void **)&S->d_a, sizeof(double) * (size_t)S->nnz_loc);
-    if (rc == SPK_OK) rc = spk_malloc((void **)&S->d_b, vb);
-    if (rc == SPK_OK) rc = spk_malloc((void **)&S->d_x, vb);
-    if (rc == SPK_OK) rc = spk_malloc((void **)&S->d_r, vb);
+    const int h = S->h, m = S->rows, nl = S->n_loc, nr = S->nrhs;
+    const size_t off = (size_t)SHARD_HALO_MAX - (size_t)h;
+    S->d_rp = S->d_rp_buf + off;
+    S->d_ci = S->d_ci_buf + off;
+    S->d_a = S->d_a_buf + off;
     void *st = S->c->stream;
-    if (rc == SPK_OK) rc = spk_memcpy_h2d(S->d_rp, rp, sizeof(int) * ((size_t)nl + 1), st);
-    if (rc == SPK_OK) rc = spk_memcpy_h2d(S->d_ci, ci, sizeof(int) * (size_t)S->nnz_loc, st);
-    if (rc == SPK_OK) rc = spk_memcpy_h2d(S->d_a, a, sizeof(double) * (size_t)S->nnz_loc, st);
-    if (rc == SPK_OK) rc = spk_memcpy_h2d(S->d_b, bl, vb, st);
-    if (rc == SPK_OK) rc = spk_memset(S->d_x, 0, vb, st);
-    if (rc == SPK_OK) rc = spk_stream_sync(st);
-    free(rp);
-    free(ci);
-    free(a);
-    free(bl);
-    free(ps);
-    return rc;
+    const size_t vb = sizeof(double) * (size_t)nl * nr;
+    TRY(spk_shard_local(m, S->nnz, h, S->row0, S->d_rp, S->d_ci, S->d_a, st));
+    TRY(spk_memset(S->d_b, 0, vb, st));
+    for (int k = 0; k < nr; k++)
+        TRY(spk_memcpy_h2d(S->d_b + (size_t)k * nl + h, b + (size_t)k * m, sizeof(double) * m, st));
+    return spk_memset(S->d_x, 0, vb, st);
 }
 
 /* Local interface j's record of the interface blocks: P X (bottom tips of its
- * left partition) | Q Y (top tips of its right partition), KB x KB each. */
+ * left partition) | Q Y (top tips of its right partition), KB x KB each,
+ * copied from the plan's block arrays straight into the records (pitched) */
 static int pack_blocks(shard_t *S)
 {
     const size_t TS = (size_t)S->KB * S->KB, ni = (size_t)S->nloc_if, rec = 4 * TS;
     spk_plan *P = S->P;
-    double *blk[4] = {S->h_dev, S->h_dev + ni * TS, S->h_dev + 2 * ni * TS, S->h_dev + 3 * ni * TS};
-    void *src[4] = {P->d_RP, P->d_RX, P->d_RQ, P->d_RY};
-    for (int q = 0; q < 4; q++) TRY(spk_memcpy_d2h(blk[q], src[q], sizeof(double) * ni * TS, S->c->stream));
-    TRY(spk_stream_sync(S->c->stream));
-    memset(S->h_loc, 0, sizeof(double) * rec * S->nrec);
-    for (size_t j = 0; j < ni; j++)
-        for (int q = 0; q < 4; q++) memcpy(S->h_loc + j * rec + q * TS, blk[q] + j * TS, sizeof(double) * TS);
-    return SPK_OK;
+    const void *src[4] = {P->d_RP, P->d_RX, P->d_RQ, P->d_RY};
+    memset(S->h_loc + ni * rec, 0, sizeof(double) * rec * ((size_t)S->nrec - ni));
+    for (int q = 0; q < 4; q++)
+        TRY(spk_memcpy_2d(S->h_loc + q * TS, sizeof(double) * rec, src[q], sizeof(double) * TS, sizeof(double) * TS,
+                          ni, S->c->stream));
+    return spk_stream_sync(S->c->stream);
 }
 
 /* rank 0: the global records -> the global reduced plan's blocks */
@@ -269,12 +326,10 @@ static int unpack_blocks(shard_t *S)
     const size_t TS = (size_t)S->KB * S->KB, ng = (size_t)S->p - 1, rec = 4 * TS;
     spk_plan *G = S->Pg;
     void *dst[4] = {G->d_RP, G->d_RX, G->d_RQ, G->d_RY};
-    for (int q = 0; q < 4; q++) {
-        for (size_t g = 0; g < ng; g++) memcpy(S->h_dev + g * TS, S->h_glob + g * rec + q * TS, sizeof(double) * TS);
-        TRY(spk_memcpy_h2d(dst[q], S->h_dev, sizeof(double) * ng * TS, S->c->stream));
-        TRY(spk_stream_sync(S->c->stream));
-    }
-    return SPK_OK;
+    for (int q = 0; q < 4; q++)
+        TRY(spk_memcpy_2d(dst[q], sizeof(double) * TS, S->h_glob + q * TS, sizeof(double) * rec, sizeof(double) * TS,
+                          ng, S->c->stream));
+    return spk_stream_sync(S->c->stream);
 }
 
 /* reduced right-hand side / solution, device layout [column][interface][2 KB]
@@ -394,26 +449,20 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
         return spk_fail(SPIKE_ERR_ARGUMENT, "%s: incomplete communicator", name);
     if (nrhs < 1 || nrhs > RHS_CHUNK) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: nrhs must be in [1, %d]", name, RHS_CHUNK);
     if (p < 2 || cm->size > p) return spk_fail(SPIKE_ERR_ARGUMENT, "%s: need p >= 2 and at most p ranks", name);
-    shard_t S;
-    memset(&S, 0, sizeof S);
-    S.cm = cm;
-    S.n = n;
-    S.p = p;
-    S.nrhs = nrhs;
-    S.rows = rows;
-    S.nnz = nnz;
     int part0, part1, row0, row1;
     if (spike_shard_range(n, p, cm->size, cm->rank, &part0, &part1, &row0, &row1) != SPIKE_SUCCESS) return SPIKE_ERROR;
-    S.part0 = part0;
-    S.part1 = part1;
-    S.row0 = row0;
     int rc = SPK_OK, peer = 0;
     if (rows != row1 - row0 || nnz < 0 || !colind || !rowptr || !aij || !x || !b || rowptr[0] != 0 ||
         rowptr[rows] != nnz)
         rc = SPK_EARG;
     spike_context_t c = rc == SPK_OK ? spk_get_ctx(ctx) : NULL;
     if (rc == SPK_OK && !c) rc = SPK_ENODEV;
-    S.c = c;
+    shard_t *S = NULL;
+    if (rc == SPK_OK) rc = shard_buffers(c, cm, n, p, nrhs, rows, nnz, part0, part1, row0, &S);
+    if (S) {
+        S->cm = cm;
+        S->c = c;
+    }
     /* bandwidth of this rank's rows (global numbering), then of all ranks'
      * (each writes its own pair of slots of a vector summed over the ranks),
      * and ||b||^2 per column summed the same way */
@@ -421,22 +470,34 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
     const int nv = 2 * size + nrhs + 1;
     double *v = (double *)calloc((size_t)nv, sizeof(double));
     if (!v) rc = SPK_EMEM;
+    int copying = 0;
     if (rc == SPK_OK) {
-        int ku = 0, kl = 0;
-        for (int r = 0; r < rows && rc == SPK_OK; r++)
-            for (long long q = rowptr[r]; q < rowptr[r + 1]; q++) {
-                const long long col = colind[q], d = col - (row0 + r);
-                if (col < 0 || col >= n || q < 0 || q >= nnz) {
-                    rc = SPK_ECSR;
-                    break;
-                }
-                if (d > ku) ku = (int)d;
-                if (-d > kl) kl = (int)-d;
-            }
-        v[2 * cm->rank] = ku;
-        v[2 * cm->rank + 1] = kl;
+        /* the rank's rows to the device: row pointers and columns first (the
+         * band scan reads them), the values behind them on the copy stream,
+         * where they overlap the scan and the agreement on the block size */
+        const size_t H = SHARD_HALO_MAX;
+        int *rp_raw = S->d_rp_buf + H, *ci_raw = S->d_ci_buf + H;
+        rc = spk_memcpy_h2d(rp_raw, rowptr, sizeof(int) * ((size_t)rows + 1), c->stream);
+        if (rc == SPK_OK && nnz > 0) rc = spk_memcpy_h2d(ci_raw, colind, sizeof(int) * (size_t)nnz, c->stream);
+        if (rc == SPK_OK && !c->copy_stream) rc = spk_stream_create(&c->copy_stream);
+        if (rc == SPK_OK) rc = spk_stream_fork(c->stream, c->copy_stream);
+        if (rc == SPK_OK && nnz > 0) {
+            copying = 1;
+            rc = spk_memcpy_h2d(S->d_a_buf + H, aij, sizeof(double) * (size_t)nnz, c->copy_stream);
+        }
+        if (rc == SPK_OK) rc = spk_rows_band(rows, nnz, row0, n, rp_raw, ci_raw, c->d_scratch, c->stream);
         for (int k = 0; k < nrhs; k++)
             for (int r = 0; r < rows; r++) v[2 * size + k] += b[(size_t)k * rows + r] * b[(size_t)k * rows + r];
+        int band[3] = {0, 0, 0};
+        if (rc == SPK_OK) rc = spk_memcpy_d2h(band, c->d_scratch, sizeof band, c->stream);
+        if (rc == SPK_OK) rc = spk_stream_sync(c->stream);
+        if (rc == SPK_OK && band[2]) rc = SPK_ECSR;
+        v[2 * cm->rank] = band[0];
+        v[2 * cm->rank + 1] = band[1];
+    }
+    if (copying) { /* everything after this on the context's stream sees the values */
+        const int jrc = spk_stream_fork(c->copy_stream, c->stream);
+        if (rc == SPK_OK) rc = jrc;
     }
     if (v) {
         v[nv - 1] = rc != SPK_OK;
@@ -447,6 +508,7 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
         }
     }
     double bnorm[RHS_CHUNK];
+    int KB = 0;
     if (rc == SPK_OK) {
         int k = 0;
         for (int r = 0; r < size; r++) {
@@ -454,81 +516,70 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
             if (v[2 * r + 1] > k) k = (int)v[2 * r + 1];
         }
         for (int j = 0; j < nrhs; j++) bnorm[j] = sqrt(v[2 * size + j]);
-        S.KB = spk_choose_block(k < 1 ? 1 : k);
-        if (!S.KB || spk_factor_smem(S.KB, 0, c->mode) == 0) rc = SPK_EBAND;
+        KB = spk_choose_block(k < 1 ? 1 : k);
+        if (!KB || spk_factor_smem(KB, 0, c->mode) == 0) rc = SPK_EBAND;
         /* every partition must hold two tiles (all ranks decide alike) */
-        else if (n / p < 2 * S.KB)
+        else if (n / p < 2 * KB)
             rc = SPK_EARG;
     }
     free(v);
     if (rc != SPK_OK) {
+        spk_shard_release(c);
         if (rc == SPK_EARG && !peer)
             return spk_fail(SPIKE_ERR_ARGUMENT, "%s: bad arguments (rows must be this rank's range, rowptr from 0 to "
                             "nnz, partitions at least two tiles long)", name);
         return shard_fail(rc, peer, name);
     }
-    S.h = 8 * S.KB;
-    S.nloc_if = (part1 - part0) + 1;
-    S.nrec = slot_records(p, size);
-    const int KB = S.KB;
-    const size_t TS = (size_t)KB * KB;
-    const size_t rec_blk = 4 * TS, rec_red = (size_t)2 * KB * nrhs;
-    const size_t rec_max = rec_blk > rec_red ? rec_blk : rec_red;
-    S.h_loc = (double *)malloc(sizeof(double) * rec_max * S.nrec);
-    S.h_dev = (double *)malloc(sizeof(double) * rec_max * (size_t)(p > S.nrec ? p : S.nrec));
-    S.h_halo = (double *)malloc(sizeof(double) * 4 * (size_t)KB * nrhs);
-    if (cm->rank == 0) {
-        S.h_all = (double *)malloc(sizeof(double) * rec_max * S.nrec * (size_t)size);
-        S.h_glob = (double *)malloc(sizeof(double) * rec_max * (size_t)p);
-    }
-    if (!S.h_loc || !S.h_dev || !S.h_halo || (cm->rank == 0 && (!S.h_all || !S.h_glob))) rc = SPK_EMEM;
+    const size_t TS = (size_t)KB * KB, rec_blk = 4 * TS;
 
     /* local system, factorization, interface blocks */
-    if (rc == SPK_OK) rc = shard_local(&S, colind, rowptr, aij, b);
+    rc = shard_plans(S, KB);
+    if (rc == SPK_OK) rc = shard_local(S, b);
     if (rc == SPK_OK) {
         int info[3];
         long long l0 = 0;
-        rc = spk_analyze(S.n_loc, S.nnz_loc, S.d_rp, S.d_ci, c->d_scratch, info, c->stream, &l0);
+        rc = spk_analyze(S->n_loc, S->nnz_loc, S->d_rp, S->d_ci, c->d_scratch, info, c->stream, &l0);
         if (rc == SPK_OK && info[2]) rc = SPK_ECSR;
     }
     if (rc == SPK_OK) {
-        S.P->twist = S.P->twist_cap && c->twist;
-        S.P->red_fp64 = c->red_fp64 && KB <= 64;
-        rc = spk_memset(S.P->d_err, 0, sizeof(unsigned) * 4, c->stream);
-        if (rc == SPK_OK) rc = spk_factor(S.P, S.d_rp, S.d_ci, S.d_a, c->stream);
-        if (rc == SPK_OK) rc = device_error(S.P, c->stream);
+        S->P->twist = S->P->twist_cap && c->twist;
+        S->P->red_fp64 = c->red_fp64 && KB <= 64;
+        rc = spk_memset(S->P->d_err, 0, sizeof(unsigned) * 4, c->stream);
+        if (rc == SPK_OK) rc = spk_factor(S->P, S->d_rp, S->d_ci, S->d_a, c->stream);
+        if (rc == SPK_OK) rc = device_error(S->P, c->stream);
     }
-    if (rc == SPK_OK) rc = pack_blocks(&S);
-    rc = agree(&S, rc, &peer);
-    if (rc == SPK_OK && cm->gather(cm->user, S.h_loc, sizeof(double) * rec_blk * S.nrec, S.h_all) != 0) rc = SPK_ECUDA;
+    if (rc == SPK_OK) rc = pack_blocks(S);
+    rc = agree(S, rc, &peer);
+    if (rc == SPK_OK && cm->gather(cm->user, S->h_loc, sizeof(double) * rec_blk * S->nrec, S->h_all) != 0)
+        rc = SPK_ECUDA;
     if (rc == SPK_OK) {
         int rc0 = SPK_OK;
         if (cm->rank == 0) {
-            rc0 = spk_plan_reduced_build(p, KB, 0, c->mode, nrhs, &S.Pg);
-            if (rc0 == SPK_OK) S.Pg->red_fp64 = c->red_fp64 && KB <= 64;
-            if (rc0 == SPK_OK) rc0 = spike_shard_assemble(p, size, 2 * TS, 2 * TS, S.h_all, S.h_glob) == SPIKE_SUCCESS
-                                         ? SPK_OK : SPK_EARG;
-            if (rc0 == SPK_OK) rc0 = unpack_blocks(&S);
-            if (rc0 == SPK_OK) rc0 = spk_memset(S.Pg->d_err, 0, sizeof(unsigned) * 4, c->stream);
-            if (rc0 == SPK_OK) rc0 = spk_reduced_factor(S.Pg, c->stream);
-            if (rc0 == SPK_OK) rc0 = device_error(S.Pg, c->stream);
+            spk_plan *G = S->Pg;
+            G->red_fp64 = c->red_fp64 && KB <= 64;
+            rc0 = spike_shard_assemble(p, size, 2 * TS, 2 * TS, S->h_all, S->h_glob) == SPIKE_SUCCESS ? SPK_OK : SPK_EARG;
+            if (rc0 == SPK_OK) rc0 = unpack_blocks(S);
+            if (rc0 == SPK_OK) rc0 = spk_memset(G->d_err, 0, sizeof(unsigned) * 4, c->stream);
+            if (rc0 == SPK_OK) rc0 = spk_reduced_factor(G, c->stream);
+            if (rc0 == SPK_OK) rc0 = device_error(G, c->stream);
         }
-        rc = agree(&S, rc0, &peer);
+        rc = agree(S, rc0, &peer);
     }
 
     /* solve and FP64 refinement */
-    const int red = c && c->red_refine > 0 ? c->red_refine : (c && c->mode == SPK_MIXED && !(c->red_fp64 && KB <= 64) ? 2 : 1);
+    const int red = c->red_refine > 0 ? c->red_refine : (c->mode == SPK_MIXED && !(c->red_fp64 && KB <= 64) ? 2 : 1);
     double relres = 0.0;
     int sweeps = 0;
-    if (rc == SPK_OK) rc = shard_apply(&S, S.d_b, 0, red, &peer);
+    if (rc == SPK_OK) rc = shard_apply(S, S->d_b, 0, red, &peer);
     for (int sweep = 0; rc == SPK_OK; sweep++) {
-        rc = shard_halo(&S, &peer);
+        rc = shard_halo(S, &peer);
         if (rc != SPK_OK) break;
         double nrm[RHS_CHUNK + 1];
-        int lrc = spk_residual(S.P, S.d_rp, S.d_ci, S.d_a, S.d_x, S.d_b, S.d_r, nrhs, 0, S.P->d_norms, c->stream);
-        if (lrc == SPK_OK) lrc = spk_memcpy_d2h(nrm, S.P->d_norms, sizeof(double) * nrhs, c->stream);
+        int lrc = spk_residual(S->P, S->d_rp, S->d_ci, S->d_a, S->d_x, S->d_b, S->d_r, nrhs, 0, S->P->d_norms,
+                               c->stream);
+        if (lrc == SPK_OK) lrc = spk_memcpy_d2h(nrm, S->P->d_norms, sizeof(double) * nrhs, c->stream);
         if (lrc == SPK_OK) lrc = spk_stream_sync(c->stream);
-        rc = agree(&S, lrc, &peer);
+        rc = agree(S, lrc, &peer);
         if (rc != SPK_OK) break;
         if (cm->allreduce_sum(cm->user, nrm, nrhs) != 0) {
             rc = SPK_ECUDA;
@@ -546,12 +597,12 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
             rc = SPK_ECONV;
             break;
         }
-        rc = shard_apply(&S, S.d_r, 1, red, &peer);
+        rc = shard_apply(S, S->d_r, 1, red, &peer);
     }
     if (rc == SPK_OK || rc == SPK_ECONV) {
         int lrc = SPK_OK;
         for (int k = 0; k < nrhs && lrc == SPK_OK; k++)
-            lrc = spk_memcpy_d2h(x + (size_t)k * rows, S.d_x + (size_t)k * S.n_loc + S.h, sizeof(double) * rows,
+            lrc = spk_memcpy_d2h(x + (size_t)k * rows, S->d_x + (size_t)k * S->n_loc + S->h, sizeof(double) * rows,
                                  c->stream);
         if (lrc == SPK_OK) lrc = spk_stream_sync(c->stream);
         if (lrc != SPK_OK) rc = lrc;
@@ -559,11 +610,12 @@ Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *cm, integer_
         c->info.refine_sweeps = sweeps;
         c->info.partitions = p;
         c->info.block = KB;
-        c->info.twisted = S.P ? S.P->twist : 0;
+        c->info.twisted = S->P->twist;
         c->info.columns_implied = 0;
         c->info.reduced_fp64 = (c->red_fp64 && KB <= 64) || c->mode == SPK_PLAIN;
     }
-    shard_free(&S);
+    /* a failed call leaves nothing behind for the next one */
+    if (rc != SPK_OK && rc != SPK_ECONV) spk_shard_release(c);
     if (rc == SPK_OK) return spk_succeed();
     return shard_fail(rc, peer, name);
 }

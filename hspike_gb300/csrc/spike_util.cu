@@ -145,6 +145,31 @@ extern "C" int spk_memcpy_d2d(void *dst, const void *src, size_t bytes, void *st
 {
     return ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
 }
+// height rows of width bytes each, rows dpitch / spitch bytes apart, either
+// direction (the pointers say which)
+extern "C" int spk_memcpy_2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
+                             void *stream)
+{
+    if (!width || !height) return SPK_OK;
+    return ck(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, cudaMemcpyDefault, (cudaStream_t)stream));
+}
+// page-locked host memory (staging that is copied to and from the device)
+extern "C" int spk_host_alloc(void **p, size_t bytes)
+{
+    *p = nullptr;
+    cudaError_t e = cudaMallocHost(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        g_last_cuda = e;
+        cudaGetLastError();
+        *p = nullptr;
+        return SPK_EMEM;
+    }
+    return SPK_OK;
+}
+extern "C" void spk_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+}
 extern "C" int spk_memset(void *dst, int v, size_t bytes, void *stream)
 {
     return ck(cudaMemsetAsync(dst, v, bytes, (cudaStream_t)stream));
@@ -692,4 +717,83 @@ extern "C" void spk_phase_destroy(spk_plan *P)
     for (int i = 0; i < 2 * SPK_MAX_EVENTS; i++) cudaEventDestroy(ev[i]);
     free(ev);
     P->ev = NULL;
+}
+
+// ------------------------------------------------------------ sharded solve: a rank's rows
+// Bandwidth of rows [row0, row0 + m) of a matrix whose entries carry GLOBAL
+// column indices (rowptr from 0): out[0] = max(c - row), out[1] = max(row - c),
+// out[2] = 1 if a row pointer or column is out of range.  Grid-stride over
+// entries; a row per thread with its entries.
+__global__ void k_rows_band(int m, long long nnz, int row0, int n, const int *__restrict__ rowptr,
+                            const int *__restrict__ colind, int *out)
+{
+    int ku = 0, kl = 0, bad = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const int t0 = rowptr[r], t1 = rowptr[r + 1];
+        if (t0 < 0 || t1 < t0 || (long long)t1 > nnz) {
+            bad = 1;
+            continue;
+        }
+        for (int t = t0; t < t1; t++) {
+            const int c = colind[t];
+            if (c < 0 || c >= n) bad = 1;
+            ku = max(ku, c - (row0 + r));
+            kl = max(kl, (row0 + r) - c);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ku = max(ku, __shfl_xor_sync(0xffffffffu, ku, o));
+        kl = max(kl, __shfl_xor_sync(0xffffffffu, kl, o));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, ku);
+        atomicMax(out + 1, kl);
+        if (bad) atomicOr(out + 2, 1);
+    }
+}
+
+extern "C" int spk_rows_band(int m, long long nnz, int row0, int n, const int *d_rowptr, const int *d_colind,
+                             int *d_out, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    int r = ck(cudaMemsetAsync(d_out, 0, 4 * sizeof(int), st));
+    if (r == SPK_OK && m > 0) {
+        long long blocks = ((long long)m + 255) / 256;
+        if (blocks > 152 * 8) blocks = 152 * 8;
+        k_rows_band<<<(unsigned)blocks, 256, 0, st>>>(m, nnz, row0, n, d_rowptr, d_colind, d_out);
+        r = ck(cudaGetLastError());
+    }
+    return r;
+}
+
+// The local system of a sharded solve, in place: the rank's rows (rowptr from
+// 0, global columns, values) were copied to rows [h, h + m) of rowptr and to
+// entries [h, h + nnz) of colind / aij.  Shifts those row pointers by h and
+// columns by h - row0, and writes h identity rows before and after.
+__global__ void k_shard_local(int m, long long nnz, int h, int row0, int *rowptr, int *colind, double *aij)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (long long i = tid; i < h; i += stride) {
+        rowptr[i] = (int)i;
+        colind[i] = (int)i;
+        aij[i] = 1.0;
+        rowptr[h + m + 1 + i] = (int)(h + nnz + 1 + i);
+        colind[h + nnz + i] = (int)(h + m + i);
+        aij[h + nnz + i] = 1.0;
+    }
+    for (long long r = tid; r <= m; r += stride) rowptr[h + r] += h;
+    for (long long t = tid; t < nnz; t += stride) colind[h + t] += h - row0;
+}
+
+extern "C" int spk_shard_local(int m, long long nnz, int h, int row0, int *d_rowptr, int *d_colind, double *d_aij,
+                               void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    long long blocks = (nnz + 255) / 256;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_shard_local<<<(unsigned)blocks, 256, 0, st>>>(m, nnz, h, row0, d_rowptr, d_colind, d_aij);
+    return ck(cudaGetLastError());
 }

@@ -64,12 +64,10 @@ class TorchComm:
     def _gather(self, user, send, nbytes, recv):
         try:
             t = self._t(send, nbytes)
-            if self.rank == 0:
-                out = [self.torch.empty(nbytes, dtype=self.torch.uint8) for _ in range(self.size)]
-                self.dist.gather(t, out, dst=self._root, group=self.group)
+            if self.rank == 0:  # each rank's part lands in its slot of recv
                 dst = _bytes_at(recv, nbytes * self.size)
-                for r, o in enumerate(out):
-                    dst[r * nbytes:(r + 1) * nbytes] = o.numpy()
+                out = [self.torch.from_numpy(dst[r * nbytes:(r + 1) * nbytes]) for r in range(self.size)]
+                self.dist.gather(t, out, dst=self._root, group=self.group)
             else:
                 self.dist.gather(t, None, dst=self._root, group=self.group)
             return 0
@@ -81,7 +79,7 @@ class TorchComm:
             t = self._t(recv, nbytes)
             if self.rank == 0:
                 src = _bytes_at(send, nbytes * self.size)
-                parts = [self.torch.from_numpy(src[r * nbytes:(r + 1) * nbytes].copy()) for r in range(self.size)]
+                parts = [self.torch.from_numpy(src[r * nbytes:(r + 1) * nbytes]) for r in range(self.size)]
                 self.dist.scatter(t, parts, src=self._root, group=self.group)
             else:
                 self.dist.scatter(t, None, src=self._root, group=self.group)

@@ -105,3 +105,79 @@ def test_sharded_solve_matches_the_oracle_and_one_gpu(size, case):
     assert np.linalg.norm(x - x1) / np.linalg.norm(x1) <= ERR_TOL
     if k == 64:
         assert all(r[6] == 1 for r in res)  # the ranks' partitions were eliminated from both ends
+
+
+def _rank_sequence(rank, size, port, outq):
+    """One context through a sequence of sharded solves: the same system twice
+    (the plans and buffers kept from the first call), a different shape, a
+    wider band (a larger tile), a call with an out-of-range column on rank 1
+    only (every rank gets an error, nothing is kept), then the first system
+    again."""
+    try:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(0)
+        dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=size)
+        comm = shard.TorchComm()
+        ctx = hs.Context()
+        out = []
+
+        def one(n, k, p, seed, corrupt=False):
+            rp, ci, a, xt, b = hs.gen_banded(n, k, k, 1.5, seed, nrhs=1)
+            part0, part1, row0, row1 = shard.shard_range(n, p, size, rank)
+            lrp, lci, la = shard.rows_of(rp, ci, a, row0, row1)
+            if corrupt and rank == 1:
+                lci = lci.copy()
+                lci[len(lci) // 2] = n + 5
+            try:
+                x = shard.shard_solve(comm, n, p, lrp, lci, la, b[row0:row1], ctx=ctx)
+            except hs.SpikeError as e:
+                out.append(("error", e.code))
+                return
+            xr = np.asarray(xt).reshape(n, -1)[row0:row1, 0]
+            err = float(np.linalg.norm(x.ravel() - xr) / np.linalg.norm(xr))
+            out.append(("ok", ctx.info().block, ctx.info().relres_max, err))
+
+        one(40_000, 8, 16, 21)
+        one(40_000, 8, 16, 21)
+        one(52_000, 8, 20, 22)
+        one(52_000, 40, 20, 23)
+        one(52_000, 40, 20, 23, corrupt=True)
+        one(40_000, 8, 16, 21)
+        outq.put((rank, out))
+        ctx.close()
+        dist.destroy_process_group()
+    except BaseException as e:  # noqa: BLE001 -- reported to the parent
+        outq.put((rank, f"{type(e).__name__}: {e}"))
+        raise
+
+
+def test_sharded_solves_in_sequence_on_one_context():
+    import multiprocessing as mp
+
+    size = 2
+    mpc = mp.get_context("spawn")
+    q = mpc.Queue()
+    port = _free_port()
+    procs = [mpc.Process(target=_rank_sequence, args=(r, size, port, q)) for r in range(size)]
+    for pr in procs:
+        pr.start()
+    res = sorted(q.get(timeout=600) for _ in range(size))
+    for pr in procs:
+        pr.join(timeout=120)
+    for pr in procs:
+        if pr.is_alive():
+            pr.kill()
+    assert all(isinstance(r[1], list) for r in res), res
+    for rank, out in res:
+        ok = [o for o in out if o[0] == "ok"]
+        assert [o[1] for o in ok] == [8, 8, 8, 64, 8]  # tile size of each successful call
+        assert all(o[2] <= RES_TOL and o[3] <= 1e-10 for o in ok), out
+        assert out[4][0] == "error"
+    # the rank with the bad column reports it; the other learns that a peer failed
+    assert res[1][1][4][1] == 2  # SPIKE_ERR_CSR-class code on rank 1
+    assert res[0][1][4][1] != 0
+    for rank, out in res:  # same system, same x each time (the norms' float atomics may move relres's last bits)
+        assert out[0][3] == out[1][3] == out[5][3]
+        assert out[1][2] == pytest.approx(out[0][2], rel=1e-6) and out[5][2] == pytest.approx(out[0][2], rel=1e-6)
