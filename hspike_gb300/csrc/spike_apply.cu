@@ -898,12 +898,82 @@ __global__ void k_u_narrow(const typename HighOf<T>::type *__restrict__ u, T *ut
         ut[q] = cvt_fast<T, H>(u[q]);
 }
 
-// x (+)= y - V_i t_{i+1} - W_i b_{i-1} for tiles up to 32 rows: one thread per
-// (padded row, column), consecutive threads on consecutive rows (a CTA per row
-// block would leave most of its threads idle).
+// x (+)= y - V_i t_{i+1} - W_i b_{i-1} for tiles of 8 to 32 rows: one thread per
+// padded row, consecutive threads on consecutive rows (a CTA per row block
+// would leave most of its threads idle).  Each V and W entry the row needs is
+// loaded once per pass of eight right-hand-side columns and applied to all of
+// them, so at up to eight columns the spikes cross HBM once per call.
 template <class T, int KB>
 __global__ void __launch_bounds__(256)
     k_retrieve_rows(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                    const int *__restrict__ blk_part, const T *__restrict__ gV, const T *__restrict__ gW,
+                    const T *__restrict__ gy, const T *__restrict__ ut, long long NP, int n_iface, int n, int nrhs,
+                    typename HighOf<T>::type *x, int accumulate, const spk_sysref *__restrict__ sys,
+                    const int *__restrict__ part_sys)
+{
+    using H = typename HighOf<T>::type;
+    constexpr size_t TS = (size_t)KB * KB;
+    const long long NR = (long long)n_iface * 2 * KB;
+    for (long long pr = blockIdx.x * (long long)blockDim.x + threadIdx.x; pr < NP;
+         pr += (long long)gridDim.x * blockDim.x) {
+        const int gb = (int)(pr / KB), lr = (int)(pr - (long long)gb * KB);
+        const int part = blk_part[gb];
+        const int lrow = (gb - blk_off[part]) * KB + lr;
+        int s = part_start[part];
+        if (lrow >= part_start[part + 1] - s) continue; // identity padding row
+        H *xb = x;
+        int ld = n;
+        if (sys) {
+            const spk_sysref &S = sys[part_sys[part]];
+            xb = (H *)S.x;
+            ld = S.n;
+            s -= (int)S.row0;
+        }
+        const bool hasV = part < p - 1, hasW = part > 0;
+        constexpr int HC = 8; // columns per pass: each spike entry is loaded once per pass
+        for (int h0 = 0; h0 < nrhs; h0 += HC) {
+            const int nh = min(HC, nrhs - h0);
+            T acc[HC];
+#pragma unroll
+            for (int hh = 0; hh < HC; hh++) acc[hh] = hh < nh ? gy[(size_t)(h0 + hh) * NP + pr] : sc_zero<T>();
+            if (hasV) {
+                const T *t = ut + (size_t)h0 * NR + (size_t)part * 2 * KB + KB;
+#pragma unroll 4
+                for (int c = 0; c < KB; c++) {
+                    const T vc = gV[(size_t)gb * TS + (size_t)c * KB + lr];
+#pragma unroll
+                    for (int hh = 0; hh < HC; hh++)
+                        if (hh < nh) acc[hh] = msub(acc[hh], vc, t[(size_t)hh * NR + c]);
+                }
+            }
+            if (hasW) {
+                const T *bw = ut + (size_t)h0 * NR + (size_t)(part - 1) * 2 * KB;
+#pragma unroll 4
+                for (int c = 0; c < KB; c++) {
+                    const T wc = gW[(size_t)gb * TS + (size_t)c * KB + lr];
+#pragma unroll
+                    for (int hh = 0; hh < HC; hh++)
+                        if (hh < nh) acc[hh] = msub(acc[hh], wc, bw[(size_t)hh * NR + c]);
+                }
+            }
+#pragma unroll
+            for (int hh = 0; hh < HC; hh++)
+                if (hh < nh) {
+                    H *xp = xb + (size_t)(h0 + hh) * ld + s + lrow;
+                    const H d = cvt_fast<H, T>(acc[hh]);
+                    *xp = accumulate ? *xp + d : d;
+                }
+        }
+    }
+}
+
+// The same for tiles of up to 4 rows: one thread per (padded row, column).
+// Their spike tiles are a few dozen bytes, so reading them once per column
+// costs little, and the independent (row, column) items keep more
+// arithmetic in flight than a loop over the columns.
+template <class T, int KB>
+__global__ void __launch_bounds__(256)
+    k_retrieve_rc(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
                     const int *__restrict__ blk_part, const T *__restrict__ gV, const T *__restrict__ gW,
                     const T *__restrict__ gy, const T *__restrict__ ut, long long NP, int n_iface, int n, int nrhs,
                     typename HighOf<T>::type *x, int accumulate, const spk_sysref *__restrict__ sys,
@@ -1043,12 +1113,21 @@ template <class T, int KB> int run_retrieve(spk_plan *P, void *x, int nrhs, int 
         int sms = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const long long tot = P->NP * nrhs;
-        const int grid = (int)std::min<long long>((tot + 255) / 256, (long long)(sms > 0 ? sms : 152) * 8);
-        k_retrieve_rows<T, KB><<<grid, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, P->d_blk_part,
-                                                     (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y, ut,
-                                                     P->NP, P->n_iface, P->n, nrhs, (H *)x, accumulate, P->d_sys,
-                                                     P->d_part_sys);
+        const int cap = (sms > 0 ? sms : 152) * 8;
+        if constexpr (KB <= 4) {
+            const long long tot = P->NP * nrhs;
+            const int grid = (int)std::min<long long>((tot + 255) / 256, (long long)cap);
+            k_retrieve_rc<T, KB><<<grid, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, P->d_blk_part,
+                                                       (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y, ut,
+                                                       P->NP, P->n_iface, P->n, nrhs, (H *)x, accumulate, P->d_sys,
+                                                       P->d_part_sys);
+        } else {
+            const int grid = (int)std::min<long long>((P->NP + 255) / 256, (long long)cap);
+            k_retrieve_rows<T, KB><<<grid, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, P->d_blk_part,
+                                                         (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y, ut,
+                                                         P->NP, P->n_iface, P->n, nrhs, (H *)x, accumulate, P->d_sys,
+                                                         P->d_part_sys);
+        }
     } else {
         k_retrieve<T, KB><<<P->total_blocks, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, P->d_blk_part,
                                                            (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y,
