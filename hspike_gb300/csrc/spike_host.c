@@ -1519,7 +1519,8 @@ Error_t spike_dsolve_device_noalloc(integer_t n, integer_t nnz, integer_t nrhs, 
     if (blk_off[p] > NOALLOC_MAX_BLOCKS)
         return spk_fail(SPIKE_ERR_MEMORY, "%s: %d row blocks exceed the fixed schedule's %d (system too large for the "
                     "%u-byte no-allocation workspace)", name, blk_off[p], NOALLOC_MAX_BLOCKS, SPK_NOALLOC_SCRATCH_BYTES);
-    int blk_part[NOALLOC_MAX_BLOCKS];
+    /* the block -> partition map (64 KB): per thread, not on the caller's stack */
+    static _Thread_local int blk_part[NOALLOC_MAX_BLOCKS];
     for (int i = 0; i < p; i++)
         for (int b = blk_off[i]; b < blk_off[i + 1]; b++) blk_part[b] = i;
     P.n = n;
