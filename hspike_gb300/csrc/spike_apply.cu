@@ -899,10 +899,14 @@ __global__ void k_u_narrow(const typename HighOf<T>::type *__restrict__ u, T *ut
 }
 
 // x (+)= y - V_i t_{i+1} - W_i b_{i-1} for tiles of 8 to 32 rows: one thread per
-// padded row, consecutive threads on consecutive rows (a CTA per row block
-// would leave most of its threads idle).  Each V and W entry the row needs is
-// loaded once per pass of eight right-hand-side columns and applied to all of
-// them, so at up to eight columns the spikes cross HBM once per call.
+// (padded row, pass of eight right-hand-side columns), consecutive threads on
+// consecutive rows (a CTA per row block would leave most of its threads
+// idle).  Each V and W entry a row needs is loaded once per pass and applied
+// to all of the pass's columns, so at up to eight columns the spikes cross
+// HBM once per call; wider right-hand sides keep one thread per pass, so a
+// small system with many columns still fills the GPU.
+constexpr int RET_HC = 8; // right-hand-side columns per pass of k_retrieve_rows
+
 template <class T, int KB>
 __global__ void __launch_bounds__(256)
     k_retrieve_rows(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
@@ -913,9 +917,13 @@ __global__ void __launch_bounds__(256)
 {
     using H = typename HighOf<T>::type;
     constexpr size_t TS = (size_t)KB * KB;
+    constexpr int HC = RET_HC;
     const long long NR = (long long)n_iface * 2 * KB;
-    for (long long pr = blockIdx.x * (long long)blockDim.x + threadIdx.x; pr < NP;
-         pr += (long long)gridDim.x * blockDim.x) {
+    const long long tot = NP * ((nrhs + HC - 1) / HC);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < tot;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int h0 = (int)(q / NP) * HC;
+        const long long pr = q - (long long)(h0 / HC) * NP;
         const int gb = (int)(pr / KB), lr = (int)(pr - (long long)gb * KB);
         const int part = blk_part[gb];
         const int lrow = (gb - blk_off[part]) * KB + lr;
@@ -930,40 +938,37 @@ __global__ void __launch_bounds__(256)
             s -= (int)S.row0;
         }
         const bool hasV = part < p - 1, hasW = part > 0;
-        constexpr int HC = 8; // columns per pass: each spike entry is loaded once per pass
-        for (int h0 = 0; h0 < nrhs; h0 += HC) {
-            const int nh = min(HC, nrhs - h0);
-            T acc[HC];
+        const int nh = min(HC, nrhs - h0);
+        T acc[HC];
 #pragma unroll
-            for (int hh = 0; hh < HC; hh++) acc[hh] = hh < nh ? gy[(size_t)(h0 + hh) * NP + pr] : sc_zero<T>();
-            if (hasV) {
-                const T *t = ut + (size_t)h0 * NR + (size_t)part * 2 * KB + KB;
+        for (int hh = 0; hh < HC; hh++) acc[hh] = hh < nh ? gy[(size_t)(h0 + hh) * NP + pr] : sc_zero<T>();
+        if (hasV) {
+            const T *t = ut + (size_t)h0 * NR + (size_t)part * 2 * KB + KB;
 #pragma unroll 4
-                for (int c = 0; c < KB; c++) {
-                    const T vc = gV[(size_t)gb * TS + (size_t)c * KB + lr];
+            for (int c = 0; c < KB; c++) {
+                const T vc = gV[(size_t)gb * TS + (size_t)c * KB + lr];
 #pragma unroll
-                    for (int hh = 0; hh < HC; hh++)
-                        if (hh < nh) acc[hh] = msub(acc[hh], vc, t[(size_t)hh * NR + c]);
-                }
+                for (int hh = 0; hh < HC; hh++)
+                    if (hh < nh) acc[hh] = msub(acc[hh], vc, t[(size_t)hh * NR + c]);
             }
-            if (hasW) {
-                const T *bw = ut + (size_t)h0 * NR + (size_t)(part - 1) * 2 * KB;
-#pragma unroll 4
-                for (int c = 0; c < KB; c++) {
-                    const T wc = gW[(size_t)gb * TS + (size_t)c * KB + lr];
-#pragma unroll
-                    for (int hh = 0; hh < HC; hh++)
-                        if (hh < nh) acc[hh] = msub(acc[hh], wc, bw[(size_t)hh * NR + c]);
-                }
-            }
-#pragma unroll
-            for (int hh = 0; hh < HC; hh++)
-                if (hh < nh) {
-                    H *xp = xb + (size_t)(h0 + hh) * ld + s + lrow;
-                    const H d = cvt_fast<H, T>(acc[hh]);
-                    *xp = accumulate ? *xp + d : d;
-                }
         }
+        if (hasW) {
+            const T *bw = ut + (size_t)h0 * NR + (size_t)(part - 1) * 2 * KB;
+#pragma unroll 4
+            for (int c = 0; c < KB; c++) {
+                const T wc = gW[(size_t)gb * TS + (size_t)c * KB + lr];
+#pragma unroll
+                for (int hh = 0; hh < HC; hh++)
+                    if (hh < nh) acc[hh] = msub(acc[hh], wc, bw[(size_t)hh * NR + c]);
+            }
+        }
+#pragma unroll
+        for (int hh = 0; hh < HC; hh++)
+            if (hh < nh) {
+                H *xp = xb + (size_t)(h0 + hh) * ld + s + lrow;
+                const H d = cvt_fast<H, T>(acc[hh]);
+                *xp = accumulate ? *xp + d : d;
+            }
     }
 }
 
@@ -1122,7 +1127,8 @@ template <class T, int KB> int run_retrieve(spk_plan *P, void *x, int nrhs, int 
                                                        P->NP, P->n_iface, P->n, nrhs, (H *)x, accumulate, P->d_sys,
                                                        P->d_part_sys);
         } else {
-            const int grid = (int)std::min<long long>((P->NP + 255) / 256, (long long)cap);
+            const long long tot = P->NP * ((nrhs + RET_HC - 1) / RET_HC);
+            const int grid = (int)std::min<long long>((tot + 255) / 256, (long long)cap);
             k_retrieve_rows<T, KB><<<grid, 256, 0, st>>>(P->d_part_start, P->d_blk_off, P->p, P->d_blk_part,
                                                          (const T *)P->d_V, (const T *)P->d_W, (const T *)P->d_y, ut,
                                                          P->NP, P->n_iface, P->n, nrhs, (H *)x, accumulate, P->d_sys,
