@@ -328,6 +328,150 @@ __global__ void __launch_bounds__(NTOf<KB>::value * FactorSmem<T, KB>::BG)
     }
 }
 
+// K1 for tiles of up to 4 rows: one thread per padded row.  A block of such
+// tiles holds a few dozen entries, so a CTA per block group spends its time
+// on dependent memory round trips; here every row's entries are in flight at
+// once and the row goes straight to its tiles in global memory: first zeros
+// (the identity on D's diagonal for a padding row) across its row of every
+// tile the block writes, then its entries over them, in this thread's program
+// order.  The tiles, layouts, couplings, validation and bandwidth are those
+// of k_band_tiles.
+template <class T, int KB>
+__global__ void __launch_bounds__(256)
+    k_band_rows(const int *__restrict__ rowptr, const int *__restrict__ colind,
+                const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
+                const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
+                unsigned *err, const spk_sysref *__restrict__ sys, const int *__restrict__ part_sys, int twist,
+                int validate, int n, long long nnz, int gb0, int gb_end, int nb_total, int impl_kl)
+{
+    using H = typename HighOf<T>::type;
+    constexpr size_t TS = (size_t)KB * KB;
+    int ku = 0, kl = 0;
+    bool bad_csr = false, bad_band = false;
+    const long long r0 = (long long)gb0 * KB, r1 = (long long)gb_end * KB;
+    for (long long pr = r0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; pr < r1;
+         pr += (long long)gridDim.x * blockDim.x) {
+        const int gb = (int)(pr / KB), lr = (int)(pr - (long long)gb * KB);
+        const int part = blk_part[gb];
+        const int J = gb - blk_off[part];
+        const int M = twist ? (blk_off[part + 1] - blk_off[part]) / 2 : 1 << 30; // middle block
+        int s = part_start[part], e = part_start[part + 1];
+        const int *rp = rowptr, *ci = colind;
+        const H *av = aij;
+        if (sys) { // batch group: the partition's own system, in its local rows
+            const spk_sysref &S = sys[part_sys[part]];
+            rp = S.rowptr;
+            ci = S.colind;
+            av = (const H *)S.aij;
+            s -= (int)S.row0;
+            e -= (int)S.row0;
+        }
+        const int m = e - s, lrow = J * KB + lr;
+        T *gD = gT + (size_t)gb * 3 * TS, *g1 = gD + TS, *g2 = gD + 2 * TS, *gEb = gE + (size_t)gb * TS;
+        const bool cm1 = J <= M; // A(J,J-1) in slot 1: column-major up to the middle block
+        const bool cm2 = J >= M; // A(J,J+1) in slot 2: column-major from the middle block on
+        T *gz = (J == 0 && part > 0) ? gZ + (size_t)blk_off[part] * TS : nullptr; // C^ (W's first tile)
+        auto put = [&](T *t, int c, bool cm, T v) { (cm ? t[c * KB + lr] : t[lr * KB + c]) = v; };
+#pragma unroll
+        for (int c = 0; c < KB; c++) {
+            put(gD, c, false, (lrow >= m && c == lr) ? sc_one<T>() : sc_zero<T>());
+            put(g1, c, cm1, sc_zero<T>());
+            put(g2, c, cm2, sc_zero<T>());
+            if (J != M) put(gEb, c, true, sc_zero<T>());
+            if (gz) gz[lr * KB + c] = sc_zero<T>();
+        }
+        if (validate && lr == 0 && ((gb == 0 && rowptr[0] != 0) || (gb == nb_total - 1 && (long long)rowptr[n] != nnz)))
+            bad_csr = true;
+        if (lrow >= m) continue; // identity padding row
+        const int grow = s + lrow;
+        const int t0 = rp[grow], t1 = rp[grow + 1];
+        if (t0 < 0 || t1 < t0 || (long long)t1 > nnz) { // a row that cannot be read
+            if (validate) bad_csr = true;
+            continue;
+        }
+        const int cfirst = impl_kl >= 0 ? max(0, grow - impl_kl) - t0 : 0; // implied columns: cfirst + t
+        for (int t = t0; t < t1; t++) {
+            const int c = impl_kl >= 0 ? cfirst + t : __ldg(ci + t);
+            const T v = cvt_fast<T, H>(av[t]);
+            if (validate) {
+                if (c < 0 || c >= n || (t > t0 && __ldg(ci + t - 1) >= c)) bad_csr = true;
+                ku = max(ku, c - grow);
+                kl = max(kl, grow - c);
+            }
+            const int lc = c - s;
+            if (lc < 0) {
+                const int cc = lc + KB;
+                if (cc >= 0 && lrow < KB) {
+                    if (gz) gz[lr * KB + cc] = v;
+                } else
+                    bad_band = true;
+            } else if (lc >= m) {
+                const int br = lrow - (m - KB), bc = lc - m;
+                if (br >= 0 && bc < KB)
+                    gBhat[(size_t)part * TS + br * KB + bc] = v;
+                else
+                    bad_band = true;
+            } else {
+                const int bc = lc / KB, cc = lc - bc * KB, d = bc - J;
+                if (d == 0) {
+                    put(gD, cc, false, v);
+                } else if (d == -1) {
+                    put(g1, cc, cm1, v);
+                    if (J > M) put(gEb, cc, true, v); // A(J,J-1) column-major for the bottom chain
+                } else if (d == 1) {
+                    put(g2, cc, cm2, v);
+                    if (J < M) put(gEb, cc, true, v); // A(J,J+1) column-major for the top chain
+                } else {
+                    bad_band = true;
+                }
+            }
+        }
+    }
+    if (bad_csr) atomicOr(err, SPK_DEV_ERR_CSR);
+    if (bad_band) atomicOr(err, SPK_DEV_ERR_BAND);
+    if (validate) {
+        for (int o = 16; o > 0; o >>= 1) {
+            ku = max(ku, __shfl_xor_sync(0xffffffffu, ku, o));
+            kl = max(kl, __shfl_xor_sync(0xffffffffu, kl, o));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if ((unsigned)ku > *(volatile const unsigned *)(err + 1)) atomicMax(err + 1, (unsigned)ku);
+            if ((unsigned)kl > *(volatile const unsigned *)(err + 2)) atomicMax(err + 2, (unsigned)kl);
+        }
+    }
+}
+
+// K1 over row blocks [b0, b1) of the plan: k_band_rows for tiles of up to 4
+// rows (at 4-row complex tiles 0.56 against 0.78 ms for k_band_tiles; at 8
+// rows, whose 17-entry rows write twice as much per thread, 1.42 against
+// 1.13 ms), k_band_tiles above
+template <class T, int KB>
+int launch_band_tiles(spk_plan *P, const int *rowptr, const int *colind, const void *aij, int b0, int b1,
+                      cudaStream_t st)
+{
+    using H = typename HighOf<T>::type;
+    using S = FactorSmem<T, KB>;
+    constexpr int NT = NTOf<KB>::value;
+    const int val = P->validate && !P->d_sys && !P->impl_cols;
+    const int ikl = P->impl_cols ? P->impl_kl : -1;
+    if constexpr (KB <= 4) {
+        const long long rows = (long long)(b1 - b0) * KB;
+        const long long g = (rows + 255) / 256 < 152LL * 16 ? (rows + 255) / 256 : 152LL * 16;
+        const int grid = (int)g;
+        k_band_rows<T, KB><<<grid > 0 ? grid : 1, 256, 0, st>>>(
+            rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
+            (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist, val, P->n, P->nnz, b0, b1,
+            P->total_blocks, ikl);
+    } else {
+        k_band_tiles<T, KB><<<(b1 - b0 + S::BG - 1) / S::BG, NT * S::BG, S::band, st>>>(
+            rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
+            (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist, val, P->n, P->nnz, b0, b1,
+            P->total_blocks, ikl);
+    }
+    SPK_CHECK_LAUNCH();
+    return SPK_OK;
+}
+
 // K2: the sequential block-LU chain of one partition per CTA.
 //   L_J = F_{J-1} G_{J-1},  S_J = D_J - L_J E_{J-1},  G_J = S_J^{-1},
 //   W forward sweep z_J = -L_J z_{J-1} (z_0 = C^).
@@ -943,20 +1087,12 @@ template <class T, int KB> int run_tips(spk_plan *P, cudaStream_t st)
 template <class T, int KB> int run_factor_range(spk_plan *P, const int *rowptr, const int *colind, const void *aij,
                                                 int part0, int part1, cudaStream_t st)
 {
-    using H = typename HighOf<T>::type;
-    using S = FactorSmem<T, KB>;
-    constexpr int NT = NTOf<KB>::value;
     if (!P->twist || part0 < 0 || part1 > P->p || part0 >= part1) return SPK_EARG;
     const size_t TS = (size_t)KB * KB;
     const int b0 = P->blk_off[part0], b1 = P->blk_off[part1];
     if (cudaMemsetAsync((T *)P->d_Bhat + (size_t)part0 * TS, 0, sizeof(T) * TS * (part1 - part0), st) != cudaSuccess)
         return SPK_ECUDA;
-    k_band_tiles<T, KB><<<(b1 - b0 + S::BG - 1) / S::BG, NT * S::BG, S::band, st>>>(
-        rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
-        (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist,
-        P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz, b0, b1, P->total_blocks,
-        P->impl_cols ? P->impl_kl : -1);
-    SPK_CHECK_LAUNCH();
+    if (const int rc_ = launch_band_tiles<T, KB>(P, rowptr, colind, aij, b0, b1, st); rc_ != SPK_OK) return rc_;
     P->launches++;
     int rc = spk_twist_factor(P, 1, part0, part1, st);
     if (rc == SPK_OK) rc = spk_twist_factor(P, 0, part0, part1, st);
@@ -1002,12 +1138,8 @@ template <class T, int KB> int run_factor(spk_plan *P, const int *rowptr, const 
     const size_t TS = (size_t)KB * KB;
     if (cudaMemsetAsync(P->d_Bhat, 0, sizeof(T) * TS * P->p, st) != cudaSuccess) return SPK_ECUDA;
     spk_phase_begin(P, SPK_PH_BAND_TILES, st);
-    k_band_tiles<T, KB><<<(P->total_blocks + S::BG - 1) / S::BG, NT * S::BG, S::band, st>>>(
-        rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
-        (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist,
-        P->validate && !P->d_sys && !P->impl_cols, P->n, P->nnz, 0, P->total_blocks, P->total_blocks,
-        P->impl_cols ? P->impl_kl : -1);
-    SPK_CHECK_LAUNCH();
+    if (const int rc_ = launch_band_tiles<T, KB>(P, rowptr, colind, aij, 0, P->total_blocks, st); rc_ != SPK_OK)
+        return rc_;
     spk_phase_end(P, st);
     if (P->twist) { // two-sided chains (spike_twist.cu)
         P->launches++;  // k_band_tiles
