@@ -974,6 +974,160 @@ template <class T, int KB> struct Tile88 {
     }
 };
 
+// ------------------------------------------------------------ one warp per tile
+// A 32 x 32 FP32 tile on ONE warp, each lane owning a 4 x 8 register
+// sub-tile: lane (a, b), a = lane / 4, b = lane % 4, holds rows 4a .. 4a+3
+// and columns 8b .. 8b+7.  A chain on one warp needs no CTA barrier: the tile
+// inverse runs on shuffles alone (pivot rows and columns travel between
+// lanes).  Per k step of a product a lane reads 4 elements of the transposed
+// left operand (one 16-byte load) and 8 of the right operand (two) for 32
+// FMAs, so FMAs are most of what it issues; for tiles this small many chains
+// share each SM, and the instructions per FMA are what bound them.  Shared
+// tiles are dense (row stride KB): they arrive by single bulk copies.
+template <class T, int KB> struct TileW {
+    static_assert(KB == 32 && sizeof(T) == 4, "one warp per 32-row FP32 tile");
+    static constexpr int TR = KB / 8, TC = KB / 4;
+    static constexpr int LD = KB;
+    static constexpr int ELEMS = KB * KB;
+    static constexpr int NT = 32;
+
+    using Reg = T[TR][TC];
+
+    int a, b;
+    __device__ __forceinline__ TileW(int lane)
+    {
+        a = (lane & 31) >> 2;
+        b = lane & 3;
+    }
+    __device__ __forceinline__ int row(int i) const { return a * TR + i; }
+    __device__ __forceinline__ int col(int j) const { return b * TC + j; }
+
+    __device__ __forceinline__ void ld_row(T (&d)[TC], const T *p) const { vld<T, TC>(d, p + b * TC); }
+    __device__ __forceinline__ void st_row(T *p, const T (&d)[TC]) const { vst<T, TC>(p + b * TC, d); }
+    __device__ __forceinline__ void rzero(Reg &x) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++)
+#pragma unroll
+            for (int j = 0; j < TC; j++) x[i][j] = sc_zero<T>();
+    }
+    // dense tile (shared or global, row stride KB), row-major, and transposed
+    // (element (r, c) at c * KB + r)
+    __device__ __forceinline__ void rload(Reg &x, const T *s) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++) ld_row(x[i], s + row(i) * LD);
+    }
+    __device__ __forceinline__ void rstore(T *s, const Reg &x) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++) st_row(s + row(i) * LD, x[i]);
+    }
+    __device__ __forceinline__ void rstore_t(T *s, const Reg &x) const
+    {
+#pragma unroll
+        for (int j = 0; j < TC; j++) {
+            T c[TR];
+#pragma unroll
+            for (int i = 0; i < TR; i++) c[i] = x[i][j];
+            vst<T, TR>(s + col(j) * LD + row(0), c);
+        }
+    }
+    __device__ __forceinline__ void gload(Reg &x, const T *g) const { rload(x, g); }
+    __device__ __forceinline__ void gstore(T *g, const Reg &x) const { rstore(g, x); }
+    __device__ __forceinline__ void gstore_t(T *g, const Reg &x) const { rstore_t(g, x); }
+    // acc += D (a dense row-major tile)
+    __device__ __forceinline__ void radd(Reg &acc, const T *s) const
+    {
+#pragma unroll
+        for (int i = 0; i < TR; i++) {
+            T d[TC];
+            ld_row(d, s + row(i) * LD);
+#pragma unroll
+            for (int j = 0; j < TC; j++) acc[i][j] = acc[i][j] + d[j];
+        }
+    }
+    // acc (+|-)= A B, A given transposed (At, column-major), both dense
+    template <bool SUB> __device__ __forceinline__ void mm_tA(Reg &acc, const T *At, const T *B) const
+    {
+#pragma unroll 4
+        for (int k = 0; k < KB; k++) {
+            T x[TR], y[TC];
+            vld<T, TR>(x, At + k * LD + row(0));
+            ld_row(y, B + k * LD);
+#pragma unroll
+            for (int i = 0; i < TR; i++)
+#pragma unroll
+                for (int j = 0; j < TC; j++) acc[i][j] = SUB ? msub(acc[i][j], x[i], y[j]) : madd(acc[i][j], x[i], y[j]);
+        }
+    }
+
+    // In-place Gauss-Jordan inverse without pivoting, one pivot at a time, on
+    // shuffles: pivot k's row lives in lanes (k / TR, *), register row k % TR;
+    // its column in lanes (*, k / TC), register column k % TC.  Each pivot
+    // applies S <- S - u v' with u = (pivot column) - e_k and
+    // v = ((pivot row) + e_k) / S(k, k), which leaves S(k, k) = 1 / S(k, k),
+    // the pivot row scaled and the pivot column negated and scaled, as
+    // Gauss-Jordan does.  Rows are scaled to a unit diagonal first and the
+    // inverse's columns back after (S^{-1} = (D^{-1} S)^{-1} D^{-1}), as the
+    // CTA tiles' inverses do.  false in every lane on a zero or non-finite
+    // pivot or diagonal entry.
+    __device__ __forceinline__ bool inverse(Reg &s) const
+    {
+        constexpr unsigned FULL = 0xffffffffu;
+        bool ok = true;
+        // diagonal entry (TR a + i, TR a + i) sits in lane (a, a / 2),
+        // register [i][TR (a & 1) + i]
+        T dr[TR];
+        const bool odd = (a & 1) != 0;
+        const int dsrc = (a << 2) | (a >> 1);
+#pragma unroll
+        for (int i = 0; i < TR; i++) dr[i] = __shfl_sync(FULL, reg_sel(odd, s[i][TR + i], s[i][i]), dsrc);
+#pragma unroll
+        for (int i = 0; i < TR; i++) {
+            if (!sc_finite_nonzero(dr[i])) ok = false;
+            const T rr = sc_rcp_fast(dr[i]);
+#pragma unroll
+            for (int j = 0; j < TC; j++) s[i][j] = s[i][j] * rr;
+        }
+        for (int kb = 0; kb < KB / TC; kb++) { // TC pivots per pass: those of column group kb
+#pragma unroll
+            for (int kk = 0; kk < TC; kk++) {
+                const int ra = 2 * kb + kk / TR; // owner row group of pivot k = TC kb + kk
+                T prow[TC], pcol[TR];
+#pragma unroll
+                for (int j = 0; j < TC; j++) prow[j] = __shfl_sync(FULL, s[kk % TR][j], (ra << 2) | b);
+#pragma unroll
+                for (int i = 0; i < TR; i++) pcol[i] = __shfl_sync(FULL, s[i][kk], (a << 2) | kb);
+                const T piv = __shfl_sync(FULL, s[kk % TR][kk], (ra << 2) | kb);
+                if (!sc_finite_nonzero(piv)) ok = false;
+                const T pinv = sc_rcp_fast(piv);
+                const bool mycol = b == kb, myrow = a == ra;
+                T v[TC];
+#pragma unroll
+                for (int j = 0; j < TC; j++)
+                    v[j] = (j == kk ? prow[j] + (mycol ? sc_one<T>() : sc_zero<T>()) : prow[j]) * pinv;
+#pragma unroll
+                for (int i = 0; i < TR; i++) {
+                    const T u = i == kk % TR ? pcol[i] - (myrow ? sc_one<T>() : sc_zero<T>()) : pcol[i];
+#pragma unroll
+                    for (int j = 0; j < TC; j++) s[i][j] = msub(s[i][j], u, v[j]);
+                }
+            }
+        }
+        // columns back by the diagonal: column TC b + j's entry of dr sits in
+        // lane (2b + j / TR, *), register j % TR
+#pragma unroll
+        for (int j = 0; j < TC; j++) {
+            const T dc = __shfl_sync(FULL, dr[j % TR], ((2 * b + j / TR) << 2) | b);
+            const T rc = sc_rcp_fast(dc);
+#pragma unroll
+            for (int i = 0; i < TR; i++) s[i][j] = s[i][j] * rc;
+        }
+        return __all_sync(FULL, ok) != 0;
+    }
+};
+
 // Thread counts and tile geometry of the two-sided kernels: the elimination
 // chains of FP32 64-row tiles run on 64 threads with 8 x 8 sub-tiles (Tile88),
 // everything else on the Tile layouts above (NTOf threads for the kernels with

@@ -179,6 +179,257 @@ __global__ void __launch_bounds__(TwCfg<T, KB>::NT_LU, 4)
     if (!ok && threadIdx.x == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
 }
 
+// k_tw_lu for FP32 32-row tiles on one warp per chain (TileW): the same two
+// elimination chains and the same tiles written, with every tile inverse on
+// shuffles.  A CTA holds TW_W_CHAINS independent chains, one per warp, and
+// nothing synchronizes across warps.  Per warp, three dense shared tiles: s0
+// holds G_{J-1} / H_{J+1} and then the product L_J / U_J (as a left
+// operand); s1 and s2 take the bulk copies.  The diagonal block D_J arrives by
+// bulk copy into the buffer of the coupling tile the first product has just
+// consumed, so no tile waits in registers.
+constexpr int TW_W_CHAINS = 4; // chains (warps) per CTA of k_tw_lu_w
+
+// one shared tile's barrier as the lanes of one warp track it (the warp's
+// lane 0 issues the copy); the warp form of TileBar
+struct WarpBar {
+    uint64_t *bar;
+    unsigned phase;
+    bool inflight;
+    template <class T, int KB> __device__ __forceinline__ void issue(T *s, const T *g)
+    {
+        __syncwarp();
+        bulk_tile_dense<T, KB>(s, g, bar);
+        inflight = true;
+    }
+    __device__ __forceinline__ bool wait()
+    {
+        const bool ok = mbar_wait(bar, phase);
+        phase ^= 1u;
+        inflight = false;
+        return ok;
+    }
+    __device__ __forceinline__ void drain()
+    {
+        if (inflight) wait();
+    }
+};
+
+__device__ __forceinline__ void tw_bail_w(unsigned *err, WarpBar &a, WarpBar &b)
+{
+    if ((threadIdx.x & 31) == 0) atomicOr(err, SPK_DEV_ERR_TIMEOUT);
+    a.drain();
+    b.drain();
+}
+
+template <class T, int KB>
+__global__ void __launch_bounds__(32 * TW_W_CHAINS)
+    k_tw_lu_w(const T *__restrict__ gT, const int *__restrict__ blk_off, T *gL, T *gG, T *gE, unsigned *err,
+              int part0, int np)
+{
+    using TL = TileW<T, KB>;
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chain = blockIdx.x * TW_W_CHAINS + warp;
+    if (chain >= 2 * np) return; // the whole warp
+    const int part = (chain >> 1) + part0;
+    const bool top = (chain & 1) == 0;
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const T *gTp = gT + (size_t)blk_off[part] * 3 * TS; // per block: D, A(J,J-1), A(J,J+1)
+
+    extern __shared__ char smraw[];
+    T *base = (T *)smem_align(smraw);
+    T *s0 = base + (size_t)warp * 3 * TL::ELEMS, *s1 = s0 + TL::ELEMS, *s2 = s1 + TL::ELEMS;
+    uint64_t *bars = (uint64_t *)(base + (size_t)TW_W_CHAINS * 3 * TL::ELEMS) + 2 * warp;
+    TL t(lane);
+    typename TL::Reg acc;
+    bool ok = true, tmo = false;
+    if (lane == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    WarpBar b1{bars, 0u, false}, b2{bars + 1, 0u, false}; // tiles s1, s2
+
+    if (top) {
+        // top chain, J = 0..M-1 (M >= 4)
+        T *sG = s0, *sE = s1, *sX = s2;
+        b1.issue<T, KB>(sE, gTp + 2 * TS); // A(0,1), row-major: the right operand of S_1
+        b2.issue<T, KB>(sX, gTp + 4 * TS); // A(1,0), column-major: the left operand of L_1
+        t.gload(acc, gTp);                 // S_0 = D_0
+        for (int J = 0; J < M; J++) {
+            if (J > 0) {
+                tmo |= !b2.wait();
+                if (__any_sync(FULL, tmo)) return tw_bail_w(err, b1, b2);
+                t.rzero(acc);
+                t.template mm_tA<false>(acc, sX, sG); // L_J = A(J,J-1) G_{J-1}
+                b2.issue<T, KB>(sX, gTp + (size_t)J * 3 * TS); // D_J, lands during the next product
+                t.rstore_t(sG, acc);
+                t.gstore_t(gL + tb + J * TS, acc);
+                tmo |= !b1.wait();
+                if (__any_sync(FULL, tmo)) return tw_bail_w(err, b1, b2);
+                __syncwarp(); // L_J's shared image is complete
+                t.rzero(acc);
+                t.template mm_tA<true>(acc, sG, sE); // - L_J A(J-1,J)
+                tmo |= !b2.wait();
+                if (__any_sync(FULL, tmo)) return tw_bail_w(err, b1, b2);
+                t.radd(acc, sX); // S_J = D_J - L_J A(J-1,J)
+                if (J + 1 < M) {
+                    b1.issue<T, KB>(sE, gTp + (size_t)J * 3 * TS + 2 * TS);
+                    b2.issue<T, KB>(sX, gTp + (size_t)(J + 1) * 3 * TS + TS);
+                }
+            }
+            ok = t.inverse(acc) && ok;
+            __syncwarp();
+            t.rstore(sG, acc);
+            t.gstore_t(gG + tb + J * TS, acc);
+            __syncwarp();
+        }
+    } else {
+        // bottom chain, J = N-1..M+1, then U_M and T'_M
+        T *sH = s0, *sY = s1, *sX = s2;
+        b1.issue<T, KB>(sY, gTp + (size_t)(N - 2) * 3 * TS + 2 * TS); // A(N-2,N-1), column-major
+        b2.issue<T, KB>(sX, gTp + (size_t)(N - 1) * 3 * TS + TS);     // A(N-1,N-2), row-major
+        t.gload(acc, gTp + (size_t)(N - 1) * 3 * TS);                  // T_{N-1} = D_{N-1}
+        for (int J = N - 1; J >= M; J--) {
+            if (J < N - 1) {
+                tmo |= !b1.wait();
+                if (__any_sync(FULL, tmo)) return tw_bail_w(err, b1, b2);
+                t.rzero(acc);
+                t.template mm_tA<false>(acc, sY, sH); // U_J = A(J,J+1) H_{J+1}
+                b1.issue<T, KB>(sY, gTp + (size_t)J * 3 * TS); // D_J, lands during the next product
+                t.rstore_t(sH, acc);
+                t.gstore_t((J == M ? gE : gL) + tb + J * TS, acc);
+                tmo |= !b2.wait();
+                if (__any_sync(FULL, tmo)) return tw_bail_w(err, b1, b2);
+                __syncwarp(); // U_J's shared image is complete
+                t.rzero(acc);
+                t.template mm_tA<true>(acc, sH, sX); // - U_J A(J+1,J)
+                tmo |= !b1.wait();
+                if (__any_sync(FULL, tmo)) return tw_bail_w(err, b1, b2);
+                t.radd(acc, sY); // T_J = D_J - U_J A(J+1,J)
+                if (J == M) {
+                    t.gstore(gG + tb + J * TS, acc); // T'_M for k_tw_merge
+                    break;
+                }
+                b1.issue<T, KB>(sY, gTp + (size_t)(J - 1) * 3 * TS + 2 * TS);
+                b2.issue<T, KB>(sX, gTp + (size_t)J * 3 * TS + TS);
+            }
+            ok = t.inverse(acc) && ok;
+            __syncwarp();
+            t.rstore(sH, acc);
+            t.gstore_t(gG + tb + J * TS, acc);
+            __syncwarp();
+        }
+    }
+    b1.drain();
+    b2.drain();
+    if (!ok && lane == 0) atomicOr(err, SPK_DEV_ERR_PIVOT);
+}
+// k_tw_bwd on one warp per chain (TileW): the back substitution of W and V
+// from X_M outwards, chain c of a CTA's TW_W_CHAINS taking (partition c / 4,
+// spike half c % 4) in k_tw_bwd's numbering (0 W top, 1 W bottom, 2 V top,
+// 3 V bottom).  Per warp, the tiles G_J / H_J and the coupling tile arrive by
+// bulk copies; X stays in a dense shared tile as the right operand.
+template <class T, int KB>
+__global__ void __launch_bounds__(32 * TW_W_CHAINS)
+    k_tw_bwd_w(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE, T *gV,
+               T *gW, int part0, int np, unsigned *err)
+{
+    using TL = TileW<T, KB>;
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chain = blockIdx.x * TW_W_CHAINS + warp;
+    if (chain >= 4 * np) return; // the whole warp
+    const int part = (chain >> 2) + part0, which = chain & 3;
+    const bool isV = which >= 2, top = (which & 1) == 0;
+    if (isV ? part == p - 1 : part == 0) return; // no such spike
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    T *gX = isV ? gV : gW;
+    const bool hasZ = isV ? !top : top;
+    const int cnt = top ? M : N - 1 - M;
+
+    extern __shared__ char smraw[];
+    T *base = (T *)smem_align(smraw);
+    T *sG = base + (size_t)warp * 3 * TL::ELEMS, *sE = sG + TL::ELEMS, *sX = sE + TL::ELEMS;
+    uint64_t *bars = (uint64_t *)(base + (size_t)TW_W_CHAINS * 3 * TL::ELEMS) + 2 * warp;
+    TL t(lane);
+    typename TL::Reg acc, zreg;
+    if (lane == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    WarpBar bG{bars, 0u, false}, bE{bars + 1, 0u, false};
+    bool tmo = false;
+
+    const int J1 = top ? M - 1 : M + 1;
+    bG.issue<T, KB>(sG, gG + tb + (size_t)J1 * TS); // left operands: dense
+    bE.issue<T, KB>(sE, gE + tb + (size_t)J1 * TS);
+    if (hasZ) t.gload(zreg, gX + tb + (size_t)J1 * TS); // Z_J of the first step (row-major)
+    {
+        // X_M (column-major in global) -> the lane's sub-tile -> a row-major dense tile
+        const T *gm = gX + tb + (size_t)M * TS;
+#pragma unroll
+        for (int j = 0; j < TL::TC; j++) {
+            T c[TL::TR];
+            vld<T, TL::TR>(c, gm + (size_t)t.col(j) * KB + t.row(0));
+#pragma unroll
+            for (int i = 0; i < TL::TR; i++) acc[i][j] = c[i];
+        }
+        t.rstore(sX, acc);
+    }
+    __syncwarp();
+    for (int i = 0; i < cnt; i++) {
+        const int J = top ? M - 1 - i : M + 1 + i;
+        const int Jn = top ? J - 1 : J + 1;
+        const bool more = i + 1 < cnt;
+        if (hasZ) {
+#pragma unroll
+            for (int r = 0; r < TL::TR; r++)
+#pragma unroll
+                for (int c = 0; c < TL::TC; c++) acc[r][c] = zreg[r][c];
+        } else {
+            t.rzero(acc);
+        }
+        tmo |= !bE.wait();
+        if (__any_sync(FULL, tmo)) return tw_bail_w(err, bG, bE);
+        t.template mm_tA<true>(acc, sE, sX); // Z_J - A(J,J+-1) X_{J+-1}
+        if (more) bE.issue<T, KB>(sE, gE + tb + (size_t)Jn * TS); // (syncs the warp: sX reads done)
+        else
+            __syncwarp();
+        t.rstore(sX, acc);
+        if (hasZ && more) t.gload(zreg, gX + tb + (size_t)Jn * TS); // Z of the next step, lands meanwhile
+        tmo |= !bG.wait();
+        if (__any_sync(FULL, tmo)) return tw_bail_w(err, bG, bE);
+        __syncwarp(); // the updated right-hand side is in sX
+        t.rzero(acc);
+        t.template mm_tA<false>(acc, sG, sX); // X_J = G_J (...)
+        if (more) bG.issue<T, KB>(sG, gG + tb + (size_t)Jn * TS);
+        else
+            __syncwarp();
+        t.rstore(sX, acc);
+        t.gstore_t(gX + tb + (size_t)J * TS, acc);
+        __syncwarp();
+    }
+    bG.drain();
+    bE.drain();
+}
+
+// shared bytes of k_tw_lu_w: three dense tiles and two mbarriers per chain,
+// alignment
+template <class T, int KB> constexpr size_t tw_lu_w_smem()
+{
+    return (size_t)TW_W_CHAINS * 3 * sizeof(T) * KB * KB + 16 * TW_W_CHAINS + 16;
+}
+// FP32 32-row tiles take the one-warp elimination chains
+template <class T, int KB> constexpr bool tw_lu_w_ok() { return sizeof(T) == 4 && KB == 32; }
+
 // V's right-hand side [0; B^] restricted to block J: B^ fills the last KB
 // real rows of the partition, i.e. rows o..KB-1 of block J0 and rows 0..o-1
 // of block J0+1 (when o > 0).
@@ -672,13 +923,25 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
                 cudaFuncSetAttribute(k_tw_bwd<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem) !=
                     cudaSuccess)
                 return SPK_ECUDA;
+            if constexpr (tw_lu_w_ok<T, KB>()) {
+                if (cudaFuncSetAttribute(k_tw_lu_w<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tw_lu_w_smem<T, KB>()) != cudaSuccess ||
+                    cudaFuncSetAttribute(k_tw_bwd_w<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tw_lu_w_smem<T, KB>()) != cudaSuccess)
+                    return SPK_ECUDA;
+            }
             attr = true;
         }
         const int p = P->p, np = part1 - part0;
         if (np <= 0) return SPK_OK;
         if (fwd) {
-            k_tw_lu<T, KB><<<dim3(np, 2), NT_LU, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
-                                                                           (T *)P->d_G, (T *)P->d_E, P->d_err, part0);
+            if constexpr (tw_lu_w_ok<T, KB>())
+                k_tw_lu_w<T, KB><<<(2 * np + TW_W_CHAINS - 1) / TW_W_CHAINS, 32 * TW_W_CHAINS,
+                                   tw_lu_w_smem<T, KB>(), st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+                                                                (T *)P->d_G, (T *)P->d_E, P->d_err, part0, np);
+            else
+                k_tw_lu<T, KB><<<dim3(np, 2), NT_LU, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+                                                                    (T *)P->d_G, (T *)P->d_E, P->d_err, part0);
             SPK_CHECK_LAUNCH();
             P->launches++;
             if (p > 1) {
@@ -695,8 +958,15 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
             SPK_CHECK_LAUNCH();
             P->launches++;
         } else if (p > 1) {
-            k_tw_bwd<T, KB><<<dim3(np, 4), NT, C::smem, st>>>(P->d_blk_off, p, (const T *)P->d_G, (const T *)P->d_E,
-                                                              (T *)P->d_V, (T *)P->d_W, part0, P->d_err);
+            if constexpr (tw_lu_w_ok<T, KB>())
+                k_tw_bwd_w<T, KB><<<(4 * np + TW_W_CHAINS - 1) / TW_W_CHAINS, 32 * TW_W_CHAINS,
+                                    tw_lu_w_smem<T, KB>(), st>>>(P->d_blk_off, p, (const T *)P->d_G,
+                                                                 (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W, part0,
+                                                                 np, P->d_err);
+            else
+                k_tw_bwd<T, KB><<<dim3(np, 4), NT, C::smem, st>>>(P->d_blk_off, p, (const T *)P->d_G,
+                                                                  (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W, part0,
+                                                                  P->d_err);
             SPK_CHECK_LAUNCH();
             P->launches++;
         }

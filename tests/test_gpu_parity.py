@@ -122,6 +122,8 @@ CASES_TWIST = [
     (8 * 64 * 4, 64, 64, 1.5, 4, 1),    # exactly 8 blocks per partition
     (9 * 64 * 5 + 37, 64, 64, 1.5, 5, 3),  # odd block count, ragged last block
     (40000, 32, 32, 1.5, 10, 2),
+    (8 * 32 * 3, 30, 30, 1.5, 3, 1),    # 32-row tiles (one warp per chain): exactly 8 blocks per partition
+    (9 * 32 * 6 + 19, 32, 25, 1.5, 6, 3),  # 32-row tiles: odd block count, ragged last block, ku != kl
     (30000, 16, 9, 1.5, 12, 17),        # ku != kl, two right-hand-side chunks
     (60000, 20, 20, 1.2, 1, 1),         # one partition
     (20000, 1, 1, 2.0, 16, 1),          # 2-row tiles on lanes
@@ -363,6 +365,42 @@ def test_reused_plan_validates_each_call():
             hs.solve(bad_rp, ci60, a, b, ctx=ctx)
         assert e.value.name == "csr"
         x = hs.solve(rp, ci, a, b, ctx=ctx)  # and back to the first matrix
+        assert relerr(x, x1) <= 1e-12
+    finally:
+        ctx.close()
+
+
+def test_reused_plan_validates_each_call_small_tiles():
+    # the same for 4-row tiles, whose band pass runs one thread per row
+    # (k_band_rows): measured bandwidth, rejected CSR, and back
+    ctx = hs.Context()
+    try:
+        n = 40000
+        rp, ci, a, xt, b = hs.gen_banded(n, 3, 3, 1.5, seed=29)
+        x1 = hs.solve(rp, ci, a, b, ctx=ctx)
+        x2 = hs.solve(rp, ci, a, b, ctx=ctx)
+        assert np.array_equal(x1, x2)
+        assert (ctx.info().ku, ctx.info().kl, ctx.info().block) == (3, 3, 4)
+        assert relerr(x1, oracle.spike(rp, ci, a, b, p=ctx.info().partitions)) <= ERR_TOL
+        ci4 = ci.copy()
+        ci4[rp[1] - 1] = 4  # row 0's last column 3 -> 4 (still sorted): ku 4, same tile class
+        x = hs.solve(rp, ci4, a, b, ctx=ctx)
+        assert (ctx.info().ku, ctx.info().kl, ctx.info().block) == (4, 3, 4)
+        assert oracle.residual(rp, ci4, a, x, b).max() <= RES_TOL
+        for bad_ci, bad_rp in ((ci.copy(), rp), (ci.copy(), rp.copy())):
+            if bad_rp is rp:
+                bad_ci[100], bad_ci[101] = bad_ci[101], bad_ci[100]  # unsorted row
+            else:
+                bad_ci[7] = n + 5  # column out of range
+            with pytest.raises(hs.SpikeError) as e:
+                hs.solve(bad_rp, bad_ci, a, b, ctx=ctx)
+            assert e.value.name == "csr"
+        bad_rp = rp.copy()
+        bad_rp[500] = len(ci) + 100  # row pointer past nnz
+        with pytest.raises(hs.SpikeError) as e:
+            hs.solve(bad_rp, ci, a, b, ctx=ctx)
+        assert e.value.name == "csr"
+        x = hs.solve(rp, ci, a, b, ctx=ctx)
         assert relerr(x, x1) <= 1e-12
     finally:
         ctx.close()
