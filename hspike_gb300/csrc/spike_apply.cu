@@ -486,6 +486,187 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
     }
 }
 
+// The two-sided sweeps for FP32 32-row tiles on one warp per (partition,
+// half, chunk of HC columns), lane l owning row l of every block: the step's
+// coupling tile arrives straight from global memory into registers (lane l
+// reads row l of the column-major tile: consecutive addresses across the
+// warp), one step ahead, and the previous block's vector is broadcast from a
+// small shared buffer.  No CTA barrier: many chains share each SM, and a
+// step is a few hundred instructions.  The middle block is k_tw_apply_mid's.
+constexpr int TWW_CHAINS = 4; // warps (chains) per CTA of the one-warp sweeps
+
+template <class T, int KB> __device__ __forceinline__ void tww_row(T (&d)[KB], const T *g)
+{
+#pragma unroll
+    for (int k = 0; k < KB; k++) d[k] = g[(size_t)k * KB + (threadIdx.x & 31)];
+}
+// out[h] (+|-)= sum_k M[lane][k] v[k][h]; v: shared [KB][HC], read by broadcast
+template <class T, int KB, int HC, bool SUB>
+__device__ __forceinline__ void tww_mv(T (&out)[HC], const T (&m)[KB], const T *v)
+{
+#pragma unroll
+    for (int k = 0; k < KB; k++) {
+        T vk[HC];
+        vld<T, HC>(vk, v + k * HC);
+#pragma unroll
+        for (int h = 0; h < HC; h++) out[h] = SUB ? msub(out[h], m[k], vk[h]) : madd(out[h], m[k], vk[h]);
+    }
+}
+
+//   top     z_J = r_J - L_J z_{J-1},  J = 0..M-1
+//   bottom  w_J = r_J - U_J w_{J+1},  J = N-1..M   (U_M in gE)
+template <class T, int KB, int HC>
+__global__ void __launch_bounds__(32 * TWW_CHAINS)
+    k_tw_apply_fwd_w(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                     const T *__restrict__ gL, const T *__restrict__ gE, const typename HighOf<T>::type *__restrict__ r,
+                     int n, int nrhs, long long NP, T *gz)
+{
+    static_assert(KB == 32, "lane l owns row l");
+    constexpr size_t TS = (size_t)KB * KB;
+    __shared__ __align__(16) T vs[TWW_CHAINS][KB * HC];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nch = (nrhs + HC - 1) / HC;
+    const long long chain = (long long)blockIdx.x * TWW_CHAINS + warp;
+    if (chain >= (long long)p * 2 * nch) return; // the whole warp
+    const int part = (int)(chain / (2 * nch)), rem = (int)(chain - (long long)part * 2 * nch);
+    const bool top = (rem & 1) == 0;
+    const int h0 = (rem >> 1) * HC, nr = min(HC, nrhs - h0);
+    const int s = part_start[part], m = part_start[part + 1] - s;
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const long long rb = (long long)blk_off[part] * KB;
+    const int cnt = top ? M : N - M;
+    T *vw = vs[warp];
+    auto blk = [&](int i) { return top ? i : N - 1 - i; };
+    auto ctile = [&](int i) {
+        const int J = blk(i);
+        return (!top && J == M ? gE : gL) + tb + (size_t)J * TS;
+    };
+    auto fetch = [&](T (&d)[HC], int i) {
+        const int row = blk(i) * KB + lane;
+#pragma unroll
+        for (int h = 0; h < HC; h++)
+            d[h] = (h < nr && row < m) ? cvt_fast<T>(r[(size_t)(h0 + h) * n + s + row]) : sc_zero<T>();
+    };
+    T rn[HC], mc[KB], mn[KB];
+    fetch(rn, 0);
+    if (cnt > 1) tww_row<T, KB>(mn, ctile(1));
+    for (int i = 0; i < cnt; i++) {
+        const int J = blk(i);
+        T z[HC];
+#pragma unroll
+        for (int h = 0; h < HC; h++) z[h] = rn[h];
+        if (i + 1 < cnt) fetch(rn, i + 1);
+        if (i > 0) {
+#pragma unroll
+            for (int k = 0; k < KB; k++) mc[k] = mn[k];
+            if (i + 1 < cnt) tww_row<T, KB>(mn, ctile(i + 1));
+            tww_mv<T, KB, HC, true>(z, mc, vw);
+        }
+        __syncwarp(); // every lane has read the previous vector
+        vst<T, HC>(vw + lane * HC, z);
+#pragma unroll
+        for (int h = 0; h < HC; h++)
+            if (h < nr) gz[(size_t)(h0 + h) * NP + rb + (size_t)J * KB + lane] = z[h];
+        __syncwarp();
+    }
+}
+
+//   top     y_J = G_J (z_J - A(J,J+1) y_{J+1}),  J = M-1..0
+//   bottom  y_J = H_J (w_J - A(J,J-1) y_{J-1}),  J = M+1..N-1
+template <class T, int KB, int HC>
+__global__ void __launch_bounds__(32 * TWW_CHAINS)
+    k_tw_apply_bwd_w(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE,
+                     int nrhs, long long NP, const T *__restrict__ gz, T *gy)
+{
+    static_assert(KB == 32, "lane l owns row l");
+    constexpr size_t TS = (size_t)KB * KB;
+    __shared__ __align__(16) T vs[TWW_CHAINS][2][KB * HC];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nch = (nrhs + HC - 1) / HC;
+    const long long chain = (long long)blockIdx.x * TWW_CHAINS + warp;
+    if (chain >= (long long)p * 2 * nch) return; // the whole warp
+    const int part = (int)(chain / (2 * nch)), rem = (int)(chain - (long long)part * 2 * nch);
+    const bool top = (rem & 1) == 0;
+    const int h0 = (rem >> 1) * HC, nr = min(HC, nrhs - h0);
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+    const long long rb = (long long)blk_off[part] * KB;
+    const int cnt = top ? M : N - 1 - M;
+    T *yw = vs[warp][0], *tw = vs[warp][1];
+    auto blk = [&](int i) { return top ? M - 1 - i : M + 1 + i; };
+    auto fetch = [&](T (&d)[HC], int i) {
+        const size_t row = (size_t)rb + (size_t)blk(i) * KB + lane;
+#pragma unroll
+        for (int h = 0; h < HC; h++) d[h] = h < nr ? gz[(size_t)(h0 + h) * NP + row] : sc_zero<T>();
+    };
+    {
+        T ym[HC]; // y_M
+#pragma unroll
+        for (int h = 0; h < HC; h++)
+            ym[h] = h < nr ? gy[(size_t)(h0 + h) * NP + rb + (size_t)M * KB + lane] : sc_zero<T>();
+        vst<T, HC>(yw + lane * HC, ym);
+    }
+    T zn[HC], gc[KB], ec[KB], gn[KB], en[KB];
+    if (cnt > 0) {
+        fetch(zn, 0);
+        tww_row<T, KB>(gn, gG + tb + (size_t)blk(0) * TS);
+        tww_row<T, KB>(en, gE + tb + (size_t)blk(0) * TS);
+    }
+    __syncwarp();
+    for (int i = 0; i < cnt; i++) {
+        const int J = blk(i);
+        T t[HC];
+#pragma unroll
+        for (int h = 0; h < HC; h++) t[h] = zn[h];
+#pragma unroll
+        for (int k = 0; k < KB; k++) {
+            gc[k] = gn[k];
+            ec[k] = en[k];
+        }
+        if (i + 1 < cnt) {
+            fetch(zn, i + 1);
+            tww_row<T, KB>(gn, gG + tb + (size_t)blk(i + 1) * TS);
+            tww_row<T, KB>(en, gE + tb + (size_t)blk(i + 1) * TS);
+        }
+        tww_mv<T, KB, HC, true>(t, ec, yw); // z_J - A y_prev
+        vst<T, HC>(tw + lane * HC, t);
+        __syncwarp();
+        T y[HC];
+#pragma unroll
+        for (int h = 0; h < HC; h++) y[h] = sc_zero<T>();
+        tww_mv<T, KB, HC, false>(y, gc, tw); // G t
+        __syncwarp(); // every lane has read y_prev and t
+        vst<T, HC>(yw + lane * HC, y);
+#pragma unroll
+        for (int h = 0; h < HC; h++)
+            if (h < nr) gy[(size_t)(h0 + h) * NP + rb + (size_t)J * KB + lane] = y[h];
+        __syncwarp();
+    }
+}
+
+template <class T, int KB, int HC> int launch_tw_apply_w(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
+{
+    constexpr int NT = NTOf<KB>::value;
+    constexpr size_t smem = tw_apply_smem<T, KB>();
+    const long long chains = (long long)P->p * 2 * ((nrhs + HC - 1) / HC);
+    const int grid = (int)((chains + TWW_CHAINS - 1) / TWW_CHAINS);
+    k_tw_apply_fwd_w<T, KB, HC><<<grid, 32 * TWW_CHAINS, 0, st>>>(
+        P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_E,
+        (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP, (T *)P->d_z);
+    SPK_CHECK_LAUNCH();
+    const int hy = (nrhs + RC2 - 1) / RC2;
+    k_tw_apply_mid<T, KB><<<dim3(P->p, hy), NT, smem, st>>>(P->d_blk_off, (const T *)P->d_L, (const T *)P->d_G, nrhs,
+                                                            P->NP, (const T *)P->d_z, (T *)P->d_y);
+    SPK_CHECK_LAUNCH();
+    k_tw_apply_bwd_w<T, KB, HC><<<grid, 32 * TWW_CHAINS, 0, st>>>(P->d_blk_off, P->p, (const T *)P->d_G,
+                                                                  (const T *)P->d_E, nrhs, P->NP, (const T *)P->d_z,
+                                                                  (T *)P->d_y);
+    SPK_CHECK_LAUNCH();
+    P->launches += 3;
+    return SPK_OK;
+}
+
 template <class T, int KB> int run_tw_apply(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
     if constexpr (!TwistFits<T, KB>::ok) {
@@ -503,6 +684,11 @@ template <class T, int KB> int run_tw_apply(spk_plan *P, const void *r, int nrhs
                     cudaSuccess)
                 return SPK_ECUDA;
             attr = true;
+        }
+        if constexpr (sizeof(T) == 4 && KB == 32) { // one warp per chain
+            if (nrhs == 1) return launch_tw_apply_w<T, KB, 1>(P, r, nrhs, st);
+            if (nrhs <= 4) return launch_tw_apply_w<T, KB, 4>(P, r, nrhs, st);
+            return launch_tw_apply_w<T, KB, 8>(P, r, nrhs, st);
         }
         const int hy = (nrhs + RC2 - 1) / RC2;
         k_tw_apply_fwd<T, KB><<<dim3(P->p, 2, hy), NT, smem, st>>>(
