@@ -781,7 +781,7 @@ __global__ void __launch_bounds__(256)
 }
 
 // ------------------------------------------------------------ small bands
-// KB <= 4: KB lanes per (partition, column) chain.  Lane r owns row r of each
+// KB <= 8 (one-sided factors): KB lanes per (partition, column) chain.  Lane r owns row r of each
 // block's vectors and tiles; z_{J-1} / y_{J+1} / t arrive by shuffles.  A ring
 // entry holds the block's L (forward) or G and E (backward) tiles plus each
 // lane's own right-hand-side or z element; z is kept in gy between the sweeps
@@ -796,6 +796,7 @@ template <class T, int KB> struct QuadApply {
     static constexpr int CPC = chain_threads(SLOT);
     static constexpr int NT = CPC * KB;
     static constexpr size_t SMEM = (size_t)CPC * SLOT;
+    static_assert(NT > 0 && NT <= 1024, "threads per CTA");
 };
 
 template <class T, int KB>
@@ -1208,6 +1209,9 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// the lane kernel's ring of 8-row tiles fits shared memory (not for complex128)
+template <class T> constexpr bool quad_apply_8_fits() { return QuadApply<T, 8>::SMEM <= 227 * 1024; }
+
 template <class T, int KB> int run_apply_1(spk_plan *P, const void *r, int nrhs, cudaStream_t st)
 {
     constexpr int NT = NTOf<KB>::value;
@@ -1218,7 +1222,10 @@ template <class T, int KB> int run_apply_1(spk_plan *P, const void *r, int nrhs,
             return SPK_ECUDA;
         attr = true;
     }
-    if constexpr (KB <= 4) {
+    // KB lanes per (partition, column) chain up to 8-row tiles (where the ring
+    // of 8-row tiles fits shared memory): a step is KB shuffles and
+    // multiply-adds per lane, where the CTA kernel pays a barrier per step
+    if constexpr (KB <= 4 || (KB == 8 && quad_apply_8_fits<T>())) {
         using CA = QuadApply<T, KB>;
         static bool cattr = false;
         if (!cattr) {
