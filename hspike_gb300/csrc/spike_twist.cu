@@ -427,22 +427,8 @@ template <class T, int KB> constexpr size_t tw_lu_w_smem()
 {
     return (size_t)TW_W_CHAINS * 3 * sizeof(T) * KB * KB + 16 * TW_W_CHAINS + 16;
 }
-// FP32 32-row tiles take the one-warp elimination chains and back
-// substitution when the chains fill the GPU (at least 8 per SM: one warp
-// each issues ~0.55 instructions per cycle alone on a scheduler, so with few
-// chains the 128-thread CTA per chain is faster)
+// FP32 32-row tiles take the one-warp elimination chains
 template <class T, int KB> constexpr bool tw_lu_w_ok() { return sizeof(T) == 4 && KB == 32; }
-static inline bool tw_w_many(long long chains)
-{
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 152;
-    }
-    return chains >= 8LL * sms;
-}
 
 // V's right-hand side [0; B^] restricted to block J: B^ fills the last KB
 // real rows of the partition, i.e. rows o..KB-1 of block J0 and rows 0..o-1
@@ -949,20 +935,13 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
         const int p = P->p, np = part1 - part0;
         if (np <= 0) return SPK_OK;
         if (fwd) {
-            auto lu_cta = [&] {
+            if constexpr (tw_lu_w_ok<T, KB>())
+                k_tw_lu_w<T, KB><<<(2 * np + TW_W_CHAINS - 1) / TW_W_CHAINS, 32 * TW_W_CHAINS,
+                                   tw_lu_w_smem<T, KB>(), st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
+                                                                (T *)P->d_G, (T *)P->d_E, P->d_err, part0, np);
+            else
                 k_tw_lu<T, KB><<<dim3(np, 2), NT_LU, C::smem, st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
                                                                     (T *)P->d_G, (T *)P->d_E, P->d_err, part0);
-            };
-            if constexpr (tw_lu_w_ok<T, KB>()) {
-                if (tw_w_many(2LL * np))
-                    k_tw_lu_w<T, KB><<<(2 * np + TW_W_CHAINS - 1) / TW_W_CHAINS, 32 * TW_W_CHAINS,
-                                       tw_lu_w_smem<T, KB>(), st>>>((const T *)P->d_T, P->d_blk_off, (T *)P->d_L,
-                                                                    (T *)P->d_G, (T *)P->d_E, P->d_err, part0, np);
-                else
-                    lu_cta();
-            } else {
-                lu_cta();
-            }
             SPK_CHECK_LAUNCH();
             P->launches++;
             if (p > 1) {
@@ -979,22 +958,15 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
             SPK_CHECK_LAUNCH();
             P->launches++;
         } else if (p > 1) {
-            auto bwd_cta = [&] {
+            if constexpr (tw_lu_w_ok<T, KB>())
+                k_tw_bwd_w<T, KB><<<(4 * np + TW_W_CHAINS - 1) / TW_W_CHAINS, 32 * TW_W_CHAINS,
+                                    tw_lu_w_smem<T, KB>(), st>>>(P->d_blk_off, p, (const T *)P->d_G,
+                                                                 (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W, part0,
+                                                                 np, P->d_err);
+            else
                 k_tw_bwd<T, KB><<<dim3(np, 4), NT, C::smem, st>>>(P->d_blk_off, p, (const T *)P->d_G,
                                                                   (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W, part0,
                                                                   P->d_err);
-            };
-            if constexpr (tw_lu_w_ok<T, KB>()) {
-                if (tw_w_many(4LL * np))
-                    k_tw_bwd_w<T, KB><<<(4 * np + TW_W_CHAINS - 1) / TW_W_CHAINS, 32 * TW_W_CHAINS,
-                                        tw_lu_w_smem<T, KB>(), st>>>(P->d_blk_off, p, (const T *)P->d_G,
-                                                                     (const T *)P->d_E, (T *)P->d_V, (T *)P->d_W,
-                                                                     part0, np, P->d_err);
-                else
-                    bwd_cta();
-            } else {
-                bwd_cta();
-            }
             SPK_CHECK_LAUNCH();
             P->launches++;
         }

@@ -122,9 +122,9 @@ CASES_TWIST = [
     (8 * 64 * 4, 64, 64, 1.5, 4, 1),    # exactly 8 blocks per partition
     (9 * 64 * 5 + 37, 64, 64, 1.5, 5, 3),  # odd block count, ragged last block
     (40000, 32, 32, 1.5, 10, 2),
-    (8 * 32 * 3, 30, 30, 1.5, 3, 1),    # 32-row tiles, few chains (a CTA per chain): exactly 8 blocks per partition
+    (8 * 32 * 3, 30, 30, 1.5, 3, 1),    # 32-row tiles (one warp per chain), few chains: exactly 8 blocks per partition
     (9 * 32 * 6 + 19, 32, 25, 1.5, 6, 3),  # the same: odd block count, ragged last block, ku != kl
-    (8 * 32 * 620, 30, 30, 1.5, 620, 1),     # 32-row tiles, >= 8 chains per SM (one warp per chain): 8 blocks
+    (8 * 32 * 620, 30, 30, 1.5, 620, 1),     # 32-row tiles, more than 8 chains per SM: 8 blocks
     (9 * 32 * 620 + 19, 32, 25, 1.5, 620, 3),  # the same: odd block count, ragged last block, ku != kl
     (30000, 16, 9, 1.5, 12, 17),        # ku != kl, two right-hand-side chunks
     (60000, 20, 20, 1.2, 1, 1),         # one partition
