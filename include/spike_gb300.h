@@ -340,7 +340,10 @@ Error_t spike_shard_range(integer_t n, integer_t p, integer_t size, integer_t ra
  * ld = rows), and receives the same rows of x.  Mixed precision or FP64 and
  * the tolerance come from the context (the partition count is `p`, every
  * partition at least two tiles long); nrhs <= 64 per call.  Returns the same
- * status on every rank (an error on one rank is reported on all). */
+ * status on every rank (an error on one rank is reported on all).  The
+ * context keeps this rank's plans, device copy of its rows and page-locked
+ * staging for the next call of the same shape (n, p, nrhs, rows, nnz, ranks);
+ * a call of another shape, a failed call or spike_context_destroy frees them. */
 Error_t spike_shard_dsolve(spike_context_t ctx, const spike_comm_t *comm, integer_t n, integer_t p, integer_t nrhs,
                            integer_t rows, integer_t nnz, const integer_t *colind, const integer_t *rowptr,
                            const double *aij, double *x, const double *b);
