@@ -410,6 +410,14 @@ static int launch_residual(const spk_plan *P, const int *rp, const int *ci, cons
     return SPK_OK;
 }
 
+// lanes per row of the residual: 4 for long rows with one column, 2 for long
+// rows with several columns and for medium rows, 1 for short rows
+static int res_lanes(double per_row, int nrhs)
+{
+    if (per_row >= 64) return nrhs == 1 ? 4 : 2;
+    return per_row >= 12 ? 2 : 1;
+}
+
 template <class H>
 static int residual_g(const spk_plan *P, const int *rp, const int *ci, const void *a, const void *x, const void *b,
                       void *r, int nrhs, int want_b, double *norms, cudaStream_t st)
@@ -417,13 +425,16 @@ static int residual_g(const spk_plan *P, const int *rp, const int *ci, const voi
     // few lanes per row: every shuffle step of the row reduction is an FP64
     // add per lane, and GB300's FP64 pipe is the residual's bottleneck
     const double per_row = P->n > 0 ? (double)P->nnz / P->n : 1.0;
+    // one column: 4 lanes from 64 entries a row; several columns: 2 lanes (a
+    // lane's multiply-adds per reduction step grow with the columns)
+    const int g = res_lanes(per_row, nrhs);
     if (P->impl_cols) {
-        if (per_row >= 64) return launch_residual<H, 4, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-        if (per_row >= 12) return launch_residual<H, 2, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+        if (g == 4) return launch_residual<H, 4, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+        if (g == 2) return launch_residual<H, 2, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
         return launch_residual<H, 1, true>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
     }
-    if (per_row >= 64) return launch_residual<H, 4, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
-    if (per_row >= 12) return launch_residual<H, 2, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (g == 4) return launch_residual<H, 4, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
+    if (g == 2) return launch_residual<H, 2, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
     return launch_residual<H, 1, false>(P, rp, ci, a, x, b, r, nrhs, want_b, norms, st);
 }
 
@@ -557,12 +568,12 @@ extern "C" int spk_residual_batch(const spk_sysref *d_sys, const int *d_chunks, 
     const int R = rows_per_chunk;
     // lanes per row from the rows' length (as in the single-system residual)
     if (is_complex) {
-        if (row_len >= 64) return residual_batch_g<cdouble, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
-        if (row_len >= 12) return residual_batch_g<cdouble, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+        if (res_lanes(row_len, nrhs) == 4) return residual_batch_g<cdouble, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+        if (res_lanes(row_len, nrhs) == 2) return residual_batch_g<cdouble, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
         return residual_batch_g<cdouble, 1>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
     }
-    if (row_len >= 64) return residual_batch_g<double, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
-    if (row_len >= 12) return residual_batch_g<double, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    if (res_lanes(row_len, nrhs) == 4) return residual_batch_g<double, 4>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
+    if (res_lanes(row_len, nrhs) == 2) return residual_batch_g<double, 2>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
     return residual_batch_g<double, 1>(d_sys, d_chunks, nchunks, R, n_rows, nrhs, have_x, d_r, d_norms, st);
 }
 
