@@ -5,9 +5,14 @@
 //                Replaces the reference's per-partition directSolver_SolveForRHS
 //                on f_i (OpenMP/spike_interfaces.c:143) -- SuperLU dgstrs +
 //                dgsrfs per column (OpenMP/spike_superlu.c:986,1002).
+//                Two-sided partitions: k_tw_apply_fwd / mid / bwd (CTA per chain),
+//                k_tw_apply_fwd_w / bwd_w (FP32 32-row tiles, one warp per chain),
+//                k_qtw_apply_* (KB <= 4 on lanes); one-sided small bands on
+//                lanes: k_quad_apply (KB <= 8).
 //   k_ytips      bottom / top tips of y into the reduced right-hand side
 //                (block_AddTipTOReducedRHS, OpenMP/spike_matrix.c:1272-1297).
-//   k_retrieve   x_i (+)= y_i - V_i t_{i+1} - W_i b_{i-1} with the stored spikes.
+//   k_retrieve   x_i (+)= y_i - V_i t_{i+1} - W_i b_{i-1} with the stored spikes
+//                (k_retrieve_rows for KB 8..32, k_retrieve_rc for KB <= 4).
 //                The reference re-factors A_i and re-solves
 //                A_i x_i = f_i - B_i x_t - C_i x_b (OpenMP/spike_interfaces.c
 //                :259-396); with the spikes resident this is one parallel pass.

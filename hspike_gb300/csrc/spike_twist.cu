@@ -25,6 +25,9 @@
 //               W's C^ top-down through L, V's B^ bottom-up through U
 //   k_tw_merge  (grid p)     block M: L_M, G_M and X_M of both spikes
 //   k_tw_bwd    (grid p x 4) back substitution of W and V, top and bottom halves
+//   k_tw_lu_w / k_tw_bwd_w   the elimination chains and back substitution
+//               for FP32 32-row tiles on one warp per chain (TileW), four
+//               chains per CTA
 //
 // Layout, per block J of a partition (factor precision, KB x KB tiles):
 //   gL     J <= M: L_J;  J > M: U_J                           (column-major)
