@@ -975,17 +975,19 @@ template <class T, int KB> struct Tile88 {
 };
 
 // ------------------------------------------------------------ one warp per tile
-// A 32 x 32 FP32 tile on ONE warp, each lane owning a 4 x 8 register
-// sub-tile: lane (a, b), a = lane / 4, b = lane % 4, holds rows 4a .. 4a+3
-// and columns 8b .. 8b+7.  A chain on one warp needs no CTA barrier: the tile
-// inverse runs on shuffles alone (pivot rows and columns travel between
-// lanes).  Per k step of a product a lane reads 4 elements of the transposed
-// left operand (one 16-byte load) and 8 of the right operand (two) for 32
-// FMAs, so FMAs are most of what it issues; for tiles this small many chains
-// share each SM, and the instructions per FMA are what bound them.  Shared
-// tiles are dense (row stride KB): they arrive by single bulk copies.
+// A KB x KB FP32 tile (KB = 16 or 32) on ONE warp, each lane owning a
+// KB/8 x KB/4 register sub-tile: lane (a, b), a = lane / 4, b = lane % 4,
+// holds rows a KB/8 .. a KB/8 + KB/8 - 1 and columns b KB/4 .. b KB/4 +
+// KB/4 - 1 (4 x 8 at KB = 32).  A chain on one warp needs no CTA barrier:
+// the tile inverse runs on shuffles alone (pivot rows and columns travel
+// between lanes).  Per k step of a product a lane reads KB/8 elements of the
+// transposed left operand and KB/4 of the right operand in 8- or 16-byte
+// pieces for KB^2/32 FMAs, so FMAs are most of what it issues; for tiles this
+// small many chains share each SM, and the instructions per FMA are what
+// bound them.  Shared tiles are dense (row stride KB): they arrive by single
+// bulk copies.
 template <class T, int KB> struct TileW {
-    static_assert(KB == 32 && sizeof(T) == 4, "one warp per 32-row FP32 tile");
+    static_assert((KB == 16 || KB == 32) && sizeof(T) == 4, "one warp per 16- or 32-row FP32 tile");
     static constexpr int TR = KB / 8, TC = KB / 4;
     static constexpr int LD = KB;
     static constexpr int ELEMS = KB * KB;

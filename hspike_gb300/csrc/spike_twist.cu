@@ -26,7 +26,7 @@
 //   k_tw_merge  (grid p)     block M: L_M, G_M and X_M of both spikes
 //   k_tw_bwd    (grid p x 4) back substitution of W and V, top and bottom halves
 //   k_tw_lu_w / k_tw_bwd_w   the elimination chains and back substitution
-//               for FP32 32-row tiles on one warp per chain (TileW), four
+//               for FP32 16- and 32-row tiles on one warp per chain (TileW), four
 //               chains per CTA
 //
 // Layout, per block J of a partition (factor precision, KB x KB tiles):
@@ -430,8 +430,8 @@ template <class T, int KB> constexpr size_t tw_lu_w_smem()
 {
     return (size_t)TW_W_CHAINS * 3 * sizeof(T) * KB * KB + 16 * TW_W_CHAINS + 16;
 }
-// FP32 32-row tiles take the one-warp elimination chains
-template <class T, int KB> constexpr bool tw_lu_w_ok() { return sizeof(T) == 4 && KB == 32; }
+// FP32 16- and 32-row tiles take the one-warp elimination chains
+template <class T, int KB> constexpr bool tw_lu_w_ok() { return sizeof(T) == 4 && (KB == 16 || KB == 32); }
 
 // V's right-hand side [0; B^] restricted to block J: B^ fills the last KB
 // real rows of the partition, i.e. rows o..KB-1 of block J0 and rows 0..o-1
