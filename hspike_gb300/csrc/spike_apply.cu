@@ -491,21 +491,27 @@ __global__ void __launch_bounds__(NTOf<KB>::value, 4)
     }
 }
 
-// The two-sided sweeps for FP32 32-row tiles on one warp per (partition,
-// half, chunk of HC columns), lane l owning row l of every block: the step's
-// coupling tile arrives straight from global memory into registers (lane l
-// reads row l of the column-major tile: consecutive addresses across the
-// warp), one step ahead, and the previous block's vector is broadcast from a
-// small shared buffer.  No CTA barrier: many chains share each SM, and a
-// step is a few hundred instructions.  The middle block is k_tw_apply_mid's.
-constexpr int TWW_CHAINS = 4; // warps (chains) per CTA of the one-warp sweeps
+// The two-sided sweeps for FP32 16- and 32-row tiles on KB lanes per
+// (partition, half, chunk of HC columns) chain -- a warp at KB = 32, a
+// half-warp at KB = 16 -- lane l of the chain owning row l of every block:
+// the step's coupling tile arrives straight from global memory into
+// registers (lane l reads row l of the column-major tile: consecutive
+// addresses across the chain), one step ahead, and the previous block's
+// vector is broadcast from a small shared buffer.  No CTA barrier (a chain's
+// lanes synchronise among themselves): many chains share each SM, and a step
+// is a few hundred instructions.  The middle block is k_tw_apply_mid's.
+constexpr int TWW_CHAINS = 4; // warps per CTA of the one-warp sweeps
 
-template <class T, int KB> __device__ __forceinline__ void tww_row(T (&d)[KB], const T *g)
+template <int KB> __device__ __forceinline__ unsigned tww_mask()
+{
+    return KB == 32 ? 0xffffffffu : (0xffffu << (threadIdx.x & 16));
+}
+template <class T, int KB> __device__ __forceinline__ void tww_row(T (&d)[KB], const T *g, int row)
 {
 #pragma unroll
-    for (int k = 0; k < KB; k++) d[k] = g[(size_t)k * KB + (threadIdx.x & 31)];
+    for (int k = 0; k < KB; k++) d[k] = g[(size_t)k * KB + row];
 }
-// out[h] (+|-)= sum_k M[lane][k] v[k][h]; v: shared [KB][HC], read by broadcast
+// out[h] (+|-)= sum_k M[row][k] v[k][h]; v: shared [KB][HC], read by broadcast
 template <class T, int KB, int HC, bool SUB>
 __device__ __forceinline__ void tww_mv(T (&out)[HC], const T (&m)[KB], const T *v)
 {
@@ -526,13 +532,16 @@ __global__ void __launch_bounds__(32 * TWW_CHAINS)
                      const T *__restrict__ gL, const T *__restrict__ gE, const typename HighOf<T>::type *__restrict__ r,
                      int n, int nrhs, long long NP, T *gz)
 {
-    static_assert(KB == 32, "lane l owns row l");
+    static_assert(KB == 16 || KB == 32, "KB lanes per chain");
+    constexpr int CPW = 32 / KB; // chains per warp
     constexpr size_t TS = (size_t)KB * KB;
-    __shared__ __align__(16) T vs[TWW_CHAINS][KB * HC];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ __align__(16) T vs[TWW_CHAINS * CPW][KB * HC];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = lane % KB;
+    const int slot = warp * CPW + lane / KB;
     const int nch = (nrhs + HC - 1) / HC;
-    const long long chain = (long long)blockIdx.x * TWW_CHAINS + warp;
-    if (chain >= (long long)p * 2 * nch) return; // the whole warp
+    const long long chain = (long long)blockIdx.x * TWW_CHAINS * CPW + slot;
+    if (chain >= (long long)p * 2 * nch) return; // the whole chain
+    const unsigned msk = tww_mask<KB>();
     const int part = (int)(chain / (2 * nch)), rem = (int)(chain - (long long)part * 2 * nch);
     const bool top = (rem & 1) == 0;
     const int h0 = (rem >> 1) * HC, nr = min(HC, nrhs - h0);
@@ -541,21 +550,21 @@ __global__ void __launch_bounds__(32 * TWW_CHAINS)
     const size_t tb = (size_t)blk_off[part] * TS;
     const long long rb = (long long)blk_off[part] * KB;
     const int cnt = top ? M : N - M;
-    T *vw = vs[warp];
+    T *vw = vs[slot];
     auto blk = [&](int i) { return top ? i : N - 1 - i; };
     auto ctile = [&](int i) {
         const int J = blk(i);
         return (!top && J == M ? gE : gL) + tb + (size_t)J * TS;
     };
     auto fetch = [&](T (&d)[HC], int i) {
-        const int row = blk(i) * KB + lane;
+        const int rw = blk(i) * KB + row;
 #pragma unroll
         for (int h = 0; h < HC; h++)
-            d[h] = (h < nr && row < m) ? cvt_fast<T>(r[(size_t)(h0 + h) * n + s + row]) : sc_zero<T>();
+            d[h] = (h < nr && rw < m) ? cvt_fast<T>(r[(size_t)(h0 + h) * n + s + rw]) : sc_zero<T>();
     };
     T rn[HC], mc[KB], mn[KB];
     fetch(rn, 0);
-    if (cnt > 1) tww_row<T, KB>(mn, ctile(1));
+    if (cnt > 1) tww_row<T, KB>(mn, ctile(1), row);
     for (int i = 0; i < cnt; i++) {
         const int J = blk(i);
         T z[HC];
@@ -565,15 +574,15 @@ __global__ void __launch_bounds__(32 * TWW_CHAINS)
         if (i > 0) {
 #pragma unroll
             for (int k = 0; k < KB; k++) mc[k] = mn[k];
-            if (i + 1 < cnt) tww_row<T, KB>(mn, ctile(i + 1));
+            if (i + 1 < cnt) tww_row<T, KB>(mn, ctile(i + 1), row);
             tww_mv<T, KB, HC, true>(z, mc, vw);
         }
-        __syncwarp(); // every lane has read the previous vector
-        vst<T, HC>(vw + lane * HC, z);
+        __syncwarp(msk); // every lane of the chain has read the previous vector
+        vst<T, HC>(vw + row * HC, z);
 #pragma unroll
         for (int h = 0; h < HC; h++)
-            if (h < nr) gz[(size_t)(h0 + h) * NP + rb + (size_t)J * KB + lane] = z[h];
-        __syncwarp();
+            if (h < nr) gz[(size_t)(h0 + h) * NP + rb + (size_t)J * KB + row] = z[h];
+        __syncwarp(msk);
     }
 }
 
@@ -584,13 +593,16 @@ __global__ void __launch_bounds__(32 * TWW_CHAINS)
     k_tw_apply_bwd_w(const int *__restrict__ blk_off, int p, const T *__restrict__ gG, const T *__restrict__ gE,
                      int nrhs, long long NP, const T *__restrict__ gz, T *gy)
 {
-    static_assert(KB == 32, "lane l owns row l");
+    static_assert(KB == 16 || KB == 32, "KB lanes per chain");
+    constexpr int CPW = 32 / KB;
     constexpr size_t TS = (size_t)KB * KB;
-    __shared__ __align__(16) T vs[TWW_CHAINS][2][KB * HC];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __shared__ __align__(16) T vs[TWW_CHAINS * CPW][2][KB * HC];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = lane % KB;
+    const int slot = warp * CPW + lane / KB;
     const int nch = (nrhs + HC - 1) / HC;
-    const long long chain = (long long)blockIdx.x * TWW_CHAINS + warp;
-    if (chain >= (long long)p * 2 * nch) return; // the whole warp
+    const long long chain = (long long)blockIdx.x * TWW_CHAINS * CPW + slot;
+    if (chain >= (long long)p * 2 * nch) return; // the whole chain
+    const unsigned msk = tww_mask<KB>();
     const int part = (int)(chain / (2 * nch)), rem = (int)(chain - (long long)part * 2 * nch);
     const bool top = (rem & 1) == 0;
     const int h0 = (rem >> 1) * HC, nr = min(HC, nrhs - h0);
@@ -598,27 +610,27 @@ __global__ void __launch_bounds__(32 * TWW_CHAINS)
     const size_t tb = (size_t)blk_off[part] * TS;
     const long long rb = (long long)blk_off[part] * KB;
     const int cnt = top ? M : N - 1 - M;
-    T *yw = vs[warp][0], *tw = vs[warp][1];
+    T *yw = vs[slot][0], *tw = vs[slot][1];
     auto blk = [&](int i) { return top ? M - 1 - i : M + 1 + i; };
     auto fetch = [&](T (&d)[HC], int i) {
-        const size_t row = (size_t)rb + (size_t)blk(i) * KB + lane;
+        const size_t rw = (size_t)rb + (size_t)blk(i) * KB + row;
 #pragma unroll
-        for (int h = 0; h < HC; h++) d[h] = h < nr ? gz[(size_t)(h0 + h) * NP + row] : sc_zero<T>();
+        for (int h = 0; h < HC; h++) d[h] = h < nr ? gz[(size_t)(h0 + h) * NP + rw] : sc_zero<T>();
     };
     {
         T ym[HC]; // y_M
 #pragma unroll
         for (int h = 0; h < HC; h++)
-            ym[h] = h < nr ? gy[(size_t)(h0 + h) * NP + rb + (size_t)M * KB + lane] : sc_zero<T>();
-        vst<T, HC>(yw + lane * HC, ym);
+            ym[h] = h < nr ? gy[(size_t)(h0 + h) * NP + rb + (size_t)M * KB + row] : sc_zero<T>();
+        vst<T, HC>(yw + row * HC, ym);
     }
     T zn[HC], gc[KB], ec[KB], gn[KB], en[KB];
     if (cnt > 0) {
         fetch(zn, 0);
-        tww_row<T, KB>(gn, gG + tb + (size_t)blk(0) * TS);
-        tww_row<T, KB>(en, gE + tb + (size_t)blk(0) * TS);
+        tww_row<T, KB>(gn, gG + tb + (size_t)blk(0) * TS, row);
+        tww_row<T, KB>(en, gE + tb + (size_t)blk(0) * TS, row);
     }
-    __syncwarp();
+    __syncwarp(msk);
     for (int i = 0; i < cnt; i++) {
         const int J = blk(i);
         T t[HC];
@@ -631,22 +643,22 @@ __global__ void __launch_bounds__(32 * TWW_CHAINS)
         }
         if (i + 1 < cnt) {
             fetch(zn, i + 1);
-            tww_row<T, KB>(gn, gG + tb + (size_t)blk(i + 1) * TS);
-            tww_row<T, KB>(en, gE + tb + (size_t)blk(i + 1) * TS);
+            tww_row<T, KB>(gn, gG + tb + (size_t)blk(i + 1) * TS, row);
+            tww_row<T, KB>(en, gE + tb + (size_t)blk(i + 1) * TS, row);
         }
         tww_mv<T, KB, HC, true>(t, ec, yw); // z_J - A y_prev
-        vst<T, HC>(tw + lane * HC, t);
-        __syncwarp();
+        vst<T, HC>(tw + row * HC, t);
+        __syncwarp(msk);
         T y[HC];
 #pragma unroll
         for (int h = 0; h < HC; h++) y[h] = sc_zero<T>();
         tww_mv<T, KB, HC, false>(y, gc, tw); // G t
-        __syncwarp(); // every lane has read y_prev and t
-        vst<T, HC>(yw + lane * HC, y);
+        __syncwarp(msk); // every lane of the chain has read y_prev and t
+        vst<T, HC>(yw + row * HC, y);
 #pragma unroll
         for (int h = 0; h < HC; h++)
-            if (h < nr) gy[(size_t)(h0 + h) * NP + rb + (size_t)J * KB + lane] = y[h];
-        __syncwarp();
+            if (h < nr) gy[(size_t)(h0 + h) * NP + rb + (size_t)J * KB + row] = y[h];
+        __syncwarp(msk);
     }
 }
 
@@ -655,7 +667,8 @@ template <class T, int KB, int HC> int launch_tw_apply_w(spk_plan *P, const void
     constexpr int NT = NTOf<KB>::value;
     constexpr size_t smem = tw_apply_smem<T, KB>();
     const long long chains = (long long)P->p * 2 * ((nrhs + HC - 1) / HC);
-    const int grid = (int)((chains + TWW_CHAINS - 1) / TWW_CHAINS);
+    const int per_cta = TWW_CHAINS * (32 / KB);
+    const int grid = (int)((chains + per_cta - 1) / per_cta);
     k_tw_apply_fwd_w<T, KB, HC><<<grid, 32 * TWW_CHAINS, 0, st>>>(
         P->d_part_start, P->d_blk_off, P->p, (const T *)P->d_L, (const T *)P->d_E,
         (const typename HighOf<T>::type *)r, P->n, nrhs, P->NP, (T *)P->d_z);
@@ -690,7 +703,7 @@ template <class T, int KB> int run_tw_apply(spk_plan *P, const void *r, int nrhs
                 return SPK_ECUDA;
             attr = true;
         }
-        if constexpr (sizeof(T) == 4 && KB == 32) { // one warp per chain
+        if constexpr (sizeof(T) == 4 && (KB == 16 || KB == 32)) { // KB lanes per chain
             if (nrhs == 1) return launch_tw_apply_w<T, KB, 1>(P, r, nrhs, st);
             if (nrhs <= 4) return launch_tw_apply_w<T, KB, 4>(P, r, nrhs, st);
             return launch_tw_apply_w<T, KB, 8>(P, r, nrhs, st);
