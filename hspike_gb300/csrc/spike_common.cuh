@@ -992,6 +992,7 @@ template <class T, int KB> struct TileW {
     static constexpr int LD = KB;
     static constexpr int ELEMS = KB * KB;
     static constexpr int NT = 32;
+    static constexpr bool act = true; // every lane holds part of the tile
 
     using Reg = T[TR][TC];
 

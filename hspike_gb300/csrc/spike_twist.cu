@@ -25,7 +25,8 @@
 //               W's C^ top-down through L, V's B^ bottom-up through U
 //   k_tw_merge  (grid p)     block M: L_M, G_M and X_M of both spikes
 //   k_tw_bwd    (grid p x 4) back substitution of W and V, top and bottom halves
-//   k_tw_lu_w / k_tw_bwd_w   the elimination chains and back substitution
+//   k_tw_lu_w / k_tw_sweep_w / k_tw_bwd_w   the elimination chains, forward
+//               sweeps and back substitution
 //               for FP32 16- and 32-row tiles on one warp per chain (TileW), four
 //               chains per CTA
 //
@@ -453,6 +454,104 @@ __device__ __forceinline__ void bhat_block(const TL &t, typename TL::Reg &a, con
             }
             a[i][j] = v;
         }
+}
+
+// k_tw_sweep on one warp per chain (TileW): the spikes' forward sweeps, W's
+// C^ top-down through L and V's B^ bottom-up through U, chain c of a CTA
+// taking (partition c / 2, top or bottom).  The factor tiles of consecutive
+// blocks alternate between two dense shared tiles filled by bulk copies one
+// block ahead; z stays in a third as the right operand.
+template <class T, int KB>
+__global__ void __launch_bounds__(32 * TW_W_CHAINS)
+    k_tw_sweep_w(const int *__restrict__ part_start, const int *__restrict__ blk_off, int p,
+                 const T *__restrict__ gL, const T *__restrict__ gE, const T *__restrict__ gBhat, T *gV, T *gW,
+                 int part0, int np, unsigned *err)
+{
+    using TL = TileW<T, KB>;
+    constexpr unsigned FULL = 0xffffffffu;
+    constexpr size_t TS = (size_t)KB * KB;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int chain = blockIdx.x * TW_W_CHAINS + warp;
+    if (chain >= 2 * np) return; // the whole warp
+    const int part = (chain >> 1) + part0;
+    const bool top = (chain & 1) == 0;
+    if (top ? part == 0 : part == p - 1) return; // no such spike
+    const int N = blk_off[part + 1] - blk_off[part], M = N / 2;
+    const size_t tb = (size_t)blk_off[part] * TS;
+
+    extern __shared__ char smraw[];
+    T *base = (T *)smem_align(smraw);
+    T *sZ = base + (size_t)warp * 3 * TL::ELEMS, *sA = sZ + TL::ELEMS, *sB = sA + TL::ELEMS;
+    uint64_t *bars = (uint64_t *)(base + (size_t)TW_W_CHAINS * 3 * TL::ELEMS) + 3 * warp;
+    TL t(lane);
+    typename TL::Reg acc;
+    if (lane == 0) {
+        mbar_init(bars, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init(bars + 2, 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    WarpBar bA{bars, 0u, false}, bB{bars + 1, 0u, false}, bZ{bars + 2, 0u, false};
+    auto ring = [&](int J) { return (J & 1) ? sB : sA; };
+    auto rbar = [&](int J) -> WarpBar & { return (J & 1) ? bB : bA; };
+    auto bail = [&] {
+        if (lane == 0) atomicOr(err, SPK_DEV_ERR_TIMEOUT);
+        bA.drain();
+        bB.drain();
+        bZ.drain();
+    };
+    bool tmo = false;
+
+    if (top) {
+        // W: z_0 = C^ (gW tile 0, from the band pass), z_J = -L_J z_{J-1}, J = 1..M-1
+        bZ.issue<T, KB>(sZ, gW + tb);
+        rbar(1).template issue<T, KB>(ring(1), gL + tb + TS);
+        tmo |= !bZ.wait();
+        if (__any_sync(FULL, tmo)) return bail();
+        for (int J = 1; J < M; J++) {
+            if (J + 1 < M) rbar(J + 1).template issue<T, KB>(ring(J + 1), gL + tb + (size_t)(J + 1) * TS);
+            tmo |= !rbar(J).wait();
+            if (__any_sync(FULL, tmo)) return bail();
+            t.rzero(acc);
+            t.template mm_tA<true>(acc, ring(J), sZ);
+            __syncwarp(); // every lane has read z_{J-1}
+            t.rstore(sZ, acc);
+            t.gstore(gW + tb + (size_t)J * TS, acc);
+            __syncwarp();
+        }
+    } else {
+        // V: w_J = r_J - U_J w_{J+1}, J = N-1..M (U_M lives in gE)
+        const int m = part_start[part + 1] - part_start[part];
+        const int J0 = (m - KB) / KB, o = (m - KB) - J0 * KB; // m >= 8 KB: o >= 0, J0 > M
+        const T *bh = gBhat + (size_t)part * TS;
+        auto utile = [&](int J) { return (J == M ? gE : gL) + tb + (size_t)J * TS; };
+        rbar(N - 2).template issue<T, KB>(ring(N - 2), utile(N - 2));
+        bhat_block<T, KB>(t, acc, bh, N - 1, J0, o);
+        t.rstore(sZ, acc);
+        t.gstore(gV + tb + (size_t)(N - 1) * TS, acc);
+        __syncwarp();
+        for (int J = N - 2; J >= M; J--) {
+            if (J - 1 >= M) rbar(J - 1).template issue<T, KB>(ring(J - 1), utile(J - 1));
+            bhat_block<T, KB>(t, acc, bh, J, J0, o);
+            tmo |= !rbar(J).wait();
+            if (__any_sync(FULL, tmo)) return bail();
+            t.template mm_tA<true>(acc, ring(J), sZ);
+            __syncwarp(); // every lane has read w_{J+1}
+            t.rstore(sZ, acc);
+            t.gstore(gV + tb + (size_t)J * TS, acc);
+            __syncwarp();
+        }
+    }
+    bA.drain();
+    bB.drain();
+    bZ.drain();
+}
+// shared bytes of k_tw_sweep_w: three dense tiles and three mbarriers per
+// chain, alignment
+template <class T, int KB> constexpr size_t tw_sweep_w_smem()
+{
+    return (size_t)TW_W_CHAINS * 3 * sizeof(T) * KB * KB + 24 * TW_W_CHAINS + 16;
 }
 
 // The spikes' forward sweeps.  The factor tiles of consecutive blocks
@@ -930,7 +1029,9 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
                 if (cudaFuncSetAttribute(k_tw_lu_w<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tw_lu_w_smem<T, KB>()) != cudaSuccess ||
                     cudaFuncSetAttribute(k_tw_bwd_w<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)tw_lu_w_smem<T, KB>()) != cudaSuccess)
+                                         (int)tw_lu_w_smem<T, KB>()) != cudaSuccess ||
+                    cudaFuncSetAttribute(k_tw_sweep_w<T, KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tw_sweep_w_smem<T, KB>()) != cudaSuccess)
                     return SPK_ECUDA;
             }
             attr = true;
@@ -948,10 +1049,16 @@ template <class T, int KB> int run_twist(spk_plan *P, cudaStream_t st, bool fwd,
             SPK_CHECK_LAUNCH();
             P->launches++;
             if (p > 1) {
-                k_tw_sweep<T, KB><<<dim3(np, 2), NT, C::smem, st>>>(P->d_part_start, P->d_blk_off, p,
-                                                                    (const T *)P->d_L, (const T *)P->d_E,
-                                                                    (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W,
-                                                                    part0, P->d_err);
+                if constexpr (tw_lu_w_ok<T, KB>())
+                    k_tw_sweep_w<T, KB><<<(2 * np + TW_W_CHAINS - 1) / TW_W_CHAINS, 32 * TW_W_CHAINS,
+                                          tw_sweep_w_smem<T, KB>(), st>>>(
+                        P->d_part_start, P->d_blk_off, p, (const T *)P->d_L, (const T *)P->d_E,
+                        (const T *)P->d_Bhat, (T *)P->d_V, (T *)P->d_W, part0, np, P->d_err);
+                else
+                    k_tw_sweep<T, KB><<<dim3(np, 2), NT, C::smem, st>>>(P->d_part_start, P->d_blk_off, p,
+                                                                        (const T *)P->d_L, (const T *)P->d_E,
+                                                                        (const T *)P->d_Bhat, (T *)P->d_V,
+                                                                        (T *)P->d_W, part0, P->d_err);
                 SPK_CHECK_LAUNCH();
                 P->launches++;
             }
