@@ -38,10 +38,11 @@ WORKLOAD = (f"large-band real SPIKE: n={N:,} kl=ku={K_BAND} partitions={P} nrhs=
 
 
 # DRAM bytes (read + write) per row block of each kernel family, from one ncu
-# capture of `bench.py --n 600000 --partitions 300` (same 64-row tiles and
-# partition length, CSR larger than L2); traffic per launch = this x the
-# launch's row blocks.
-TRAFFIC_PER_BLOCK = {"factor_fwd": 100_905, "factor_bwd": 108_004, "band_tiles": 158_175, "rhs_sweeps": 48_796}
+# capture of this workload at full size (n = 2,000,000, 31,490 row blocks;
+# factor_fwd = k_tw_lu 79,741 + k_tw_sweep 30,961); rhs_sweeps from a capture
+# of `bench.py --n 600000 --partitions 300` (same 64-row tiles and partition
+# length).  Traffic per launch = this x the launch's row blocks.
+TRAFFIC_PER_BLOCK = {"factor_fwd": 110_702, "factor_bwd": 111_898, "band_tiles": 162_757, "rhs_sweeps": 48_796}
 
 
 def nnz_of(n, k):
@@ -748,7 +749,7 @@ def main():
                                "algorithmic_tflop_per_launch": alg / 1e12, "executed_tflop_per_launch": exe / 1e12,
                                "executed_frac": exe / dur / 1e12 / p32, "ms_per_launch": dur * 1000.0,
                                "traffic_source": "ncu dram__bytes_read+write per row block of this kernel "
-                                                 "(n=600,000 capture) x row blocks"}
+                                                 "(n=2,000,000 capture) x row blocks"}
         else:
             out["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": alg / dur / 1e9, "peak": hbm_peak,
                                "unit": "GB/s", "frac": alg / dur / 1e9 / hbm_peak,
