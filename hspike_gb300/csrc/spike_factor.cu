@@ -328,16 +328,22 @@ __global__ void __launch_bounds__(NTOf<KB>::value * FactorSmem<T, KB>::BG)
     }
 }
 
-// K1 for tiles of up to 4 rows: one thread per padded row.  A block of such
-// tiles holds a few dozen entries, so a CTA per block group spends its time
-// on dependent memory round trips; here every row's entries are in flight at
-// once and the row goes straight to its tiles in global memory: first zeros
-// (the identity on D's diagonal for a padding row) across its row of every
-// tile the block writes, then its entries over them, in this thread's program
-// order.  The tiles, layouts, couplings, validation and bandwidth are those
-// of k_band_tiles.
+// K1 for tiles of up to 4 rows: one thread per padded row, one warp per 32
+// consecutive rows (32 / KB blocks).  A block of such tiles holds a few dozen
+// entries, so a CTA per block group spends its time on dependent memory round
+// trips; here every row's entries are in flight at once.  Each row goes into
+// the warp's copy of its blocks' tiles in shared memory (zeros, the identity
+// on D's diagonal for a padding row, then its entries), and the warp writes
+// the tiles out with coalesced stores: a row written straight to global
+// memory would touch every 32-byte sector of its tiles once per column, and
+// those partial-sector writes, not DRAM, set the time.  The C^ and B^
+// coupling tiles (one block per partition) are still written per row.  The
+// tiles, layouts, couplings, validation and bandwidth are those of
+// k_band_tiles.
+constexpr int BAND_ROWS_WARPS = 4; // warps per CTA
+
 template <class T, int KB>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * BAND_ROWS_WARPS)
     k_band_rows(const int *__restrict__ rowptr, const int *__restrict__ colind,
                 const typename HighOf<T>::type *__restrict__ aij, const int *__restrict__ part_start,
                 const int *__restrict__ blk_off, const int *__restrict__ blk_part, T *gT, T *gE, T *gZ, T *gBhat,
@@ -345,87 +351,116 @@ __global__ void __launch_bounds__(256)
                 int validate, int n, long long nnz, int gb0, int gb_end, int nb_total, int impl_kl)
 {
     using H = typename HighOf<T>::type;
-    constexpr size_t TS = (size_t)KB * KB;
+    constexpr int TS = KB * KB;
+    constexpr int BW = 32 / KB;      // blocks per warp pass
+    constexpr int ST = 3 * TS + 1;   // shared stride of a block's (D, slot 1, slot 2); +1 spreads the banks
+    constexpr int SE = TS + 1;       // shared stride of a block's column-major coupling tile for gE
+    __shared__ T stage[BAND_ROWS_WARPS][BW * (ST + SE)];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    T *sT = stage[wib], *sE = sT + BW * ST;
+    const int bw = lane / KB, lr = lane - bw * KB; // this lane's block in the pass and row in the block
     int ku = 0, kl = 0;
     bool bad_csr = false, bad_band = false;
     const long long r0 = (long long)gb0 * KB, r1 = (long long)gb_end * KB;
-    for (long long pr = r0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; pr < r1;
-         pr += (long long)gridDim.x * blockDim.x) {
-        const int gb = (int)(pr / KB), lr = (int)(pr - (long long)gb * KB);
-        const int part = blk_part[gb];
-        const int J = gb - blk_off[part];
-        const int M = twist ? (blk_off[part + 1] - blk_off[part]) / 2 : 1 << 30; // middle block
-        int s = part_start[part], e = part_start[part + 1];
-        const int *rp = rowptr, *ci = colind;
-        const H *av = aij;
-        if (sys) { // batch group: the partition's own system, in its local rows
-            const spk_sysref &S = sys[part_sys[part]];
-            rp = S.rowptr;
-            ci = S.colind;
-            av = (const H *)S.aij;
-            s -= (int)S.row0;
-            e -= (int)S.row0;
-        }
-        const int m = e - s, lrow = J * KB + lr;
-        T *gD = gT + (size_t)gb * 3 * TS, *g1 = gD + TS, *g2 = gD + 2 * TS, *gEb = gE + (size_t)gb * TS;
-        const bool cm1 = J <= M; // A(J,J-1) in slot 1: column-major up to the middle block
-        const bool cm2 = J >= M; // A(J,J+1) in slot 2: column-major from the middle block on
-        T *gz = (J == 0 && part > 0) ? gZ + (size_t)blk_off[part] * TS : nullptr; // C^ (W's first tile)
-        auto put = [&](T *t, int c, bool cm, T v) { (cm ? t[c * KB + lr] : t[lr * KB + c]) = v; };
-#pragma unroll
-        for (int c = 0; c < KB; c++) {
-            put(gD, c, false, (lrow >= m && c == lr) ? sc_one<T>() : sc_zero<T>());
-            put(g1, c, cm1, sc_zero<T>());
-            put(g2, c, cm2, sc_zero<T>());
-            if (J != M) put(gEb, c, true, sc_zero<T>());
-            if (gz) gz[lr * KB + c] = sc_zero<T>();
-        }
-        if (validate && lr == 0 && ((gb == 0 && rowptr[0] != 0) || (gb == nb_total - 1 && (long long)rowptr[n] != nnz)))
-            bad_csr = true;
-        if (lrow >= m) continue; // identity padding row
-        const int grow = s + lrow;
-        const int t0 = rp[grow], t1 = rp[grow + 1];
-        if (t0 < 0 || t1 < t0 || (long long)t1 > nnz) { // a row that cannot be read
-            if (validate) bad_csr = true;
-            continue;
-        }
-        const int cfirst = impl_kl >= 0 ? max(0, grow - impl_kl) - t0 : 0; // implied columns: cfirst + t
-        for (int t = t0; t < t1; t++) {
-            const int c = impl_kl >= 0 ? cfirst + t : __ldg(ci + t);
-            const T v = cvt_fast<T, H>(av[t]);
-            if (validate) {
-                if (c < 0 || c >= n || (t > t0 && __ldg(ci + t - 1) >= c)) bad_csr = true;
-                ku = max(ku, c - grow);
-                kl = max(kl, grow - c);
+    const long long wstride = (long long)gridDim.x * BAND_ROWS_WARPS * 32;
+    // warp-uniform passes: every lane runs every pass (the shuffles and
+    // __syncwarp below need the whole warp)
+    for (long long wb = r0 + ((long long)blockIdx.x * BAND_ROWS_WARPS + wib) * 32; wb < r1; wb += wstride) {
+        const int gbw = (int)(wb / KB); // first block of the pass (wb is a multiple of KB)
+        const int nb = (int)min((long long)BW, (long long)gb_end - gbw);
+        for (int q = lane; q < BW * (ST + SE); q += 32) sT[q] = sc_zero<T>(); // sT and sE are consecutive
+        __syncwarp();
+        const int gb = gbw + bw;
+        const bool act = bw < nb;
+        int write_e = 0; // gE is written for every block but the middle one
+        if (act) {
+            const int part = blk_part[gb];
+            const int J = gb - blk_off[part];
+            const int M = twist ? (blk_off[part + 1] - blk_off[part]) / 2 : 1 << 30; // middle block
+            write_e = J != M;
+            int s = part_start[part], e = part_start[part + 1];
+            const int *rp = rowptr, *ci = colind;
+            const H *av = aij;
+            if (sys) { // batch group: the partition's own system, in its local rows
+                const spk_sysref &S = sys[part_sys[part]];
+                rp = S.rowptr;
+                ci = S.colind;
+                av = (const H *)S.aij;
+                s -= (int)S.row0;
+                e -= (int)S.row0;
             }
-            const int lc = c - s;
-            if (lc < 0) {
-                const int cc = lc + KB;
-                if (cc >= 0 && lrow < KB) {
-                    if (gz) gz[lr * KB + cc] = v;
-                } else
-                    bad_band = true;
-            } else if (lc >= m) {
-                const int br = lrow - (m - KB), bc = lc - m;
-                if (br >= 0 && bc < KB)
-                    gBhat[(size_t)part * TS + br * KB + bc] = v;
-                else
-                    bad_band = true;
+            const int m = e - s, lrow = J * KB + lr;
+            T *tD = sT + bw * ST, *t1 = tD + TS, *t2 = tD + 2 * TS, *tE = sE + bw * SE;
+            const bool cm1 = J <= M; // A(J,J-1) in slot 1: column-major up to the middle block
+            const bool cm2 = J >= M; // A(J,J+1) in slot 2: column-major from the middle block on
+            T *gz = (J == 0 && part > 0) ? gZ + (size_t)blk_off[part] * TS : nullptr; // C^ (W's first tile)
+            auto put = [&](T *t, int c, bool cm, T v) { (cm ? t[c * KB + lr] : t[lr * KB + c]) = v; };
+            if (gz)
+#pragma unroll
+                for (int c = 0; c < KB; c++) gz[lr * KB + c] = sc_zero<T>();
+            if (validate && lr == 0 && ((gb == 0 && rowptr[0] != 0) || (gb == nb_total - 1 && (long long)rowptr[n] != nnz)))
+                bad_csr = true;
+            const int grow = s + lrow;
+            const int t0 = lrow < m ? rp[grow] : 0, t1e = lrow < m ? rp[grow + 1] : 0;
+            if (lrow >= m) {
+                tD[lr * KB + lr] = sc_one<T>(); // identity padding row
+            } else if (t0 < 0 || t1e < t0 || (long long)t1e > nnz) { // a row that cannot be read
+                if (validate) bad_csr = true;
             } else {
-                const int bc = lc / KB, cc = lc - bc * KB, d = bc - J;
-                if (d == 0) {
-                    put(gD, cc, false, v);
-                } else if (d == -1) {
-                    put(g1, cc, cm1, v);
-                    if (J > M) put(gEb, cc, true, v); // A(J,J-1) column-major for the bottom chain
-                } else if (d == 1) {
-                    put(g2, cc, cm2, v);
-                    if (J < M) put(gEb, cc, true, v); // A(J,J+1) column-major for the top chain
-                } else {
-                    bad_band = true;
+                const int cfirst = impl_kl >= 0 ? max(0, grow - impl_kl) - t0 : 0; // implied columns: cfirst + t
+                for (int t = t0; t < t1e; t++) {
+                    const int c = impl_kl >= 0 ? cfirst + t : __ldg(ci + t);
+                    const T v = cvt_fast<T, H>(av[t]);
+                    if (validate) {
+                        if (c < 0 || c >= n || (t > t0 && __ldg(ci + t - 1) >= c)) bad_csr = true;
+                        ku = max(ku, c - grow);
+                        kl = max(kl, grow - c);
+                    }
+                    const int lc = c - s;
+                    if (lc < 0) {
+                        const int cc = lc + KB;
+                        if (cc >= 0 && lrow < KB) {
+                            if (gz) gz[lr * KB + cc] = v;
+                        } else
+                            bad_band = true;
+                    } else if (lc >= m) {
+                        const int br = lrow - (m - KB), bc = lc - m;
+                        if (br >= 0 && bc < KB)
+                            gBhat[(size_t)part * TS + br * KB + bc] = v;
+                        else
+                            bad_band = true;
+                    } else {
+                        const int bc = lc / KB, cc = lc - bc * KB, d = bc - J;
+                        if (d == 0) {
+                            put(tD, cc, false, v);
+                        } else if (d == -1) {
+                            put(t1, cc, cm1, v);
+                            if (J > M) put(tE, cc, true, v); // A(J,J-1) column-major for the bottom chain
+                        } else if (d == 1) {
+                            put(t2, cc, cm2, v);
+                            if (J < M) put(tE, cc, true, v); // A(J,J+1) column-major for the top chain
+                        } else {
+                            bad_band = true;
+                        }
+                    }
                 }
             }
         }
+        __syncwarp();
+        // the pass's tiles out: (D, slot 1, slot 2) of its blocks are one
+        // contiguous run of gT, their gE tiles one run of gE
+        T *oT = gT + (size_t)gbw * 3 * TS;
+        for (int q = lane; q < nb * 3 * TS; q += 32) {
+            const int b = q / (3 * TS);
+            oT[q] = sT[b * ST + (q - b * 3 * TS)];
+        }
+        T *oE = gE + (size_t)gbw * TS;
+        for (int q0 = 0; q0 < BW * TS; q0 += 32) {
+            const int q = q0 + lane, b = q / TS < BW ? q / TS : BW - 1;
+            const int we = __shfl_sync(0xffffffffu, write_e, b * KB);
+            if (q < nb * TS && we) oE[q] = sE[b * SE + (q - b * TS)];
+        }
+        __syncwarp(); // the next pass zeroes the staging tiles
     }
     if (bad_csr) atomicOr(err, SPK_DEV_ERR_CSR);
     if (bad_band) atomicOr(err, SPK_DEV_ERR_BAND);
@@ -442,9 +477,9 @@ __global__ void __launch_bounds__(256)
 }
 
 // K1 over row blocks [b0, b1) of the plan: k_band_rows for tiles of up to 4
-// rows (at 4-row complex tiles 0.56 against 0.78 ms for k_band_tiles; at 8
-// rows, whose 17-entry rows write twice as much per thread, 1.42 against
-// 1.13 ms), k_band_tiles above
+// rows (at 4-row complex tiles and 4 million rows 0.27 ms, against 0.56 ms
+// with each row written straight to global memory and 0.78 ms for
+// k_band_tiles), k_band_tiles above
 template <class T, int KB>
 int launch_band_tiles(spk_plan *P, const int *rowptr, const int *colind, const void *aij, int b0, int b1,
                       cudaStream_t st)
@@ -455,10 +490,10 @@ int launch_band_tiles(spk_plan *P, const int *rowptr, const int *colind, const v
     const int val = P->validate && !P->d_sys && !P->impl_cols;
     const int ikl = P->impl_cols ? P->impl_kl : -1;
     if constexpr (KB <= 4) {
-        const long long rows = (long long)(b1 - b0) * KB;
-        const long long g = (rows + 255) / 256 < 152LL * 16 ? (rows + 255) / 256 : 152LL * 16;
+        const long long rows = (long long)(b1 - b0) * KB, per = 32LL * BAND_ROWS_WARPS;
+        const long long g = (rows + per - 1) / per < 152LL * 16 ? (rows + per - 1) / per : 152LL * 16;
         const int grid = (int)g;
-        k_band_rows<T, KB><<<grid > 0 ? grid : 1, 256, 0, st>>>(
+        k_band_rows<T, KB><<<grid > 0 ? grid : 1, 32 * BAND_ROWS_WARPS, 0, st>>>(
             rowptr, colind, (const H *)aij, P->d_part_start, P->d_blk_off, P->d_blk_part, (T *)P->d_T, (T *)P->d_E,
             (T *)P->d_W, (T *)P->d_Bhat, P->d_err, P->d_sys, P->d_part_sys, P->twist, val, P->n, P->nnz, b0, b1,
             P->total_blocks, ikl);
