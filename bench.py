@@ -45,6 +45,14 @@ WORKLOAD = (f"large-band real SPIKE: n={N:,} kl=ku={K_BAND} partitions={P} nrhs=
 TRAFFIC_PER_BLOCK = {"factor_fwd": 110_702, "factor_bwd": 111_898, "band_tiles": 162_757, "rhs_sweeps": 48_796}
 
 
+def row_blocks(n, p, kb):
+    """row blocks of kb rows in the plan of n rows on p caller-set partitions:
+    floor(n / p) rows each, the remainder in the last, each padded to a
+    multiple of kb"""
+    nreg = n // p
+    return (p - 1) * (-(-nreg // kb)) + (-(-(n - (p - 1) * nreg) // kb))
+
+
 def nnz_of(n, k):
     return (2 * k + 1) * n - k * (k + 1)
 
@@ -721,8 +729,7 @@ def main():
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
         p32 = sgemm_tflops(torch, dev)
         KB = info.block
-        nreg = n // p
-        blocks = (p - 1) * (-(-nreg // KB)) + (-(-(n - (p - 1) * nreg) // KB))
+        blocks = row_blocks(n, p, KB)
         k = K_BAND
         csr_bytes = 12 * nnz + 4 * (n + 1)
         # per family: (bound, algorithmic work per launch, executed work per launch, units)
