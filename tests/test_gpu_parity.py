@@ -130,6 +130,8 @@ CASES_TWIST = [
     (60000, 20, 20, 1.2, 1, 1),         # one partition
     (20000, 1, 1, 2.0, 16, 1),          # 2-row tiles on lanes
     (30001, 3, 2, 1.2, 8, 4),           # 4-row tiles on lanes, ku != kl
+    (30001, 3, 2, 1.2, 8, 7),           # the same, lane sweeps over two column chunks (4 + 3)
+    (20000, 1, 1, 2.0, 16, 6),          # 2-row tiles, two column chunks (4 + 2)
 ]
 
 
